@@ -1,0 +1,283 @@
+/*
+ * vxr.h - C ABI of the GB300-native Voxel ReSTIR renderer (libvxr.so).
+ *
+ * Drop-in boundary for the per-frame render path of the WrldTmpl8/SmallProject
+ * reference: the World class (template/world.h:164-758) and the worldapi free
+ * functions (template/worldapi.h:1-102, bodies template/template.cpp:49-341).
+ * Every entry point names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status: VXR_OK (0) or a negative VXR_E_* code.
+ *    vxr_last_error() returns a thread-local message for the last failure.
+ *    (The reference calls FatalError and exits instead: template.cpp:1161-1224.)
+ *  - Plain pointers and sizes only; no C++ or torch types cross the boundary.
+ *  - A vxr_world is a host-side voxel store (1024^3 map in 8^3 bricks, exactly the
+ *    reference's fixed map: common.h:16-21). A vxr_view renders one camera view of
+ *    one world on the GPU. Calls on one view are not thread-safe; separate views
+ *    own separate CUDA streams.
+ *  - Render calls are asynchronous (like World::Render, world.cpp:2127); vxr_wait
+ *    blocks and reports device-side errors (like World::Commit, world.cpp:2357).
+ */
+#ifndef VXR_H
+#define VXR_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define VXR_OK             0
+#define VXR_E_INVALID     -1   /* bad argument (null pointer, size out of range) */
+#define VXR_E_CUDA        -2   /* CUDA runtime error (message in vxr_last_error) */
+#define VXR_E_NOMEM       -3   /* host or device allocation failed */
+#define VXR_E_STATE       -4   /* call out of order (e.g. render before upload) */
+#define VXR_E_DEVICE      -5   /* a kernel raised its device error flag */
+#define VXR_E_NODEVICE    -6   /* no CUDA device visible */
+#define VXR_E_IO          -7   /* file read/write failed or malformed file */
+
+/* ---- map geometry (fixed, reference common.h:16-21, 176-183) --------------- */
+#define VXR_MAPDIM     1024u  /* MAPWIDTH = MAPHEIGHT = MAPDEPTH */
+#define VXR_BRICKDIM   8u     /* BRICKDIM */
+#define VXR_GRIDDIM    128u   /* GRIDWIDTH = MAPWIDTH / BRICKDIM */
+#define VXR_UBERDIM    32u    /* UBERWIDTH = GRIDWIDTH / 4 */
+#define VXR_BRICKSIZE  512u   /* BRICKSIZE = 8^3 voxels */
+
+/* Voxel payload: 32-bit 0x00MMARGB (common.h:32-37, tools.cl:294-322):
+ * B bits 0-3, G 4-7, R 8-11, alpha 12-15 (0xF = opaque), emitter strength M 16-23. */
+#define VXR_VOXEL(r4, g4, b4, a4, m8) \
+    ((((uint32_t)(m8) & 255u) << 16) | (((uint32_t)(a4) & 15u) << 12) | \
+     (((uint32_t)(r4) & 15u) << 8) | (((uint32_t)(g4) & 15u) << 4) | ((uint32_t)(b4) & 15u))
+
+/* ---- records shared with the reference -------------------------------------- */
+
+/* Emitter record, identical to the reference struct Light (common.h:134-139):
+ * position = x + z*1024 + y*1024*1024, voxel = payload, size = 1 (voxel) or 8 (solid brick). */
+typedef struct vxr_light {
+    uint32_t position;
+    uint32_t voxel;
+    uint32_t size;
+} vxr_light;
+
+/* Canonical G-buffer record: the reference CLRay (common.h:125-132) without the
+ * ray direction, which is a pure function of the camera and the pixel. */
+typedef struct vxr_gbuffer_rec {
+    uint32_t voxel;   /* re-encoded albedo voxel (ris.cl:381) */
+    float    dist;    /* hit distance along the primary ray */
+    uint32_t side;    /* axis of the hit face, 0..2 */
+    uint32_t seed;    /* per-pixel xorshift32 state after the stage that last advanced it */
+} vxr_gbuffer_rec;
+
+/* Canonical reservoir record: the fields of the reference struct Reservoir
+ * (common.h:141-151) in declaration order, float3 members unpacked. */
+typedef struct vxr_reservoir_rec {
+    float    sumOfWeights;
+    uint32_t streamLength;          /* M */
+    uint32_t lightIndex;
+    float    adjustedWeight;        /* W */
+    float    positionOnVoxel[3];
+    float    invPositionProbability;
+    float    Nlight[3];
+    float    pHat;
+} vxr_reservoir_rec;
+
+/* Per-frame constants of the render path: the subset of RenderParams
+ * (common.h:100-118) read by the five stage kernels, plus the resolution
+ * (a compile-time constant in the reference, common.h:2-3). Filled by
+ * vxr_view_begin_frame from the camera exactly as World::Render does
+ * (world.cpp:2144-2191); exposed so tests can drive stages with explicit inputs. */
+typedef struct vxr_frame_consts {
+    float    E[3];                  /* camera position */
+    float    p0[3], p1[3], p2[3];   /* screen-plane corners */
+    float    oneOverRes[2];         /* 1/W, 1/H */
+    uint32_t R0;                    /* per-frame random seed (world.cpp:2184) */
+    uint32_t frame;                 /* (frame+1) & 255 */
+    uint32_t framecount;
+    uint32_t restirtemporalframe;   /* temporal reuse is skipped when 0 (ris.cl:85) */
+    float    Nleft[4], Nright[4], Ntop[4], Nbottom[4];  /* previous-frame frustum planes */
+    int32_t  accumulate, spatial, temporal;
+    uint32_t numberOfLights;
+    uint32_t numberOfCandidates;    /* NUMBEROFCANDIDATES (32) */
+    uint32_t numberOfMaxTemporalImportance;  /* TEMPORALMAXIMPORTANCE (20) */
+    uint32_t spatialRadius;         /* SPATIALRADIUS (30) */
+    uint32_t spatialTaps;           /* SPATIALTAPS (5) */
+    uint32_t width, height;         /* SCRWIDTH, SCRHEIGHT */
+} vxr_frame_consts;
+
+/* Light model, the reference's compile-time VOXELSAREPOINTLIGHTS (common.h:70). */
+#define VXR_LIGHTS_AREA   0   /* solid-angle voxel-side importance sampling (tools.cl:499-577) */
+#define VXR_LIGHTS_POINT  1   /* emitter = point at the voxel centre (tools.cl:609-616) */
+
+/* ---- library ------------------------------------------------------------------ */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* vxr_last_error(void);
+/* Library version string. */
+const char* vxr_version(void);
+
+/* ---- world: host voxel store (World, template/world.h:164-758) ------------------ */
+typedef struct vxr_world vxr_world;
+
+/* World::World + World::Clear (world.cpp:47-193, 726-745): an empty 1024^3 map. */
+int vxr_world_create(vxr_world** out);
+int vxr_world_destroy(vxr_world* w);
+/* World::Clear (world.cpp:726-745) / ClearWorld (template.cpp:60). */
+int vxr_world_clear(vxr_world* w);
+/* World::Set (world.h:456-513) / Plot (template.cpp:64). Out-of-map coordinates are
+ * ignored like the reference. When light tracking is on (the default), an emitter
+ * voxel is appended to the light list (World::AddLight, world.cpp:228-246) and an
+ * overwritten emitter is removed (World::RemoveLight, world.cpp:506-561). */
+int vxr_world_set(vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t voxel);
+/* World::Get (world.h:293-306) / Read (template.cpp:67). Out-of-map reads wrap like
+ * the reference's masking. */
+int vxr_world_get(const vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t* voxel);
+/* Box (template.cpp:98-101): Plot over [x1,x2) x [y1,y2) x [z1,z2). */
+int vxr_world_box(vxr_world* w, int x1, int y1, int z1, int x2, int y2, int z2, uint32_t voxel);
+/* Enable/disable incremental light tracking in vxr_world_set (AddLight/RemoveLight). */
+int vxr_world_track_lights(vxr_world* w, int enable);
+/* World::OptimizeBricks (world.cpp:655-683): collapse single-valued bricks into solid
+ * grid cells. Returns the number of bricks replaced in *replaced (may be NULL). */
+int vxr_world_optimize(vxr_world* w, uint32_t* replaced);
+/* World::FindLightsInWord + SetupLightBuffer (world.cpp:438-504, 563-612): rebuild the
+ * light list by scanning the map (brick cells y->z->x, voxels y->z->x; a solid emitter
+ * cell is one light of size 8). Returns the count in *count (may be NULL). */
+int vxr_world_scan_lights(vxr_world* w, uint32_t* count);
+/* World::SetupLightBuffer (world.cpp:563-612) with an explicit list (replaces the list). */
+int vxr_world_set_lights(vxr_world* w, const vxr_light* lights, uint32_t n);
+/* Read-only views of the host arrays (valid until the next edit): top-level grid
+ * (128^3 uint32, index x + z*128 + y*16384; 0 empty, even = solid colour << 1,
+ * odd = brick index << 1 | 1), brick pool (nbricks * 512 uint32, voxel lx + ly*8 + lz*64),
+ * light list. Any out-pointer may be NULL. */
+int vxr_world_arrays(const vxr_world* w, const uint32_t** grid, const uint32_t** bricks,
+                     uint32_t* nbricks, const vxr_light** lights, uint32_t* nlights);
+/* Number of bricks in use (allocated minus recycled). */
+int vxr_world_brick_count(const vxr_world* w, uint32_t* in_use);
+
+/* ---- procedural scenes (no reference counterpart: the thesis scenes need assets
+ * that are not available; these generate the benchmark worlds) -------------------- */
+#define VXR_EMIT_ABOVE_SURFACE 0  /* uniform (x,z), 1..8 voxels above the terrain */
+#define VXR_EMIT_AIR           1  /* uniform through the air volume above the terrain */
+#define VXR_EMIT_BLOBS         2  /* blob_fraction in Gaussian blobs, rest uniform in air */
+#define VXR_EMIT_LAYER         3  /* a glowing stratum [layer_lo, layer_hi] plus scattered */
+
+typedef struct vxr_scene_desc {
+    uint32_t extent;          /* world side in voxels (256, 512 or 1024), at the map origin */
+    uint32_t seed;
+    uint32_t octaves;         /* fBm octaves */
+    float    base_freq;       /* lattice frequency at extent 256 (1/64) */
+    float    gain;            /* fBm amplitude gain (0.5) */
+    float    height_base;     /* h = s*(height_base + height_amp*fbm), s = extent/256 */
+    float    height_amp;
+    float    albedo_lo, albedo_hi;   /* per-voxel RGB uniform range, quantised to 4 bit */
+    float    cave_threshold;  /* carve where 3D value noise > threshold; 0 disables */
+    uint32_t emitters;        /* number of emitter voxels */
+    uint32_t emitter_mode;    /* VXR_EMIT_* */
+    float    radiance_lo, radiance_hi;   /* emitter RGB uniform range */
+    uint32_t blob_count;      /* VXR_EMIT_BLOBS */
+    float    blob_sigma;
+    float    blob_fraction;
+    uint32_t layer_lo, layer_hi;         /* VXR_EMIT_LAYER */
+    float    scatter_fraction;
+} vxr_scene_desc;
+
+/* Fill desc with the preset of benchmark configuration `config` (0..4). */
+int vxr_scene_preset(int config, vxr_scene_desc* desc);
+/* Clear the world and generate the scene; ends with OptimizeBricks and a light scan. */
+int vxr_scene_generate(vxr_world* w, const vxr_scene_desc* desc);
+/* Terrain height (first empty y) of the generated heightfield at column (x, z). */
+int vxr_scene_height(const vxr_scene_desc* desc, uint32_t x, uint32_t z, uint32_t* height);
+/* Seeded Catmull-Rom camera path through 8 control points above the terrain:
+ * position and look-at target for frame f of n_frames. */
+int vxr_camera_path(const vxr_scene_desc* desc, uint32_t path_seed, uint32_t f, uint32_t n_frames,
+                    float pos[3], float target[3]);
+/* 64-bit FNV-1a checksum of the world's canonical content (voxel values by map
+ * position, independent of brick numbering) and of its light list. */
+int vxr_world_checksum(const vxr_world* w, uint64_t* voxels, uint64_t* lights);
+
+/* ---- GPU copy of a world --------------------------------------------------------- */
+/* World::ForceSyncAllBricks + the updateUberGrid kernel + SetupLightBuffer's device copy
+ * (world.cpp:639-651, kernels.cl:498-513, world.cpp:563-612): upload the grid, the
+ * bricks and the light list to the current CUDA device, build the 32^3 uber grid and
+ * the per-light table there. Re-upload after edits; views pick up the new copy at their
+ * next frame. Synchronous. */
+int vxr_world_upload(vxr_world* w);
+/* Device bytes held by the world's GPU copy. */
+int vxr_world_device_bytes(const vxr_world* w, uint64_t* bytes);
+
+/* ---- views: one camera on one world (World::Render / Commit path) ------------------ */
+typedef struct vxr_view vxr_view;
+
+typedef struct vxr_view_desc {
+    uint32_t width, height;                /* SCRWIDTH, SCRHEIGHT */
+    uint32_t light_model;                  /* VXR_LIGHTS_AREA or VXR_LIGHTS_POINT */
+    uint32_t num_candidates;               /* NUMBEROFCANDIDATES, default 32 */
+    uint32_t spatial_taps;                 /* SPATIALTAPS, default 5 */
+    uint32_t spatial_radius;               /* SPATIALRADIUS, default 30 */
+    uint32_t temporal_max_importance;      /* TEMPORALMAXIMPORTANCE, default 20 */
+    int32_t  spatial, temporal, accumulate;/* RenderParams toggles (defaults 1, 1, 0) */
+    uint32_t rng_seed;                     /* host RandomUInt seed for R0, default 0x12345678 */
+    uint32_t tile_x, tile_y;               /* threads per block; 0 = library default */
+} vxr_view_desc;
+
+int vxr_view_default_desc(vxr_view_desc* d);
+/* World::InitReSTIR + SetupReservoirBuffers (world.cpp:195-226): allocate the view's
+ * G-buffers, reservoirs and frame buffers on the current device, own CUDA stream. */
+int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out);
+int vxr_view_destroy(vxr_view* v);
+/* LookAt (template.cpp:204-207) -> World::SetCameraMatrix(mat4::LookAt(pos, target)). */
+int vxr_view_lookat(vxr_view* v, const float pos[3], const float target[3]);
+/* World::SetCameraMatrix with an explicit row-major 4x4 camera-to-world matrix. */
+int vxr_view_set_camera_matrix(vxr_view* v, const float m[16]);
+/* Change the toggles/knobs of an existing view (RenderParams console knobs,
+ * mygame.cpp:112-121); resolution and light model are fixed at creation. */
+int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d);
+
+/* Host part of World::Render (world.cpp:2144-2223): frame constants from the camera,
+ * R0, G-buffer swap. Writes the constants to *k when k is not NULL. */
+int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* k);
+/* Replace the constants of the frame in progress (stage-isolated testing). */
+int vxr_view_set_frame_consts(vxr_view* v, const vxr_frame_consts* k);
+/* Launch one stage asynchronously on the view's stream:
+ * VXR_STAGE_ALBEDO renderAlbedo, VXR_STAGE_CANDIDATES perPixelInitialSampling,
+ * VXR_STAGE_SPATIAL perPixelSpatialResampling, VXR_STAGE_SHADE renderRIS,
+ * VXR_STAGE_ACCUMULATE accumulatorFinalizer (world.cpp:2263-2307). */
+#define VXR_STAGE_ALBEDO      1
+#define VXR_STAGE_CANDIDATES  2
+#define VXR_STAGE_SPATIAL     3
+#define VXR_STAGE_SHADE       4
+#define VXR_STAGE_ACCUMULATE  5
+int vxr_view_stage(vxr_view* v, int stage);
+/* Frame counters (world.cpp:2335-2337). */
+int vxr_view_end_frame(vxr_view* v);
+/* World::Render: begin_frame, the five stages (shading and accumulation fused in one
+ * kernel), end_frame. Asynchronous. */
+int vxr_view_render(vxr_view* v);
+/* World::Commit's wait (world.cpp:2432-2438): block until the view's work is done,
+ * read the stage timings, and report device-side errors as VXR_E_DEVICE. */
+int vxr_view_wait(vxr_view* v);
+/* Per-stage GPU milliseconds of the last waited frame: albedo, candidates+temporal,
+ * spatial, shading, accumulate (GetAlbedoTime ... GetShadingTime, world.h:215-220).
+ * A fused shading+accumulate frame reports accumulate as 0. */
+int vxr_view_stage_times(vxr_view* v, float ms[5]);
+
+/* Readback / injection in the canonical record formats. which: 0 = current G-buffer,
+ * 1 = previous. role: 0 = candidate-stage reservoirs, 1 = spatial-stage reservoirs
+ * (after shading's discard write-back, i.e. the next frame's temporal history). */
+int vxr_view_read_gbuffer(vxr_view* v, int which, vxr_gbuffer_rec* out);
+int vxr_view_write_gbuffer(vxr_view* v, int which, const vxr_gbuffer_rec* in);
+int vxr_view_read_reservoirs(vxr_view* v, int role, vxr_reservoir_rec* out);
+int vxr_view_write_reservoirs(vxr_view* v, int role, const vxr_reservoir_rec* in);
+/* Shaded frame (rgb, primary-hit distance) and accumulator (rgb, 1): float4 per pixel. */
+int vxr_view_read_frame(vxr_view* v, float* rgba);
+int vxr_view_read_accum(vxr_view* v, float* rgba);
+/* End-to-end frame through host memory: LookAt(pos, target), render, copy the
+ * accumulated image into host_rgba (W*H float4; page-locked memory is fastest), wait. */
+int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VXR_H */

@@ -1,0 +1,249 @@
+"""ctypes binding of the CPU oracles (test infrastructure only: imported by tests/,
+__graft_entry__.smoke() and bench.py's CPU baseline, never by the product)."""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+GBUF_DTYPE = np.dtype([("voxel", "<u4"), ("dist", "<f4"), ("side", "<u4"), ("seed", "<u4")])
+RES_DTYPE = np.dtype([("sumOfWeights", "<f4"), ("streamLength", "<u4"), ("lightIndex", "<u4"),
+                      ("adjustedWeight", "<f4"), ("positionOnVoxel", "<f4", (3,)),
+                      ("invPositionProbability", "<f4"), ("Nlight", "<f4", (3,)), ("pHat", "<f4")])
+LIGHT_DTYPE = np.dtype([("position", "<u4"), ("voxel", "<u4"), ("size", "<u4")])
+
+
+class FrameConsts(C.Structure):
+    _fields_ = [("E", C.c_float * 3), ("p0", C.c_float * 3), ("p1", C.c_float * 3), ("p2", C.c_float * 3),
+                ("oneOverRes", C.c_float * 2), ("R0", C.c_uint32), ("frame", C.c_uint32),
+                ("framecount", C.c_uint32), ("restirtemporalframe", C.c_uint32),
+                ("Nleft", C.c_float * 4), ("Nright", C.c_float * 4), ("Ntop", C.c_float * 4),
+                ("Nbottom", C.c_float * 4), ("accumulate", C.c_int32), ("spatial", C.c_int32),
+                ("temporal", C.c_int32), ("numberOfLights", C.c_uint32), ("numberOfCandidates", C.c_uint32),
+                ("numberOfMaxTemporalImportance", C.c_uint32), ("spatialRadius", C.c_uint32),
+                ("spatialTaps", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("M", C.c_float * 16), ("E", C.c_float * 3), ("p0", C.c_float * 3), ("p1", C.c_float * 3),
+                ("p2", C.c_float * 3), ("first", C.c_int), ("rng", C.c_uint32), ("frame", C.c_uint32),
+                ("framecount", C.c_uint32), ("restirtemporalframe", C.c_uint32)]
+
+
+def copy_consts(src, dst_cls):
+    """Field-wise copy between FrameConsts classes of different modules (same layout)."""
+    d = dst_cls()
+    C.memmove(C.byref(d), C.byref(src), C.sizeof(d))
+    return d
+
+
+_P = C.c_void_p
+_U32P = C.POINTER(C.c_uint32)
+_F = C.POINTER(C.c_float)
+
+_port = None
+_ref = None
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def load_port():
+    global _port
+    if _port is not None:
+        return _port
+    from . import build as B  # noqa: PLC0415
+    lib = C.CDLL(B.build_port())
+    sig = {
+        "orc_build_uber": (None, [_P, _P]),
+        "orc_world_get": (C.c_uint32, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32]),
+        "orc_scan_lights": (C.c_uint32, [_P, _P, _P, C.c_uint32]),
+        "orc_store_create": (_P, []), "orc_store_destroy": (None, [_P]),
+        "orc_store_set": (None, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
+        "orc_store_get": (C.c_uint32, [_P, C.c_uint32, C.c_uint32, C.c_uint32]),
+        "orc_store_optimize": (C.c_uint32, [_P]), "orc_store_lights": (C.c_uint32, [_P, _P, C.c_uint32]),
+        "orc_store_grid": (_U32P, [_P]), "orc_store_bricks": (_U32P, [_P]),
+        "orc_camera_init": (None, [C.POINTER(Camera), C.c_uint32]),
+        "orc_lookat": (None, [C.POINTER(Camera), _F, _F]),
+        "orc_begin_frame": (None, [C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(FrameConsts)]),
+        "orc_end_frame": (None, [C.POINTER(Camera)]),
+        "orc_create": (_P, [C.c_int, C.c_int, C.c_int]), "orc_destroy": (None, [_P]),
+        "orc_set_world": (None, [_P, _P, _P, _P]), "orc_set_lights": (None, [_P, _P, C.c_uint32]),
+        "orc_frame_start": (None, [_P]),
+        "orc_stage": (None, [_P, C.POINTER(FrameConsts), C.c_int, C.c_int, C.c_int]),
+        "orc_read_gbuffer": (None, [_P, C.c_int, _P]),
+        "orc_write_gbuffer": (None, [_P, C.c_int, _P, C.POINTER(FrameConsts)]),
+        "orc_read_reservoirs": (None, [_P, C.c_int, _P]), "orc_write_reservoirs": (None, [_P, C.c_int, _P]),
+        "orc_read_image": (None, [_P, C.c_int, _P]),
+        "orc_trace": (C.c_uint32, [_P, C.c_int, _F, _F, C.c_int, C.c_uint32, C.c_uint32, _F, _U32P]),
+        "orc_sincos": (None, [C.c_float, _F, _F]),
+    }
+    for n, (res, args) in sig.items():
+        f = getattr(lib, n)
+        f.restype = res
+        f.argtypes = args
+    _port = lib
+    return lib
+
+
+def load_ref():
+    """The reference oracle, or None when it is not available on this machine."""
+    global _ref
+    if _ref is not None:
+        return _ref or None
+    from . import build as B  # noqa: PLC0415
+    try:
+        path = B.build_ref()
+    except RuntimeError:
+        path = None
+    if not path:
+        _ref = False
+        return None
+    lib = C.CDLL(path)
+    for v in ("area", "point"):
+        sig = {
+            f"vxref_create_{v}": (_P, [C.c_int, C.c_int]), f"vxref_destroy_{v}": (None, [_P]),
+            f"vxref_set_world_{v}": (None, [_P, _P, _P, _P]), f"vxref_set_lights_{v}": (None, [_P, _P, C.c_uint32]),
+            f"vxref_update_uber_{v}": (None, [_P, _P]), f"vxref_begin_frame_{v}": (None, [_P]),
+            f"vxref_stage_{v}": (None, [_P, C.POINTER(FrameConsts), C.c_int]),
+            f"vxref_read_gbuffer_{v}": (None, [_P, C.c_int, _P, _P]),
+            f"vxref_read_reservoirs_{v}": (None, [_P, C.c_int, _P]),
+            f"vxref_write_reservoirs_{v}": (None, [_P, C.c_int, _P]),
+            f"vxref_read_image_{v}": (None, [_P, C.c_int, _P]),
+            f"vxref_trace_{v}": (C.c_uint32, [_P, C.c_int, _F, _F, C.c_int, C.c_uint32, C.c_uint32, _F, _U32P]),
+        }
+        for n, (res, args) in sig.items():
+            f = getattr(lib, n)
+            f.restype = res
+            f.argtypes = args
+    _ref = lib
+    return lib
+
+
+class WorldArrays:
+    """grid / uber / bricks / lights kept alive as numpy arrays for the oracles."""
+
+    def __init__(self, grid, bricks, lights):
+        self.grid = _u32(grid)
+        self.bricks = _u32(bricks).reshape(-1)
+        if self.bricks.size == 0:
+            self.bricks = np.zeros(512, np.uint32)
+        self.lights = np.ascontiguousarray(lights, dtype=LIGHT_DTYPE)
+        self.uber = np.zeros(32 ** 3, np.uint8)
+        load_port().orc_build_uber(self.grid.ctypes.data, self.uber.ctypes.data)
+
+
+class Renderer:
+    """Common frame driver over the port ("port") or the reference oracle ("ref")."""
+
+    def __init__(self, kind, world, W, H, point):
+        self.kind, self.W, self.H, self.point, self.world = kind, W, H, point, world
+        self.n = W * H
+        if kind == "port":
+            self.lib = load_port()
+            self.h = self.lib.orc_create(W, H, 1 if point else 0)
+            self.lib.orc_set_world(self.h, world.grid.ctypes.data, world.uber.ctypes.data, world.bricks.ctypes.data)
+            self.lib.orc_set_lights(self.h, world.lights.ctypes.data, len(world.lights))
+        else:
+            self.lib = load_ref()
+            if self.lib is None:
+                raise RuntimeError("reference oracle unavailable")
+            self.v = "point" if point else "area"
+            self.h = self._f("create")(W, H)
+            uber = np.zeros(32 ** 3, np.uint8)
+            self._f("update_uber")(world.grid.ctypes.data, uber.ctypes.data)
+            self.ref_uber = uber
+            self._f("set_world")(self.h, world.grid.ctypes.data, uber.ctypes.data, world.bricks.ctypes.data)
+            self._f("set_lights")(self.h, world.lights.ctypes.data, len(world.lights))
+
+    def _f(self, name):
+        return getattr(self.lib, f"vxref_{name}_{self.v}")
+
+    def close(self):
+        if self.h:
+            (self.lib.orc_destroy if self.kind == "port" else self._f("destroy"))(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def frame_start(self):
+        if self.kind == "port":
+            self.lib.orc_frame_start(self.h)
+        else:
+            self._f("begin_frame")(self.h)
+
+    def stage(self, k, s, y0=0, y1=0):
+        kk = copy_consts(k, FrameConsts)
+        if self.kind == "port":
+            self.lib.orc_stage(self.h, C.byref(kk), s, y0, y1)
+        else:
+            self._f("stage")(self.h, C.byref(kk), s)
+
+    def gbuffer(self, which=0):
+        out = np.zeros(self.n, GBUF_DTYPE)
+        if self.kind == "port":
+            self.lib.orc_read_gbuffer(self.h, which, out.ctypes.data)
+        else:
+            self._f("read_gbuffer")(self.h, which, out.ctypes.data, None)
+        return out
+
+    def reservoirs(self, role):
+        out = np.zeros(self.n, RES_DTYPE)
+        (self.lib.orc_read_reservoirs if self.kind == "port" else self._f("read_reservoirs"))(self.h, role, out.ctypes.data)
+        return out
+
+    def write_reservoirs(self, role, recs):
+        a = np.ascontiguousarray(recs, dtype=RES_DTYPE)
+        (self.lib.orc_write_reservoirs if self.kind == "port" else self._f("write_reservoirs"))(self.h, role, a.ctypes.data)
+
+    def image(self, which):
+        out = np.zeros((self.n, 4), np.float32)
+        (self.lib.orc_read_image if self.kind == "port" else self._f("read_image"))(self.h, which, out.ctypes.data)
+        return out
+
+    def trace(self, mode, O, D, steps=999999, through=0, mask=0):
+        o = (C.c_float * 3)(*O)
+        d = (C.c_float * 3)(*D)
+        dist = C.c_float(0)
+        side = C.c_uint32(0)
+        if self.kind == "port":
+            v = self.lib.orc_trace(self.h, mode, o, d, steps, through, mask, C.byref(dist), C.byref(side))
+        else:
+            v = self._f("trace")(self.h, mode, o, d, steps, through, mask, C.byref(dist), C.byref(side))
+        return v, dist.value, side.value
+
+
+class CameraPath:
+    """The oracle's restatement of the camera / frame-constant host code."""
+
+    def __init__(self, W, H, rng_seed=0x12345678):
+        self.lib = load_port()
+        self.W, self.H = W, H
+        self.cam = Camera()
+        self.lib.orc_camera_init(C.byref(self.cam), rng_seed)
+
+    def lookat(self, pos, target):
+        self.lib.orc_lookat(C.byref(self.cam), (C.c_float * 3)(*pos), (C.c_float * 3)(*target))
+
+    def begin(self, **params):
+        k = FrameConsts()
+        self.lib.orc_begin_frame(C.byref(self.cam), self.W, self.H, C.byref(k))
+        for n, v in params.items():
+            setattr(k, n, v)
+        return k
+
+    def end(self):
+        self.lib.orc_end_frame(C.byref(self.cam))
+
+
+def sincos(a):
+    s, c = C.c_float(), C.c_float()
+    load_port().orc_sincos(a, C.byref(s), C.byref(c))
+    return s.value, c.value

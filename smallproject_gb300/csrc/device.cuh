@@ -1,0 +1,314 @@
+// device.cuh - device-side building blocks of the Voxel ReSTIR render path (sm_103a).
+//
+// Arithmetic contract (shared with the CPU oracle, which checks it bit for bit):
+// every float operation is an IEEE-754 binary32 op with round-to-nearest and no
+// contraction (this translation unit builds with --fmad=false, IEEE div/sqrt),
+// evaluated in the order the reference kernels write them. That makes the DDA hit
+// (voxel, distance bits, side) and every reservoir field reproducible exactly.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vxr {
+namespace dev {
+
+// ---- world as seen by the kernels ----------------------------------------------------
+// Light table: per light two float4, built once per upload by build_light_table:
+//   geom = (cx, cy, cz, size)      centre = coords + 0.5*size      (tools.cl:606-607)
+//   emit = (er, eg, eb, bits(pos)) rgb/15 * strength * 1/pi        (phat.cl:8-12)
+struct World {
+    const uint32_t* __restrict__ grid;    // 128^3 cells, x + z*128 + y*16384
+    const uint8_t* __restrict__ uber;     // 32^3 occupancy, x + z*32 + y*1024
+    const uint32_t* __restrict__ bricks;  // nbricks * 512 voxels
+    const float4* __restrict__ lgeom;
+    const float4* __restrict__ lemit;
+    uint32_t nlights;
+};
+
+// Frame constants (kernel parameter, by value; mirrors RenderParams, common.h:100-118)
+struct Frame {
+    float3 E, p0, dx, dy;        // dx = p1 - p0, dy = p2 - p0 (the kernel's own subtractions)
+    float oorx, oory;
+    float4 Nl, Nr, Nt, Nb;
+    uint32_t R0, framecount, restirtemporalframe;
+    int32_t spatial, temporal, accumulate;
+    uint32_t nlights, ncand;     // ncand = min(numberOfLights, numberOfCandidates) (ris.cl:48)
+    uint32_t maxTemporal, radius, taps;
+    int32_t W, H;
+};
+
+// ---- small float3 helpers (each op one IEEE rounding) ---------------------------------
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 mul(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 mulv(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float comp(float3 v, uint32_t i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+// normalize = v * (1 / sqrt(dot(v, v))): the reference's own definition (precomp.h:283,656)
+__device__ __forceinline__ float3 normalize3(float3 v) {
+    const float inv = 1.0f / sqrtf(dot3(v, v));
+    return mul(v, inv);
+}
+
+// float -> uint, round toward zero, saturating, NaN -> 0 (convert_uint semantics on GPU)
+__device__ __forceinline__ uint32_t f2u(float f) { return __float2uint_rz(f); }
+__device__ __forceinline__ int32_t f2i(float f) { return __float2int_rz(f); }
+
+// ---- RNG (tools.cl:17-19) ------------------------------------------------------------
+__device__ __forceinline__ uint32_t wang_hash(uint32_t s) {
+    s = (s ^ 61u) ^ (s >> 16);
+    s *= 9u;
+    s = s ^ (s >> 4);
+    s *= 0x27d4eb2du;
+    s = s ^ (s >> 15);
+    return s;
+}
+__device__ __forceinline__ uint32_t xs32(uint32_t& s) {
+    s ^= s << 13;
+    s ^= s >> 17;
+    s ^= s << 5;
+    return s;
+}
+__device__ __forceinline__ float rnd(uint32_t& s) { return __uint2float_rn(xs32(s)) * 2.3283064365387e-10f; }
+
+// ---- voxel payload (tools.cl:294-322, common.h:203-211) --------------------------------
+__device__ __forceinline__ float3 to_rgb(uint32_t v) {
+    return f3((float)((v >> 8) & 15u) * (1.0f / 15.0f), (float)((v >> 4) & 15u) * (1.0f / 15.0f),
+              (float)(v & 15u) * (1.0f / 15.0f));
+}
+__device__ __forceinline__ float alphaf(uint32_t v) { return (float)((v & 0xf000u) >> 12) / 15.0f; }
+__device__ __forceinline__ float strength(uint32_t v) { return (float)((v & 0xff0000u) >> 16); }
+__device__ __forceinline__ bool emitter(uint32_t v) { return ((v >> 16) & 255u) > 0; }
+__device__ __forceinline__ uint32_t from_rgba(float3 c, float a, uint32_t m) {
+    return (m << 16) + (f2u(a * 15.0f) << 12) + (f2u(c.x * 15.0f) << 8) + (f2u(c.y * 15.0f) << 4) + f2u(c.z * 15.0f);
+}
+// VoxelNormal (tools.cl:416-421): axis `side`, facing against the ray
+__device__ __forceinline__ float side_sign(uint32_t side, float3 D) { return comp(D, side) > 0.0f ? -1.0f : 1.0f; }
+__device__ __forceinline__ float3 side_normal(uint32_t side, float s) {
+    return f3(side == 0 ? s : 0.0f, side == 1 ? s : 0.0f, side == 2 ? s : 0.0f);
+}
+
+// ---- camera ray (tools.cl:102-127, TAA = PANINI = 0) ------------------------------------
+__device__ __forceinline__ float3 camera_ray(const Frame& k, int x, int y) {
+    const float u = (float)x * k.oorx, v = (float)y * k.oory;
+    const float3 P = f3((k.p0.x + k.dx.x * u) + k.dy.x * v, (k.p0.y + k.dx.y * u) + k.dy.y * v,
+                        (k.p0.z + k.dx.z * u) + k.dy.z * v);
+    return normalize3(sub(P, k.E));
+}
+
+// ---- sin/cos for the spatial tap offsets (spatialSampling.cl:24-27) -----------------
+// OpenCL leaves cos/sin accuracy to the implementation; the oracle fixes this one:
+// Cody-Waite reduction by pi/2 (three-part constant, exact products for |q| <= 4) and
+// Taylor polynomials on [-pi/4, pi/4] in Horner form, every op a separate IEEE
+// rounding. Within 2 ulp of the correctly rounded values on [0, 2pi].
+__device__ __forceinline__ void sincos_vx(float a, float* s, float* c) {
+    const float q = rintf(a * 0.636619772367581343f);
+    const int qi = (int)q;
+    const float r = ((a - q * 1.5703125f) - q * 4.83751296997070312e-4f) - q * 7.54978995489188216e-8f;
+    const float r2 = r * r;
+    const float ps = r + (r * r2) * (-1.0f / 6.0f + r2 * (1.0f / 120.0f + r2 * (-1.0f / 5040.0f + r2 * (1.0f / 362880.0f))));
+    const float pc = 1.0f + r2 * (-0.5f + r2 * (1.0f / 24.0f + r2 * (-1.0f / 720.0f + r2 * (1.0f / 40320.0f + r2 * (-1.0f / 3628800.0f)))));
+    switch (qi & 3) {
+    case 0: *s = ps; *c = pc; break;
+    case 1: *s = pc; *c = -ps; break;
+    case 2: *s = -ps; *c = -pc; break;
+    default: *s = -pc; *c = ps; break;
+    }
+}
+
+// ---- brick-grid DDA ------------------------------------------------------------------
+// Three nested levels: 32^3 uber cells (32 voxels), 128^3 grid cells (8 voxels), 8^3
+// bricks. Same visiting order, step budget and float arithmetic as the reference's
+// TraceRay/TraceOpaqueRay/TraceThrough (trace.cl:121-362): `steps` loses 4 per uber
+// step and 1 per grid step, bricks are free; multi-axis steps when t ties; `side` is
+// the last axis stepped. Levels keep integer coordinates instead of packed bitfields.
+// MODE 0: first non-zero voxel. MODE 1: first opaque voxel (alpha 0xF). MODE 2: first
+// voxel whose masked value differs from `through` (empty space included).
+// dist/side are written only when a voxel is returned (reference behaviour).
+template <int MODE>
+__device__ __forceinline__ bool dda_hit(uint32_t v, uint32_t through, uint32_t mask) {
+    if (MODE == 0) return v != 0u;
+    if (MODE == 1) return ((v & 0xf000u) >> 12) == 15u;
+    return (v & mask) != (through & mask);
+}
+
+template <int MODE>
+__device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float az, float vx, float vy, float vz,
+                                       int steps, uint32_t through, uint32_t mask, float* dist, uint32_t* side) {
+    // FixZeroDeltas (trace.cl:37-43)
+    if (fabsf(vx) < 1e-8f) vx = vx < 0.0f ? -1e-8f : 1e-8f;
+    if (fabsf(vy) < 1e-8f) vy = vy < 0.0f ? -1e-8f : 1e-8f;
+    if (fabsf(vz) < 1e-8f) vz = vz < 0.0f ? -1e-8f : 1e-8f;
+    const float rx = 1.0f / vx, ry = 1.0f / vy, rz = 1.0f / vz;
+    const int sx = vx > 0.0f ? 1 : -1, sy = vy > 0.0f ? 1 : -1, sz = vz > 0.0f ? 1 : -1;
+    const int ox = vx > 0.0f ? 1 : 0, oy = vy > 0.0f ? 1 : 0, oz = vz > 0.0f ? 1 : 0;
+    float to = 0.0f;
+    uint32_t last = 0;
+    if (ax < 0.0f || ay < 0.0f || az < 0.0f || ax > 1024.0f || ay > 1024.0f || az > 1024.0f) {
+        // slab-clip the origin against the map (trace.cl:139-153)
+        const float tx1 = -ax * rx, tx2 = (1024.0f - ax) * rx;
+        float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
+        const float ty1 = -ay * ry, ty2 = (1024.0f - ay) * ry;
+        tmin = fmaxf(tmin, fminf(ty1, ty2));
+        tmax = fminf(tmax, fmaxf(ty1, ty2));
+        const float tz1 = -az * rz, tz2 = (1024.0f - az) * rz;
+        tmin = fmaxf(tmin, fminf(tz1, tz2));
+        tmax = fminf(tmax, fmaxf(tz1, tz2));
+        if (tmax < tmin || tmax <= 0.0f) return 0u;
+        ax = ax + tmin * vx;
+        ay = ay + tmin * vy;
+        az = az + tmin * vz;
+        to = tmin;
+        const float hi = 1024.0f - 1.01f;
+        if (ay < 0.01f || ay > hi) last = 1;
+        if (az < 0.01f || az > hi) last = 2;
+    }
+    int ux = (int)min(f2u(ax) >> 5, 31u), uy = (int)min(f2u(ay) >> 5, 31u), uz = (int)min(f2u(az) >> 5, 31u);
+    float tmx = ((float)(uint32_t)(ux + ox) - ax * 0.03125f) * rx;
+    float tmy = ((float)(uint32_t)(uy + oy) - ay * 0.03125f) * ry;
+    float tmz = ((float)(uint32_t)(uz + oz) - az * 0.03125f) * rz;
+    const float tdx = (float)sx * rx, tdy = (float)sy * ry, tdz = (float)sz * rz;
+    float t = 0.0f;
+    uint32_t o = __ldg(w.uber + ux + uz * 32 + uy * 1024);
+    while (true) {
+        if ((steps -= 4) <= 0) break;
+        if (MODE == 2 ? (o != 0u || through != 0u) : (o != 0u)) {
+            const float ux_m = tmx, uy_m = tmy, uz_m = tmz;
+            t *= 4.0f;
+            const uint32_t qx = f2u(0.125f * ax + vx * t), qy = f2u(0.125f * ay + vy * t), qz = f2u(0.125f * az + vz * t);
+            int gx = (int)min(max(qx, (uint32_t)ux * 4u), (uint32_t)ux * 4u + 3u);
+            int gy = (int)min(max(qy, (uint32_t)uy * 4u), (uint32_t)uy * 4u + 3u);
+            int gz = (int)min(max(qz, (uint32_t)uz * 4u), (uint32_t)uz * 4u + 3u);
+            tmx = ((float)(uint32_t)(gx + ox) - ax * 0.125f) * rx;
+            tmy = ((float)(uint32_t)(gy + oy) - ay * 0.125f) * ry;
+            tmz = ((float)(uint32_t)(gz + oz) - az * 0.125f) * rz;
+            o = __ldg(w.grid + gx + gz * 128 + gy * 16384);
+            while (true) {
+                if (!--steps) break;
+                if ((o & 1u) == 0u) {
+                    const uint32_t v = o >> 1;
+                    if (dda_hit<MODE>(v, through, mask)) {
+                        *dist = t * 8.0f + to;
+                        *side = last;
+                        return v;
+                    }
+                } else {
+                    const float gx_m = tmx, gy_m = tmy, gz_m = tmz;
+                    t *= 8.0f;
+                    const uint32_t px = f2u(ax + vx * t), py = f2u(ay + vy * t), pz = f2u(az + vz * t);
+                    const uint32_t bx0 = (uint32_t)gx * 8u, by0 = (uint32_t)gy * 8u, bz0 = (uint32_t)gz * 8u;
+                    const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u),
+                                   cz = min(max(pz, bz0), bz0 + 7u);
+                    tmx = ((float)(cx + (uint32_t)ox) - ax) * rx;
+                    tmy = ((float)(cy + (uint32_t)oy) - ay) * ry;
+                    tmz = ((float)(cz + (uint32_t)oz) - az) * rz;
+                    int lx = (int)(cx & 7u), ly = (int)(cy & 7u), lz = (int)(cz & 7u);
+                    const uint32_t* br = w.bricks + (size_t)(o >> 1) * 512u;
+#pragma unroll 1
+                    for (int i = 0; i < 24; i++) {
+                        const uint32_t v = __ldg(br + lx + ly * 8 + lz * 64);
+                        if (dda_hit<MODE>(v, through, mask)) {
+                            *dist = t + to;
+                            *side = last;
+                            return v;
+                        }
+                        t = fminf(tmx, fminf(tmy, tmz));
+                        last = 0;
+                        if (t == tmx) { tmx += tdx; lx += sx; }
+                        if (t == tmy) { tmy += tdy; ly += sy; last = 1; }
+                        if (t == tmz) { tmz += tdz; lz += sz; last = 2; }
+                        if ((lx | ly | lz) & ~7) break;
+                    }
+                    tmx = gx_m; tmy = gy_m; tmz = gz_m;
+                }
+                t = fminf(tmx, fminf(tmy, tmz));
+                last = 0;
+                if (t == tmx) { tmx += tdx; gx += sx; }
+                if (t == tmy) { tmy += tdy; gy += sy; last = 1; }
+                if (t == tmz) { tmz += tdz; gz += sz; last = 2; }
+                if (((gx >> 2) != ux) | ((gy >> 2) != uy) | ((gz >> 2) != uz)) break;
+                o = __ldg(w.grid + gx + gz * 128 + gy * 16384);
+            }
+            tmx = ux_m; tmy = uy_m; tmz = uz_m;
+        }
+        t = fminf(tmx, fminf(tmy, tmz));
+        last = 0;
+        if (t == tmx) { tmx += tdx; ux += sx; }
+        if (t == tmy) { tmy += tdy; uy += sy; last = 1; }
+        if (t == tmz) { tmz += tdz; uz += sz; last = 2; }
+        if ((ux | uy | uz) & ~31) break;
+        o = __ldg(w.uber + ux + uz * 32 + uy * 1024);
+    }
+    return 0u;
+}
+
+// ---- reservoirs --------------------------------------------------------------------
+// In HBM a reservoir is 32 bytes in two SoA planes:
+//   a = (lightIndex, M | nlight << 29, bits(sumOfWeights), bits(pHat))
+//   b = (positionOnVoxel.xyz, invPositionProbability)
+// nlight: 0..5 = Nlight is one of the six face normals (+x,+y,+z,-x,-y,-z, the order of
+// tools.cl:502-510); 6 = zero vector. W is not stored: every producer ends with
+// AdjustWeight(res, res.pHat) or zeroes both W and sumOfWeights, so
+// W = sumOfWeights / max(1e-5, pHat * M) reproduces the stored value exactly.
+struct Res {
+    float sumW;
+    uint32_t M;
+    uint32_t idx;
+    float pHat;
+    float3 pos;
+    float inv;
+    uint32_t ncode;
+};
+__device__ __forceinline__ float res_W(const Res& r) { return r.sumW / fmaxf(1e-5f, r.pHat * (float)r.M); }
+__device__ __forceinline__ Res res_load(const uint4* __restrict__ a, const float4* __restrict__ b, size_t i) {
+    const uint4 qa = __ldg(a + i);
+    const float4 qb = __ldg(b + i);
+    Res r;
+    r.idx = qa.x;
+    r.M = qa.y & 0x1FFFFFFFu;
+    r.ncode = qa.y >> 29;
+    r.sumW = __uint_as_float(qa.z);
+    r.pHat = __uint_as_float(qa.w);
+    r.pos = f3(qb.x, qb.y, qb.z);
+    r.inv = qb.w;
+    return r;
+}
+__device__ __forceinline__ void res_store(uint4* a, float4* b, size_t i, const Res& r) {
+    a[i] = make_uint4(r.idx, (r.M & 0x1FFFFFFFu) | (r.ncode << 29), __float_as_uint(r.sumW), __float_as_uint(r.pHat));
+    b[i] = make_float4(r.pos.x, r.pos.y, r.pos.z, r.inv);
+}
+__device__ __forceinline__ Res res_zero() {
+    Res r;
+    r.sumW = 0.0f; r.M = 0; r.idx = 0; r.pHat = 0.0f; r.pos = f3(0.0f, 0.0f, 0.0f); r.inv = 0.0f; r.ncode = 6;
+    return r;
+}
+
+// UpdateReservoir (reservoir.cl:3-15)
+__device__ __forceinline__ void res_update(Res& r, float weight, float pHat, uint32_t idx, float r0, float3 pos,
+                                           float inv, uint32_t ncode) {
+    r.M += 1u;
+    r.sumW = r.sumW + weight;
+    if (r0 < weight / fmaxf(1e-5f, r.sumW)) {
+        r.idx = idx;
+        r.pos = pos;
+        r.inv = inv;
+        r.ncode = ncode;
+        r.pHat = pHat;
+    }
+}
+// ReWeighSumOfWeights (reservoir.cl:22-28) applied to a stored reservoir with weight W
+__device__ __forceinline__ void res_reweigh(Res& r, float W, float newPHat, uint32_t M) {
+    r.sumW = (W * (float)M) * newPHat;
+    r.M = M;
+    r.pHat = newPHat;
+}
+// CombineReservoir (reservoir.cl:30-38)
+__device__ __forceinline__ void res_combine(Res& r, const Res& o, float r0) {
+    const uint32_t m1 = r.M, m2 = o.M;
+    res_update(r, o.sumW, o.pHat, o.idx, r0, o.pos, o.inv, o.ncode);
+    r.M = m1 + m2;
+}
+
+}  // namespace dev
+}  // namespace vxr

@@ -1,0 +1,553 @@
+// runtime.cu - device world copies, views (one camera on one world) and the render
+// orchestration behind the C ABI: the GB300 counterpart of World::Render/Commit
+// (template/world.cpp:2127-2483) on one CUDA stream per view.
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "camera.hpp"
+#include "internal.hpp"
+#include "kernels.hpp"
+#include "world.hpp"
+
+namespace vxr {
+
+struct DeviceWorld {
+    uint32_t* grid = nullptr;
+    uint8_t* uber = nullptr;
+    uint32_t* bricks = nullptr;
+    size_t brickBytes = 0;
+    uint4* lraw = nullptr;
+    float4* lgeom = nullptr;
+    float4* lemit = nullptr;
+    uint32_t nl = 0;
+    size_t lcap = 0;
+    uint64_t version = 0, lightVersion = 0;
+    int device = -1;
+};
+
+static int cuda_fail(cudaError_t e, const char* what) {
+    return set_error(VXR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CU(call, what)                                  \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+void release_device_world(World& w) {
+    DeviceWorld* d = w.dev;
+    if (!d) return;
+    cudaFree(d->grid);
+    cudaFree(d->uber);
+    cudaFree(d->bricks);
+    cudaFree(d->lraw);
+    cudaFree(d->lgeom);
+    cudaFree(d->lemit);
+    delete d;
+    w.dev = nullptr;
+}
+
+static int upload(World& w) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(VXR_E_NODEVICE, "no CUDA device visible");
+    // every brick cell must point into the pool
+    for (uint32_t i = 0; i < kGridSize; i++)
+        if ((w.grid[i] & 1u) && (w.grid[i] >> 1) >= w.brickHigh)
+            return set_error(VXR_E_STATE, "vxr_world_upload: grid cell references a brick outside the pool");
+    if (!w.dev) w.dev = new DeviceWorld();
+    DeviceWorld& d = *w.dev;
+    int dev = 0;
+    CU(cudaGetDevice(&dev), "cudaGetDevice");
+    d.device = dev;
+    if (!d.grid) CU(cudaMalloc(&d.grid, kGridSize * sizeof(uint32_t)), "cudaMalloc(grid)");
+    if (!d.uber) CU(cudaMalloc(&d.uber, 32 * 32 * 32), "cudaMalloc(uber)");
+    const size_t bb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * kBrick * sizeof(uint32_t);
+    if (bb > d.brickBytes) {
+        cudaFree(d.bricks);
+        d.bricks = nullptr;
+        CU(cudaMalloc(&d.bricks, bb), "cudaMalloc(bricks)");
+        d.brickBytes = bb;
+    }
+    CU(cudaMemcpy(d.grid, w.grid.data(), kGridSize * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload grid");
+    if (w.brickHigh)
+        CU(cudaMemcpy(d.bricks, w.bricks.data(), (size_t)w.brickHigh * kBrick * sizeof(uint32_t), cudaMemcpyHostToDevice),
+           "upload bricks");
+    const uint32_t nl = (uint32_t)w.lights.size();
+    const size_t need = std::max<uint32_t>(nl, 1u);
+    if (need > d.lcap) {
+        cudaFree(d.lraw);
+        cudaFree(d.lgeom);
+        cudaFree(d.lemit);
+        d.lraw = nullptr; d.lgeom = nullptr; d.lemit = nullptr;
+        CU(cudaMalloc(&d.lraw, need * sizeof(uint4)), "cudaMalloc(lights)");
+        CU(cudaMalloc(&d.lgeom, need * sizeof(float4)), "cudaMalloc(light geom)");
+        CU(cudaMalloc(&d.lemit, need * sizeof(float4)), "cudaMalloc(light emit)");
+        d.lcap = need;
+    }
+    std::vector<uint4> raw(need, make_uint4(0, 0, 1, 0));
+    for (uint32_t i = 0; i < nl; i++) raw[i] = make_uint4(w.lights[i].position, w.lights[i].voxel, w.lights[i].size, 0);
+    CU(cudaMemcpy(d.lraw, raw.data(), need * sizeof(uint4), cudaMemcpyHostToDevice), "upload lights");
+    launch_build_light_table(d.lraw, (uint32_t)need, d.lgeom, d.lemit, 0);
+    launch_build_uber(d.grid, d.uber, 0);
+    CU(cudaGetLastError(), "world kernels launch");
+    CU(cudaDeviceSynchronize(), "world kernels");
+    d.nl = nl;
+    d.version = w.version;
+    d.lightVersion = w.lightVersion;
+    return VXR_OK;
+}
+
+}  // namespace vxr
+
+// ---------------------------------------------------------------------------------------
+struct vxr_view {
+    vxr_world* world = nullptr;
+    vxr_view_desc desc{};
+    vxr::CameraState cam;
+    vxr::ViewBuffers buf;
+    int cur = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t evs[6] = {}, eve[6] = {};
+    bool ran[6] = {};
+    bool frameOpen = false;
+    vxr_frame_consts k{};
+    uint64_t seenLightVersion = 0;
+    float times[5] = {};
+    size_t npx = 0;
+};
+
+using vxr::set_error;
+
+namespace {
+
+int check_view(vxr_view* v, const char* fn) {
+    if (!v) return set_error(VXR_E_INVALID, std::string(fn) + ": null view");
+    return VXR_OK;
+}
+
+vxr::dev::World dev_world(vxr_view* v) {
+    const vxr::DeviceWorld& d = *v->world->w.dev;
+    vxr::dev::World w;
+    w.grid = d.grid;
+    w.uber = d.uber;
+    w.bricks = d.bricks;
+    w.lgeom = d.lgeom;
+    w.lemit = d.lemit;
+    w.nlights = d.nl;
+    return w;
+}
+
+vxr::dev::Frame dev_frame(const vxr_frame_consts& c) {
+    vxr::dev::Frame k;
+    k.E = make_float3(c.E[0], c.E[1], c.E[2]);
+    k.p0 = make_float3(c.p0[0], c.p0[1], c.p0[2]);
+    k.dx = make_float3(c.p1[0] - c.p0[0], c.p1[1] - c.p0[1], c.p1[2] - c.p0[2]);
+    k.dy = make_float3(c.p2[0] - c.p0[0], c.p2[1] - c.p0[1], c.p2[2] - c.p0[2]);
+    k.oorx = c.oneOverRes[0];
+    k.oory = c.oneOverRes[1];
+    k.Nl = make_float4(c.Nleft[0], c.Nleft[1], c.Nleft[2], c.Nleft[3]);
+    k.Nr = make_float4(c.Nright[0], c.Nright[1], c.Nright[2], c.Nright[3]);
+    k.Nt = make_float4(c.Ntop[0], c.Ntop[1], c.Ntop[2], c.Ntop[3]);
+    k.Nb = make_float4(c.Nbottom[0], c.Nbottom[1], c.Nbottom[2], c.Nbottom[3]);
+    k.R0 = c.R0;
+    k.framecount = c.framecount;
+    k.restirtemporalframe = c.restirtemporalframe;
+    k.spatial = c.spatial;
+    k.temporal = c.temporal;
+    k.accumulate = c.accumulate;
+    k.nlights = c.numberOfLights;
+    k.ncand = c.numberOfLights < c.numberOfCandidates ? c.numberOfLights : c.numberOfCandidates;
+    k.maxTemporal = c.numberOfMaxTemporalImportance;
+    k.radius = c.spatialRadius;
+    k.taps = c.spatialTaps;
+    k.W = (int32_t)c.width;
+    k.H = (int32_t)c.height;
+    return k;
+}
+
+int ensure_world(vxr_view* v) {
+    vxr::World& w = v->world->w;
+    if (!w.dev || w.dev->version != w.version) {
+        const int r = vxr::upload(w);
+        if (r != VXR_OK) return r;
+    }
+    return VXR_OK;
+}
+
+void free_view(vxr_view* v) {
+    vxr::ViewBuffers& b = v->buf;
+    cudaFree(b.vd[0]); cudaFree(b.vd[1]); cudaFree(b.seed);
+    cudaFree(b.cA); cudaFree(b.cB); cudaFree(b.hA); cudaFree(b.hB);
+    cudaFree(b.frame); cudaFree(b.accum); cudaFree(b.err);
+    for (int i = 0; i < 6; i++) {
+        if (v->evs[i]) cudaEventDestroy(v->evs[i]);
+        if (v->eve[i]) cudaEventDestroy(v->eve[i]);
+    }
+    if (v->stream) cudaStreamDestroy(v->stream);
+}
+
+vxr::LaunchShape shape(const vxr_view* v) {
+    vxr::LaunchShape s;
+    if (v->desc.tile_x) s.bx = (int)v->desc.tile_x;
+    if (v->desc.tile_y) s.by = (int)v->desc.tile_y;
+    return s;
+}
+
+}  // namespace
+
+#define CUV(call, what)                                                                   \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) return set_error(VXR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" {
+
+int vxr_world_upload(vxr_world* w) {
+    VXR_CHECK_ARG(w, "vxr_world_upload: null world");
+    return vxr::upload(w->w);
+}
+
+int vxr_world_device_bytes(const vxr_world* w, uint64_t* bytes) {
+    VXR_CHECK_ARG(w && bytes, "vxr_world_device_bytes: null argument");
+    const vxr::DeviceWorld* d = w->w.dev;
+    *bytes = d ? (uint64_t)(vxr::kGridSize * 4 + 32768 + d->brickBytes + d->lcap * 48) : 0;
+    return VXR_OK;
+}
+
+int vxr_view_default_desc(vxr_view_desc* d) {
+    VXR_CHECK_ARG(d, "vxr_view_default_desc: null desc");
+    std::memset(d, 0, sizeof(*d));
+    d->width = 1600;   // common.h:2-3
+    d->height = 1024;
+    d->light_model = VXR_LIGHTS_AREA;
+    d->num_candidates = 32;
+    d->spatial_taps = 5;
+    d->spatial_radius = 30;
+    d->temporal_max_importance = 20;
+    d->spatial = 1;
+    d->temporal = 1;
+    d->accumulate = 0;
+    d->rng_seed = 0x12345678u;
+    return VXR_OK;
+}
+
+int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
+    VXR_CHECK_ARG(w && d && out, "vxr_view_create: null argument");
+    VXR_CHECK_ARG(d->width >= 1 && d->height >= 1 && d->width <= 16384 && d->height <= 16384,
+                  "vxr_view_create: resolution out of range [1, 16384]");
+    VXR_CHECK_ARG(d->light_model == VXR_LIGHTS_AREA || d->light_model == VXR_LIGHTS_POINT,
+                  "vxr_view_create: unknown light model");
+    VXR_CHECK_ARG(d->spatial_radius >= 1, "vxr_view_create: spatial_radius must be >= 1");
+    VXR_CHECK_ARG(d->tile_x * d->tile_y <= 1024, "vxr_view_create: tile larger than 1024 threads");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(VXR_E_NODEVICE, "no CUDA device visible");
+    vxr_view* v = new (std::nothrow) vxr_view();
+    if (!v) return set_error(VXR_E_NOMEM, "vxr_view_create: out of host memory");
+    v->world = w;
+    v->desc = *d;
+    v->cam.rng = d->rng_seed;
+    v->npx = (size_t)d->width * d->height;
+    const size_t n = v->npx;
+    vxr::ViewBuffers& b = v->buf;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
+    };
+    alloc((void**)&b.vd[0], n * sizeof(uint2));
+    alloc((void**)&b.vd[1], n * sizeof(uint2));
+    alloc((void**)&b.seed, n * sizeof(uint32_t));
+    alloc((void**)&b.cA, n * sizeof(uint4));
+    alloc((void**)&b.cB, n * sizeof(float4));
+    alloc((void**)&b.hA, n * sizeof(uint4));
+    alloc((void**)&b.hB, n * sizeof(float4));
+    alloc((void**)&b.frame, n * sizeof(float4));
+    alloc((void**)&b.accum, n * sizeof(float4));
+    alloc((void**)&b.err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 6 && e == cudaSuccess; i++) {
+        e = cudaEventCreate(&v->evs[i]);
+        if (e == cudaSuccess) e = cudaEventCreate(&v->eve[i]);
+    }
+    if (e != cudaSuccess) {
+        free_view(v);
+        delete v;
+        return set_error(e == cudaErrorMemoryAllocation ? VXR_E_NOMEM : VXR_E_CUDA,
+                         std::string("vxr_view_create: ") + cudaGetErrorString(e));
+    }
+    const int r = ensure_world(v);
+    if (r != VXR_OK) {
+        free_view(v);
+        delete v;
+        return r;
+    }
+    v->seenLightVersion = w->w.lightVersion;
+    *out = v;
+    return VXR_OK;
+}
+
+int vxr_view_destroy(vxr_view* v) {
+    if (!v) return VXR_OK;
+    cudaStreamSynchronize(v->stream);
+    free_view(v);
+    delete v;
+    return VXR_OK;
+}
+
+int vxr_view_lookat(vxr_view* v, const float pos[3], const float target[3]) {
+    if (int r = check_view(v, "vxr_view_lookat")) return r;
+    VXR_CHECK_ARG(pos && target, "vxr_view_lookat: null argument");
+    v->cam.M = vxr::look_at(pos, target);
+    return VXR_OK;
+}
+
+int vxr_view_set_camera_matrix(vxr_view* v, const float m[16]) {
+    if (int r = check_view(v, "vxr_view_set_camera_matrix")) return r;
+    VXR_CHECK_ARG(m, "vxr_view_set_camera_matrix: null matrix");
+    std::memcpy(v->cam.M.cell, m, sizeof(float) * 16);
+    return VXR_OK;
+}
+
+int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d) {
+    if (int r = check_view(v, "vxr_view_set_params")) return r;
+    VXR_CHECK_ARG(d, "vxr_view_set_params: null desc");
+    VXR_CHECK_ARG(d->width == v->desc.width && d->height == v->desc.height && d->light_model == v->desc.light_model,
+                  "vxr_view_set_params: resolution and light model are fixed at creation");
+    VXR_CHECK_ARG(d->spatial_radius >= 1, "vxr_view_set_params: spatial_radius must be >= 1");
+    VXR_CHECK_ARG(d->tile_x * d->tile_y <= 1024, "vxr_view_set_params: tile larger than 1024 threads");
+    const uint32_t seed = v->desc.rng_seed;
+    v->desc = *d;
+    v->desc.rng_seed = seed;
+    return VXR_OK;
+}
+
+int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* out) {
+    if (int r = check_view(v, "vxr_view_begin_frame")) return r;
+    if (int r = ensure_world(v)) return r;
+    vxr::World& w = v->world->w;
+    if (w.lightVersion != v->seenLightVersion) {
+        v->cam.restirtemporalframe = 0;   // any light change resets temporal reuse (world.cpp:245)
+        v->seenLightVersion = w.lightVersion;
+    }
+    vxr_frame_consts& k = v->k;
+    std::memset(&k, 0, sizeof(k));
+    vxr::begin_frame(v->cam, v->desc.width, v->desc.height, &k);
+    k.accumulate = v->desc.accumulate;
+    k.spatial = v->desc.spatial;
+    k.temporal = v->desc.temporal;
+    k.numberOfLights = w.dev->nl;
+    k.numberOfCandidates = v->desc.num_candidates;
+    k.numberOfMaxTemporalImportance = v->desc.temporal_max_importance;
+    k.spatialRadius = v->desc.spatial_radius;
+    k.spatialTaps = v->desc.spatial_taps;
+    v->cur ^= 1;   // G-buffer swap (world.cpp:2221-2223)
+    v->frameOpen = true;
+    for (int i = 0; i < 6; i++) v->ran[i] = false;
+    if (out) *out = k;
+    return VXR_OK;
+}
+
+int vxr_view_set_frame_consts(vxr_view* v, const vxr_frame_consts* k) {
+    if (int r = check_view(v, "vxr_view_set_frame_consts")) return r;
+    VXR_CHECK_ARG(k, "vxr_view_set_frame_consts: null consts");
+    VXR_CHECK_ARG(v->frameOpen, "vxr_view_set_frame_consts: no frame in progress");
+    VXR_CHECK_ARG(k->width == v->desc.width && k->height == v->desc.height, "vxr_view_set_frame_consts: resolution mismatch");
+    VXR_CHECK_ARG(k->numberOfLights == v->world->w.dev->nl, "vxr_view_set_frame_consts: light count differs from the uploaded list");
+    VXR_CHECK_ARG(k->spatialRadius >= 1, "vxr_view_set_frame_consts: spatialRadius must be >= 1");
+    v->k = *k;
+    return VXR_OK;
+}
+
+static int run_stage(vxr_view* v, int stage, bool fuse) {
+    if (!v->frameOpen) return set_error(VXR_E_STATE, "vxr_view_stage: call vxr_view_begin_frame first");
+    if (int r = ensure_world(v)) return r;
+    const vxr::dev::World w = dev_world(v);
+    const vxr::dev::Frame k = dev_frame(v->k);
+    const bool point = v->desc.light_model == VXR_LIGHTS_POINT;
+    const vxr::LaunchShape sh = shape(v);
+    CUV(cudaEventRecord(v->evs[stage], v->stream), "cudaEventRecord");
+    switch (stage) {
+    case VXR_STAGE_ALBEDO: vxr::launch_albedo(w, k, v->buf, v->cur, sh, v->stream); break;
+    case VXR_STAGE_CANDIDATES: vxr::launch_candidates(point, w, k, v->buf, v->cur, sh, v->stream); break;
+    case VXR_STAGE_SPATIAL: vxr::launch_spatial(point, w, k, v->buf, v->cur, sh, v->stream); break;
+    case VXR_STAGE_SHADE: vxr::launch_shade(point, w, k, v->buf, v->cur, fuse, sh, v->stream); break;
+    case VXR_STAGE_ACCUMULATE: vxr::launch_accumulate(k, v->buf, sh, v->stream); break;
+    default: return set_error(VXR_E_INVALID, "vxr_view_stage: unknown stage");
+    }
+    CUV(cudaGetLastError(), "kernel launch");
+    CUV(cudaEventRecord(v->eve[stage], v->stream), "cudaEventRecord");
+    v->ran[stage] = true;
+    return VXR_OK;
+}
+
+int vxr_view_stage(vxr_view* v, int stage) {
+    if (int r = check_view(v, "vxr_view_stage")) return r;
+    return run_stage(v, stage, false);
+}
+
+int vxr_view_end_frame(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_end_frame")) return r;
+    if (!v->frameOpen) return set_error(VXR_E_STATE, "vxr_view_end_frame: no frame in progress");
+    vxr::end_frame(v->cam);
+    v->frameOpen = false;
+    return VXR_OK;
+}
+
+int vxr_view_render(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_render")) return r;
+    if (int r = vxr_view_begin_frame(v, nullptr)) return r;
+    if (int r = run_stage(v, VXR_STAGE_ALBEDO, false)) return r;
+    if (int r = run_stage(v, VXR_STAGE_CANDIDATES, false)) return r;
+    if (int r = run_stage(v, VXR_STAGE_SPATIAL, false)) return r;
+    if (int r = run_stage(v, VXR_STAGE_SHADE, true)) return r;
+    return vxr_view_end_frame(v);
+}
+
+int vxr_view_wait(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_wait")) return r;
+    CUV(cudaStreamSynchronize(v->stream), "vxr_view_wait");
+    for (int s = 1; s <= 5; s++) {
+        float ms = 0.0f;
+        if (v->ran[s]) cudaEventElapsedTime(&ms, v->evs[s], v->eve[s]);
+        v->times[s - 1] = ms;
+    }
+    uint32_t err = 0;
+    CUV(cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost), "read device error flags");
+    if (err) {
+        cudaMemset(v->buf.err, 0, sizeof(uint32_t));
+        return set_error(VXR_E_DEVICE, "device error flags 0x" + std::to_string(err) +
+                                           " (2: temporal light index, 4: spatial light index, 8: shading light index)");
+    }
+    return VXR_OK;
+}
+
+int vxr_view_stage_times(vxr_view* v, float ms[5]) {
+    if (int r = check_view(v, "vxr_view_stage_times")) return r;
+    VXR_CHECK_ARG(ms, "vxr_view_stage_times: null output");
+    for (int i = 0; i < 5; i++) ms[i] = v->times[i];
+    return VXR_OK;
+}
+
+int vxr_view_read_gbuffer(vxr_view* v, int which, vxr_gbuffer_rec* out) {
+    if (int r = check_view(v, "vxr_view_read_gbuffer")) return r;
+    VXR_CHECK_ARG(out && (which == 0 || which == 1), "vxr_view_read_gbuffer: bad argument");
+    const size_t n = v->npx;
+    std::vector<uint2> vd(n);
+    std::vector<uint32_t> seed(n);
+    CUV(cudaStreamSynchronize(v->stream), "sync");
+    CUV(cudaMemcpy(vd.data(), v->buf.vd[which == 0 ? v->cur : v->cur ^ 1], n * sizeof(uint2), cudaMemcpyDeviceToHost), "read G-buffer");
+    CUV(cudaMemcpy(seed.data(), v->buf.seed, n * sizeof(uint32_t), cudaMemcpyDeviceToHost), "read seeds");
+    for (size_t i = 0; i < n; i++) {
+        out[i].voxel = vd[i].x & 0x00FFFFFFu;
+        out[i].side = vd[i].x >> 24;
+        std::memcpy(&out[i].dist, &vd[i].y, 4);
+        out[i].seed = seed[i];
+    }
+    return VXR_OK;
+}
+
+int vxr_view_write_gbuffer(vxr_view* v, int which, const vxr_gbuffer_rec* in) {
+    if (int r = check_view(v, "vxr_view_write_gbuffer")) return r;
+    VXR_CHECK_ARG(in && (which == 0 || which == 1), "vxr_view_write_gbuffer: bad argument");
+    const size_t n = v->npx;
+    std::vector<uint2> vd(n);
+    std::vector<uint32_t> seed(n);
+    for (size_t i = 0; i < n; i++) {
+        VXR_CHECK_ARG(in[i].side <= 2 && in[i].voxel <= 0x00FFFFFFu, "vxr_view_write_gbuffer: side > 2 or voxel above 24 bits");
+        uint32_t d;
+        std::memcpy(&d, &in[i].dist, 4);
+        vd[i] = make_uint2(in[i].voxel | (in[i].side << 24), d);
+        seed[i] = in[i].seed;
+    }
+    CUV(cudaStreamSynchronize(v->stream), "sync");
+    CUV(cudaMemcpy(v->buf.vd[which == 0 ? v->cur : v->cur ^ 1], vd.data(), n * sizeof(uint2), cudaMemcpyHostToDevice), "write G-buffer");
+    if (which == 0) CUV(cudaMemcpy(v->buf.seed, seed.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice), "write seeds");
+    return VXR_OK;
+}
+
+static const float kNormals[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+
+int vxr_view_read_reservoirs(vxr_view* v, int role, vxr_reservoir_rec* out) {
+    if (int r = check_view(v, "vxr_view_read_reservoirs")) return r;
+    VXR_CHECK_ARG(out && (role == 0 || role == 1), "vxr_view_read_reservoirs: bad argument");
+    const size_t n = v->npx;
+    std::vector<uint4> a(n);
+    std::vector<float4> b(n);
+    CUV(cudaStreamSynchronize(v->stream), "sync");
+    CUV(cudaMemcpy(a.data(), role == 0 ? v->buf.cA : v->buf.hA, n * sizeof(uint4), cudaMemcpyDeviceToHost), "read reservoirs");
+    CUV(cudaMemcpy(b.data(), role == 0 ? v->buf.cB : v->buf.hB, n * sizeof(float4), cudaMemcpyDeviceToHost), "read reservoirs");
+    for (size_t i = 0; i < n; i++) {
+        vxr_reservoir_rec& r = out[i];
+        std::memcpy(&r.sumOfWeights, &a[i].z, 4);
+        std::memcpy(&r.pHat, &a[i].w, 4);
+        r.streamLength = a[i].y & 0x1FFFFFFFu;
+        r.lightIndex = a[i].x;
+        const float den = std::max(1e-5f, r.pHat * (float)r.streamLength);
+        r.adjustedWeight = r.sumOfWeights / den;
+        r.positionOnVoxel[0] = b[i].x;
+        r.positionOnVoxel[1] = b[i].y;
+        r.positionOnVoxel[2] = b[i].z;
+        r.invPositionProbability = b[i].w;
+        const uint32_t c = a[i].y >> 29;
+        for (int j = 0; j < 3; j++) r.Nlight[j] = c < 6 ? kNormals[c][j] : 0.0f;
+    }
+    return VXR_OK;
+}
+
+int vxr_view_write_reservoirs(vxr_view* v, int role, const vxr_reservoir_rec* in) {
+    if (int r = check_view(v, "vxr_view_write_reservoirs")) return r;
+    VXR_CHECK_ARG(in && (role == 0 || role == 1), "vxr_view_write_reservoirs: bad argument");
+    const size_t n = v->npx;
+    std::vector<uint4> a(n);
+    std::vector<float4> b(n);
+    for (size_t i = 0; i < n; i++) {
+        const vxr_reservoir_rec& r = in[i];
+        uint32_t c = 6;
+        for (uint32_t j = 0; j < 6; j++)
+            if (r.Nlight[0] == kNormals[j][0] && r.Nlight[1] == kNormals[j][1] && r.Nlight[2] == kNormals[j][2]) c = j;
+        VXR_CHECK_ARG(c < 6 || (r.Nlight[0] == 0.0f && r.Nlight[1] == 0.0f && r.Nlight[2] == 0.0f),
+                      "vxr_view_write_reservoirs: Nlight must be a face normal or zero");
+        VXR_CHECK_ARG(r.streamLength < (1u << 29), "vxr_view_write_reservoirs: streamLength >= 2^29");
+        uint32_t sw, ph;
+        std::memcpy(&sw, &r.sumOfWeights, 4);
+        std::memcpy(&ph, &r.pHat, 4);
+        a[i] = make_uint4(r.lightIndex, r.streamLength | (c << 29), sw, ph);
+        b[i] = make_float4(r.positionOnVoxel[0], r.positionOnVoxel[1], r.positionOnVoxel[2], r.invPositionProbability);
+    }
+    CUV(cudaStreamSynchronize(v->stream), "sync");
+    CUV(cudaMemcpy(role == 0 ? v->buf.cA : v->buf.hA, a.data(), n * sizeof(uint4), cudaMemcpyHostToDevice), "write reservoirs");
+    CUV(cudaMemcpy(role == 0 ? v->buf.cB : v->buf.hB, b.data(), n * sizeof(float4), cudaMemcpyHostToDevice), "write reservoirs");
+    return VXR_OK;
+}
+
+int vxr_view_read_frame(vxr_view* v, float* rgba) {
+    if (int r = check_view(v, "vxr_view_read_frame")) return r;
+    VXR_CHECK_ARG(rgba, "vxr_view_read_frame: null output");
+    CUV(cudaStreamSynchronize(v->stream), "sync");
+    CUV(cudaMemcpy(rgba, v->buf.frame, v->npx * sizeof(float4), cudaMemcpyDeviceToHost), "read frame");
+    return VXR_OK;
+}
+
+int vxr_view_read_accum(vxr_view* v, float* rgba) {
+    if (int r = check_view(v, "vxr_view_read_accum")) return r;
+    VXR_CHECK_ARG(rgba, "vxr_view_read_accum: null output");
+    CUV(cudaStreamSynchronize(v->stream), "sync");
+    CUV(cudaMemcpy(rgba, v->buf.accum, v->npx * sizeof(float4), cudaMemcpyDeviceToHost), "read accumulator");
+    return VXR_OK;
+}
+
+int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba) {
+    if (int r = check_view(v, "vxr_view_render_to_host")) return r;
+    VXR_CHECK_ARG(pos && target && host_rgba, "vxr_view_render_to_host: null argument");
+    if (int r = vxr_view_lookat(v, pos, target)) return r;
+    if (int r = vxr_view_render(v)) return r;
+    CUV(cudaMemcpyAsync(host_rgba, v->buf.accum, v->npx * sizeof(float4), cudaMemcpyDeviceToHost, v->stream), "copy image");
+    return vxr_view_wait(v);
+}
+
+}  // extern "C"

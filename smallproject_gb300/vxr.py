@@ -1,0 +1,341 @@
+"""ctypes binding of libvxr.so (include/vxr.h).
+
+The Python layer only marshals arguments: every render-path operation runs in the
+C++/CUDA library. Importing this module never falls back to anything else - when
+libvxr.so is missing it raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libvxr.so")
+
+VXR_OK = 0
+VXR_E_INVALID, VXR_E_CUDA, VXR_E_NOMEM, VXR_E_STATE, VXR_E_DEVICE, VXR_E_NODEVICE, VXR_E_IO = -1, -2, -3, -4, -5, -6, -7
+LIGHTS_AREA, LIGHTS_POINT = 0, 1
+STAGE_ALBEDO, STAGE_CANDIDATES, STAGE_SPATIAL, STAGE_SHADE, STAGE_ACCUMULATE = 1, 2, 3, 4, 5
+EMIT_ABOVE_SURFACE, EMIT_AIR, EMIT_BLOBS, EMIT_LAYER = 0, 1, 2, 3
+
+
+class VxrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"vxr error {code}: {msg}")
+        self.code = code
+
+
+class Light(C.Structure):
+    _fields_ = [("position", C.c_uint32), ("voxel", C.c_uint32), ("size", C.c_uint32)]
+
+
+class GBufferRec(C.Structure):
+    _fields_ = [("voxel", C.c_uint32), ("dist", C.c_float), ("side", C.c_uint32), ("seed", C.c_uint32)]
+
+
+class ReservoirRec(C.Structure):
+    _fields_ = [("sumOfWeights", C.c_float), ("streamLength", C.c_uint32), ("lightIndex", C.c_uint32),
+                ("adjustedWeight", C.c_float), ("positionOnVoxel", C.c_float * 3),
+                ("invPositionProbability", C.c_float), ("Nlight", C.c_float * 3), ("pHat", C.c_float)]
+
+
+class FrameConsts(C.Structure):
+    _fields_ = [("E", C.c_float * 3), ("p0", C.c_float * 3), ("p1", C.c_float * 3), ("p2", C.c_float * 3),
+                ("oneOverRes", C.c_float * 2), ("R0", C.c_uint32), ("frame", C.c_uint32),
+                ("framecount", C.c_uint32), ("restirtemporalframe", C.c_uint32),
+                ("Nleft", C.c_float * 4), ("Nright", C.c_float * 4), ("Ntop", C.c_float * 4),
+                ("Nbottom", C.c_float * 4), ("accumulate", C.c_int32), ("spatial", C.c_int32),
+                ("temporal", C.c_int32), ("numberOfLights", C.c_uint32), ("numberOfCandidates", C.c_uint32),
+                ("numberOfMaxTemporalImportance", C.c_uint32), ("spatialRadius", C.c_uint32),
+                ("spatialTaps", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("extent", C.c_uint32), ("seed", C.c_uint32), ("octaves", C.c_uint32), ("base_freq", C.c_float),
+                ("gain", C.c_float), ("height_base", C.c_float), ("height_amp", C.c_float),
+                ("albedo_lo", C.c_float), ("albedo_hi", C.c_float), ("cave_threshold", C.c_float),
+                ("emitters", C.c_uint32), ("emitter_mode", C.c_uint32), ("radiance_lo", C.c_float),
+                ("radiance_hi", C.c_float), ("blob_count", C.c_uint32), ("blob_sigma", C.c_float),
+                ("blob_fraction", C.c_float), ("layer_lo", C.c_uint32), ("layer_hi", C.c_uint32),
+                ("scatter_fraction", C.c_float)]
+
+
+class ViewDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("light_model", C.c_uint32),
+                ("num_candidates", C.c_uint32), ("spatial_taps", C.c_uint32), ("spatial_radius", C.c_uint32),
+                ("temporal_max_importance", C.c_uint32), ("spatial", C.c_int32), ("temporal", C.c_int32),
+                ("accumulate", C.c_int32), ("rng_seed", C.c_uint32), ("tile_x", C.c_uint32), ("tile_y", C.c_uint32)]
+
+
+GBUF_DTYPE = np.dtype([("voxel", "<u4"), ("dist", "<f4"), ("side", "<u4"), ("seed", "<u4")])
+RES_DTYPE = np.dtype([("sumOfWeights", "<f4"), ("streamLength", "<u4"), ("lightIndex", "<u4"),
+                      ("adjustedWeight", "<f4"), ("positionOnVoxel", "<f4", (3,)),
+                      ("invPositionProbability", "<f4"), ("Nlight", "<f4", (3,)), ("pHat", "<f4")])
+LIGHT_DTYPE = np.dtype([("position", "<u4"), ("voxel", "<u4"), ("size", "<u4")])
+assert GBUF_DTYPE.itemsize == C.sizeof(GBufferRec) and RES_DTYPE.itemsize == C.sizeof(ReservoirRec)
+
+_P = C.c_void_p
+_F3 = C.POINTER(C.c_float)
+# name -> argtypes (all functions return int status unless listed in _RESTYPES)
+_SIGS = {
+    "vxr_last_error": [], "vxr_version": [],
+    "vxr_world_create": [C.POINTER(_P)], "vxr_world_destroy": [_P], "vxr_world_clear": [_P],
+    "vxr_world_set": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
+    "vxr_world_get": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)],
+    "vxr_world_box": [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32],
+    "vxr_world_track_lights": [_P, C.c_int], "vxr_world_optimize": [_P, C.POINTER(C.c_uint32)],
+    "vxr_world_scan_lights": [_P, C.POINTER(C.c_uint32)],
+    "vxr_world_set_lights": [_P, C.POINTER(Light), C.c_uint32],
+    "vxr_world_arrays": [_P, C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.POINTER(C.c_uint32)),
+                         C.POINTER(C.c_uint32), C.POINTER(C.POINTER(Light)), C.POINTER(C.c_uint32)],
+    "vxr_world_brick_count": [_P, C.POINTER(C.c_uint32)],
+    "vxr_scene_preset": [C.c_int, C.POINTER(SceneDesc)], "vxr_scene_generate": [_P, C.POINTER(SceneDesc)],
+    "vxr_scene_height": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)],
+    "vxr_camera_path": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.c_uint32, _F3, _F3],
+    "vxr_world_checksum": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
+    "vxr_world_upload": [_P], "vxr_world_device_bytes": [_P, C.POINTER(C.c_uint64)],
+    "vxr_view_default_desc": [C.POINTER(ViewDesc)],
+    "vxr_view_create": [_P, C.POINTER(ViewDesc), C.POINTER(_P)], "vxr_view_destroy": [_P],
+    "vxr_view_lookat": [_P, _F3, _F3], "vxr_view_set_camera_matrix": [_P, _F3],
+    "vxr_view_set_params": [_P, C.POINTER(ViewDesc)],
+    "vxr_view_begin_frame": [_P, C.POINTER(FrameConsts)], "vxr_view_set_frame_consts": [_P, C.POINTER(FrameConsts)],
+    "vxr_view_stage": [_P, C.c_int], "vxr_view_end_frame": [_P], "vxr_view_render": [_P], "vxr_view_wait": [_P],
+    "vxr_view_stage_times": [_P, _F3],
+    "vxr_view_read_gbuffer": [_P, C.c_int, _P], "vxr_view_write_gbuffer": [_P, C.c_int, _P],
+    "vxr_view_read_reservoirs": [_P, C.c_int, _P], "vxr_view_write_reservoirs": [_P, C.c_int, _P],
+    "vxr_view_read_frame": [_P, _F3], "vxr_view_read_accum": [_P, _F3],
+    "vxr_view_render_to_host": [_P, _F3, _F3, _F3],
+}
+_RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
+
+_lib = None
+
+
+def load(path=None):
+    """Load libvxr.so (once). Raises OSError when the library has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"libvxr.so not found at {p}: run __graft_entry__.build() (nvcc, sm_103a) first")
+    lib = C.CDLL(p)
+    for name, args in _SIGS.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = _RESTYPES.get(name, C.c_int)
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def check(code):
+    if code != VXR_OK:
+        raise VxrError(code, load().vxr_last_error().decode())
+    return code
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+class World:
+    """Host voxel store (vxr_world)."""
+
+    def __init__(self):
+        self._lib = load()
+        self.h = _P()
+        check(self._lib.vxr_world_create(C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self._lib.vxr_world_destroy(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, x, y, z, v):
+        check(self._lib.vxr_world_set(self.h, x, y, z, v))
+
+    def get(self, x, y, z):
+        out = C.c_uint32()
+        check(self._lib.vxr_world_get(self.h, x, y, z, C.byref(out)))
+        return out.value
+
+    def box(self, x1, y1, z1, x2, y2, z2, v):
+        check(self._lib.vxr_world_box(self.h, x1, y1, z1, x2, y2, z2, v))
+
+    def track_lights(self, on):
+        check(self._lib.vxr_world_track_lights(self.h, 1 if on else 0))
+
+    def optimize(self):
+        r = C.c_uint32()
+        check(self._lib.vxr_world_optimize(self.h, C.byref(r)))
+        return r.value
+
+    def scan_lights(self):
+        n = C.c_uint32()
+        check(self._lib.vxr_world_scan_lights(self.h, C.byref(n)))
+        return n.value
+
+    def set_lights(self, lights):
+        arr = np.ascontiguousarray(lights, dtype=LIGHT_DTYPE)
+        check(self._lib.vxr_world_set_lights(self.h, arr.ctypes.data_as(C.POINTER(Light)), len(arr)))
+
+    def arrays(self):
+        """Copies of (grid uint32[128^3], bricks uint32[n, 512], lights LIGHT_DTYPE[n])."""
+        g = C.POINTER(C.c_uint32)()
+        b = C.POINTER(C.c_uint32)()
+        nb = C.c_uint32()
+        l = C.POINTER(Light)()
+        nl = C.c_uint32()
+        check(self._lib.vxr_world_arrays(self.h, C.byref(g), C.byref(b), C.byref(nb), C.byref(l), C.byref(nl)))
+        grid = np.ctypeslib.as_array(g, shape=(128 ** 3,)).copy()
+        bricks = (np.ctypeslib.as_array(b, shape=(nb.value * 512,)).copy() if nb.value else
+                  np.zeros(512, np.uint32)).reshape(-1, 512)
+        if nl.value:
+            lights = np.frombuffer(C.string_at(l, nl.value * 12), dtype=LIGHT_DTYPE).copy()
+        else:
+            lights = np.zeros(0, LIGHT_DTYPE)
+        return grid, bricks, lights
+
+    def checksum(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        check(self._lib.vxr_world_checksum(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def generate(self, desc):
+        check(self._lib.vxr_scene_generate(self.h, C.byref(desc)))
+
+    def upload(self):
+        check(self._lib.vxr_world_upload(self.h))
+
+    def device_bytes(self):
+        b = C.c_uint64()
+        check(self._lib.vxr_world_device_bytes(self.h, C.byref(b)))
+        return b.value
+
+
+def scene_preset(config, **overrides):
+    d = SceneDesc()
+    check(load().vxr_scene_preset(config, C.byref(d)))
+    for k, v in overrides.items():
+        setattr(d, k, v)
+    return d
+
+
+def scene_height(desc, x, z):
+    h = C.c_uint32()
+    check(load().vxr_scene_height(C.byref(desc), x, z, C.byref(h)))
+    return h.value
+
+
+def camera_path(desc, seed, f, n):
+    p, t = (C.c_float * 3)(), (C.c_float * 3)()
+    check(load().vxr_camera_path(C.byref(desc), seed, f, n, p, t))
+    return list(p), list(t)
+
+
+def view_desc(width, height, light_model=LIGHTS_AREA, **kw):
+    d = ViewDesc()
+    check(load().vxr_view_default_desc(C.byref(d)))
+    d.width, d.height, d.light_model = width, height, light_model
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+class View:
+    """One camera on one world (vxr_view)."""
+
+    def __init__(self, world, desc):
+        self._lib = load()
+        self.world = world
+        self.desc = desc
+        self.h = _P()
+        check(self._lib.vxr_view_create(world.h, C.byref(desc), C.byref(self.h)))
+        self.n = desc.width * desc.height
+
+    def close(self):
+        if self.h:
+            self._lib.vxr_view_destroy(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def lookat(self, pos, target):
+        check(self._lib.vxr_view_lookat(self.h, _f3(pos), _f3(target)))
+
+    def set_params(self, desc):
+        check(self._lib.vxr_view_set_params(self.h, C.byref(desc)))
+        self.desc = desc
+
+    def begin_frame(self):
+        k = FrameConsts()
+        check(self._lib.vxr_view_begin_frame(self.h, C.byref(k)))
+        return k
+
+    def set_frame_consts(self, k):
+        check(self._lib.vxr_view_set_frame_consts(self.h, C.byref(k)))
+
+    def stage(self, s):
+        check(self._lib.vxr_view_stage(self.h, s))
+
+    def end_frame(self):
+        check(self._lib.vxr_view_end_frame(self.h))
+
+    def render(self):
+        check(self._lib.vxr_view_render(self.h))
+
+    def wait(self):
+        check(self._lib.vxr_view_wait(self.h))
+
+    def stage_times(self):
+        ms = (C.c_float * 5)()
+        check(self._lib.vxr_view_stage_times(self.h, ms))
+        return list(ms)
+
+    def read_gbuffer(self, which=0):
+        out = np.zeros(self.n, GBUF_DTYPE)
+        check(self._lib.vxr_view_read_gbuffer(self.h, which, out.ctypes.data))
+        return out
+
+    def write_gbuffer(self, which, recs):
+        arr = np.ascontiguousarray(recs, dtype=GBUF_DTYPE)
+        assert len(arr) == self.n
+        check(self._lib.vxr_view_write_gbuffer(self.h, which, arr.ctypes.data))
+
+    def read_reservoirs(self, role):
+        out = np.zeros(self.n, RES_DTYPE)
+        check(self._lib.vxr_view_read_reservoirs(self.h, role, out.ctypes.data))
+        return out
+
+    def write_reservoirs(self, role, recs):
+        arr = np.ascontiguousarray(recs, dtype=RES_DTYPE)
+        assert len(arr) == self.n
+        check(self._lib.vxr_view_write_reservoirs(self.h, role, arr.ctypes.data))
+
+    def read_frame(self):
+        out = np.zeros((self.n, 4), np.float32)
+        check(self._lib.vxr_view_read_frame(self.h, out.ctypes.data_as(_F3)))
+        return out
+
+    def read_accum(self):
+        out = np.zeros((self.n, 4), np.float32)
+        check(self._lib.vxr_view_read_accum(self.h, out.ctypes.data_as(_F3)))
+        return out
+
+    def render_to_host(self, pos, target, out):
+        assert out.dtype == np.float32 and out.size == self.n * 4 and out.flags.c_contiguous
+        check(self._lib.vxr_view_render_to_host(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3)))
