@@ -196,6 +196,25 @@ int vxr_camera_path(const vxr_scene_desc* desc, uint32_t path_seed, uint32_t f, 
  * position, independent of brick numbering) and of its light list. */
 int vxr_world_checksum(const vxr_world* w, uint64_t* voxels, uint64_t* lights);
 
+/* ---- camera (host only) ------------------------------------------------------------ */
+/* The camera state World::Render keeps between frames (camMat + previous corners +
+ * RandomUInt state + frame counters); every view owns one. Exposed on its own so the
+ * per-frame constants can be produced and checked without a GPU. */
+typedef struct vxr_camera vxr_camera;
+int vxr_camera_create(uint32_t rng_seed, vxr_camera** out);
+int vxr_camera_destroy(vxr_camera* c);
+int vxr_camera_lookat(vxr_camera* c, const float pos[3], const float target[3]);   /* mat4::LookAt */
+int vxr_camera_set_matrix(vxr_camera* c, const float m[16]);
+/* world.cpp:2144-2191: corners, previous-frame planes, R0, counters -> *k (resolution W x H).
+ * Only the camera-derived fields of *k are written; the knobs are the caller's. */
+int vxr_camera_begin_frame(vxr_camera* c, uint32_t W, uint32_t H, vxr_frame_consts* k);
+int vxr_camera_end_frame(vxr_camera* c);                                           /* world.cpp:2335-2337 */
+
+/* ---- host memory for end-to-end transfers ------------------------------------------- */
+/* Page-locked host buffer (cudaHostAlloc) for vxr_view_render_to_host outputs. */
+int vxr_host_alloc(size_t bytes, void** p);
+int vxr_host_free(void* p);
+
 /* ---- GPU copy of a world --------------------------------------------------------- */
 /* World::ForceSyncAllBricks + the updateUberGrid kernel + SetupLightBuffer's device copy
  * (world.cpp:639-651, kernels.cl:498-513, world.cpp:563-612): upload the grid, the
@@ -272,6 +291,14 @@ int vxr_view_write_reservoirs(vxr_view* v, int role, const vxr_reservoir_rec* in
 /* Shaded frame (rgb, primary-hit distance) and accumulator (rgb, 1): float4 per pixel. */
 int vxr_view_read_frame(vxr_view* v, float* rgba);
 int vxr_view_read_accum(vxr_view* v, float* rgba);
+/* Per-stage GPU time summed over every frame finished since the last reset (CUDA
+ * events around each stage launch, kept for the last 256 frames between waits), and
+ * the number of launches timed; reset != 0 clears the sums after reading. */
+int vxr_view_stage_stats(vxr_view* v, double sum_ms[5], uint32_t count[5], int reset);
+/* Device-side timer on the view's stream: events recorded before / after the work
+ * enqueued in between; vxr_view_timer_end waits and returns the elapsed milliseconds. */
+int vxr_view_timer_begin(vxr_view* v);
+int vxr_view_timer_end(vxr_view* v, float* ms);
 /* End-to-end frame through host memory: LookAt(pos, target), render, copy the
  * accumulated image into host_rgba (W*H float4; page-locked memory is fastest), wait. */
 int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba);

@@ -109,6 +109,7 @@ def load_ref():
             f"vxref_set_world_{v}": (None, [_P, _P, _P, _P]), f"vxref_set_lights_{v}": (None, [_P, _P, C.c_uint32]),
             f"vxref_update_uber_{v}": (None, [_P, _P]), f"vxref_begin_frame_{v}": (None, [_P]),
             f"vxref_stage_{v}": (None, [_P, C.POINTER(FrameConsts), C.c_int]),
+            f"vxref_stage_rows_{v}": (None, [_P, C.POINTER(FrameConsts), C.c_int, C.c_int, C.c_int]),
             f"vxref_read_gbuffer_{v}": (None, [_P, C.c_int, _P, _P]),
             f"vxref_read_reservoirs_{v}": (None, [_P, C.c_int, _P]),
             f"vxref_write_reservoirs_{v}": (None, [_P, C.c_int, _P]),
@@ -183,6 +184,8 @@ class Renderer:
         kk = copy_consts(k, FrameConsts)
         if self.kind == "port":
             self.lib.orc_stage(self.h, C.byref(kk), s, y0, y1)
+        elif y0 or y1:
+            self._f("stage_rows")(self.h, C.byref(kk), s, y0, y1)
         else:
             self._f("stage")(self.h, C.byref(kk), s)
 

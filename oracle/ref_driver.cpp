@@ -72,11 +72,14 @@ void fill_params(Ctx* c, const vxr_frame_consts* k) {
     vxref_scr_height = c->H;
 }
 
+int g_y0 = 0, g_y1 = 0;   // row range of the next stage (0, 0 = all rows)
+
 template <class F>
 void for_pixels(Ctx* c, F f) {
-    const int W = c->W, H = c->H;
+    const int W = c->W;
+    const int y0 = g_y0, y1 = (g_y1 > 0 && g_y1 <= c->H) ? g_y1 : c->H;
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int y = 0; y < H; y++)
+    for (int y = y0; y < y1; y++)
         for (int x = 0; x < W; x++) {
             vx_gid[0] = x;
             vx_gid[1] = y;
@@ -212,6 +215,15 @@ void VXREF_FN(vxref_stage)(void* ctx, const vxr_frame_consts* k, int stage) {
     default:
         std::abort();
     }
+}
+
+// Rows [y0, y1) only (a bounded sample of a frame, for CPU timing).
+void VXREF_FN(vxref_stage_rows)(void* ctx, const vxr_frame_consts* k, int stage, int y0, int y1) {
+    g_y0 = y0;
+    g_y1 = y1;
+    VXREF_FN(vxref_stage)(ctx, k, stage);
+    g_y0 = 0;
+    g_y1 = 0;
 }
 
 // Frame epilogue is the host counter update (world.cpp:2335-2337), done by the caller

@@ -111,8 +111,15 @@ struct vxr_view {
     vxr::ViewBuffers buf;
     int cur = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t evs[6] = {}, eve[6] = {};
+    cudaEvent_t evs[6] = {}, eve[6] = {};            // [0]: vxr_view_timer_*, [1..5]: last frame's stages
     bool ran[6] = {};
+    // per-stage event ring over the last kRing frames, harvested by vxr_view_wait
+    static constexpr int kRing = 256;
+    std::vector<cudaEvent_t> ringS, ringE;             // kRing * 6
+    std::vector<uint8_t> ringUsed;                     // kRing * 6
+    uint64_t frameSerial = 0, harvested = 0;
+    double statSum[6] = {};
+    uint32_t statCount[6] = {};
     bool frameOpen = false;
     vxr_frame_consts k{};
     uint64_t seenLightVersion = 0;
@@ -187,7 +194,29 @@ void free_view(vxr_view* v) {
         if (v->evs[i]) cudaEventDestroy(v->evs[i]);
         if (v->eve[i]) cudaEventDestroy(v->eve[i]);
     }
+    for (cudaEvent_t e : v->ringS) cudaEventDestroy(e);
+    for (cudaEvent_t e : v->ringE) cudaEventDestroy(e);
     if (v->stream) cudaStreamDestroy(v->stream);
+}
+
+// Accumulate the stage durations of every finished frame still in the ring.
+void harvest(vxr_view* v) {
+    const uint64_t from = v->frameSerial > (uint64_t)vxr_view::kRing ? std::max(v->harvested, v->frameSerial - vxr_view::kRing)
+                                                                       : v->harvested;
+    for (uint64_t f = from; f < v->frameSerial; f++) {
+        const int slot = (int)(f % vxr_view::kRing);
+        for (int s = 1; s <= 5; s++) {
+            const int i = slot * 6 + s;
+            if (!v->ringUsed[i]) continue;
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, v->ringS[i], v->ringE[i]) == cudaSuccess) {
+                v->statSum[s] += ms;
+                v->statCount[s]++;
+            }
+            v->ringUsed[i] = 0;
+        }
+    }
+    v->harvested = v->frameSerial;
 }
 
 vxr::LaunchShape shape(const vxr_view* v) {
@@ -270,6 +299,13 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     alloc((void**)&b.accum, n * sizeof(float4));
     alloc((void**)&b.err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking);
+    v->ringS.assign(vxr_view::kRing * 6, nullptr);
+    v->ringE.assign(vxr_view::kRing * 6, nullptr);
+    v->ringUsed.assign(vxr_view::kRing * 6, 0);
+    for (int i = 0; i < vxr_view::kRing * 6 && e == cudaSuccess; i++) {
+        e = cudaEventCreate(&v->ringS[i]);
+        if (e == cudaSuccess) e = cudaEventCreate(&v->ringE[i]);
+    }
     for (int i = 0; i < 6 && e == cudaSuccess; i++) {
         e = cudaEventCreate(&v->evs[i]);
         if (e == cudaSuccess) e = cudaEventCreate(&v->eve[i]);
@@ -370,7 +406,9 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     const vxr::dev::Frame k = dev_frame(v->k);
     const bool point = v->desc.light_model == VXR_LIGHTS_POINT;
     const vxr::LaunchShape sh = shape(v);
+    const int ri = (int)(v->frameSerial % vxr_view::kRing) * 6 + stage;
     CUV(cudaEventRecord(v->evs[stage], v->stream), "cudaEventRecord");
+    CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");
     switch (stage) {
     case VXR_STAGE_ALBEDO: vxr::launch_albedo(w, k, v->buf, v->cur, sh, v->stream); break;
     case VXR_STAGE_CANDIDATES: vxr::launch_candidates(point, w, k, v->buf, v->cur, sh, v->stream); break;
@@ -381,6 +419,8 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     }
     CUV(cudaGetLastError(), "kernel launch");
     CUV(cudaEventRecord(v->eve[stage], v->stream), "cudaEventRecord");
+    CUV(cudaEventRecord(v->ringE[ri], v->stream), "cudaEventRecord");
+    v->ringUsed[ri] = 1;
     v->ran[stage] = true;
     return VXR_OK;
 }
@@ -395,6 +435,7 @@ int vxr_view_end_frame(vxr_view* v) {
     if (!v->frameOpen) return set_error(VXR_E_STATE, "vxr_view_end_frame: no frame in progress");
     vxr::end_frame(v->cam);
     v->frameOpen = false;
+    v->frameSerial++;
     return VXR_OK;
 }
 
@@ -416,6 +457,7 @@ int vxr_view_wait(vxr_view* v) {
         if (v->ran[s]) cudaEventElapsedTime(&ms, v->evs[s], v->eve[s]);
         v->times[s - 1] = ms;
     }
+    harvest(v);
     uint32_t err = 0;
     CUV(cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost), "read device error flags");
     if (err) {
@@ -551,3 +593,92 @@ int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[
 }
 
 }  // extern "C"
+
+// ---- host-only camera, timers, pinned memory ---------------------------------------------
+struct vxr_camera {
+    vxr::CameraState st;
+};
+
+extern "C" {
+
+int vxr_camera_create(uint32_t rng_seed, vxr_camera** out) {
+    VXR_CHECK_ARG(out, "vxr_camera_create: null out");
+    vxr_camera* c = new (std::nothrow) vxr_camera();
+    if (!c) return set_error(VXR_E_NOMEM, "vxr_camera_create: out of host memory");
+    c->st.rng = rng_seed;
+    *out = c;
+    return VXR_OK;
+}
+
+int vxr_camera_destroy(vxr_camera* c) {
+    delete c;
+    return VXR_OK;
+}
+
+int vxr_camera_lookat(vxr_camera* c, const float pos[3], const float target[3]) {
+    VXR_CHECK_ARG(c && pos && target, "vxr_camera_lookat: null argument");
+    c->st.M = vxr::look_at(pos, target);
+    return VXR_OK;
+}
+
+int vxr_camera_set_matrix(vxr_camera* c, const float m[16]) {
+    VXR_CHECK_ARG(c && m, "vxr_camera_set_matrix: null argument");
+    std::memcpy(c->st.M.cell, m, sizeof(float) * 16);
+    return VXR_OK;
+}
+
+int vxr_camera_begin_frame(vxr_camera* c, uint32_t W, uint32_t H, vxr_frame_consts* k) {
+    VXR_CHECK_ARG(c && k && W > 0 && H > 0, "vxr_camera_begin_frame: bad argument");
+    vxr::begin_frame(c->st, W, H, k);
+    return VXR_OK;
+}
+
+int vxr_camera_end_frame(vxr_camera* c) {
+    VXR_CHECK_ARG(c, "vxr_camera_end_frame: null camera");
+    vxr::end_frame(c->st);
+    return VXR_OK;
+}
+
+int vxr_host_alloc(size_t bytes, void** p) {
+    VXR_CHECK_ARG(p && bytes > 0, "vxr_host_alloc: bad argument");
+    CUV(cudaHostAlloc(p, bytes, cudaHostAllocDefault), "cudaHostAlloc");
+    return VXR_OK;
+}
+
+int vxr_host_free(void* p) {
+    if (p) CUV(cudaFreeHost(p), "cudaFreeHost");
+    return VXR_OK;
+}
+
+int vxr_view_timer_begin(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_timer_begin")) return r;
+    CUV(cudaEventRecord(v->evs[0], v->stream), "cudaEventRecord");
+    return VXR_OK;
+}
+
+int vxr_view_timer_end(vxr_view* v, float* ms) {
+    if (int r = check_view(v, "vxr_view_timer_end")) return r;
+    VXR_CHECK_ARG(ms, "vxr_view_timer_end: null output");
+    CUV(cudaEventRecord(v->eve[0], v->stream), "cudaEventRecord");
+    CUV(cudaEventSynchronize(v->eve[0]), "cudaEventSynchronize");
+    CUV(cudaEventElapsedTime(ms, v->evs[0], v->eve[0]), "cudaEventElapsedTime");
+    return VXR_OK;
+}
+
+}  // extern "C"
+
+extern "C" int vxr_view_stage_stats(vxr_view* v, double sum_ms[5], uint32_t count[5], int reset) {
+    if (int r = check_view(v, "vxr_view_stage_stats")) return r;
+    VXR_CHECK_ARG(sum_ms && count, "vxr_view_stage_stats: null output");
+    CUV(cudaStreamSynchronize(v->stream), "vxr_view_stage_stats");
+    harvest(v);
+    for (int s = 1; s <= 5; s++) {
+        sum_ms[s - 1] = v->statSum[s];
+        count[s - 1] = v->statCount[s];
+        if (reset) {
+            v->statSum[s] = 0.0;
+            v->statCount[s] = 0;
+        }
+    }
+    return VXR_OK;
+}

@@ -105,6 +105,13 @@ _SIGS = {
     "vxr_view_read_reservoirs": [_P, C.c_int, _P], "vxr_view_write_reservoirs": [_P, C.c_int, _P],
     "vxr_view_read_frame": [_P, _F3], "vxr_view_read_accum": [_P, _F3],
     "vxr_view_render_to_host": [_P, _F3, _F3, _F3],
+    "vxr_view_timer_begin": [_P], "vxr_view_timer_end": [_P, _F3],
+    "vxr_view_stage_stats": [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.c_int],
+    "vxr_camera_create": [C.c_uint32, C.POINTER(_P)], "vxr_camera_destroy": [_P],
+    "vxr_camera_lookat": [_P, _F3, _F3], "vxr_camera_set_matrix": [_P, _F3],
+    "vxr_camera_begin_frame": [_P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts)],
+    "vxr_camera_end_frame": [_P],
+    "vxr_host_alloc": [C.c_size_t, C.POINTER(_P)], "vxr_host_free": [_P],
 }
 _RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
 
@@ -336,6 +343,64 @@ class View:
         check(self._lib.vxr_view_read_accum(self.h, out.ctypes.data_as(_F3)))
         return out
 
+    def stage_stats(self, reset=False):
+        """(sum_ms[5], count[5]) per stage since the last reset."""
+        sm = (C.c_double * 5)()
+        cnt = (C.c_uint32 * 5)()
+        check(self._lib.vxr_view_stage_stats(self.h, sm, cnt, 1 if reset else 0))
+        return list(sm), list(cnt)
+
+    def timer_begin(self):
+        check(self._lib.vxr_view_timer_begin(self.h))
+
+    def timer_end(self):
+        ms = C.c_float()
+        check(self._lib.vxr_view_timer_end(self.h, C.byref(ms)))
+        return ms.value
+
     def render_to_host(self, pos, target, out):
         assert out.dtype == np.float32 and out.size == self.n * 4 and out.flags.c_contiguous
         check(self._lib.vxr_view_render_to_host(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3)))
+
+
+class Camera:
+    """Host-only camera state (vxr_camera)."""
+
+    def __init__(self, rng_seed=0x12345678):
+        self._lib = load()
+        self.h = _P()
+        check(self._lib.vxr_camera_create(rng_seed, C.byref(self.h)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                self._lib.vxr_camera_destroy(self.h)
+        except Exception:
+            pass
+
+    def lookat(self, pos, target):
+        check(self._lib.vxr_camera_lookat(self.h, _f3(pos), _f3(target)))
+
+    def begin_frame(self, W, H):
+        k = FrameConsts()
+        check(self._lib.vxr_camera_begin_frame(self.h, W, H, C.byref(k)))
+        return k
+
+    def end_frame(self):
+        check(self._lib.vxr_camera_end_frame(self.h))
+
+
+class PinnedBuffer:
+    """Page-locked float32 host buffer (vxr_host_alloc) viewed as numpy."""
+
+    def __init__(self, count):
+        self._lib = load()
+        self.p = _P()
+        check(self._lib.vxr_host_alloc(count * 4, C.byref(self.p)))
+        self.array = np.ctypeslib.as_array(C.cast(self.p, C.POINTER(C.c_float)), shape=(count,))
+
+    def close(self):
+        if self.p:
+            self._lib.vxr_host_free(self.p)
+            self.p = _P()
+            self.array = None
