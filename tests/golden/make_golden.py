@@ -1,0 +1,79 @@
+"""Generate tests/golden/*.npz from the reference oracle (the reference's own
+render-path kernel source compiled for the CPU, oracle/_ref).
+
+Each fixture: the config-0 scene (regenerated by the library; its canonical checksum
+is stored and asserted), a small frame size, a few frames with a moving camera, and
+for every frame the frame constants plus every stage output of the reference:
+G-buffer after renderAlbedo, reservoirs after perPixelInitialSampling and after
+perPixelSpatialResampling (as left by renderRIS), the shaded frame and the
+accumulator.
+
+Usage: python tests/golden/make_golden.py   (needs the reference checkout or a
+previously generated oracle/_ref/vxref_gen.inc)
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+CASES = [
+    # name, W, H, point, frames
+    ("config0_area_48x32", 48, 32, False, 3),
+    ("config0_point_48x32", 48, 32, True, 3),
+]
+KNOBS = dict(numberOfCandidates=32, numberOfMaxTemporalImportance=20, spatialRadius=30, spatialTaps=5,
+             spatial=1, temporal=1, accumulate=1)
+
+
+def camera(f):
+    return (126.0 + 5.0 * f, 150.0 - 1.0 * f, 30.0 + 2.0 * f), (128.0, 100.0, 128.0)
+
+
+def main():
+    import smallproject_gb300 as vx
+    from oracle import binding as ob
+    if ob.load_ref() is None:
+        sys.exit("reference oracle unavailable")
+    w = vx.World()
+    w.generate(vx.scene_preset(0))
+    ck = w.checksum()
+    g, b, l = w.arrays()
+    arrays = ob.WorldArrays(g, b, l)
+    for name, W, H, point, F in CASES:
+        ref = ob.Renderer("ref", arrays, W, H, point)
+        cam = ob.CameraPath(W, H)
+        out = {"checksum": np.array(ck, np.uint64), "W": W, "H": H, "point": int(point), "frames": F}
+        for f in range(F):
+            pos, tgt = camera(f)
+            cam.lookat(pos, tgt)
+            k = cam.begin(numberOfLights=len(l), **KNOBS)
+            out[f"consts{f}"] = np.frombuffer(bytes(k), np.uint8)
+            out[f"camera{f}"] = np.array(pos + tgt, np.float32)
+            ref.frame_start()
+            for s in range(1, 6):
+                ref.stage(k, s)
+                if s == 1:
+                    out[f"gbuffer{f}"] = ref.gbuffer(0)
+                elif s == 2:
+                    out[f"candidates{f}"] = ref.reservoirs(0)
+                    out[f"seed_cand{f}"] = ref.gbuffer(0)["seed"]
+                elif s == 3:
+                    out[f"seed_spatial{f}"] = ref.gbuffer(0)["seed"]
+                elif s == 4:
+                    out[f"spatial{f}"] = ref.reservoirs(1)
+                    out[f"frame{f}"] = ref.image(0)
+                else:
+                    out[f"accum{f}"] = ref.image(1)
+            cam.end()
+        ref.close()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,63 @@
+"""The C-ABI library: loads, exports every symbol include/vxr.h declares, and rejects
+bad arguments with status codes (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "vxr.h")).read()
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(vxr_[a-z0-9_]+)\s*\(", src)) - {"vxr_world", "vxr_view"})
+
+
+def test_library_exports_every_declared_symbol(lib):
+    so = C.CDLL(lib.LIB_PATH)
+    missing = [s for s in _declared() if not hasattr(so, s)]
+    assert not missing, missing
+    # and the Python binding covers them all
+    assert set(_declared()) <= set(lib.exported_symbols()), set(_declared()) - set(lib.exported_symbols())
+
+
+def test_struct_layouts_match_header(lib):
+    from smallproject_gb300 import vxr as V
+    assert C.sizeof(V.FrameConsts) == 44 * 4
+    assert C.sizeof(V.ReservoirRec) == 48 and C.sizeof(V.GBufferRec) == 16 and C.sizeof(V.Light) == 12
+    assert C.sizeof(V.SceneDesc) == 20 * 4 and C.sizeof(V.ViewDesc) == 13 * 4
+
+
+def test_invalid_arguments_return_status(lib):
+    L = lib.load()
+    assert L.vxr_world_create(None) == lib.vxr.VXR_E_INVALID
+    assert b"null" in L.vxr_last_error()
+    w = lib.World()
+    out = C.c_uint32()
+    assert L.vxr_world_get(None, 0, 0, 0, C.byref(out)) == lib.vxr.VXR_E_INVALID
+    d = lib.scene_preset(0)
+    d.extent = 4
+    with pytest.raises(lib.VxrError):
+        w.generate(d)
+    with pytest.raises(lib.VxrError):
+        lib.scene_preset(9)
+    bad = np.zeros(1, lib.LIGHT_DTYPE)
+    bad["position"] = 1024 ** 3
+    with pytest.raises(lib.VxrError):
+        w.set_lights(bad)
+    vd = lib.view_desc(0, 10)
+    h = C.c_void_p()
+    assert L.vxr_view_create(w.h, C.byref(vd), C.byref(h)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_view_stage(None, 1) == lib.vxr.VXR_E_INVALID
+
+
+def test_out_of_map_set_is_ignored(lib):
+    w = lib.World()
+    w.set(1024, 0, 0, 0xF111)
+    w.set(0, 5000, 0, 0xF111)
+    assert w.get(0, 0, 0) == 0
+    g, b, l = w.arrays()
+    assert not g.any() and len(l) == 0
