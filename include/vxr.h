@@ -303,6 +303,37 @@ int vxr_view_timer_end(vxr_view* v, float* ms);
  * accumulated image into host_rgba (W*H float4; page-locked memory is fastest), wait. */
 int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba);
 
+/* ---- rendering without allocation ---------------------------------------------------
+ * No counterpart in the reference. For callers that cannot call cudaMalloc - an
+ * application that owns all GPU memory through its own pool, a plugin that must not
+ * bypass its host's allocator - this renders ONE frame from device buffers the caller
+ * already owns into a device image the caller owns, and allocates nothing: no
+ * cudaMalloc, cudaFree or allocating library call. The G-buffer, seeds, reservoirs, the
+ * uber grid, the light table and the error word live in one fixed file-scope device
+ * array of VXR_NOALLOC_SCRATCH_BYTES that every GPU loading libvxr.so holds until exit.
+ *   grid      device uint32[128^3] top-level cells (layout of vxr_world_arrays)
+ *   bricks    device uint32[nbricks * 512]; every brick cell must index below nbricks
+ *             (checked on the device first; VXR_E_INVALID otherwise)
+ *   lights    device vxr_light[nlights], nlights <= VXR_NOALLOC_MAX_LIGHTS
+ *   k         host frame constants (e.g. from vxr_camera_begin_frame); width*height
+ *             <= VXR_NOALLOC_MAX_PIXELS, numberOfLights == nlights; larger sizes are
+ *             rejected with VXR_E_INVALID
+ *   out_rgba  device float4[width*height]: shaded rgb and primary-hit distance
+ *   stream    cudaStream_t to run on (NULL = the legacy default stream)
+ * The frame is rendered without temporal reuse or accumulation (no history is kept
+ * between calls). The call is synchronous. On its first call on a device it looks up
+ * the device address of its scratch array (cudaGetSymbolAddress), so make that first
+ * call before any stream capture on that device. All calls share the one scratch
+ * array per device and it keeps the last call's contents: calls that overlap on the
+ * GPU (different streams or threads at once) race and must be serialised by the
+ * caller. */
+#define VXR_NOALLOC_MAX_PIXELS    65536u     /* e.g. 256 x 256 */
+#define VXR_NOALLOC_MAX_LIGHTS    65536u
+#define VXR_NOALLOC_SCRATCH_BYTES 8159488u
+int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* bricks, uint32_t nbricks,
+                             const vxr_light* lights, uint32_t nlights, uint32_t light_model,
+                             const vxr_frame_consts* k, float* out_rgba, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,192 @@
+// noalloc.cu - a render entry point that allocates no memory.
+//
+// Some callers cannot call cudaMalloc: a host application that already owns all GPU
+// memory through its own pool or arena, a plugin loaded into a process whose allocator
+// must not be bypassed, or code running while a CUDA graph is being recorded elsewhere.
+// vxr_render_frame_noalloc renders one frame for them from device buffers they already
+// own (the world grid, its bricks and the light list) into an image buffer they own.
+// Everything else the frame needs - G-buffer, seeds, both reservoir planes, the 32^3
+// uber grid, the per-light table and the device error word - lives in one file-scope
+// __device__ array of fixed size, which every GPU that loads this library holds until
+// the process exits (VXR_NOALLOC_SCRATCH_BYTES = 8,159,488 bytes, 7.8 MiB).
+//
+// The stage kernels are the ones the view path launches; only the buffers differ.
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "internal.hpp"
+#include "kernels.hpp"
+
+namespace {
+
+constexpr size_t kMaxPx = VXR_NOALLOC_MAX_PIXELS;
+constexpr size_t kMaxLights = VXR_NOALLOC_MAX_LIGHTS;
+// layout (byte offsets, every region 256-byte aligned)
+constexpr size_t kOffVd = 0;                                   // uint2 [kMaxPx]
+constexpr size_t kOffSeed = kOffVd + 8 * kMaxPx;               // uint32 [kMaxPx]
+constexpr size_t kOffCA = kOffSeed + 4 * kMaxPx;               // uint4 [kMaxPx]
+constexpr size_t kOffCB = kOffCA + 16 * kMaxPx;                // float4 [kMaxPx]
+constexpr size_t kOffHA = kOffCB + 16 * kMaxPx;                // uint4 [kMaxPx]
+constexpr size_t kOffHB = kOffHA + 16 * kMaxPx;                // float4 [kMaxPx]
+constexpr size_t kOffUber = kOffHB + 16 * kMaxPx;              // uint8 [32^3]
+constexpr size_t kOffGeom = kOffUber + 32 * 32 * 32;           // float4 [kMaxLights]
+constexpr size_t kOffEmit = kOffGeom + 16 * kMaxLights;        // float4 [kMaxLights]
+constexpr size_t kOffRaw = kOffEmit + 16 * kMaxLights;         // uint4 [kMaxLights]
+constexpr size_t kOffErr = kOffRaw + 16 * kMaxLights;          // uint32 error word (+ pad)
+constexpr size_t kScratchBytes = kOffErr + 256;
+static_assert(kScratchBytes == VXR_NOALLOC_SCRATCH_BYTES, "scratch size must match the header");
+static_assert(kOffSeed % 256 == 0 && kOffCA % 256 == 0 && kOffUber % 256 == 0 && kOffGeom % 256 == 0 &&
+                  kOffErr % 256 == 0, "scratch regions must stay 256-byte aligned");
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+// Host-side address of g_noalloc_scratch per device. The symbol's name in host code is
+// only a host stand-in, so the device address is looked up once per device with
+// cudaGetSymbolAddress while that device is current.
+constexpr int kMaxDevices = 64;
+unsigned char* g_scratch_ptr[kMaxDevices] = {};
+std::mutex g_scratch_mutex;
+
+int scratch_for_current_device(unsigned char** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return vxr::set_error(VXR_E_NODEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return vxr::set_error(VXR_E_INVALID, "vxr_render_frame_noalloc: device index >= 64");
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return vxr::set_error(VXR_E_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_scratch_ptr[dev] = (unsigned char*)p;
+    }
+    *out = g_scratch_ptr[dev];
+    return VXR_OK;
+}
+
+// vxr_light (12 bytes) -> the 16-byte records the light-table kernel reads
+__global__ void widen_lights_kernel(const vxr_light* __restrict__ in, uint32_t n, uint4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_uint4(in[i].position, in[i].voxel, in[i].size, 0u);
+}
+
+// every brick cell of the grid must index inside the caller's brick array
+__global__ void check_grid_kernel(const uint32_t* __restrict__ grid, uint32_t nbricks, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 128u * 128u * 128u) return;
+    const uint32_t c = grid[i];
+    if ((c & 1u) && (c >> 1) >= nbricks) atomicOr(err, 16u);
+}
+
+}  // namespace
+
+#define CUN(call, what)                                                                                     \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess) return vxr::set_error(VXR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* bricks, uint32_t nbricks,
+                                        const vxr_light* lights, uint32_t nlights, uint32_t light_model,
+                                        const vxr_frame_consts* k, float* out_rgba, void* stream) {
+    VXR_CHECK_ARG(grid && bricks && k && out_rgba && (lights || nlights == 0), "vxr_render_frame_noalloc: null argument");
+    VXR_CHECK_ARG(light_model == VXR_LIGHTS_AREA || light_model == VXR_LIGHTS_POINT,
+                  "vxr_render_frame_noalloc: unknown light model");
+    VXR_CHECK_ARG(k->width >= 1 && k->height >= 1, "vxr_render_frame_noalloc: empty frame");
+    if ((size_t)k->width * k->height > kMaxPx)
+        return vxr::set_error(VXR_E_INVALID, "vxr_render_frame_noalloc: " + std::to_string(k->width) + "x" +
+                                                 std::to_string(k->height) + " exceeds the fixed scratch of " +
+                                                 std::to_string(kMaxPx) + " pixels");
+    if (nlights > kMaxLights)
+        return vxr::set_error(VXR_E_INVALID, "vxr_render_frame_noalloc: " + std::to_string(nlights) +
+                                                 " lights exceed the fixed scratch of " + std::to_string(kMaxLights));
+    VXR_CHECK_ARG(k->numberOfLights == nlights, "vxr_render_frame_noalloc: numberOfLights differs from nlights");
+    VXR_CHECK_ARG(k->spatialRadius >= 1, "vxr_render_frame_noalloc: spatialRadius must be >= 1");
+    VXR_CHECK_ARG(nbricks >= 1, "vxr_render_frame_noalloc: nbricks must be >= 1");
+
+    unsigned char* s = nullptr;
+    if (int r = scratch_for_current_device(&s)) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t* err = (uint32_t*)(s + kOffErr);
+    CUN(cudaMemsetAsync(err, 0, sizeof(uint32_t), st), "clear error word");
+
+    // validate the grid before any traversal reads the bricks through it
+    check_grid_kernel<<<(128 * 128 * 128 + 255) / 256, 256, 0, st>>>(grid, nbricks, err);
+    CUN(cudaGetLastError(), "grid check");
+    uint32_t herr = 0;
+    CUN(cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "read error word");
+    CUN(cudaStreamSynchronize(st), "grid check");
+    if (herr & 16u) return vxr::set_error(VXR_E_INVALID, "vxr_render_frame_noalloc: grid references a brick >= nbricks");
+
+    // derive the uber grid and the light table in scratch
+    uint4* raw = (uint4*)(s + kOffRaw);
+    float4* geom = (float4*)(s + kOffGeom);
+    float4* emit = (float4*)(s + kOffEmit);
+    if (nlights) {
+        widen_lights_kernel<<<(nlights + 255) / 256, 256, 0, st>>>(lights, nlights, raw);
+        vxr::launch_build_light_table(raw, nlights, geom, emit, st);
+    }
+    vxr::launch_build_uber(grid, s + kOffUber, st);
+    CUN(cudaGetLastError(), "world kernels");
+
+    vxr::dev::World w;
+    w.grid = grid;
+    w.uber = s + kOffUber;
+    w.bricks = bricks;
+    w.lgeom = geom;
+    w.lemit = emit;
+    w.nlights = nlights;
+
+    // a single frame: no temporal history is read (the scratch keeps the previous
+    // call's contents, which may belong to another world or camera)
+    vxr::dev::Frame f;
+    f.E = make_float3(k->E[0], k->E[1], k->E[2]);
+    f.p0 = make_float3(k->p0[0], k->p0[1], k->p0[2]);
+    f.dx = make_float3(k->p1[0] - k->p0[0], k->p1[1] - k->p0[1], k->p1[2] - k->p0[2]);
+    f.dy = make_float3(k->p2[0] - k->p0[0], k->p2[1] - k->p0[1], k->p2[2] - k->p0[2]);
+    f.oorx = k->oneOverRes[0];
+    f.oory = k->oneOverRes[1];
+    f.Nl = make_float4(k->Nleft[0], k->Nleft[1], k->Nleft[2], k->Nleft[3]);
+    f.Nr = make_float4(k->Nright[0], k->Nright[1], k->Nright[2], k->Nright[3]);
+    f.Nt = make_float4(k->Ntop[0], k->Ntop[1], k->Ntop[2], k->Ntop[3]);
+    f.Nb = make_float4(k->Nbottom[0], k->Nbottom[1], k->Nbottom[2], k->Nbottom[3]);
+    f.R0 = k->R0;
+    f.framecount = k->framecount;
+    f.restirtemporalframe = 0;
+    f.spatial = k->spatial;
+    f.temporal = 0;
+    f.accumulate = 0;
+    f.nlights = nlights;
+    f.ncand = nlights < k->numberOfCandidates ? nlights : k->numberOfCandidates;
+    f.maxTemporal = k->numberOfMaxTemporalImportance;
+    f.radius = k->spatialRadius;
+    f.taps = k->spatialTaps;
+    f.W = (int32_t)k->width;
+    f.H = (int32_t)k->height;
+
+    vxr::ViewBuffers b;
+    b.vd[0] = (uint2*)(s + kOffVd);
+    b.vd[1] = (uint2*)(s + kOffVd);          // previous G-buffer: never read without temporal reuse
+    b.seed = (uint32_t*)(s + kOffSeed);
+    b.cA = (uint4*)(s + kOffCA);
+    b.cB = (float4*)(s + kOffCB);
+    b.hA = (uint4*)(s + kOffHA);
+    b.hB = (float4*)(s + kOffHB);
+    b.frame = (float4*)out_rgba;
+    b.accum = (float4*)out_rgba;             // unused: shading runs without the accumulate fusion
+    b.err = err;
+    const bool point = light_model == VXR_LIGHTS_POINT;
+    const vxr::LaunchShape sh;
+    vxr::launch_albedo(w, f, b, 0, sh, st);
+    vxr::launch_candidates(point, w, f, b, 0, sh, st);
+    vxr::launch_spatial(point, w, f, b, 0, sh, st);
+    vxr::launch_shade(point, w, f, b, 0, false, sh, st);
+    CUN(cudaGetLastError(), "stage kernels");
+    CUN(cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "read error word");
+    CUN(cudaStreamSynchronize(st), "vxr_render_frame_noalloc");
+    if (herr) return vxr::set_error(VXR_E_DEVICE, "vxr_render_frame_noalloc: device error flags 0x" + std::to_string(herr));
+    return VXR_OK;
+}

@@ -112,6 +112,7 @@ _SIGS = {
     "vxr_camera_begin_frame": [_P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts)],
     "vxr_camera_end_frame": [_P],
     "vxr_host_alloc": [C.c_size_t, C.POINTER(_P)], "vxr_host_free": [_P],
+    "vxr_render_frame_noalloc": [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts), _P, _P],
 }
 _RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
 
