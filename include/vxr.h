@@ -155,6 +155,15 @@ int vxr_world_arrays(const vxr_world* w, const uint32_t** grid, const uint32_t**
 /* Number of bricks in use (allocated minus recycled). */
 int vxr_world_brick_count(const vxr_world* w, uint32_t* in_use);
 
+/* ---- emitter clusters (no reference counterpart: the learned candidate proposal
+ * chooses a cluster, then an emitter inside it) ---------------------------------------- */
+/* Seeded k-means over light centres: k clusters (clamped to the light count),
+ * `iters` Lloyd iterations. Deterministic for a given light list and seed. Any later
+ * change of the light list invalidates the clustering (re-run it). */
+int vxr_world_cluster_lights(vxr_world* w, uint32_t k, uint32_t seed, uint32_t iters);
+/* Cluster id per light (valid until the next light-list change) and the cluster count. */
+int vxr_world_light_clusters(const vxr_world* w, const uint32_t** ids, uint32_t* k);
+
 /* ---- procedural scenes (no reference counterpart: the thesis scenes need assets
  * that are not available; these generate the benchmark worlds) -------------------- */
 #define VXR_EMIT_ABOVE_SURFACE 0  /* uniform (x,z), 1..8 voxels above the terrain */
@@ -303,13 +312,69 @@ int vxr_view_timer_end(vxr_view* v, float* ms);
  * accumulated image into host_rgba (W*H float4; page-locked memory is fastest), wait. */
 int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba);
 
+/* ---- learned candidate proposal (no reference counterpart) ------------------------------
+ * Replaces the uniform source pdf of RIS (GenerateLightCandidate, tools.cl:593-598) by a
+ * small network over the world's emitter clusters (vxr_world_cluster_lights): input =
+ * 2-level hash-grid encoding of the shading point + one-hot voxel side, 3 hidden ReLU
+ * layers, softmax over K clusters. A candidate draws cluster c from
+ * q(c) = (1 - epsilon) softmax_c + epsilon / K, then an emitter of c uniformly, and RIS
+ * weighs it with p_hat / (q(c) / |c|). Inference: BF16 tensor cores, FP32 accumulation.
+ * Training: online, weighted cross-entropy towards the cluster of each final reservoir's
+ * emitter (weight W * p_hat), Adam; FP32 kernels. */
+typedef struct vxr_proposal_desc {
+    uint32_t hidden;          /* hidden width (64) */
+    uint32_t table_log2;      /* hash-table entries per level, log2 (16) */
+    uint32_t res0, res1;      /* grid resolution of the two levels over the 1024^3 map (32, 128) */
+    float    epsilon;         /* weight of the uniform cluster mixture (0.1) */
+    float    learning_rate;   /* Adam (1e-3) */
+    uint32_t batch;           /* training samples per step (65536) */
+    uint32_t seed;            /* parameter initialisation */
+} vxr_proposal_desc;
+int vxr_proposal_default_desc(vxr_proposal_desc* d);
+/* Allocate and initialise the network for this view; K = the world's cluster count. */
+int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* d);
+/* on = 1: candidates come from the learned proposal; on = 0: uniform (the plain method). */
+int vxr_view_proposal_use(vxr_view* v, int on);
+/* `steps` Adam steps, each on a batch gathered from the view's current frame (hit
+ * pixels, final reservoirs); the last step's loss in *loss (may be NULL). */
+int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss);
+int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden);
+int vxr_view_proposal_get_params(vxr_view* v, float* out);
+int vxr_view_proposal_set_params(vxr_view* v, const float* in);
+/* Loss and gradient (no update) on caller samples: samples = B x (x, y, z, side code as
+ * uint32 bits; code = axis * 2 + (normal negative)), target cluster, weight. */
+int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const uint32_t* target,
+                           const float* weight, float* loss, float* grad);
+/* softmax probabilities (B x K) of the inference path for caller samples */
+int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float* probs);
+/* Checkpoint: parameters, Adam moments and step count (versioned binary). */
+int vxr_view_proposal_save(vxr_view* v, const char* path);
+int vxr_view_proposal_load(vxr_view* v, const char* path);
+
+/* ---- converged reference and error metric --------------------------------------------
+ * No counterpart on the reference's GPU path: its validation compared dumped frames
+ * offline against a path-traced ground truth (mse.cpp:252-391). Here a view keeps an
+ * optional FP64 running sum of its shaded frames (rgb). A converged reference is a view
+ * rendered with spatial and temporal reuse off (the unbiased RIS + visibility estimator,
+ * same shading) and summed over many frames with distinct seeds. */
+/* Clear the view's FP64 sum (allocates it on first use: width*height*3 doubles). */
+int vxr_view_sum64_reset(vxr_view* v);
+/* Add the current shaded frame (after VXR_STAGE_SHADE / vxr_view_render) to the sum. */
+int vxr_view_sum64_add(vxr_view* v);
+/* Frames summed so far, and the FP64 mean (width*height*3 doubles) when mean != NULL. */
+int vxr_view_sum64_mean(vxr_view* v, uint32_t* count, double* mean);
+/* CalculateMSE and CalculateRMAE (mse.cpp:33-65) of view img's image against view ref's
+ * FP64 mean (rounded to float as the reference's float images are): which = 0 the
+ * shaded frame, 1 the accumulator. Same resolution required. FP64 accumulation. */
+int vxr_view_error(vxr_view* img, int which, vxr_view* ref, double* mse, double* mae);
+
 /* ---- rendering without allocation ---------------------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc - an
  * application that owns all GPU memory through its own pool, a plugin that must not
  * bypass its host's allocator - this renders ONE frame from device buffers the caller
  * already owns into a device image the caller owns, and allocates nothing: no
  * cudaMalloc, cudaFree or allocating library call. The G-buffer, seeds, reservoirs, the
- * uber grid, the light table and the error word live in one fixed file-scope device
+ * hit list, the shadow-ray queue, the uber grid, the light table and the error word live in one fixed file-scope device
  * array of VXR_NOALLOC_SCRATCH_BYTES that every GPU loading libvxr.so holds until exit.
  *   grid      device uint32[128^3] top-level cells (layout of vxr_world_arrays)
  *   bricks    device uint32[nbricks * 512]; every brick cell must index below nbricks
@@ -329,7 +394,7 @@ int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[
  * caller. */
 #define VXR_NOALLOC_MAX_PIXELS    65536u     /* e.g. 256 x 256 */
 #define VXR_NOALLOC_MAX_LIGHTS    65536u
-#define VXR_NOALLOC_SCRATCH_BYTES 8159488u
+#define VXR_NOALLOC_SCRATCH_BYTES 10518784u
 int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* bricks, uint32_t nbricks,
                              const vxr_light* lights, uint32_t nlights, uint32_t light_model,
                              const vxr_frame_consts* k, float* out_rgba, void* stream);

@@ -18,9 +18,12 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvxr.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["kernels.cu", "runtime.cu", "noalloc.cu"]
-CPP_SOURCES = ["world.cpp", "scene.cpp", "camera.cpp", "capi_world.cpp"]
-HEADERS = ["device.cuh", "kernels.hpp", "world.hpp", "camera.hpp", "internal.hpp"]
+CU_SOURCES = ["kernels.cu", "runtime.cu", "noalloc.cu", "proposal.cu", "proposal_api.cu"]
+CPP_SOURCES = ["world.cpp", "scene.cpp", "camera.cpp", "capi_world.cpp", "cluster.cpp"]
+HEADERS = ["device.cuh", "kernels.hpp", "world.hpp", "camera.hpp", "internal.hpp", "proposal.cuh", "proposal.hpp", "view.hpp"]
+
+# the learned proposal is checked with tolerances, not bit for bit: FMA contraction on
+FMA_SOURCES = {"proposal.cu"}
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -60,7 +63,8 @@ def build(force=False, verbose=False):
     objs = []
     for s in CU_SOURCES:
         o = os.path.join(objdir, s + ".o")
-        jobs.append([NVCC, *NVCC_FLAGS, "-Xptxas", "-v", "-c", os.path.join(CSRC, s), "-o", o])
+        flags = [f for f in NVCC_FLAGS if f != "--fmad=false"] if s in FMA_SOURCES else NVCC_FLAGS
+        jobs.append([NVCC, *flags, "-Xptxas", "-v", "-c", os.path.join(CSRC, s), "-o", o])
         objs.append(o)
     for s in CPP_SOURCES:
         o = os.path.join(objdir, s + ".o")

@@ -12,6 +12,7 @@ int scene_generate(World& w, const vxr_scene_desc& d);
 int scene_height(const vxr_scene_desc* d, uint32_t x, uint32_t z, uint32_t* h);
 int camera_path(const vxr_scene_desc* d, uint32_t seed, uint32_t f, uint32_t n, float pos[3], float target[3]);
 void release_device_world(World& w);
+int cluster_lights(World& w, uint32_t k, uint32_t seed, uint32_t iters);
 
 static thread_local std::string g_err;
 int set_error(int code, const std::string& msg) {
@@ -125,6 +126,24 @@ int vxr_world_arrays(const vxr_world* w, const uint32_t** grid, const uint32_t**
 int vxr_world_brick_count(const vxr_world* w, uint32_t* in_use) {
     VXR_CHECK_ARG(w && in_use, "vxr_world_brick_count: null argument");
     *in_use = w->w.bricks_in_use();
+    return VXR_OK;
+}
+
+int vxr_world_cluster_lights(vxr_world* w, uint32_t k, uint32_t seed, uint32_t iters) {
+    VXR_CHECK_ARG(w, "vxr_world_cluster_lights: null world");
+    VXR_CHECK_ARG(k >= 1 && k <= 65536, "vxr_world_cluster_lights: k must be in [1, 65536]");
+    try {
+        return vxr::cluster_lights(w->w, k, seed, iters);
+    } catch (const std::bad_alloc&) {
+        return set_error(VXR_E_NOMEM, "vxr_world_cluster_lights: out of host memory");
+    }
+}
+
+int vxr_world_light_clusters(const vxr_world* w, const uint32_t** ids, uint32_t* k) {
+    VXR_CHECK_ARG(w && ids && k, "vxr_world_light_clusters: null argument");
+    const bool valid = w->w.clusterCount > 0 && w->w.lightCluster.size() == w->w.lights.size();
+    *ids = valid ? w->w.lightCluster.data() : nullptr;
+    *k = valid ? w->w.clusterCount : 0;
     return VXR_OK;
 }
 

@@ -1,22 +1,35 @@
-// kernels.cu - the five per-frame stage kernels of Voxel ReSTIR on sm_103a, plus the
+// kernels.cu - the per-frame stage kernels of Voxel ReSTIR on sm_103a, plus the
 // one-time world kernels (uber grid, light table).
 //
-// One thread per pixel on 2D tiles. Memory layout in HBM (per view):
+// Memory layout in HBM (per view):
 //   G-buffer   vd[2]  uint2  (voxel | side << 24, bits(dist))   current / previous frame
 //              seed   uint32 per-pixel xorshift32 state
 //   reservoirs C, H   uint4 + float4 planes (see Res in device.cuh), 32 B/pixel each:
 //              C = candidate+temporal output, H = spatial output = temporal history
 //   frame      float4 (rgb, dist); accum float4 (running mean, the output image)
+//   hits       uint32 list of the pixels whose primary ray hit a voxel
+//   queue      float4 x 2 per entry: shadow-ray requests (origin | pixel, dir | light)
+//   counters   uint32[8]: hit count, request count / fetch cursor of the two queues
 // The reference cycles two 80-byte reservoir buffers through three roles per frame
 // (world.cpp:2209-2219) and copies the shaded reservoir at the end of shading
 // (ris.cl:412). Here the spatial pass writes H in place of the previous history,
 // which the candidate pass has finished reading, and shading patches H on a failed
 // visibility test; H is then next frame's history without any copy.
+//
+// Work decomposition (wavefront): the reference runs one work item per pixel through
+// each whole kernel, so sky pixels idle beside terrain pixels and every warp waits for
+// its longest shadow ray. Here (1) hit pixels are compacted into a list, (2) the
+// candidate loop, the temporal step and the shading request run over that list, and
+// (3) every shadow ray goes through one persistent tracer whose lanes take a new ray
+// as soon as theirs ends. Each pixel's arithmetic is unchanged, so results are the
+// same bit for bit whatever order pixels and rays are processed in.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "device.cuh"
 #include "kernels.hpp"
+#include "proposal.hpp"
 
 namespace vxr {
 namespace dev {
@@ -90,6 +103,33 @@ __global__ void __launch_bounds__(128) albedo_kernel(World w, Frame k, uint2* __
     seeds[i] = seed;
 }
 
+// warp-aggregated append to a list: one atomic per group of lanes that call it together
+__device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+// Hit list for the frame; pixels without a hit get the empty reservoir (ris.cl:34,123).
+__global__ void __launch_bounds__(256) compact_hits_kernel(Frame k, const uint2* __restrict__ vd, uint32_t* __restrict__ hits,
+                                                           uint32_t* counters, uint4* __restrict__ cA,
+                                                           float4* __restrict__ cB) {
+    const uint32_t n = (uint32_t)k.W * (uint32_t)k.H;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t voxel = vd[i].x & 0x00FFFFFFu;
+        if (voxel != 0u) {
+            hits[append_slot(&counters[0])] = i;
+        } else {
+            cA[i] = make_uint4(0u, 6u << 29, 0u, 0u);
+            cB[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
 // ---- target function (phat.cl:2-41) ------------------------------------------------------
 // length(brdf * Le/pi * cos(theta) * cos(theta_l) * size^2 / d^2), NaN/Inf -> 0.
 // The zero cases are decided from signs before any division: N is an axis normal, so
@@ -131,24 +171,76 @@ __device__ __forceinline__ float phat(float3 pos, uint32_t ncode, float3 sp, uin
     return r;
 }
 
-// ---- visibility (isLightOccluded, ris.cl:1-17) ---------------------------------------
-// Shadow ray with the reference's budget of GRIDWIDTH (128) steps; a miss leaves
-// dist/side at 0 (the oracle's fixed convention for the reference's uninitialised
-// locals); visible iff the hit voxel lies in the emitter cube [pos, pos + size).
-__device__ __forceinline__ bool occluded(const World& w, float4 geom, float4 em, float3 o, float3 L) {
-    float d2 = 0.0f;
-    uint32_t s2 = 0;
-    trace<1>(w, o.x, o.y, o.z, L.x, L.y, L.z, 128, 0u, 0u, &d2, &s2);
+// ---- visibility (isLightOccluded, ris.cl:1-17) -----------------------------------------
+// Persistent shadow tracer. Requests: qA = (origin, bits(pixel)), qB = (dir, bits(light)).
+// Budget GRIDWIDTH = 128 steps (ris.cl:10); a miss leaves dist/side at 0 (the fixed
+// convention for the reference's uninitialised locals); visible iff the hit voxel
+// (hit point - 0.1 N, truncated) lies in the emitter cube [pos, pos + size)
+// (GridCoordinatesFromHit / Uint3CubeEquals, tools.cl:452-472). An occluded request
+// zeroes sumOfWeights of its pixel in `plane` (W follows: ris.cl:79-80, 248-250).
+// Lanes refill from the queue as soon as enough of them are idle.
+__device__ __forceinline__ void shadow_finish(const World& w, int st, const Walker& wk, float3 o, float3 L, uint32_t pix,
+                                              uint32_t li, uint32_t* plane) {
+    const float d2 = st == WALK_HIT ? wk.dist : 0.0f;
+    const uint32_t s2 = st == WALK_HIT ? wk.side : 0u;
     const float ns = side_sign(s2, L);
     const float hx = L.x * d2 + o.x, hy = L.y * d2 + o.y, hz = L.z * d2 + o.z;
     const uint32_t vx = f2u(hx - (s2 == 0 ? ns * 0.1f : 0.0f));
     const uint32_t vy = f2u(hy - (s2 == 1 ? ns * 0.1f : 0.0f));
     const uint32_t vz = f2u(hz - (s2 == 2 ? ns * 0.1f : 0.0f));
-    const uint32_t pos = __float_as_uint(em.w);
+    const uint32_t pos = __float_as_uint(__ldg(&w.lemit[li].w));
+    const uint32_t size = (uint32_t)__ldg(&w.lgeom[li].w);
     const uint32_t ey = pos / (1024u * 1024u), ez = (pos / 1024u) % 1024u, ex = pos % 1024u;
-    const uint32_t size = (uint32_t)geom.w;
     const bool inside = ex <= vx && ex + size > vx && ey <= vy && ey + size > vy && ez <= vz && ez + size > vz;
-    return !inside;
+    if (!inside) plane[(size_t)pix * 4u + 2u] = 0u;
+}
+
+__global__ void __launch_bounds__(128) shadow_kernel(World w, const float4* __restrict__ qA, const float4* __restrict__ qB,
+                                                     const uint32_t* count, uint32_t* fetch, uint32_t* plane,
+                                                     int refill) {
+    const uint32_t n = *count;
+    const int lane = threadIdx.x & 31;
+    Walker wk;
+    bool active = false, exhausted = false;
+    float3 o = f3(0.0f, 0.0f, 0.0f), L = f3(0.0f, 0.0f, 0.0f);
+    uint32_t pix = 0, li = 0;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && (idle == 0xffffffffu || __popc(idle) >= refill)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(fetch, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (!active) {
+                const uint32_t r = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (r < n) {
+                    const float4 a = __ldg(qA + r), b = __ldg(qB + r);
+                    o = f3(a.x, a.y, a.z);
+                    L = f3(b.x, b.y, b.z);
+                    pix = __float_as_uint(a.w);
+                    li = __float_as_uint(b.w);
+                    const int st = walk_init(wk, w, o.x, o.y, o.z, L.x, L.y, L.z, 128);
+                    if (st == WALK_CONTINUE) active = true;
+                    else shadow_finish(w, st, wk, o, L, pix, li, plane);
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active) {
+#pragma unroll 1
+            for (int s = 0; s < 4; s++) {
+                const int st = walk_step(wk, w);
+                if (st != WALK_CONTINUE) {
+                    shadow_finish(w, st, wk, o, L, pix, li, plane);
+                    active = false;
+                    break;
+                }
+            }
+        }
+    }
 }
 
 // Area-light sample (RandomPointOnVoxel, tools.cl:499-577): one random point per face
@@ -219,20 +311,32 @@ __device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32
     return face_point(g, index, r0, r1);
 }
 
-// ---- stage 2: candidates + visibility + temporal (perPixelInitialSampling, ris.cl:20-124) ----
-template <bool POINT>
-__global__ void __launch_bounds__(128) candidates_kernel(World w, Frame k, const uint2* __restrict__ vd,
-                                                         const uint2* __restrict__ vdPrev, uint32_t* __restrict__ seeds,
-                                                         const uint4* __restrict__ hA, const float4* __restrict__ hB,
-                                                         uint4* __restrict__ cA, float4* __restrict__ cB, uint32_t* err) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= k.W || y >= k.H) return;
-    const size_t i = (size_t)y * k.W + x;
-    const uint2 g = vd[i];
-    const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
-    const float dist = __uint_as_float(g.y);
-    Res res = res_zero();
-    if (voxel != 0u) {
+// ---- stage 2a: candidates (perPixelInitialSampling, ris.cl:20-82) ---------------------------
+// Over the hit list. Ends with AdjustWeight(res, res.pHat) (implied by the stored
+// sumW, pHat, M) and a shadow-ray request for the selected sample when sumW > 0 (when
+// sumW == 0 the discard of ris.cl:79-80 changes nothing).
+// LEARNED: the light index comes from the learned proposal instead of
+// GenerateLightCandidate: cluster c with probability q(c) (drawn by the inference kernel),
+// then a member of c uniformly; the source pdf p = q(c) / |c| replaces 1 / N.
+struct LearnedLists {
+    const uint2* cand;          // [hit][kMaxCand] (cluster, bits(q))
+    const uint32_t* clOff;      // cluster c members: clMembers[clOff[c] .. clOff[c+1])
+    const uint32_t* clMembers;
+};
+
+template <bool POINT, bool LEARNED>
+__global__ void __launch_bounds__(128) ris_kernel(World w, Frame k, const uint2* __restrict__ vd,
+                                                  uint32_t* __restrict__ seeds, const uint32_t* __restrict__ hits,
+                                                  uint32_t* counters, uint4* __restrict__ cA, float4* __restrict__ cB,
+                                                  float4* __restrict__ qA, float4* __restrict__ qB, LearnedLists ll) {
+    const uint32_t nh = counters[0];
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
+        const uint32_t i = hits[j];
+        const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
+        const uint2 g = vd[i];
+        const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
+        const float dist = __uint_as_float(g.y);
+        Res res = res_zero();
         uint32_t seed = seeds[i];
         const float3 D = camera_ray(k, x, y);
         const float nsign = side_sign(side, D);
@@ -241,10 +345,20 @@ __global__ void __launch_bounds__(128) candidates_kernel(World w, Frame k, const
         const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
                               sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
         const uint32_t nL = k.nlights;
-        const float p = 1.0f / (float)nL;
+        const float puni = 1.0f / (float)nL;
         for (uint32_t c = 0; c < k.ncand; c++) {
-            // GenerateLightCandidate (tools.cl:593-598)
-            const int li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
+            int li;
+            float p = puni;
+            if (LEARNED) {
+                const uint2 cq = __ldg(ll.cand + (size_t)j * prop::kMaxCand + c);
+                const uint32_t off = __ldg(ll.clOff + cq.x), sz = __ldg(ll.clOff + cq.x + 1) - off;
+                const uint32_t mi = min((uint32_t)f2i(rnd(seed) * (float)sz), sz - 1u);
+                li = (int)__ldg(ll.clMembers + off + mi);
+                p = __uint_as_float(cq.y) / (float)sz;
+            } else {
+                // GenerateLightCandidate (tools.cl:593-598)
+                li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
+            }
             const float4 lg = __ldg(w.lgeom + li);
             const float4 le = __ldg(w.lemit + li);
             float3 pos;
@@ -260,49 +374,65 @@ __global__ void __launch_bounds__(128) candidates_kernel(World w, Frame k, const
             const float ph = phat<POINT>(pos, nc, sp, side, nsign, brdf, le, lg.w) * inv;
             res_update(res, ph / p, ph, (uint32_t)li, rnd(seed), pos, inv, nc);
         }
-        // AdjustWeight with the selected pHat; visibility of the selected sample
-        if (k.ncand > 0) {
-            const uint32_t li = res.idx;
-            const float4 lg = __ldg(w.lgeom + li), le = __ldg(w.lemit + li);
+        if (k.ncand > 0 && res.sumW > 0.0f) {
             const float3 L = normalize3(sub(res.pos, spo));
-            if (occluded(w, lg, le, spo, L)) res.sumW = 0.0f;   // W = 0 follows from sumW = 0
+            const uint32_t slot = append_slot(&counters[1]);
+            qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(i));
+            qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(res.idx));
         }
-        // temporal reuse (ris.cl:84-119)
-        if (k.restirtemporalframe > 0 && k.temporal) {
-            const float dl = ((sp.x * k.Nl.x + sp.y * k.Nl.y) + sp.z * k.Nl.z) - k.Nl.w;
-            const float dr = ((sp.x * k.Nr.x + sp.y * k.Nr.y) + sp.z * k.Nr.z) - k.Nr.w;
-            const float dt = ((sp.x * k.Nt.x + sp.y * k.Nt.y) + sp.z * k.Nt.z) - k.Nt.w;
-            const float db = ((sp.x * k.Nb.x + sp.y * k.Nb.y) + sp.z * k.Nb.z) - k.Nb.w;
-            const float up = (float)k.W * (dl / (dl + dr));
-            const float vp = (float)k.H * (dt / (dt + db));
-            const float ru = roundf(up), rv = roundf(vp);
-            if (ru == ru && rv == rv) {
-                const int px = f2i(ru), py = f2i(rv);
-                if (px >= 0 && py >= 0 && px < k.W && py < k.H) {
-                    const size_t j = (size_t)py * k.W + px;
-                    const uint2 pg = __ldg(vdPrev + j);
-                    const uint32_t pside = pg.x >> 24;
-                    const float pdist = __uint_as_float(pg.y);
-                    if (pside == side && fabsf(dist - pdist) <= 0.1f * dist) {
-                        Res prev = res_load(hA, hB, j);
-                        const uint32_t pm = min(k.maxTemporal * k.ncand, prev.M);
-                        if (pm > 0u) {
-                            uint32_t pli = prev.idx;
-                            if (pli >= nL) { raise_error(err, 2u); pli = 0; }
-                            const float4 pg4 = __ldg(w.lgeom + pli), pe4 = __ldg(w.lemit + pli);
-                            const float pph = phat<POINT>(prev.pos, prev.ncode, sp, side, nsign, brdf, pe4, pg4.w) * prev.inv;
-                            const float W = res_W(prev);
-                            res_reweigh(prev, W, pph, pm);
-                            res_combine(res, prev, rnd(seed));
-                            // AdjustWeight(res, pHat of the selected sample here) equals res.pHat
-                        }
-                    }
-                }
-            }
-        }
+        res_store(cA, cB, i, res);
         seeds[i] = seed;
     }
-    res_store(cA, cB, i, res);
+}
+
+// ---- stage 2c: temporal reuse (ris.cl:84-119) over the hit list, after visibility ------------
+template <bool POINT>
+__global__ void __launch_bounds__(128) temporal_kernel(World w, Frame k, const uint2* __restrict__ vd,
+                                                       const uint2* __restrict__ vdPrev, uint32_t* __restrict__ seeds,
+                                                       const uint32_t* __restrict__ hits, const uint32_t* counters,
+                                                       const uint4* __restrict__ hA, const float4* __restrict__ hB,
+                                                       uint4* __restrict__ cA, float4* __restrict__ cB, uint32_t* err) {
+    const uint32_t nh = counters[0];
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
+        const uint32_t i = hits[j];
+        const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
+        const uint2 g = vd[i];
+        const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
+        const float dist = __uint_as_float(g.y);
+        const float3 D = camera_ray(k, x, y);
+        const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+        const float dl = ((sp.x * k.Nl.x + sp.y * k.Nl.y) + sp.z * k.Nl.z) - k.Nl.w;
+        const float dr = ((sp.x * k.Nr.x + sp.y * k.Nr.y) + sp.z * k.Nr.z) - k.Nr.w;
+        const float dt = ((sp.x * k.Nt.x + sp.y * k.Nt.y) + sp.z * k.Nt.z) - k.Nt.w;
+        const float db = ((sp.x * k.Nb.x + sp.y * k.Nb.y) + sp.z * k.Nb.z) - k.Nb.w;
+        const float up = (float)k.W * (dl / (dl + dr));
+        const float vp = (float)k.H * (dt / (dt + db));
+        const float ru = roundf(up), rv = roundf(vp);
+        if (!(ru == ru && rv == rv)) continue;
+        const int px = f2i(ru), py = f2i(rv);
+        if (px < 0 || py < 0 || px >= k.W || py >= k.H) continue;
+        const size_t jp = (size_t)py * k.W + px;
+        const uint2 pg = __ldg(vdPrev + jp);
+        const float pdist = __uint_as_float(pg.y);
+        if ((pg.x >> 24) != side || !(fabsf(dist - pdist) <= 0.1f * dist)) continue;
+        Res prev = res_load(hA, hB, jp);
+        const uint32_t pm = min(k.maxTemporal * k.ncand, prev.M);
+        if (pm == 0u) continue;
+        uint32_t pli = prev.idx;
+        if (pli >= k.nlights) { raise_error(err, 2u); pli = 0; }
+        const float nsign = side_sign(side, D);
+        const float3 brdf = mul(to_rgb(voxel), 0.31830988618379067153777f);
+        const float4 pg4 = __ldg(w.lgeom + pli), pe4 = __ldg(w.lemit + pli);
+        const float pph = phat<POINT>(prev.pos, prev.ncode, sp, side, nsign, brdf, pe4, pg4.w) * prev.inv;
+        const float W = res_W(prev);
+        res_reweigh(prev, W, pph, pm);
+        Res res = res_load(cA, cB, i);
+        uint32_t seed = seeds[i];
+        res_combine(res, prev, rnd(seed));
+        // AdjustWeight(res, pHat of the selected sample here) equals res.pHat
+        res_store(cA, cB, i, res);
+        seeds[i] = seed;
+    }
 }
 
 // ---- stage 3: spatial reuse (perPixelSpatialResampling, ris.cl:126-151,
@@ -357,13 +487,45 @@ __global__ void __launch_bounds__(128) spatial_kernel(World w, Frame k, const ui
     res_store(hA, hB, i, res);
 }
 
-// ---- stage 4+5: shading (renderRIS / render_di_ris, ris.cl:155-293, 391-413) fused with
-//      accumulation (accumulatorFinalizer, kernels.cl:304-326) -----------------------------
+// ---- stage 4: shading (renderRIS / render_di_ris, ris.cl:155-293, 391-413) ------------------
+// 4a: a shadow-ray request for every hit pixel whose reservoir has W > 0 and M > 0.
+__global__ void __launch_bounds__(128) shade_request_kernel(Frame k, const uint2* __restrict__ vd,
+                                                            const uint32_t* __restrict__ hits, uint32_t* counters,
+                                                            const uint4* __restrict__ hA, const float4* __restrict__ hB,
+                                                            float4* __restrict__ qA, float4* __restrict__ qB, uint32_t* err) {
+    const uint32_t nh = counters[0];
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
+        const uint32_t i = hits[j];
+        const uint4 qa = hA[i];
+        const uint32_t M = qa.y & 0x1FFFFFFFu;
+        const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, __uint_as_float(qa.w) * (float)M);
+        if (!(W > 0.0f && M > 0u)) continue;
+        const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
+        const uint2 g = vd[i];
+        const uint32_t side = g.x >> 24;
+        const float dist = __uint_as_float(g.y);
+        const float3 D = camera_ray(k, x, y);
+        const float nsign = side_sign(side, D);
+        const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+        const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
+                              sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
+        uint32_t li = qa.x;
+        if (li >= k.nlights) { raise_error(err, 8u); li = 0; }
+        const float4 qb = __ldg(hB + i);
+        const float3 L = normalize3(sub(f3(qb.x, qb.y, qb.z), spo));
+        const uint32_t slot = append_slot(&counters[3]);
+        qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(i));
+        qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(li));
+    }
+}
+
+// 4c: colour per pixel once visibility has zeroed the occluded reservoirs; optionally
+// fused with the accumulator (accumulatorFinalizer, kernels.cl:304-326).
 template <bool POINT>
-__global__ void __launch_bounds__(128) shade_kernel(World w, Frame k, const uint2* __restrict__ vd,
-                                                    uint4* __restrict__ hA, const float4* __restrict__ hB,
-                                                    float4* __restrict__ frame, float4* __restrict__ accum,
-                                                    int fuse_accumulate, uint32_t* err) {
+__global__ void __launch_bounds__(128) shade_finish_kernel(World w, Frame k, const uint2* __restrict__ vd,
+                                                           const uint4* __restrict__ hA, const float4* __restrict__ hB,
+                                                           float4* __restrict__ frame, float4* __restrict__ accum,
+                                                           int fuse_accumulate) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= k.W || y >= k.H) return;
     const size_t i = (size_t)y * k.W + x;
@@ -379,31 +541,20 @@ __global__ void __launch_bounds__(128) shade_kernel(World w, Frame k, const uint
             color = add(color, f3((c.x * m) * INVPI, (c.y * m) * INVPI, (c.z * m) * INVPI));
         }
         const uint4 qa = hA[i];
-        const float sumW = __uint_as_float(qa.z), pH = __uint_as_float(qa.w);
         const uint32_t M = qa.y & 0x1FFFFFFFu;
-        const float W = sumW / fmaxf(1e-5f, pH * (float)M);
-        if (W > 0.0f && M > 0u) {
+        const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, __uint_as_float(qa.w) * (float)M);
+        if (W > 0.0f && M > 0u) {   // visible: occluded reservoirs were zeroed by the tracer
             const uint32_t side = g.x >> 24;
             const float4 qb = __ldg(hB + i);
             const float3 D = camera_ray(k, x, y);
             const float nsign = side_sign(side, D);
             const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
-            const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
-                                  sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
-            uint32_t li = qa.x;
-            if (li >= k.nlights) { raise_error(err, 8u); li = 0; }
+            const uint32_t li = qa.x < k.nlights ? qa.x : 0u;
             const float4 lg = __ldg(w.lgeom + li), le = __ldg(w.lemit + li);
-            const float3 pos = f3(qb.x, qb.y, qb.z);
-            const float3 L = normalize3(sub(pos, spo));
-            if (!occluded(w, lg, le, spo, L)) {
-                const float3 brdf = mul(to_rgb(voxel), INVPI);
-                bool zero;
-                const float3 inc = phat_full<POINT>(pos, qa.y >> 29, sp, side, nsign, brdf, le, lg.w, &zero);
-                color = add(color, f3((inc.x * W) * qb.w, (inc.y * W) * qb.w, (inc.z * W) * qb.w));
-            } else {
-                // discard: W = sumOfWeights = 0 written back into the history
-                hA[i] = make_uint4(qa.x, qa.y, 0u, qa.w);
-            }
+            const float3 brdf = mul(to_rgb(voxel), INVPI);
+            bool zero;
+            const float3 inc = phat_full<POINT>(f3(qb.x, qb.y, qb.z), qa.y >> 29, sp, side, nsign, brdf, le, lg.w, &zero);
+            color = add(color, f3((inc.x * W) * qb.w, (inc.y * W) * qb.w, (inc.z * W) * qb.w));
         }
         const float a = alphaf(voxel);
         color = f3(color.x + ((a * color.x) + ((1.0f - a) * 0.0f)), color.y + ((a * color.y) + ((1.0f - a) * 0.0f)),
@@ -445,6 +596,23 @@ static dim3 grid_for(const dev::Frame& k, LaunchShape sh) {
     return dim3((unsigned)((k.W + sh.bx - 1) / sh.bx), (unsigned)((k.H + sh.by - 1) / sh.by), 1);
 }
 
+static int g_sms = 0;
+static int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+// grid-stride kernels over a list of at most n items
+static unsigned list_blocks(size_t n, int threads, int per_sm) {
+    const size_t need = (n + threads - 1) / threads;
+    const size_t cap = (size_t)sm_count() * per_sm;
+    return (unsigned)std::max<size_t>(1, std::min(need, cap));
+}
+
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s) {
     if (n == 0) return;
     dev::build_light_table_kernel<<<(n + 255) / 256, 256, 0, s>>>(raw, n, geom, emit);
@@ -458,14 +626,56 @@ void launch_albedo(const dev::World& w, const dev::Frame& k, const ViewBuffers& 
     dev::albedo_kernel<<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.seed);
 }
 
+static int g_shadow_per_sm = 0;
+static void launch_shadow(const dev::World& w, const ViewBuffers& b, const uint32_t* count, uint32_t* fetch,
+                          uint32_t* plane, size_t max_rays, cudaStream_t s) {
+    // persistent: exactly the blocks that fit on the machine at once, never more than the rays
+    if (!g_shadow_per_sm) {
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dev::shadow_kernel, 128, 0) != cudaSuccess || per < 1) per = 4;
+        g_shadow_per_sm = per;
+    }
+    dev::shadow_kernel<<<list_blocks(max_rays, 128, g_shadow_per_sm), 128, 0, s>>>(w, b.qA, b.qB, count, fetch, plane, 8);
+}
+
 void launch_candidates(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh,
-                       cudaStream_t s) {
-    if (point)
-        dev::candidates_kernel<true><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.vd[cur ^ 1], b.seed,
-                                                                                  b.hA, b.hB, b.cA, b.cB, b.err);
-    else
-        dev::candidates_kernel<false><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.vd[cur ^ 1], b.seed,
-                                                                                   b.hA, b.hB, b.cA, b.cB, b.err);
+                       cudaStream_t s, const LearnedHook* learned) {
+    (void)sh;
+    const size_t n = (size_t)k.W * k.H;
+    cudaMemsetAsync(b.counters, 0, 8 * sizeof(uint32_t), s);
+    dev::compact_hits_kernel<<<list_blocks(n, 256, 8), 256, 0, s>>>(k, b.vd[cur], b.hits, b.counters, b.cA, b.cB);
+    const unsigned nb = list_blocks(n, 128, 16);
+    dev::LearnedLists ll{nullptr, nullptr, nullptr};
+    if (learned && k.ncand > 0) {
+        prop::InferArgs ia = learned->infer;
+        ia.k = k;
+        ia.vd = b.vd[cur];
+        ia.hits = b.hits;
+        ia.count = b.counters;
+        ia.ncand = k.ncand;
+        ia.cand = learned->cand;
+        ia.samples = nullptr;
+        ia.probs = nullptr;
+        prop::launch_infer(ia, (uint32_t)n, s);
+        ll = dev::LearnedLists{learned->cand, learned->clOff, learned->clMembers};
+        if (point)
+            dev::ris_kernel<true, true><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
+        else
+            dev::ris_kernel<false, true><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
+    } else if (point) {
+        dev::ris_kernel<true, false><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
+    } else {
+        dev::ris_kernel<false, false><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
+    }
+    launch_shadow(w, b, &b.counters[1], &b.counters[2], (uint32_t*)b.cA, n, s);
+    if (k.restirtemporalframe > 0 && k.temporal) {
+        if (point)
+            dev::temporal_kernel<true><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.vd[cur ^ 1], b.seed, b.hits, b.counters, b.hA,
+                                                          b.hB, b.cA, b.cB, b.err);
+        else
+            dev::temporal_kernel<false><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.vd[cur ^ 1], b.seed, b.hits, b.counters,
+                                                           b.hA, b.hB, b.cA, b.cB, b.err);
+    }
 }
 
 void launch_spatial(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh,
@@ -480,16 +690,78 @@ void launch_spatial(bool point, const dev::World& w, const dev::Frame& k, const 
 
 void launch_shade(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool fuse_accumulate,
                   LaunchShape sh, cudaStream_t s) {
+    const size_t n = (size_t)k.W * k.H;
+    dev::shade_request_kernel<<<list_blocks(n, 128, 16), 128, 0, s>>>(k, b.vd[cur], b.hits, b.counters, b.hA, b.hB, b.qA,
+                                                                      b.qB, b.err);
+    launch_shadow(w, b, &b.counters[3], &b.counters[4], (uint32_t*)b.hA, n, s);
     if (point)
-        dev::shade_kernel<true><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.hA, b.hB, b.frame, b.accum,
-                                                                             fuse_accumulate ? 1 : 0, b.err);
+        dev::shade_finish_kernel<true><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.hA, b.hB, b.frame,
+                                                                                    b.accum, fuse_accumulate ? 1 : 0);
     else
-        dev::shade_kernel<false><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.hA, b.hB, b.frame,
-                                                                              b.accum, fuse_accumulate ? 1 : 0, b.err);
+        dev::shade_finish_kernel<false><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.hA, b.hB, b.frame,
+                                                                                     b.accum, fuse_accumulate ? 1 : 0);
 }
 
 void launch_accumulate(const dev::Frame& k, const ViewBuffers& b, LaunchShape sh, cudaStream_t s) {
     dev::accumulate_kernel<<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(k, b.frame, b.accum);
+}
+
+}  // namespace vxr
+
+// ---- converged reference and error metric ----------------------------------------------
+namespace vxr {
+namespace dev {
+
+// FP64 running sum of the shaded frame's rgb (converged reference render).
+__global__ void __launch_bounds__(256) sum64_add_kernel(const float4* __restrict__ frame, double* __restrict__ sum,
+                                                        uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 f = frame[i];
+        sum[3 * (size_t)i + 0] += (double)f.x;
+        sum[3 * (size_t)i + 1] += (double)f.y;
+        sum[3 * (size_t)i + 2] += (double)f.z;
+    }
+}
+
+// CalculateMSE / CalculateRMAE (mse.cpp:33-65): the ground truth is the FP64 mean
+// rounded to float (the reference compares float images); per pixel the squared and
+// absolute channel errors are summed in float as mse.cpp does, then accumulated in FP64.
+__global__ void __launch_bounds__(256) error_kernel(const float4* __restrict__ img, const double* __restrict__ sum,
+                                                    double inv_count, uint32_t n, double* out) {
+    double se = 0.0, ae = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 x = img[i];
+        const float gx = (float)(sum[3 * (size_t)i + 0] * inv_count);
+        const float gy = (float)(sum[3 * (size_t)i + 1] * inv_count);
+        const float gz = (float)(sum[3 * (size_t)i + 2] * inv_count);
+        const float dx = gx - x.x, dy = gy - x.y, dz = gz - x.z;
+        se += (double)((dx * dx + dy * dy) + dz * dz);
+        ae += (double)((fabsf(dx) + fabsf(dy)) + fabsf(dz));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        se += __shfl_down_sync(0xffffffffu, se, o);
+        ae += __shfl_down_sync(0xffffffffu, ae, o);
+    }
+    __shared__ double s_se[8], s_ae[8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { s_se[warp] = se; s_ae[warp] = ae; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) { a += s_se[i]; b += s_ae[i]; }
+        atomicAdd(&out[0], a);
+        atomicAdd(&out[1], b);
+    }
+}
+
+}  // namespace dev
+
+void launch_sum64_add(const float4* frame, double* sum, uint32_t n, cudaStream_t s) {
+    dev::sum64_add_kernel<<<list_blocks(n, 256, 8), 256, 0, s>>>(frame, sum, n);
+}
+
+void launch_error(const float4* img, const double* sum, double inv_count, uint32_t n, double* out, cudaStream_t s) {
+    dev::error_kernel<<<list_blocks(n, 256, 4), 256, 0, s>>>(img, sum, inv_count, n, out);
 }
 
 }  // namespace vxr

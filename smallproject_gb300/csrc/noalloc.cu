@@ -5,10 +5,11 @@
 // must not be bypassed, or code running while a CUDA graph is being recorded elsewhere.
 // vxr_render_frame_noalloc renders one frame for them from device buffers they already
 // own (the world grid, its bricks and the light list) into an image buffer they own.
-// Everything else the frame needs - G-buffer, seeds, both reservoir planes, the 32^3
-// uber grid, the per-light table and the device error word - lives in one file-scope
+// Everything else the frame needs - G-buffer, seeds, both reservoir planes, the hit
+// list, the shadow-ray queue, the 32^3 uber grid, the per-light table, the counters and
+// the device error word - lives in one file-scope
 // __device__ array of fixed size, which every GPU that loads this library holds until
-// the process exits (VXR_NOALLOC_SCRATCH_BYTES = 8,159,488 bytes, 7.8 MiB).
+// the process exits (VXR_NOALLOC_SCRATCH_BYTES = 10,518,784 bytes, 10.0 MiB).
 //
 // The stage kernels are the ones the view path launches; only the buffers differ.
 #include <cstring>
@@ -35,11 +36,15 @@ constexpr size_t kOffUber = kOffHB + 16 * kMaxPx;              // uint8 [32^3]
 constexpr size_t kOffGeom = kOffUber + 32 * 32 * 32;           // float4 [kMaxLights]
 constexpr size_t kOffEmit = kOffGeom + 16 * kMaxLights;        // float4 [kMaxLights]
 constexpr size_t kOffRaw = kOffEmit + 16 * kMaxLights;         // uint4 [kMaxLights]
-constexpr size_t kOffErr = kOffRaw + 16 * kMaxLights;          // uint32 error word (+ pad)
+constexpr size_t kOffHits = kOffRaw + 16 * kMaxLights;         // uint32 [kMaxPx] hit list
+constexpr size_t kOffQA = kOffHits + 4 * kMaxPx;               // float4 [kMaxPx] shadow requests
+constexpr size_t kOffQB = kOffQA + 16 * kMaxPx;                // float4 [kMaxPx]
+constexpr size_t kOffErr = kOffQB + 16 * kMaxPx;               // uint32 error word, then 8 counters
 constexpr size_t kScratchBytes = kOffErr + 256;
 static_assert(kScratchBytes == VXR_NOALLOC_SCRATCH_BYTES, "scratch size must match the header");
 static_assert(kOffSeed % 256 == 0 && kOffCA % 256 == 0 && kOffUber % 256 == 0 && kOffGeom % 256 == 0 &&
-                  kOffErr % 256 == 0, "scratch regions must stay 256-byte aligned");
+                  kOffHits % 256 == 0 && kOffQA % 256 == 0 && kOffErr % 256 == 0,
+              "scratch regions must stay 256-byte aligned");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -178,6 +183,10 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     b.frame = (float4*)out_rgba;
     b.accum = (float4*)out_rgba;             // unused: shading runs without the accumulate fusion
     b.err = err;
+    b.hits = (uint32_t*)(s + kOffHits);
+    b.qA = (float4*)(s + kOffQA);
+    b.qB = (float4*)(s + kOffQB);
+    b.counters = (uint32_t*)(s + kOffErr + 64);
     const bool point = light_model == VXR_LIGHTS_POINT;
     const vxr::LaunchShape sh;
     vxr::launch_albedo(w, f, b, 0, sh, st);

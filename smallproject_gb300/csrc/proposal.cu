@@ -1,0 +1,584 @@
+// proposal.cu - kernels of the learned candidate proposal (see proposal.cuh).
+//
+// Inference (one launch per frame, over the hit-pixel list): per warp of 32 pixels the
+// hash-grid encoding is built in shared memory, the MLP runs on the tensor cores with
+// BF16 mma.sync.m16n8k16 (FP32 accumulation, hidden layers kept in registers: the
+// accumulator fragment of one layer is the A fragment of the next), the K logits land
+// in shared memory as FP16, and every lane draws its pixel's candidate clusters from
+// q = (1 - eps) softmax + eps / K with a two-level (16 groups) inverse CDF. Output per
+// pixel: kMaxCand (cluster, q(cluster)) pairs that the candidate kernel consumes.
+//
+// Training (FP32 CUDA cores): batch gather from the reservoirs, encoding, a tiled
+// strided GEMM with fused epilogues for every forward / backward product, softmax
+// cross-entropy, encoding scatter, Adam.
+//
+// This file builds with FMA contraction on: the learned path is checked against FP64
+// with tolerances, not bit for bit.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "device.cuh"
+#include "proposal.cuh"
+#include "proposal.hpp"
+
+namespace vxr {
+namespace prop {
+
+// ---- hash-grid encoding ------------------------------------------------------------------
+__device__ __forceinline__ uint32_t grid_hash(uint32_t x, uint32_t y, uint32_t z, uint32_t mask) {
+    return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & mask;
+}
+
+struct Corner {
+    uint32_t idx[kLevels][8];
+    float w[kLevels][8];
+};
+
+// corner table indices and trilinear weights of point p (map coordinates) on both levels
+__device__ __forceinline__ void corners(const Dims& d, float px, float py, float pz, Corner& c) {
+    const uint32_t mask = (1u << d.tableLog2) - 1u;
+#pragma unroll
+    for (int l = 0; l < kLevels; l++) {
+        const int R = l == 0 ? d.res0 : d.res1;
+        const float s = (float)R * (1.0f / 1024.0f);
+        const float ux = fminf(fmaxf(px * s, 0.0f), (float)R), uy = fminf(fmaxf(py * s, 0.0f), (float)R),
+                    uz = fminf(fmaxf(pz * s, 0.0f), (float)R);
+        const int ix = min((int)ux, R - 1), iy = min((int)uy, R - 1), iz = min((int)uz, R - 1);
+        const float fx = ux - (float)ix, fy = uy - (float)iy, fz = uz - (float)iz;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
+            c.idx[l][q] = (uint32_t)l * (mask + 1u) + grid_hash((uint32_t)(ix + ox), (uint32_t)(iy + oy), (uint32_t)(iz + oz), mask);
+            c.w[l][q] = (ox ? fx : 1.0f - fx) * (oy ? fy : 1.0f - fy) * (oz ? fz : 1.0f - fz);
+        }
+    }
+}
+
+// network input row: 16 encoding features, one-hot side (6), zeros
+__device__ __forceinline__ void input_row(const float* __restrict__ enc, const Dims& d, float4 pin, float* x) {
+    Corner c;
+    corners(d, pin.x, pin.y, pin.z, c);
+#pragma unroll
+    for (int l = 0; l < kLevels; l++) {
+        float a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const float4* e = reinterpret_cast<const float4*>(enc + (size_t)c.idx[l][q] * kFeat);
+            const float4 e0 = __ldg(e), e1 = __ldg(e + 1);
+            const float w = c.w[l][q];
+            a[0] += w * e0.x; a[1] += w * e0.y; a[2] += w * e0.z; a[3] += w * e0.w;
+            a[4] += w * e1.x; a[5] += w * e1.y; a[6] += w * e1.z; a[7] += w * e1.w;
+        }
+#pragma unroll
+        for (int f = 0; f < 8; f++) x[l * 8 + f] = a[f];
+    }
+    const uint32_t code = __float_as_uint(pin.w);
+#pragma unroll
+    for (int s = 0; s < 6; s++) x[16 + s] = (code == (uint32_t)s) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int s = 22; s < kIn; s++) x[s] = 0.0f;
+}
+
+// side code of a voxel face: axis * 2 + (normal points to negative axis)
+__device__ __forceinline__ uint32_t side_code(uint32_t side, float nsign) { return side * 2u + (nsign < 0.0f ? 1u : 0u); }
+
+// ---- tensor-core helpers (mma.sync m16n8k16, BF16 in, FP32 accumulate) ------------------
+__device__ __forceinline__ void mma16816(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// one hidden layer on register fragments: out = relu(in * W^T + b); in/out as A fragments
+// act[mt][kt][4] for 2 m-tiles (32 rows) and H/16 k-tiles
+template <int H>
+__device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][H / 16][4], uint32_t (&out)[2][H / 16][4],
+                                             const __nv_bfloat16* Ws, int ldw, const float* bs, int g, int t) {
+    float c[2][H / 8][4];
+#pragma unroll
+    for (int nt = 0; nt < H / 8; nt++) {
+        const float b0 = bs[nt * 8 + 2 * t], b1 = bs[nt * 8 + 2 * t + 1];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) { c[mt][nt][0] = b0; c[mt][nt][1] = b1; c[mt][nt][2] = b0; c[mt][nt][3] = b1; }
+    }
+#pragma unroll
+    for (int kt = 0; kt < H / 16; kt++) {
+#pragma unroll
+        for (int nt = 0; nt < H / 8; nt++) {
+            const __nv_bfloat16* row = Ws + (size_t)(nt * 8 + g) * ldw + kt * 16 + 2 * t;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
+            mma16816(c[0][nt], in[0][kt], b0, b1);
+            mma16816(c[1][nt], in[1][kt], b0, b1);
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int kt = 0; kt < H / 16; kt++) {
+            out[mt][kt][0] = pack_bf16(fmaxf(c[mt][2 * kt][0], 0.f), fmaxf(c[mt][2 * kt][1], 0.f));
+            out[mt][kt][1] = pack_bf16(fmaxf(c[mt][2 * kt][2], 0.f), fmaxf(c[mt][2 * kt][3], 0.f));
+            out[mt][kt][2] = pack_bf16(fmaxf(c[mt][2 * kt + 1][0], 0.f), fmaxf(c[mt][2 * kt + 1][1], 0.f));
+            out[mt][kt][3] = pack_bf16(fmaxf(c[mt][2 * kt + 1][2], 0.f), fmaxf(c[mt][2 * kt + 1][3], 0.f));
+        }
+}
+
+// ---- inference --------------------------------------------------------------------------
+// Shared memory (per CTA of 8 warps): W1 [H][kIn+8], W2,W3 [H][H+8], W4 [K][H+8] (BF16,
+// rows padded against bank conflicts), biases (FP32), per warp X [32][kIn+8] (BF16) and
+// logits [32][K+2] (FP16).
+template <int H>
+__global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Dims d = a.dims;
+    const int K = d.K;
+    const int ld1 = kIn + 8, ldh = H + 8, ldl = K + 2, ldx = kIn + 8;
+    __nv_bfloat16* W1s = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* W2s = W1s + H * ld1;
+    __nv_bfloat16* W3s = W2s + H * ldh;
+    __nv_bfloat16* W4s = W3s + H * ldh;
+    float* bs = reinterpret_cast<float*>(W4s + (size_t)K * ldh);           // b1 | b2 | b3 | b4
+    __nv_bfloat16* Xall = reinterpret_cast<__nv_bfloat16*>(bs + 3 * H + K);
+    __half* Lall = reinterpret_cast<__half*>(Xall + 8 * 32 * ldx);
+    // weights -> shared memory
+    {
+        const __nv_bfloat16* wg = a.wbf;   // W1 [H][kIn] | W2 [H][H] | W3 [H][H] | W4 [K][H]
+        for (int e = threadIdx.x; e < H * kIn; e += blockDim.x) W1s[(e / kIn) * ld1 + e % kIn] = wg[e];
+        wg += H * kIn;
+        for (int e = threadIdx.x; e < H * H; e += blockDim.x) W2s[(e / H) * ldh + e % H] = wg[e];
+        wg += H * H;
+        for (int e = threadIdx.x; e < H * H; e += blockDim.x) W3s[(e / H) * ldh + e % H] = wg[e];
+        wg += H * H;
+        for (int e = threadIdx.x; e < K * H; e += blockDim.x) W4s[(e / H) * ldh + e % H] = wg[e];
+        const float* p = a.params;
+        for (int e = threadIdx.x; e < H; e += blockDim.x) {
+            bs[e] = p[a.L.b1 + e];
+            bs[H + e] = p[a.L.b2 + e];
+            bs[2 * H + e] = p[a.L.b3 + e];
+        }
+        for (int e = threadIdx.x; e < K; e += blockDim.x) bs[3 * H + e] = p[a.L.b4 + e];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __nv_bfloat16* Xs = Xall + warp * 32 * ldx;
+    __half* Ls = Lall + (size_t)warp * 32 * ldl;
+    const float* enc = a.params + a.L.enc;
+    const uint32_t n = a.count ? *a.count : a.n;
+    for (uint32_t base = (blockIdx.x * 8 + warp) * 32; base < n; base += gridDim.x * 8 * 32) {
+        const uint32_t j = base + lane;
+        const bool valid = j < n;
+        float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
+        uint32_t pix = 0;
+        if (valid) {
+            if (a.samples) {
+                pin = a.samples[j];
+            } else {
+                pix = a.hits[j];
+                const int x = (int)(pix % (uint32_t)a.k.W), y = (int)(pix / (uint32_t)a.k.W);
+                const uint2 gv = a.vd[pix];
+                const uint32_t side = gv.x >> 24;
+                const float dist = __uint_as_float(gv.y);
+                const float3 D = dev::camera_ray(a.k, x, y);
+                const float ns = dev::side_sign(side, D);
+                pin = make_float4(D.x * dist + a.k.E.x, D.y * dist + a.k.E.y, D.z * dist + a.k.E.z,
+                                  __uint_as_float(side_code(side, ns)));
+            }
+        }
+        float xr[kIn];
+        input_row(enc, d, pin, xr);
+#pragma unroll
+        for (int f = 0; f < kIn; f += 2)
+            *reinterpret_cast<uint32_t*>(Xs + lane * ldx + f) = valid ? pack_bf16(xr[f], xr[f + 1]) : 0u;
+        __syncwarp();
+        // layer 1 (kIn = 32 -> H) from shared memory
+        uint32_t act[2][H / 16][4], act2[2][H / 16][4];
+        {
+            uint32_t xa[2][2][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int kt = 0; kt < 2; kt++) {
+                    const __nv_bfloat16* r0 = Xs + (mt * 16 + g) * ldx + kt * 16 + 2 * t;
+                    const __nv_bfloat16* r1 = r0 + 8 * ldx;
+                    xa[mt][kt][0] = *reinterpret_cast<const uint32_t*>(r0);
+                    xa[mt][kt][1] = *reinterpret_cast<const uint32_t*>(r1);
+                    xa[mt][kt][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+                    xa[mt][kt][3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+                }
+            float c[2][H / 8][4];
+#pragma unroll
+            for (int nt = 0; nt < H / 8; nt++) {
+                const float b0 = bs[nt * 8 + 2 * t], b1 = bs[nt * 8 + 2 * t + 1];
+#pragma unroll
+                for (int mt = 0; mt < 2; mt++) { c[mt][nt][0] = b0; c[mt][nt][1] = b1; c[mt][nt][2] = b0; c[mt][nt][3] = b1; }
+            }
+#pragma unroll
+            for (int kt = 0; kt < 2; kt++)
+#pragma unroll
+                for (int nt = 0; nt < H / 8; nt++) {
+                    const __nv_bfloat16* row = W1s + (nt * 8 + g) * ld1 + kt * 16 + 2 * t;
+                    const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
+                    const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
+                    mma16816(c[0][nt], xa[0][kt], b0, b1);
+                    mma16816(c[1][nt], xa[1][kt], b0, b1);
+                }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int kt = 0; kt < H / 16; kt++) {
+                    act[mt][kt][0] = pack_bf16(fmaxf(c[mt][2 * kt][0], 0.f), fmaxf(c[mt][2 * kt][1], 0.f));
+                    act[mt][kt][1] = pack_bf16(fmaxf(c[mt][2 * kt][2], 0.f), fmaxf(c[mt][2 * kt][3], 0.f));
+                    act[mt][kt][2] = pack_bf16(fmaxf(c[mt][2 * kt + 1][0], 0.f), fmaxf(c[mt][2 * kt + 1][1], 0.f));
+                    act[mt][kt][3] = pack_bf16(fmaxf(c[mt][2 * kt + 1][2], 0.f), fmaxf(c[mt][2 * kt + 1][3], 0.f));
+                }
+        }
+        hidden_layer<H>(act, act2, W2s, ldh, bs + H, g, t);
+        hidden_layer<H>(act2, act, W3s, ldh, bs + 2 * H, g, t);
+        // output layer: K logits, 8 columns at a time, to shared memory as FP16
+        for (int nt = 0; nt < K / 8; nt++) {
+            const float b0 = bs[3 * H + nt * 8 + 2 * t], b1 = bs[3 * H + nt * 8 + 2 * t + 1];
+            float c0[4] = {b0, b1, b0, b1}, c1[4] = {b0, b1, b0, b1};
+#pragma unroll
+            for (int kt = 0; kt < H / 16; kt++) {
+                const __nv_bfloat16* row = W4s + (size_t)(nt * 8 + g) * ldh + kt * 16 + 2 * t;
+                const uint32_t bb0 = *reinterpret_cast<const uint32_t*>(row);
+                const uint32_t bb1 = *reinterpret_cast<const uint32_t*>(row + 8);
+                mma16816(c0, act[0][kt], bb0, bb1);
+                mma16816(c1, act[1][kt], bb0, bb1);
+            }
+            const int col = nt * 8 + 2 * t;
+            *reinterpret_cast<__half2*>(Ls + g * ldl + col) = __floats2half2_rn(c0[0], c0[1]);
+            *reinterpret_cast<__half2*>(Ls + (g + 8) * ldl + col) = __floats2half2_rn(c0[2], c0[3]);
+            *reinterpret_cast<__half2*>(Ls + (16 + g) * ldl + col) = __floats2half2_rn(c1[0], c1[1]);
+            *reinterpret_cast<__half2*>(Ls + (24 + g) * ldl + col) = __floats2half2_rn(c1[2], c1[3]);
+        }
+        __syncwarp();
+        if (valid) {
+            // softmax over the lane's row, summed in 16 groups
+            const __half* row = Ls + lane * ldl;
+            const int G = 16, gs = K / 16;
+            float mx = -INFINITY;
+            for (int c = 0; c < K; c++) mx = fmaxf(mx, __half2float(row[c]));
+            float S[16];
+            float Z = 0.0f;
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+                float s = 0.0f;
+                for (int c = q * gs; c < (q + 1) * gs; c++) s += __expf(__half2float(row[c]) - mx);
+                S[q] = s;
+                Z += s;
+            }
+            if (a.probs) {
+                for (int c = 0; c < K; c++) a.probs[(size_t)j * K + c] = __expf(__half2float(row[c]) - mx) / Z;
+            } else {
+                uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
+                const float eps = d.eps, invK = 1.0f / (float)K;
+                uint2* out = a.cand + (size_t)j * kMaxCand;
+                for (uint32_t m = 0; m < a.ncand; m++) {
+                    const float u = dev::rnd(s);
+                    const float v = dev::rnd(s);
+                    int c;
+                    if (u < eps) {
+                        c = min((int)(v * (float)K), K - 1);
+                    } else {
+                        float target = v * Z;
+                        int q = 0;
+                        while (q < G - 1 && target >= S[q]) { target -= S[q]; q++; }
+                        c = q * gs + gs - 1;
+                        for (int cc = q * gs; cc < (q + 1) * gs; cc++) {
+                            const float e = __expf(__half2float(row[cc]) - mx);
+                            if (target < e) { c = cc; break; }
+                            target -= e;
+                        }
+                    }
+                    const float qc = (1.0f - eps) * (__expf(__half2float(row[c]) - mx) / Z) + eps * invK;
+                    out[m] = make_uint2((uint32_t)c, __float_as_uint(qc));
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---- training ------------------------------------------------------------------------------
+// training batch from the view's final reservoirs: sample b takes the hit pixel at
+// stratum b of the hit list; target = cluster of the selected emitter, weight = W * pHat
+__global__ void gather_kernel(GatherArgs a) {
+    const uint32_t nh = *a.count;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < a.B; b += gridDim.x * blockDim.x) {
+        float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
+        uint32_t tgt = 0;
+        float w = 0.0f;
+        if (nh > 0) {
+            const uint32_t j = (uint32_t)(((uint64_t)b * nh + a.offset) / a.B) % nh;
+            const uint32_t pix = a.hits[j];
+            const uint4 qa = a.hA[pix];
+            const uint32_t M = qa.y & 0x1FFFFFFFu;
+            const float pH = __uint_as_float(qa.w);
+            const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, pH * (float)M);
+            if (M > 0u && W > 0.0f && qa.x < a.nlights) {
+                w = W * pH;
+                tgt = a.lightCluster[qa.x];
+            }
+            const int x = (int)(pix % (uint32_t)a.k.W), y = (int)(pix / (uint32_t)a.k.W);
+            const uint2 gv = a.vd[pix];
+            const uint32_t side = gv.x >> 24;
+            const float dist = __uint_as_float(gv.y);
+            const float3 D = dev::camera_ray(a.k, x, y);
+            const float ns = dev::side_sign(side, D);
+            pin = make_float4(D.x * dist + a.k.E.x, D.y * dist + a.k.E.y, D.z * dist + a.k.E.z,
+                              __uint_as_float(side_code(side, ns)));
+        }
+        a.samples[b] = pin;
+        a.target[b] = tgt;
+        a.weight[b] = w;
+    }
+}
+
+__global__ void encode_kernel(const float* __restrict__ params, Layout L, Dims d, const float4* __restrict__ samples,
+                              uint32_t B, float* __restrict__ X) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+        float xr[kIn];
+        input_row(params + L.enc, d, samples[b], xr);
+#pragma unroll
+        for (int f = 0; f < kIn; f++) X[(size_t)b * kIn + f] = xr[f];
+    }
+}
+
+// C(m, n) = sum_k A(m, k) B(k, n) with arbitrary strides; 64x64 tiles, 4x4 per thread.
+// mode: 0 store, 1 +bias & relu, 2 +bias, 3 store * (mask(m, n) > 0), 4 atomic add (split-K)
+__global__ void __launch_bounds__(256) gemm_kernel(GemmArgs g) {
+    __shared__ float As[16][68];
+    __shared__ float Bs[16][68];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const long kbeg = (long)blockIdx.z * g.kchunk;
+    const long kend = min((long)g.K, kbeg + g.kchunk);
+    float acc[4][4] = {};
+    for (long k0 = kbeg; k0 < kend; k0 += 16) {
+        for (int e = threadIdx.x; e < 1024; e += 256) {
+            int mm, kk;
+            if (g.sak == 1) { mm = e >> 4; kk = e & 15; } else { kk = e >> 6; mm = e & 63; }
+            const long m = m0 + mm, k = k0 + kk;
+            As[kk][mm] = (m < g.M && k < kend) ? g.A[m * g.sam + k * g.sak] : 0.0f;
+        }
+        for (int e = threadIdx.x; e < 1024; e += 256) {
+            int kk, nn;
+            if (g.sbn == 1) { kk = e >> 6; nn = e & 63; } else { nn = e >> 4; kk = e & 15; }
+            const long k = k0 + kk, nI = n0 + nn;
+            Bs[kk][nn] = (k < kend && nI < g.N) ? g.B[k * g.sbk + nI * g.sbn] : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++) {
+            float av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) { av[i] = As[kk][ty * 4 + i]; bv[i] = Bs[kk][tx * 4 + i]; }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] += av[i] * bv[j];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const long m = m0 + ty * 4 + i, nI = n0 + tx * 4 + j;
+            if (m >= g.M || nI >= g.N) continue;
+            float v = acc[i][j];
+            float* dst = g.C + m * g.scm + nI * g.scn;
+            if (g.mode == 4) { atomicAdd(dst, v); continue; }
+            if (g.mode == 1 || g.mode == 2) v += g.bias[nI];
+            if (g.mode == 1) v = fmaxf(v, 0.0f);
+            if (g.mode == 3 && !(g.mask[m * g.smm + nI] > 0.0f)) v = 0.0f;
+            *dst = v;
+        }
+}
+
+// weighted softmax cross-entropy per row; dZ = w/sum(w) * (softmax - onehot); one warp per row
+__global__ void softmax_ce_kernel(float* __restrict__ Z, const uint32_t* __restrict__ target,
+                                  const float* __restrict__ weight, uint32_t B, int K, const float* __restrict__ wsum,
+                                  float* loss) {
+    const int lane = threadIdx.x & 31;
+    const float inv = *wsum > 0.0f ? 1.0f / *wsum : 0.0f;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < B; b += (gridDim.x * blockDim.x) >> 5) {
+        float* z = Z + (size_t)b * K;
+        float mx = -INFINITY;
+        for (int c = lane; c < K; c += 32) mx = fmaxf(mx, z[c]);
+        for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        float s = 0.0f;
+        for (int c = lane; c < K; c += 32) s += expf(z[c] - mx);
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const float w = weight[b] * inv;
+        const uint32_t t = target[b];
+        float lt = 0.0f;
+        for (int c = lane; c < K; c += 32) {
+            const float p = expf(z[c] - mx) / s;
+            if ((uint32_t)c == t) lt = -(z[c] - mx - logf(s));
+            z[c] = w * (p - ((uint32_t)c == t ? 1.0f : 0.0f));
+        }
+        for (int o = 16; o; o >>= 1) lt += __shfl_xor_sync(0xffffffffu, lt, o);
+        if (lane == 0 && w > 0.0f) atomicAdd(loss, w * lt);
+    }
+}
+
+__global__ void sum_kernel(const float* __restrict__ v, uint32_t n, float* out) {
+    float s = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += v[i];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+// column sums of a row-major [B][N] matrix into out[N] (bias gradients)
+__global__ void colsum_kernel(const float* __restrict__ X, uint32_t B, int N, float* out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    float s = 0.0f;
+    for (uint32_t b = blockIdx.y; b < B; b += gridDim.y) s += X[(size_t)b * N + c];
+    atomicAdd(&out[c], s);
+}
+
+// encoding gradients: scatter dX[:, 0:16] into the hash tables with the trilinear weights
+__global__ void encode_backward_kernel(Dims d, Layout L, const float4* __restrict__ samples, const float* __restrict__ dX,
+                                       uint32_t B, float* grad) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+        Corner c;
+        const float4 p = samples[b];
+        corners(d, p.x, p.y, p.z, c);
+#pragma unroll
+        for (int l = 0; l < kLevels; l++)
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                float* dst = grad + L.enc + (size_t)c.idx[l][q] * kFeat;
+                const float w = c.w[l][q];
+#pragma unroll
+                for (int f = 0; f < kFeat; f++) {
+                    const float gv = w * dX[(size_t)b * kIn + l * 8 + f];
+                    if (gv != 0.0f) atomicAdd(dst + f, gv);
+                }
+            }
+    }
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                            float* __restrict__ v, size_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float g = gr[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * g;
+        const float vi = b2 * v[i] + (1.0f - b2) * g * g;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+// seeded initialisation: encoding U(-1e-4, 1e-4), weights U(-a, a) with a = sqrt(6 / fan_in), biases 0
+__global__ void init_kernel(float* p, Layout L, Dims d, uint32_t seed) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < L.total; i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t s = dev::wang_hash((uint32_t)i * 2654435761u ^ dev::wang_hash(seed + (uint32_t)(i >> 32)));
+        const float u = dev::rnd(s) * 2.0f - 1.0f;
+        float v = 0.0f;
+        if (i < L.W1) v = 1e-4f * u;
+        else if (i < L.b1) v = u * sqrtf(6.0f / (float)kIn);
+        else if (i >= L.W2 && i < L.b2) v = u * sqrtf(6.0f / (float)d.H);
+        else if (i >= L.W3 && i < L.b3) v = u * sqrtf(6.0f / (float)d.H);
+        else if (i >= L.W4 && i < L.b4) v = u * sqrtf(6.0f / (float)d.H);
+        p[i] = v;
+    }
+}
+
+}  // namespace prop
+
+// ---- host launchers ---------------------------------------------------------------------
+namespace prop {
+
+static int sms() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+size_t infer_smem_bytes(const Dims& d) {
+    const int H = d.H, K = d.K;
+    return (size_t)H * (kIn + 8) * 2 + 2 * (size_t)H * (H + 8) * 2 + (size_t)K * (H + 8) * 2 + (3 * H + K) * 4 +
+           8 * 32 * (kIn + 8) * 2 + 8 * 32 * (size_t)(K + 2) * 2;
+}
+
+bool infer_supported(const Dims& d) {
+    return d.H == 64 && d.K >= 16 && d.K % 16 == 0 && d.K <= 1024 && infer_smem_bytes(d) <= 227 * 1024;
+}
+
+cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s) {
+    const size_t sm = infer_smem_bytes(a.dims);
+    cudaError_t e = cudaFuncSetAttribute(infer_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((max_items + 255) / 256, (uint32_t)sms() * 2));
+    infer_kernel<64><<<blocks, 256, sm, s>>>(a);
+    return cudaGetLastError();
+}
+
+void launch_gather(const GatherArgs& a, cudaStream_t s) { gather_kernel<<<(a.B + 255) / 256, 256, 0, s>>>(a); }
+
+void launch_encode(const float* params, const Layout& L, const Dims& d, const float4* samples, uint32_t B, float* X,
+                   cudaStream_t s) {
+    encode_kernel<<<(B + 255) / 256, 256, 0, s>>>(params, L, d, samples, B, X);
+}
+
+void launch_gemm(const GemmArgs& g0, cudaStream_t s) {
+    GemmArgs g = g0;
+    if (g.kchunk <= 0) g.kchunk = g.K;
+    const unsigned gz = (unsigned)((g.K + g.kchunk - 1) / g.kchunk);
+    gemm_kernel<<<dim3((g.N + 63) / 64, (g.M + 63) / 64, gz), 256, 0, s>>>(g);
+}
+
+void launch_softmax_ce(float* Z, const uint32_t* target, const float* weight, uint32_t B, int K, const float* wsum,
+                       float* loss, cudaStream_t s) {
+    softmax_ce_kernel<<<std::max<uint32_t>(1, std::min<uint32_t>((B + 7) / 8, 4096)), 256, 0, s>>>(Z, target, weight, B, K,
+                                                                                                   wsum, loss);
+}
+
+void launch_sum(const float* v, uint32_t n, float* out, cudaStream_t s) {
+    sum_kernel<<<std::max<uint32_t>(1, std::min<uint32_t>((n + 255) / 256, 1024)), 256, 0, s>>>(v, n, out);
+}
+
+void launch_colsum(const float* X, uint32_t B, int N, float* out, cudaStream_t s) {
+    colsum_kernel<<<dim3((N + 127) / 128, std::min<uint32_t>(B, 256)), 128, 0, s>>>(X, B, N, out);
+}
+
+void launch_encode_backward(const Dims& d, const Layout& L, const float4* samples, const float* dX, uint32_t B, float* grad,
+                            cudaStream_t s) {
+    encode_backward_kernel<<<(B + 255) / 256, 256, 0, s>>>(d, L, samples, dX, B, grad);
+}
+
+void launch_adam(float* p, const float* g, float* m, float* v, size_t n, float lr, int step, cudaStream_t s) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f / (1.0f - powf(b1, (float)step)), c2 = 1.0f / (1.0f - powf(b2, (float)step));
+    adam_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, c1, c2);
+}
+
+void launch_to_bf16(const float* src, __nv_bfloat16* dst, size_t n, cudaStream_t s) {
+    to_bf16_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(src, dst, n);
+}
+
+void launch_init(float* p, const Layout& L, const Dims& d, uint32_t seed, cudaStream_t s) {
+    init_kernel<<<(unsigned)std::min<size_t>((L.total + 255) / 256, 8192), 256, 0, s>>>(p, L, d, seed);
+}
+
+}  // namespace prop
+}  // namespace vxr

@@ -1,0 +1,465 @@
+// proposal_api.cu - C ABI of the learned candidate proposal (no reference counterpart):
+// per-view network state, online training on the view's reservoirs, checkpoints.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "internal.hpp"
+#include "proposal.hpp"
+#include "view.hpp"
+
+namespace vxr {
+
+struct Proposal {
+    prop::Dims d;
+    prop::Layout L;
+    vxr_proposal_desc desc{};
+    float* params = nullptr;       // FP32 master
+    float* grads = nullptr;
+    float* m = nullptr;            // Adam moments
+    float* v = nullptr;
+    __nv_bfloat16* wbf = nullptr;  // W1 | W2 | W3 | W4 in BF16
+    uint32_t* clOff = nullptr;     // cluster CSR
+    uint32_t* clMembers = nullptr;
+    uint32_t* lightCluster = nullptr;
+    uint64_t clusterVersion = 0;
+    uint2* cand = nullptr;         // [pixels][kMaxCand]
+    // training batch
+    uint32_t B = 0;
+    float4* samples = nullptr;
+    uint32_t* target = nullptr;
+    float* weight = nullptr;
+    float* X = nullptr;
+    float* H1 = nullptr;
+    float* H2 = nullptr;
+    float* H3 = nullptr;
+    float* Z = nullptr;
+    float* dA = nullptr;
+    float* dB = nullptr;
+    float* dX = nullptr;
+    float* scal = nullptr;         // [loss, wsum]
+    int step = 0;
+    uint32_t gatherOffset = 0;
+};
+
+void destroy_proposal(Proposal* p) {
+    if (!p) return;
+    void* bufs[] = {p->params, p->grads, p->m, p->v, p->wbf, p->clOff, p->clMembers, p->lightCluster, p->cand,
+                    p->samples, p->target, p->weight, p->X, p->H1, p->H2, p->H3, p->Z, p->dA, p->dB, p->dX, p->scal};
+    for (void* b : bufs) cudaFree(b);
+    delete p;
+}
+
+}  // namespace vxr
+
+using vxr::set_error;
+using vxr::check_view;
+
+#define CUP(call, what)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return set_error(VXR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+size_t weights_count(const vxr::prop::Dims& d) {
+    return (size_t)d.H * vxr::prop::kIn + 2 * (size_t)d.H * d.H + (size_t)d.K * d.H;
+}
+
+// refresh the BF16 inference copy of W1..W4 from the FP32 master
+void refresh_bf16(vxr::Proposal* p, cudaStream_t s) {
+    using namespace vxr::prop;
+    const vxr::prop::Layout& L = p->L;
+    const vxr::prop::Dims& d = p->d;
+    __nv_bfloat16* o = p->wbf;
+    launch_to_bf16(p->params + L.W1, o, (size_t)d.H * kIn, s);
+    o += (size_t)d.H * kIn;
+    launch_to_bf16(p->params + L.W2, o, (size_t)d.H * d.H, s);
+    o += (size_t)d.H * d.H;
+    launch_to_bf16(p->params + L.W3, o, (size_t)d.H * d.H, s);
+    o += (size_t)d.H * d.H;
+    launch_to_bf16(p->params + L.W4, o, (size_t)d.K * d.H, s);
+}
+
+// cluster CSR (members sorted by cluster, then light index) from the world's clustering
+int upload_clusters(vxr_view* v, vxr::Proposal* p) {
+    const vxr::World& w = v->world->w;
+    const uint32_t n = (uint32_t)w.lights.size();
+    const uint32_t K = (uint32_t)p->d.K;
+    if (w.clusterCount != K || w.lightCluster.size() != n)
+        return set_error(VXR_E_STATE, "proposal: the world's clustering does not match (run vxr_world_cluster_lights with k = " +
+                                          std::to_string(K) + " after the last light change)");
+    std::vector<uint32_t> off(K + 1, 0), mem(n);
+    for (uint32_t i = 0; i < n; i++) off[w.lightCluster[i] + 1]++;
+    for (uint32_t c = 0; c < K; c++) off[c + 1] += off[c];
+    std::vector<uint32_t> pos(off.begin(), off.end() - 1);
+    for (uint32_t i = 0; i < n; i++) mem[pos[w.lightCluster[i]]++] = i;
+    for (uint32_t c = 0; c < K; c++)
+        if (off[c + 1] == off[c]) return set_error(VXR_E_STATE, "proposal: empty cluster " + std::to_string(c));
+    cudaFree(p->clOff);
+    cudaFree(p->clMembers);
+    cudaFree(p->lightCluster);
+    p->clOff = nullptr; p->clMembers = nullptr; p->lightCluster = nullptr;
+    CUP(cudaMalloc(&p->clOff, (K + 1) * sizeof(uint32_t)), "cudaMalloc(cluster offsets)");
+    CUP(cudaMalloc(&p->clMembers, std::max<uint32_t>(n, 1) * sizeof(uint32_t)), "cudaMalloc(cluster members)");
+    CUP(cudaMalloc(&p->lightCluster, std::max<uint32_t>(n, 1) * sizeof(uint32_t)), "cudaMalloc(light clusters)");
+    CUP(cudaMemcpy(p->clOff, off.data(), (K + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload clusters");
+    if (n) {
+        CUP(cudaMemcpy(p->clMembers, mem.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload clusters");
+        CUP(cudaMemcpy(p->lightCluster, w.lightCluster.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice),
+            "upload clusters");
+    }
+    p->clusterVersion = w.clusterVersion;
+    return VXR_OK;
+}
+
+int ensure_batch(vxr::Proposal* p, uint32_t B) {
+    using vxr::prop::kIn;
+    if (B <= p->B) return VXR_OK;
+    void** bufs[] = {(void**)&p->samples, (void**)&p->target, (void**)&p->weight, (void**)&p->X, (void**)&p->H1,
+                     (void**)&p->H2, (void**)&p->H3, (void**)&p->Z, (void**)&p->dA, (void**)&p->dB, (void**)&p->dX};
+    for (void** b : bufs) { cudaFree(*b); *b = nullptr; }
+    const size_t H = p->d.H, K = p->d.K;
+    CUP(cudaMalloc(&p->samples, B * sizeof(float4)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->target, B * sizeof(uint32_t)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->weight, B * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->X, (size_t)B * kIn * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->H1, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->H2, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->H3, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->Z, (size_t)B * K * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->dA, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->dB, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
+    CUP(cudaMalloc(&p->dX, (size_t)B * kIn * sizeof(float)), "cudaMalloc(batch)");
+    p->B = B;
+    return VXR_OK;
+}
+
+// forward + backward of the weighted cross-entropy on the batch in p->samples/target/weight;
+// gradients (zeroed first) in p->grads, [loss, weight sum] in p->scal
+void forward_backward(vxr::Proposal* p, uint32_t B, cudaStream_t s) {
+    using namespace vxr::prop;
+    const Layout& L = p->L;
+    const Dims& d = p->d;
+    const int H = d.H, K = d.K;
+    float* P = p->params;
+    float* G = p->grads;
+    cudaMemsetAsync(G, 0, L.total * sizeof(float), s);
+    cudaMemsetAsync(p->scal, 0, 2 * sizeof(float), s);
+    launch_encode(P, L, d, p->samples, B, p->X, s);
+    auto fwd = [&](const float* in, int kin, size_t wo, size_t bo, float* out, int nout, int mode) {
+        GemmArgs g{};
+        g.A = in; g.sam = kin; g.sak = 1;
+        g.B = P + wo; g.sbk = 1; g.sbn = kin;
+        g.C = out; g.scm = nout; g.scn = 1;
+        g.M = (int)B; g.N = nout; g.K = kin;
+        g.bias = P + bo; g.mode = mode;
+        launch_gemm(g, s);
+    };
+    fwd(p->X, kIn, L.W1, L.b1, p->H1, H, 1);
+    fwd(p->H1, H, L.W2, L.b2, p->H2, H, 1);
+    fwd(p->H2, H, L.W3, L.b3, p->H3, H, 1);
+    fwd(p->H3, H, L.W4, L.b4, p->Z, K, 2);
+    launch_sum(p->weight, B, p->scal + 1, s);
+    launch_softmax_ce(p->Z, p->target, p->weight, B, K, p->scal + 1, p->scal, s);
+    // dW (out x in) += dY^T X over the batch (split-K, atomic), db = column sums of dY
+    auto wgrad = [&](const float* dY, int nout, const float* Xin, int kin, size_t wo, size_t bo) {
+        GemmArgs g{};
+        g.A = dY; g.sam = 1; g.sak = nout;
+        g.B = Xin; g.sbk = kin; g.sbn = 1;
+        g.C = G + wo; g.scm = kin; g.scn = 1;
+        g.M = nout; g.N = kin; g.K = (int)B;
+        g.mode = 4; g.kchunk = 2048;
+        launch_gemm(g, s);
+        launch_colsum(dY, B, nout, G + bo, s);
+    };
+    // dX_in = dY W (masked by relu of the layer input when mask != null)
+    auto dgrad = [&](const float* dY, int nout, size_t wo, int kin, float* dXin, const float* mask) {
+        GemmArgs g{};
+        g.A = dY; g.sam = nout; g.sak = 1;
+        g.B = P + wo; g.sbk = kin; g.sbn = 1;
+        g.C = dXin; g.scm = kin; g.scn = 1;
+        g.M = (int)B; g.N = kin; g.K = nout;
+        g.mask = mask; g.smm = kin; g.mode = mask ? 3 : 0;
+        launch_gemm(g, s);
+    };
+    wgrad(p->Z, K, p->H3, H, L.W4, L.b4);
+    dgrad(p->Z, K, L.W4, H, p->dA, p->H3);        // dH3
+    wgrad(p->dA, H, p->H2, H, L.W3, L.b3);
+    dgrad(p->dA, H, L.W3, H, p->dB, p->H2);       // dH2
+    wgrad(p->dB, H, p->H1, H, L.W2, L.b2);
+    dgrad(p->dB, H, L.W2, H, p->dA, p->H1);       // dH1
+    wgrad(p->dA, H, p->X, kIn, L.W1, L.b1);
+    dgrad(p->dA, H, L.W1, kIn, p->dX, nullptr);   // dX
+    launch_encode_backward(d, L, p->samples, p->dX, B, G, s);
+}
+
+}  // namespace
+
+namespace vxr {
+// the candidate stage's hook (nullptr when the view samples uniformly)
+bool learned_hook(vxr_view* v, LearnedHook* h) {
+    Proposal* p = v->prop;
+    if (!v->useProposal || !p) return false;
+    h->infer = prop::InferArgs{};
+    h->infer.dims = p->d;
+    h->infer.L = p->L;
+    h->infer.params = p->params;
+    h->infer.wbf = p->wbf;
+    h->cand = p->cand;
+    h->clOff = p->clOff;
+    h->clMembers = p->clMembers;
+    return true;
+}
+}  // namespace vxr
+
+extern "C" {
+
+int vxr_proposal_default_desc(vxr_proposal_desc* d) {
+    VXR_CHECK_ARG(d, "vxr_proposal_default_desc: null desc");
+    std::memset(d, 0, sizeof(*d));
+    d->hidden = 64;
+    d->table_log2 = 16;
+    d->res0 = 32;
+    d->res1 = 128;
+    d->epsilon = 0.1f;
+    d->learning_rate = 1e-3f;
+    d->batch = 65536;
+    d->seed = 1;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
+    if (int r = check_view(v, "vxr_view_proposal_enable")) return r;
+    VXR_CHECK_ARG(desc, "vxr_view_proposal_enable: null desc");
+    VXR_CHECK_ARG(desc->epsilon > 0.0f && desc->epsilon <= 1.0f, "vxr_view_proposal_enable: epsilon must be in (0, 1]");
+    VXR_CHECK_ARG(desc->table_log2 >= 8 && desc->table_log2 <= 22, "vxr_view_proposal_enable: table_log2 in [8, 22]");
+    VXR_CHECK_ARG(desc->batch >= 1 && desc->batch <= (1u << 22), "vxr_view_proposal_enable: batch in [1, 2^22]");
+    VXR_CHECK_ARG(v->desc.num_candidates <= (uint32_t)vxr::prop::kMaxCand,
+                  "vxr_view_proposal_enable: at most 32 candidates per pixel with the learned proposal");
+    vxr::prop::Dims d;
+    d.H = (int)desc->hidden;
+    d.K = (int)v->world->w.clusterCount;
+    d.tableLog2 = (int)desc->table_log2;
+    d.res0 = (int)desc->res0;
+    d.res1 = (int)desc->res1;
+    d.eps = desc->epsilon;
+    VXR_CHECK_ARG(d.K > 0, "vxr_view_proposal_enable: cluster the world's lights first (vxr_world_cluster_lights)");
+    if (!vxr::prop::infer_supported(d))
+        return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: supported shapes are hidden = 64 and 16 <= clusters <= 1024, "
+                                        "clusters a multiple of 16");
+    if (v->prop) vxr::destroy_proposal(v->prop);
+    vxr::Proposal* p = new (std::nothrow) vxr::Proposal();
+    if (!p) return set_error(VXR_E_NOMEM, "vxr_view_proposal_enable: out of host memory");
+    v->prop = p;
+    p->d = d;
+    p->L = vxr::prop::layout(d);
+    p->desc = *desc;
+    const size_t n = p->L.total;
+    CUP(cudaMalloc(&p->params, n * sizeof(float)), "cudaMalloc(params)");
+    CUP(cudaMalloc(&p->grads, n * sizeof(float)), "cudaMalloc(grads)");
+    CUP(cudaMalloc(&p->m, n * sizeof(float)), "cudaMalloc(adam)");
+    CUP(cudaMalloc(&p->v, n * sizeof(float)), "cudaMalloc(adam)");
+    CUP(cudaMalloc(&p->wbf, weights_count(d) * sizeof(__nv_bfloat16)), "cudaMalloc(bf16 weights)");
+    CUP(cudaMalloc(&p->cand, v->npx * vxr::prop::kMaxCand * sizeof(uint2)), "cudaMalloc(candidates)");
+    CUP(cudaMalloc(&p->scal, 2 * sizeof(float)), "cudaMalloc(scalars)");
+    CUP(cudaMemsetAsync(p->m, 0, n * sizeof(float), v->stream), "clear adam");
+    CUP(cudaMemsetAsync(p->v, 0, n * sizeof(float), v->stream), "clear adam");
+    vxr::prop::launch_init(p->params, p->L, d, desc->seed, v->stream);
+    refresh_bf16(p, v->stream);
+    CUP(cudaGetLastError(), "proposal init");
+    if (int r = upload_clusters(v, p)) return r;
+    CUP(cudaStreamSynchronize(v->stream), "proposal init");
+    return VXR_OK;
+}
+
+int vxr_view_proposal_use(vxr_view* v, int on) {
+    if (int r = check_view(v, "vxr_view_proposal_use")) return r;
+    if (on && !v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_use: enable the proposal first");
+    if (on && v->prop->clusterVersion != v->world->w.clusterVersion)
+        if (int r = upload_clusters(v, v->prop)) return r;
+    v->useProposal = on != 0;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
+    if (int r = check_view(v, "vxr_view_proposal_train")) return r;
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_train: enable the proposal first");
+    if (p->clusterVersion != v->world->w.clusterVersion)
+        if (int r = upload_clusters(v, p)) return r;
+    const uint32_t B = p->desc.batch;
+    if (int r = ensure_batch(p, B)) return r;
+    float last = 0.0f;
+    for (uint32_t it = 0; it < steps; it++) {
+        vxr::prop::GatherArgs ga{};
+        ga.k = vxr::dev_frame(v->k);
+        ga.vd = v->buf.vd[v->cur];
+        ga.hits = v->buf.hits;
+        ga.count = v->buf.counters;
+        ga.hA = v->buf.hA;
+        ga.lightCluster = p->lightCluster;
+        ga.nlights = (uint32_t)v->world->w.dev->nl;
+        ga.B = B;
+        ga.offset = p->gatherOffset;
+        ga.samples = p->samples;
+        ga.target = p->target;
+        ga.weight = p->weight;
+        p->gatherOffset = p->gatherOffset * 1664525u + 1013904223u;
+        vxr::prop::launch_gather(ga, v->stream);
+        forward_backward(p, B, v->stream);
+        p->step++;
+        vxr::prop::launch_adam(p->params, p->grads, p->m, p->v, p->L.total, p->desc.learning_rate, p->step, v->stream);
+        refresh_bf16(p, v->stream);
+        CUP(cudaGetLastError(), "proposal training");
+        if (it + 1 == steps && loss) {
+            float h[2];
+            CUP(cudaMemcpyAsync(h, p->scal, sizeof(h), cudaMemcpyDeviceToHost, v->stream), "read loss");
+            CUP(cudaStreamSynchronize(v->stream), "proposal training");
+            last = h[0];
+        }
+    }
+    if (loss) *loss = last;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden) {
+    if (int r = check_view(v, "vxr_view_proposal_param_count")) return r;
+    VXR_CHECK_ARG(n, "vxr_view_proposal_param_count: null output");
+    if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_param_count: enable the proposal first");
+    *n = v->prop->L.total;
+    if (clusters) *clusters = (uint32_t)v->prop->d.K;
+    if (hidden) *hidden = (uint32_t)v->prop->d.H;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_get_params(vxr_view* v, float* out) {
+    if (int r = check_view(v, "vxr_view_proposal_get_params")) return r;
+    VXR_CHECK_ARG(out, "vxr_view_proposal_get_params: null output");
+    if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_get_params: enable the proposal first");
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    CUP(cudaMemcpy(out, v->prop->params, v->prop->L.total * sizeof(float), cudaMemcpyDeviceToHost), "read params");
+    return VXR_OK;
+}
+
+int vxr_view_proposal_set_params(vxr_view* v, const float* in) {
+    if (int r = check_view(v, "vxr_view_proposal_set_params")) return r;
+    VXR_CHECK_ARG(in, "vxr_view_proposal_set_params: null input");
+    if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_set_params: enable the proposal first");
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    CUP(cudaMemcpy(v->prop->params, in, v->prop->L.total * sizeof(float), cudaMemcpyHostToDevice), "write params");
+    refresh_bf16(v->prop, v->stream);
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    return VXR_OK;
+}
+
+int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const uint32_t* target, const float* weight,
+                           float* loss, float* grad) {
+    if (int r = check_view(v, "vxr_view_proposal_grad")) return r;
+    VXR_CHECK_ARG(B >= 1 && samples && target && weight && loss && grad, "vxr_view_proposal_grad: bad argument");
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_grad: enable the proposal first");
+    for (uint32_t b = 0; b < B; b++)
+        VXR_CHECK_ARG(target[b] < (uint32_t)p->d.K, "vxr_view_proposal_grad: target cluster out of range");
+    if (int r = ensure_batch(p, B)) return r;
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    CUP(cudaMemcpy(p->samples, samples, B * sizeof(float4), cudaMemcpyHostToDevice), "upload samples");
+    CUP(cudaMemcpy(p->target, target, B * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload targets");
+    CUP(cudaMemcpy(p->weight, weight, B * sizeof(float), cudaMemcpyHostToDevice), "upload weights");
+    forward_backward(p, B, v->stream);
+    CUP(cudaGetLastError(), "proposal gradient");
+    float h[2];
+    CUP(cudaMemcpyAsync(h, p->scal, sizeof(h), cudaMemcpyDeviceToHost, v->stream), "read loss");
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    *loss = h[0];
+    CUP(cudaMemcpy(grad, p->grads, p->L.total * sizeof(float), cudaMemcpyDeviceToHost), "read gradients");
+    return VXR_OK;
+}
+
+int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float* probs) {
+    if (int r = check_view(v, "vxr_view_proposal_probs")) return r;
+    VXR_CHECK_ARG(n >= 1 && samples && probs, "vxr_view_proposal_probs: bad argument");
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_probs: enable the proposal first");
+    float4* ds = nullptr;
+    float* dp = nullptr;
+    CUP(cudaMalloc(&ds, n * sizeof(float4)), "cudaMalloc");
+    if (cudaMalloc(&dp, (size_t)n * p->d.K * sizeof(float)) != cudaSuccess) {
+        cudaFree(ds);
+        return set_error(VXR_E_NOMEM, "vxr_view_proposal_probs: cudaMalloc");
+    }
+    cudaMemcpy(ds, samples, n * sizeof(float4), cudaMemcpyHostToDevice);
+    vxr::prop::InferArgs a{};
+    a.dims = p->d;
+    a.L = p->L;
+    a.params = p->params;
+    a.wbf = p->wbf;
+    a.samples = ds;
+    a.n = n;
+    a.probs = dp;
+    cudaError_t e = vxr::prop::launch_infer(a, n, v->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(v->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(probs, dp, (size_t)n * p->d.K * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(ds);
+    cudaFree(dp);
+    if (e != cudaSuccess) return set_error(VXR_E_CUDA, std::string("vxr_view_proposal_probs: ") + cudaGetErrorString(e));
+    return VXR_OK;
+}
+
+// checkpoint: magic, version, dims, step, params, Adam moments
+int vxr_view_proposal_save(vxr_view* v, const char* path) {
+    if (int r = check_view(v, "vxr_view_proposal_save")) return r;
+    VXR_CHECK_ARG(path, "vxr_view_proposal_save: null path");
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_save: enable the proposal first");
+    const size_t n = p->L.total;
+    std::vector<float> buf(3 * n);
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    CUP(cudaMemcpy(buf.data(), p->params, n * sizeof(float), cudaMemcpyDeviceToHost), "read params");
+    CUP(cudaMemcpy(buf.data() + n, p->m, n * sizeof(float), cudaMemcpyDeviceToHost), "read adam");
+    CUP(cudaMemcpy(buf.data() + 2 * n, p->v, n * sizeof(float), cudaMemcpyDeviceToHost), "read adam");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return set_error(VXR_E_IO, std::string("vxr_view_proposal_save: cannot open ") + path);
+    const uint32_t hdr[8] = {0x56585250u /* "VXRP" */, 1u, (uint32_t)p->d.H, (uint32_t)p->d.K, (uint32_t)p->d.tableLog2,
+                             (uint32_t)p->d.res0, (uint32_t)p->d.res1, (uint32_t)p->step};
+    bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 && std::fwrite(&p->d.eps, sizeof(float), 1, f) == 1 &&
+              std::fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return set_error(VXR_E_IO, std::string("vxr_view_proposal_save: write failed: ") + path);
+    return VXR_OK;
+}
+
+int vxr_view_proposal_load(vxr_view* v, const char* path) {
+    if (int r = check_view(v, "vxr_view_proposal_load")) return r;
+    VXR_CHECK_ARG(path, "vxr_view_proposal_load: null path");
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_load: enable the proposal first (same shape)");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_error(VXR_E_IO, std::string("vxr_view_proposal_load: cannot open ") + path);
+    uint32_t hdr[8];
+    float eps = 0.0f;
+    const size_t n = p->L.total;
+    std::vector<float> buf(3 * n);
+    const bool ok = std::fread(hdr, sizeof(hdr), 1, f) == 1 && std::fread(&eps, sizeof(float), 1, f) == 1 &&
+                    hdr[0] == 0x56585250u && hdr[1] == 1u && hdr[2] == (uint32_t)p->d.H && hdr[3] == (uint32_t)p->d.K &&
+                    hdr[4] == (uint32_t)p->d.tableLog2 && hdr[5] == (uint32_t)p->d.res0 && hdr[6] == (uint32_t)p->d.res1 &&
+                    std::fread(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    std::fclose(f);
+    if (!ok) return set_error(VXR_E_IO, std::string("vxr_view_proposal_load: malformed or mismatched checkpoint: ") + path);
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    CUP(cudaMemcpy(p->params, buf.data(), n * sizeof(float), cudaMemcpyHostToDevice), "write params");
+    CUP(cudaMemcpy(p->m, buf.data() + n, n * sizeof(float), cudaMemcpyHostToDevice), "write adam");
+    CUP(cudaMemcpy(p->v, buf.data() + 2 * n, n * sizeof(float), cudaMemcpyHostToDevice), "write adam");
+    p->step = (int)hdr[7];
+    refresh_bf16(p, v->stream);
+    CUP(cudaStreamSynchronize(v->stream), "sync");
+    return VXR_OK;
+}
+
+}  // extern "C"

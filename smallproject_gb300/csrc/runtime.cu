@@ -12,22 +12,11 @@
 #include "internal.hpp"
 #include "kernels.hpp"
 #include "world.hpp"
+#include "view.hpp"
 
 namespace vxr {
 
-struct DeviceWorld {
-    uint32_t* grid = nullptr;
-    uint8_t* uber = nullptr;
-    uint32_t* bricks = nullptr;
-    size_t brickBytes = 0;
-    uint4* lraw = nullptr;
-    float4* lgeom = nullptr;
-    float4* lemit = nullptr;
-    uint32_t nl = 0;
-    size_t lcap = 0;
-    uint64_t version = 0, lightVersion = 0;
-    int device = -1;
-};
+
 
 static int cuda_fail(cudaError_t e, const char* what) {
     return set_error(VXR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -103,33 +92,14 @@ static int upload(World& w) {
 
 }  // namespace vxr
 
-// ---------------------------------------------------------------------------------------
-struct vxr_view {
-    vxr_world* world = nullptr;
-    vxr_view_desc desc{};
-    vxr::CameraState cam;
-    vxr::ViewBuffers buf;
-    int cur = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t evs[6] = {}, eve[6] = {};            // [0]: vxr_view_timer_*, [1..5]: last frame's stages
-    bool ran[6] = {};
-    // per-stage event ring over the last kRing frames, harvested by vxr_view_wait
-    static constexpr int kRing = 256;
-    std::vector<cudaEvent_t> ringS, ringE;             // kRing * 6
-    std::vector<uint8_t> ringUsed;                     // kRing * 6
-    uint64_t frameSerial = 0, harvested = 0;
-    double statSum[6] = {};
-    uint32_t statCount[6] = {};
-    bool frameOpen = false;
-    vxr_frame_consts k{};
-    uint64_t seenLightVersion = 0;
-    float times[5] = {};
-    size_t npx = 0;
-};
+
+namespace vxr {
+bool learned_hook(vxr_view* v, LearnedHook* h);
+}
 
 using vxr::set_error;
 
-namespace {
+namespace vxr {
 
 int check_view(vxr_view* v, const char* fn) {
     if (!v) return set_error(VXR_E_INVALID, std::string(fn) + ": null view");
@@ -190,6 +160,10 @@ void free_view(vxr_view* v) {
     cudaFree(b.vd[0]); cudaFree(b.vd[1]); cudaFree(b.seed);
     cudaFree(b.cA); cudaFree(b.cB); cudaFree(b.hA); cudaFree(b.hB);
     cudaFree(b.frame); cudaFree(b.accum); cudaFree(b.err);
+    cudaFree(b.hits); cudaFree(b.qA); cudaFree(b.qB); cudaFree(b.counters);
+    cudaFree(v->sum64); cudaFree(v->errOut);
+    if (v->prop) vxr::destroy_proposal(v->prop);
+    v->prop = nullptr;
     for (int i = 0; i < 6; i++) {
         if (v->evs[i]) cudaEventDestroy(v->evs[i]);
         if (v->eve[i]) cudaEventDestroy(v->eve[i]);
@@ -226,7 +200,15 @@ vxr::LaunchShape shape(const vxr_view* v) {
     return s;
 }
 
-}  // namespace
+}  // namespace vxr
+
+using vxr::check_view;
+using vxr::dev_world;
+using vxr::dev_frame;
+using vxr::ensure_world;
+using vxr::free_view;
+using vxr::harvest;
+using vxr::shape;
 
 #define CUV(call, what)                                                                   \
     do {                                                                                  \
@@ -298,6 +280,10 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     alloc((void**)&b.frame, n * sizeof(float4));
     alloc((void**)&b.accum, n * sizeof(float4));
     alloc((void**)&b.err, sizeof(uint32_t));
+    alloc((void**)&b.hits, n * sizeof(uint32_t));
+    alloc((void**)&b.qA, n * sizeof(float4));
+    alloc((void**)&b.qB, n * sizeof(float4));
+    alloc((void**)&b.counters, 8 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking);
     v->ringS.assign(vxr_view::kRing * 6, nullptr);
     v->ringE.assign(vxr_view::kRing * 6, nullptr);
@@ -411,7 +397,12 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");
     switch (stage) {
     case VXR_STAGE_ALBEDO: vxr::launch_albedo(w, k, v->buf, v->cur, sh, v->stream); break;
-    case VXR_STAGE_CANDIDATES: vxr::launch_candidates(point, w, k, v->buf, v->cur, sh, v->stream); break;
+    case VXR_STAGE_CANDIDATES: {
+        vxr::LearnedHook hook;
+        const bool learned = vxr::learned_hook(v, &hook);
+        vxr::launch_candidates(point, w, k, v->buf, v->cur, sh, v->stream, learned ? &hook : nullptr);
+        break;
+    }
     case VXR_STAGE_SPATIAL: vxr::launch_spatial(point, w, k, v->buf, v->cur, sh, v->stream); break;
     case VXR_STAGE_SHADE: vxr::launch_shade(point, w, k, v->buf, v->cur, fuse, sh, v->stream); break;
     case VXR_STAGE_ACCUMULATE: vxr::launch_accumulate(k, v->buf, sh, v->stream); break;
@@ -682,3 +673,59 @@ extern "C" int vxr_view_stage_stats(vxr_view* v, double sum_ms[5], uint32_t coun
     }
     return VXR_OK;
 }
+
+// ---- converged reference and error metric ----------------------------------------------
+extern "C" {
+
+int vxr_view_sum64_reset(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_sum64_reset")) return r;
+    if (!v->sum64) CUV(cudaMalloc(&v->sum64, v->npx * 3 * sizeof(double)), "cudaMalloc(sum64)");
+    CUV(cudaMemsetAsync(v->sum64, 0, v->npx * 3 * sizeof(double), v->stream), "clear sum64");
+    v->sum64Count = 0;
+    return VXR_OK;
+}
+
+int vxr_view_sum64_add(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_sum64_add")) return r;
+    if (!v->sum64) return set_error(VXR_E_STATE, "vxr_view_sum64_add: call vxr_view_sum64_reset first");
+    vxr::launch_sum64_add(v->buf.frame, v->sum64, (uint32_t)v->npx, v->stream);
+    CUV(cudaGetLastError(), "sum64 kernel");
+    v->sum64Count++;
+    return VXR_OK;
+}
+
+int vxr_view_sum64_mean(vxr_view* v, uint32_t* count, double* mean) {
+    if (int r = check_view(v, "vxr_view_sum64_mean")) return r;
+    VXR_CHECK_ARG(count, "vxr_view_sum64_mean: null count");
+    *count = v->sum64Count;
+    if (mean) {
+        if (!v->sum64 || !v->sum64Count) return set_error(VXR_E_STATE, "vxr_view_sum64_mean: no frames summed");
+        CUV(cudaStreamSynchronize(v->stream), "sync");
+        CUV(cudaMemcpy(mean, v->sum64, v->npx * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read sum64");
+        const double inv = 1.0 / (double)v->sum64Count;
+        for (size_t i = 0; i < v->npx * 3; i++) mean[i] *= inv;
+    }
+    return VXR_OK;
+}
+
+int vxr_view_error(vxr_view* img, int which, vxr_view* ref, double* mse, double* mae) {
+    if (int r = check_view(img, "vxr_view_error")) return r;
+    if (int r = check_view(ref, "vxr_view_error")) return r;
+    VXR_CHECK_ARG(mse && mae && (which == 0 || which == 1), "vxr_view_error: bad argument");
+    VXR_CHECK_ARG(img->npx == ref->npx && img->desc.width == ref->desc.width, "vxr_view_error: resolution mismatch");
+    if (!ref->sum64 || !ref->sum64Count) return set_error(VXR_E_STATE, "vxr_view_error: reference has no summed frames");
+    if (!img->errOut) CUV(cudaMalloc(&img->errOut, 2 * sizeof(double)), "cudaMalloc(error)");
+    CUV(cudaStreamSynchronize(ref->stream), "sync reference");
+    CUV(cudaMemsetAsync(img->errOut, 0, 2 * sizeof(double), img->stream), "clear error");
+    vxr::launch_error(which == 0 ? img->buf.frame : img->buf.accum, ref->sum64, 1.0 / (double)ref->sum64Count,
+                      (uint32_t)img->npx, img->errOut, img->stream);
+    CUV(cudaGetLastError(), "error kernel");
+    double h[2];
+    CUV(cudaMemcpyAsync(h, img->errOut, sizeof(h), cudaMemcpyDeviceToHost, img->stream), "read error");
+    CUV(cudaStreamSynchronize(img->stream), "sync");
+    *mse = h[0] / ((double)img->npx * 3.0);
+    *mae = h[1] / ((double)img->npx * 3.0);
+    return VXR_OK;
+}
+
+}  // extern "C"

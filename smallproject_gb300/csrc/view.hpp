@@ -1,0 +1,68 @@
+// view.hpp - the view object behind the C ABI (shared by runtime.cu and proposal_api.cu).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "camera.hpp"
+#include "kernels.hpp"
+#include "world.hpp"
+
+namespace vxr {
+// GPU copy of a World (runtime.cu)
+struct DeviceWorld {
+    uint32_t* grid = nullptr;
+    uint8_t* uber = nullptr;
+    uint32_t* bricks = nullptr;
+    size_t brickBytes = 0;
+    uint4* lraw = nullptr;
+    float4* lgeom = nullptr;
+    float4* lemit = nullptr;
+    uint32_t nl = 0;
+    size_t lcap = 0;
+    uint64_t version = 0, lightVersion = 0;
+    int device = -1;
+};
+struct Proposal;   // learned candidate proposal state (proposal_api.cu)
+void destroy_proposal(Proposal* p);
+}  // namespace vxr
+
+struct vxr_view {
+    vxr_world* world = nullptr;
+    vxr_view_desc desc{};
+    vxr::CameraState cam;
+    vxr::ViewBuffers buf;
+    int cur = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t evs[6] = {}, eve[6] = {};            // [0]: vxr_view_timer_*, [1..5]: last frame's stages
+    bool ran[6] = {};
+    // per-stage event ring over the last kRing frames, harvested by vxr_view_wait
+    static constexpr int kRing = 256;
+    std::vector<cudaEvent_t> ringS, ringE;             // kRing * 6
+    std::vector<uint8_t> ringUsed;                     // kRing * 6
+    uint64_t frameSerial = 0, harvested = 0;
+    double statSum[6] = {};
+    uint32_t statCount[6] = {};
+    double* sum64 = nullptr;                          // FP64 running sum of shaded frames (rgb)
+    uint32_t sum64Count = 0;
+    double* errOut = nullptr;                         // [mse sum, mae sum]
+    vxr::Proposal* prop = nullptr;                    // learned proposal (optional)
+    bool useProposal = false;
+    bool frameOpen = false;
+    vxr_frame_consts k{};
+    uint64_t seenLightVersion = 0;
+    float times[5] = {};
+    size_t npx = 0;
+};
+
+
+namespace vxr {
+int check_view(vxr_view* v, const char* fn);
+dev::World dev_world(vxr_view* v);
+dev::Frame dev_frame(const vxr_frame_consts& c);
+int ensure_world(vxr_view* v);
+void free_view(vxr_view* v);
+void harvest(vxr_view* v);
+LaunchShape shape(const vxr_view* v);
+}  // namespace vxr

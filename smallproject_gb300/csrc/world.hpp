@@ -30,6 +30,9 @@ struct World {
     std::vector<uint32_t> freeList;    // recycled brick indices
     uint32_t brickHigh = 0;            // bricks ever allocated (pool high-water mark)
     std::vector<vxr_light> lights;
+    std::vector<uint32_t> lightCluster;   // cluster id per light (cluster_lights)
+    uint32_t clusterCount = 0;
+    uint64_t clusterVersion = 0;
     bool trackLights = true;
     uint64_t version = 1;              // bumps on every edit (device copy stale when different)
     uint64_t lightVersion = 1;         // bumps on every light-list change (temporal reset)

@@ -60,6 +60,11 @@ class SceneDesc(C.Structure):
                 ("scatter_fraction", C.c_float)]
 
 
+class ProposalDesc(C.Structure):
+    _fields_ = [("hidden", C.c_uint32), ("table_log2", C.c_uint32), ("res0", C.c_uint32), ("res1", C.c_uint32),
+                ("epsilon", C.c_float), ("learning_rate", C.c_float), ("batch", C.c_uint32), ("seed", C.c_uint32)]
+
+
 class ViewDesc(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("light_model", C.c_uint32),
                 ("num_candidates", C.c_uint32), ("spatial_taps", C.c_uint32), ("spatial_radius", C.c_uint32),
@@ -89,6 +94,8 @@ _SIGS = {
     "vxr_world_arrays": [_P, C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.POINTER(C.c_uint32)),
                          C.POINTER(C.c_uint32), C.POINTER(C.POINTER(Light)), C.POINTER(C.c_uint32)],
     "vxr_world_brick_count": [_P, C.POINTER(C.c_uint32)],
+    "vxr_world_cluster_lights": [_P, C.c_uint32, C.c_uint32, C.c_uint32],
+    "vxr_world_light_clusters": [_P, C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_uint32)],
     "vxr_scene_preset": [C.c_int, C.POINTER(SceneDesc)], "vxr_scene_generate": [_P, C.POINTER(SceneDesc)],
     "vxr_scene_height": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)],
     "vxr_camera_path": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.c_uint32, _F3, _F3],
@@ -112,6 +119,17 @@ _SIGS = {
     "vxr_camera_begin_frame": [_P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts)],
     "vxr_camera_end_frame": [_P],
     "vxr_host_alloc": [C.c_size_t, C.POINTER(_P)], "vxr_host_free": [_P],
+    "vxr_view_sum64_reset": [_P], "vxr_view_sum64_add": [_P],
+    "vxr_view_sum64_mean": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_double)],
+    "vxr_view_error": [_P, C.c_int, _P, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+    "vxr_proposal_default_desc": [C.POINTER(ProposalDesc)],
+    "vxr_view_proposal_enable": [_P, C.POINTER(ProposalDesc)], "vxr_view_proposal_use": [_P, C.c_int],
+    "vxr_view_proposal_train": [_P, C.c_uint32, C.POINTER(C.c_float)],
+    "vxr_view_proposal_param_count": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
+    "vxr_view_proposal_get_params": [_P, _F3], "vxr_view_proposal_set_params": [_P, _F3],
+    "vxr_view_proposal_grad": [_P, C.c_uint32, _F3, C.POINTER(C.c_uint32), _F3, C.POINTER(C.c_float), _F3],
+    "vxr_view_proposal_probs": [_P, C.c_uint32, _F3, _F3],
+    "vxr_view_proposal_save": [_P, C.c_char_p], "vxr_view_proposal_load": [_P, C.c_char_p],
     "vxr_render_frame_noalloc": [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts), _P, _P],
 }
 _RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
@@ -213,6 +231,18 @@ class World:
         else:
             lights = np.zeros(0, LIGHT_DTYPE)
         return grid, bricks, lights
+
+    def cluster_lights(self, k, seed=1, iters=8):
+        check(self._lib.vxr_world_cluster_lights(self.h, k, seed, iters))
+
+    def light_clusters(self):
+        p = C.POINTER(C.c_uint32)()
+        k = C.c_uint32()
+        check(self._lib.vxr_world_light_clusters(self.h, C.byref(p), C.byref(k)))
+        if not k.value:
+            return np.zeros(0, np.uint32), 0
+        n = self.arrays()[2].shape[0]
+        return np.ctypeslib.as_array(p, shape=(n,)).copy(), k.value
 
     def checksum(self):
         a, b = C.c_uint64(), C.c_uint64()
@@ -350,6 +380,79 @@ class View:
         cnt = (C.c_uint32 * 5)()
         check(self._lib.vxr_view_stage_stats(self.h, sm, cnt, 1 if reset else 0))
         return list(sm), list(cnt)
+
+    def sum64_reset(self):
+        check(self._lib.vxr_view_sum64_reset(self.h))
+
+    def sum64_add(self):
+        check(self._lib.vxr_view_sum64_add(self.h))
+
+    def sum64_mean(self):
+        n = C.c_uint32()
+        out = np.zeros(self.n * 3, np.float64)
+        check(self._lib.vxr_view_sum64_mean(self.h, C.byref(n), out.ctypes.data_as(C.POINTER(C.c_double))))
+        return n.value, out.reshape(-1, 3)
+
+    def error_vs(self, ref, which=0):
+        """(MSE, MAE) of this view's frame (which=0) or accumulator (1) vs ref's FP64 mean."""
+        mse, mae = C.c_double(), C.c_double()
+        check(self._lib.vxr_view_error(self.h, which, ref.h, C.byref(mse), C.byref(mae)))
+        return mse.value, mae.value
+
+    # ---- learned proposal
+    def proposal_enable(self, **kw):
+        d = ProposalDesc()
+        check(self._lib.vxr_proposal_default_desc(C.byref(d)))
+        for k, v in kw.items():
+            setattr(d, k, v)
+        check(self._lib.vxr_view_proposal_enable(self.h, C.byref(d)))
+        return d
+
+    def proposal_use(self, on):
+        check(self._lib.vxr_view_proposal_use(self.h, 1 if on else 0))
+
+    def proposal_train(self, steps=1):
+        loss = C.c_float()
+        check(self._lib.vxr_view_proposal_train(self.h, steps, C.byref(loss)))
+        return loss.value
+
+    def proposal_shape(self):
+        n, k, h = C.c_uint64(), C.c_uint32(), C.c_uint32()
+        check(self._lib.vxr_view_proposal_param_count(self.h, C.byref(n), C.byref(k), C.byref(h)))
+        return n.value, k.value, h.value
+
+    def proposal_params(self):
+        out = np.zeros(self.proposal_shape()[0], np.float32)
+        check(self._lib.vxr_view_proposal_get_params(self.h, out.ctypes.data_as(_F3)))
+        return out
+
+    def proposal_set_params(self, p):
+        a = np.ascontiguousarray(p, np.float32)
+        check(self._lib.vxr_view_proposal_set_params(self.h, a.ctypes.data_as(_F3)))
+
+    def proposal_grad(self, samples, target, weight):
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 4)
+        t = np.ascontiguousarray(target, np.uint32)
+        w = np.ascontiguousarray(weight, np.float32)
+        g = np.zeros(self.proposal_shape()[0], np.float32)
+        loss = C.c_float()
+        check(self._lib.vxr_view_proposal_grad(self.h, len(t), s.ctypes.data_as(_F3),
+                                               t.ctypes.data_as(C.POINTER(C.c_uint32)), w.ctypes.data_as(_F3),
+                                               C.byref(loss), g.ctypes.data_as(_F3)))
+        return loss.value, g
+
+    def proposal_probs(self, samples):
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 4)
+        k = self.proposal_shape()[1]
+        out = np.zeros((len(s), k), np.float32)
+        check(self._lib.vxr_view_proposal_probs(self.h, len(s), s.ctypes.data_as(_F3), out.ctypes.data_as(_F3)))
+        return out
+
+    def proposal_save(self, path):
+        check(self._lib.vxr_view_proposal_save(self.h, str(path).encode()))
+
+    def proposal_load(self, path):
+        check(self._lib.vxr_view_proposal_load(self.h, str(path).encode()))
 
     def timer_begin(self):
         check(self._lib.vxr_view_timer_begin(self.h))

@@ -1,0 +1,98 @@
+"""The product's device-side traversal and trig (smallproject_gb300/csrc/device.cuh),
+compiled for the host CPU by tests/native/build_devhost.py, against the oracle:
+- trace<MODE> (primary rays, shadow rays, trace-through) bit-exact with the oracle's
+  DDA for fuzzed rays;
+- the resumable walker used by the persistent shadow tracer bit-exact with trace<1>;
+- sincos_vx identical to the oracle's sin/cos on reachable tap angles.
+A CPU check of the GPU code's arithmetic; the GPU tests check the compiled kernels."""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import binding as ob
+
+sys.path.insert(0, os.path.join(ROOT, "tests", "native"))
+import build_devhost  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def dh():
+    path = build_devhost.build()
+    if path is None:
+        pytest.skip("CUDA headers unavailable")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    F = C.POINTER(C.c_float)
+    lib.dh_trace.restype = C.c_uint32
+    lib.dh_trace.argtypes = [C.c_int, P, P, P, F, F, C.c_int, C.c_uint32, C.c_uint32, F, C.POINTER(C.c_uint32)]
+    lib.dh_walk.restype = C.c_uint32
+    lib.dh_walk.argtypes = [P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.dh_sincos.argtypes = [C.c_float, F, F]
+    return lib
+
+
+def _rays(n, seed, lo=-300.0, hi=1300.0, inside=(0.0, 256.0)):
+    rng = np.random.default_rng(seed)
+    o = np.concatenate([rng.uniform(lo, hi, (n // 2, 3)), rng.uniform(*inside, (n - n // 2, 3))]).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[::7, 0] = 0.0
+    d[::13, 2] = 1e-9
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o, d.astype(np.float32), rng
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_device_trace_matches_oracle(dh, world0_arrays, mode):
+    wa = world0_arrays
+    port = ob.Renderer("port", wa, 4, 4, False)
+    o, d, rng = _rays(3000, 100 + mode)
+    for i in range(len(o)):
+        steps = int(rng.choice([128, 999999, 9]))
+        through = int(rng.choice([0, 0x7F44, 0xF888]))
+        dist, side = C.c_float(0), C.c_uint32(0)
+        v = dh.dh_trace(mode, wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, _f3(o[i]), _f3(d[i]),
+                        steps, through, 0xFFFF, C.byref(dist), C.byref(side))
+        want = port.trace(mode, o[i], d[i], steps, through, 0xFFFF)
+        assert (v, side.value) == (want[0], want[2]) and \
+            np.float32(dist.value).view(np.uint32) == np.float32(want[1]).view(np.uint32), (i, o[i], d[i])
+
+
+def test_walker_matches_recursive_trace(dh, world0_arrays):
+    wa = world0_arrays
+    o, d, rng = _rays(6000, 7)
+    # shadow-ray-like rays: from just above the terrain surface towards random points
+    total_visits = 0
+    for i in range(len(o)):
+        steps = int(rng.choice([128, 128, 999999, 5, 1]))
+        dist, side = C.c_float(0), C.c_uint32(0)
+        v = dh.dh_trace(1, wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, _f3(o[i]), _f3(d[i]),
+                        steps, 0, 0, C.byref(dist), C.byref(side))
+        dist2, side2, st, nv = C.c_float(0), C.c_uint32(0), C.c_int(0), C.c_int(0)
+        v2 = dh.dh_walk(wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, _f3(o[i]), _f3(d[i]), steps,
+                        C.byref(dist2), C.byref(side2), C.byref(st), C.byref(nv))
+        total_visits += nv.value
+        if st.value == 1:
+            assert v == v2 and side.value == side2.value and \
+                np.float32(dist.value).view(np.uint32) == np.float32(dist2.value).view(np.uint32), (i, o[i], d[i])
+        else:
+            assert v == 0, (i, o[i], d[i], v)
+    assert total_visits > 10000
+
+
+def test_device_sincos_matches_oracle(dh):
+    rng = np.random.default_rng(5)
+    s = rng.integers(0, 2 ** 32, 50000, dtype=np.uint64).astype(np.uint32)
+    a = (s.astype(np.float32) * np.float32(2.3283064365387e-10)).astype(np.float32) * np.float32(6.28318530717958647692528)
+    for x in a.astype(np.float32):
+        sn, cs = C.c_float(), C.c_float()
+        dh.dh_sincos(float(x), C.byref(sn), C.byref(cs))
+        osn, ocs = ob.sincos(float(x))
+        assert np.float32(sn.value) == np.float32(osn) and np.float32(cs.value) == np.float32(ocs), x

@@ -1,0 +1,153 @@
+"""Learned candidate proposal on the GPU: FP32 gradients against the FP64 restatement
+(oracle/proposal_ref.py), BF16 inference probabilities against FP64, checkpoint round
+trip, unbiasedness of the learned source pdf, and the gain of a trained network over
+the uniform source at equal candidate count."""
+import numpy as np
+import pytest
+
+from oracle import proposal_ref as pr
+
+pytestmark = pytest.mark.gpu
+
+
+def _samples(rng, n, lo=0.0, hi=256.0):
+    pos = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    code = rng.integers(0, 6, n).astype(np.uint32)
+    s = np.zeros((n, 4), np.float32)
+    s[:, :3] = pos
+    s[:, 3] = code.view(np.float32)
+    return s
+
+
+@pytest.fixture(scope="module")
+def clustered_view(lib, cuda_device):
+    w = lib.World()
+    w.generate(lib.scene_preset(0))
+    w.cluster_lights(16, seed=3, iters=6)
+    v = lib.View(w, lib.view_desc(96, 64, lib.LIGHTS_AREA))
+    v.proposal_enable(seed=7, batch=4096)
+    yield w, v
+    v.close()
+
+
+def test_gradients_match_fp64(lib, clustered_view):
+    w, v = clustered_view
+    n, K, H = v.proposal_shape()
+    rng = np.random.default_rng(1)
+    params = v.proposal_params().astype(np.float64)
+    # make the encoding and biases non-trivial so every tensor's gradient is exercised
+    L = pr.layout(H, K)
+    o, sz = L["enc"]
+    params[o:o + sz] = rng.normal(0, 0.5, sz)
+    for b in ("b1", "b2", "b3", "b4"):
+        o, sz = L[b]
+        params[o:o + sz] = rng.normal(0, 0.1, sz)
+    v.proposal_set_params(params.astype(np.float32))
+    p32 = v.proposal_params().astype(np.float64)
+    B = 256
+    s = _samples(rng, B)
+    t = rng.integers(0, K, B).astype(np.uint32)
+    wt = rng.uniform(0.0, 2.0, B).astype(np.float32)
+    wt[::9] = 0.0
+    loss, g = v.proposal_grad(s, t, wt)
+    rloss, rg, L = pr.loss_and_grad(p32, s, t, wt.astype(np.float64), H, K)
+    assert loss == pytest.approx(rloss, rel=1e-4)
+    for name in ("enc", "W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4"):
+        o, sz = L[name]
+        a, b = g[o:o + sz].astype(np.float64), rg[o:o + sz]
+        err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        assert err < 1e-3, (name, err)
+
+
+def test_inference_probabilities_match_fp64(lib, clustered_view):
+    w, v = clustered_view
+    n, K, H = v.proposal_shape()
+    rng = np.random.default_rng(2)
+    s = _samples(rng, 300)
+    probs = v.proposal_probs(s)
+    ref = pr.softmax(pr.forward(v.proposal_params().astype(np.float64), s, H, K)[-1])
+    assert np.allclose(probs.sum(1), 1.0, atol=1e-3)
+    # BF16 weights/activations and FP16 logits: absolute error on probabilities
+    assert np.abs(probs - ref).max() < 2e-2
+
+
+def test_checkpoint_round_trip(lib, clustered_view, tmp_path):
+    w, v = clustered_view
+    p0 = v.proposal_params()
+    v.proposal_save(tmp_path / "prop.bin")
+    v.proposal_set_params(np.zeros_like(p0))
+    v.proposal_load(tmp_path / "prop.bin")
+    assert np.array_equal(v.proposal_params(), p0)
+
+
+def _converged_mean(lib, world, learned, frames, pos, tgt, seed, W=96, H=64, train_view=None):
+    v = lib.View(world, lib.view_desc(W, H, lib.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=seed))
+    v.lookat(pos, tgt)
+    if learned:
+        v.proposal_enable(seed=5, batch=4096)
+        if train_view is not None:
+            v.proposal_set_params(train_view.proposal_params())
+        v.proposal_use(True)
+    v.sum64_reset()
+    for _ in range(frames):
+        v.render()
+        v.sum64_add()
+    n, mean = v.sum64_mean()
+    v.close()
+    return mean
+
+
+def test_learned_source_is_unbiased(lib, cuda_device):
+    """Spatial/temporal off: RIS is unbiased for any source pdf > 0, so the learned
+    (untrained, random) proposal and the uniform one converge to the same image."""
+    w = lib.World()
+    w.generate(lib.scene_preset(0))
+    w.cluster_lights(16, seed=3, iters=6)
+    pos, tgt = (128.0, 150.0, 20.0), (128.0, 100.0, 128.0)
+    a = _converged_mean(lib, w, False, 384, pos, tgt, 11)
+    b = _converged_mean(lib, w, True, 384, pos, tgt, 12)
+    ma, mb = a.mean(), b.mean()
+    assert ma > 0 and abs(ma - mb) / ma < 0.03, (ma, mb)
+
+
+def test_trained_proposal_beats_uniform(lib, cuda_device):
+    """Many emitters (config 3 lights), a short online training on the plain method's
+    reservoirs: at equal candidate count the learned source lowers the single-frame MSE
+    against the converged render."""
+    w = lib.World()
+    w.generate(lib.scene_preset(3))
+    w.cluster_lights(256, seed=1, iters=6)
+    d = lib.scene_preset(3)
+    pos, tgt = lib.camera_path(d, 1, 0, 300)
+    W, H = 192, 108
+    ref = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=77))
+    ref.lookat(pos, tgt)
+    ref.sum64_reset()
+    for _ in range(1024):
+        ref.render()
+        ref.sum64_add()
+    trainer = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, rng_seed=5))
+    trainer.lookat(pos, tgt)
+    trainer.proposal_enable(seed=2, batch=8192)
+    losses = []
+    for it in range(60):
+        trainer.render()
+        losses.append(trainer.proposal_train(2))
+    assert np.mean(losses[-10:]) < np.mean(losses[:5])
+    errs = {}
+    for learned in (False, True):
+        v = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=31))
+        v.lookat(pos, tgt)
+        if learned:
+            v.proposal_enable(seed=2, batch=8192)
+            v.proposal_set_params(trainer.proposal_params())
+            v.proposal_use(True)
+        e = []
+        for _ in range(16):
+            v.render()
+            e.append(v.error_vs(ref, 0)[0])
+        errs[learned] = float(np.mean(e))
+        v.close()
+    assert errs[True] < errs[False], errs
+    trainer.close()
+    ref.close()
