@@ -368,6 +368,32 @@ int vxr_view_sum64_mean(vxr_view* v, uint32_t* count, double* mean);
  * shaded frame, 1 the accumulator. Same resolution required. FP64 accumulation. */
 int vxr_view_error(vxr_view* img, int which, vxr_view* ref, double* mse, double* mae);
 
+/* ---- batches: several views rendered as one frame -------------------------------------
+ * No counterpart in the reference: World::Render (world.cpp:2127-2340) draws one camera
+ * per call, so several views are rendered one after another. A batch renders one frame of
+ * up to VXR_BATCH_MAX_VIEWS views - each with its own world, resolution, light model and
+ * parameters - with every stage as one launch over all of them: the pixel stages pull
+ * (view, tile) work items from a device queue, and the candidate loop, the temporal step
+ * and the shadow rays run over one list of every view's hit pixels. Each view's images,
+ * G-buffers and reservoirs are bit-identical to rendering it alone with vxr_view_render.
+ * Views must be on one device, hold at most 2^27 - 1 pixels each and not use a learned
+ * proposal. tile_x * tile_y = threads of a pixel-stage block (0, 0 = 16 x 8), a multiple
+ * of 32 up to 1024. flags: VXR_BATCH_GRAPH records the frame once as a CUDA graph and
+ * replays it: one graph launch per frame. */
+#define VXR_BATCH_MAX_VIEWS 16u
+#define VXR_BATCH_GRAPH     1u
+typedef struct vxr_batch vxr_batch;
+int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32_t tile_y, uint32_t flags,
+                     vxr_batch** out);
+int vxr_batch_destroy(vxr_batch* b);
+/* One frame of every view: vxr_view_begin_frame, stages 1-4 with the accumulator fused
+ * into shading, vxr_view_end_frame. Asynchronous; ordered after earlier work on each
+ * view's stream and before later work on it (read results with the view calls). */
+int vxr_batch_render(vxr_batch* b);
+/* Wait for the batch's frames. ms (may be NULL): GPU time of the last frame. A device
+ * error flag raised in any view -> VXR_E_DEVICE. */
+int vxr_batch_wait(vxr_batch* b, float* ms);
+
 /* ---- rendering without allocation ---------------------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc - an
  * application that owns all GPU memory through its own pool, a plugin that must not

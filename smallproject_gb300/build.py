@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvxr.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["kernels.cu", "runtime.cu", "noalloc.cu", "proposal.cu", "proposal_api.cu"]
+CU_SOURCES = ["kernels.cu", "runtime.cu", "batch.cu", "noalloc.cu", "proposal.cu", "proposal_api.cu"]
 CPP_SOURCES = ["world.cpp", "scene.cpp", "camera.cpp", "capi_world.cpp", "cluster.cpp"]
 HEADERS = ["device.cuh", "kernels.hpp", "world.hpp", "camera.hpp", "internal.hpp", "proposal.cuh", "proposal.hpp", "view.hpp"]
 

@@ -1,0 +1,246 @@
+// batch.cu - several views rendered as one frame (no reference counterpart: World::Render
+// draws one camera per call, template/world.cpp:2127-2340).
+//
+// A batch owns the work lists of all its views (hit list, shadow-ray queue, counters:
+// sized for the sum of their pixels) and a device table of ViewDev records that every
+// stage kernel reads. Each frame the host fills the table in page-locked memory, copies
+// it to the device on the batch stream and launches the four stages once for all views
+// (kernels.cu, VARIANT 2). With VXR_BATCH_GRAPH the table copy and the stage launches are
+// recorded once per staging slot as a CUDA graph and a frame is one cudaGraphLaunch.
+//
+// Staging: two page-locked table slots used alternately; before the host rewrites a
+// slot it waits for the frame that last read it (an event recorded after that frame).
+// Graph validity: the captured launches depend only on the view count, the views'
+// resolutions and the tile shape, all fixed at creation; everything that changes per
+// frame (frame constants, camera, world buffers after a re-upload, G-buffer plane) is in
+// the table.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "internal.hpp"
+#include "kernels.hpp"
+#include "view.hpp"
+
+struct vxr_batch {
+    std::vector<vxr_view*> views;
+    vxr::BatchDev bd;                       // table pointer, totals, list buffers
+    vxr::ViewDev* table = nullptr;          // device table [n]
+    vxr::ViewDev* staging[2] = {nullptr, nullptr};   // page-locked host slots
+    cudaEvent_t slotDone[2] = {nullptr, nullptr};
+    bool slotUsed[2] = {false, false};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool useGraph = false;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> viewReady;     // per view: its stream's work before the frame
+    cudaEvent_t frameDone = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr; // GPU time of the last frame
+    bool timed = false;
+    uint64_t frames = 0;
+};
+
+namespace {
+
+void free_batch(vxr_batch* b) {
+    for (int i = 0; i < 2; i++) {
+        if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+        if (b->staging[i]) cudaFreeHost(b->staging[i]);
+        if (b->slotDone[i]) cudaEventDestroy(b->slotDone[i]);
+    }
+    cudaFree(b->table);
+    cudaFree(b->bd.hits);
+    cudaFree(b->bd.qA);
+    cudaFree(b->bd.qB);
+    cudaFree(b->bd.counters);
+    for (cudaEvent_t e : b->viewReady)
+        if (e) cudaEventDestroy(e);
+    if (b->frameDone) cudaEventDestroy(b->frameDone);
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->t1) cudaEventDestroy(b->t1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// The frame's device work on the batch stream: table upload from slot `slot`, stages 1-4.
+void enqueue_frame(vxr_batch* b, int slot) {
+    const size_t n = b->views.size();
+    cudaMemcpyAsync(b->table, b->staging[slot], n * sizeof(vxr::ViewDev), cudaMemcpyHostToDevice, b->stream);
+    vxr::launch_batch_albedo(b->bd, 2, b->stream);
+    vxr::launch_batch_candidates(b->bd, 2, nullptr, b->stream);
+    vxr::launch_batch_spatial(b->bd, 2, b->stream);
+    vxr::launch_batch_shade(b->bd, 2, b->stream);
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+    return vxr::set_error(e == cudaErrorMemoryAllocation ? VXR_E_NOMEM : VXR_E_CUDA,
+                          std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+extern "C" {
+
+int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32_t tile_y, uint32_t flags, vxr_batch** out) {
+    VXR_CHECK_ARG(views && out, "vxr_batch_create: null argument");
+    VXR_CHECK_ARG(n >= 1 && n <= VXR_BATCH_MAX_VIEWS, "vxr_batch_create: view count out of range [1, VXR_BATCH_MAX_VIEWS]");
+    VXR_CHECK_ARG((flags & ~VXR_BATCH_GRAPH) == 0, "vxr_batch_create: unknown flags");
+    const uint32_t tx = tile_x ? tile_x : 16, ty = tile_y ? tile_y : 8;
+    VXR_CHECK_ARG(tx * ty >= 32 && tx * ty <= 1024 && (tx * ty) % 32 == 0,
+                  "vxr_batch_create: tile must hold a multiple of 32 threads, at most 1024");
+    uint64_t total = 0, tiles = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        VXR_CHECK_ARG(views[i], "vxr_batch_create: null view");
+        for (uint32_t j = 0; j < i; j++) VXR_CHECK_ARG(views[j] != views[i], "vxr_batch_create: a view appears twice");
+        VXR_CHECK_ARG(views[i]->npx < (1ull << 27), "vxr_batch_create: a batched view holds at most 2^27 - 1 pixels");
+        VXR_CHECK_ARG(!views[i]->world->w.dev || views[i]->world->w.dev->device == views[0]->world->w.dev->device,
+                      "vxr_batch_create: views on different devices");
+        total += views[i]->npx;
+        tiles += (uint64_t)((views[i]->desc.width + tx - 1) / tx) * ((views[i]->desc.height + ty - 1) / ty);
+    }
+    VXR_CHECK_ARG(total < (1ull << 32) && tiles < (1ull << 32), "vxr_batch_create: batch too large");
+    vxr_batch* b = new (std::nothrow) vxr_batch();
+    if (!b) return vxr::set_error(VXR_E_NOMEM, "vxr_batch_create: out of host memory");
+    b->views.assign(views, views + n);
+    b->useGraph = (flags & VXR_BATCH_GRAPH) != 0;
+    cudaGetDevice(&b->device);
+    vxr::BatchDev& bd = b->bd;
+    bd.nviews = n;
+    bd.totalPixels = (uint32_t)total;
+    bd.totalTiles = (uint32_t)tiles;
+    bd.tx = (int)tx;
+    bd.ty = (int)ty;
+    bd.fuse = 1;
+    cudaError_t e = cudaSuccess;
+    auto dalloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
+    };
+    dalloc((void**)&b->table, n * sizeof(vxr::ViewDev));
+    dalloc((void**)&bd.hits, total * sizeof(uint32_t));
+    dalloc((void**)&bd.qA, total * sizeof(float4));
+    dalloc((void**)&bd.qB, total * sizeof(float4));
+    dalloc((void**)&bd.counters, vxr::kCounters * sizeof(uint32_t));
+    bd.views = b->table;
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        e = cudaHostAlloc((void**)&b->staging[i], n * sizeof(vxr::ViewDev), cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->slotDone[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    b->viewReady.assign(n, nullptr);
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->viewReady[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->frameDone, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        delete b;
+        return cuda_error(e, "vxr_batch_create");
+    }
+    *out = b;
+    return VXR_OK;
+}
+
+int vxr_batch_destroy(vxr_batch* b) {
+    if (!b) return VXR_OK;
+    cudaStreamSynchronize(b->stream);
+    free_batch(b);
+    delete b;
+    return VXR_OK;
+}
+
+int vxr_batch_render(vxr_batch* b) {
+    VXR_CHECK_ARG(b, "vxr_batch_render: null batch");
+    const size_t n = b->views.size();
+    for (vxr_view* v : b->views) {
+        if (v->useProposal) return vxr::set_error(VXR_E_INVALID, "vxr_batch_render: a view uses a learned proposal");
+        if (v->frameOpen) return vxr::set_error(VXR_E_STATE, "vxr_batch_render: a view has a frame in progress");
+    }
+    const int slot = (int)(b->frames & 1u);
+    if (b->slotUsed[slot]) {
+        const cudaError_t e = cudaEventSynchronize(b->slotDone[slot]);
+        if (e != cudaSuccess) return cuda_error(e, "vxr_batch_render: wait for staging slot");
+    }
+    // begin every view's frame (camera, frame constants, G-buffer swap) and fill the table
+    uint32_t tileBase = 0;
+    for (size_t i = 0; i < n; i++) {
+        vxr_view* v = b->views[i];
+        if (int r = vxr_view_begin_frame(v, nullptr)) {
+            for (size_t j = 0; j < i; j++) vxr_view_end_frame(b->views[j]);
+            return r;
+        }
+        vxr::ViewDev& d = b->staging[slot][i];
+        d = vxr::ViewDev();
+        d.w = vxr::dev_world(v);
+        d.k = vxr::dev_frame(v->k);
+        d.b = v->buf;
+        d.cur = v->cur;
+        d.point = v->desc.light_model == VXR_LIGHTS_POINT ? 1 : 0;
+        d.tilesX = (v->desc.width + (uint32_t)b->bd.tx - 1) / (uint32_t)b->bd.tx;
+        d.tileBase = tileBase;
+        tileBase += d.tilesX * ((v->desc.height + (uint32_t)b->bd.ty - 1) / (uint32_t)b->bd.ty);
+    }
+    cudaError_t e = cudaSuccess;
+    // order after each view's earlier work
+    for (size_t i = 0; i < n && e == cudaSuccess; i++) {
+        e = cudaEventRecord(b->viewReady[i], b->views[i]->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->viewReady[i], 0);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->t0, b->stream);
+    if (e == cudaSuccess && b->useGraph) {
+        if (!b->graph[slot]) {
+            cudaGraph_t g = nullptr;
+            e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                enqueue_frame(b, slot);
+                e = cudaStreamEndCapture(b->stream, &g);
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[slot], g, 0);
+            if (g) cudaGraphDestroy(g);
+        }
+        if (e == cudaSuccess) e = cudaGraphLaunch(b->graph[slot], b->stream);
+    } else if (e == cudaSuccess) {
+        enqueue_frame(b, slot);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->t1, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->slotDone[slot], b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->frameDone, b->stream);
+    // later work on each view's stream waits for the frame
+    for (size_t i = 0; i < n && e == cudaSuccess; i++) e = cudaStreamWaitEvent(b->views[i]->stream, b->frameDone, 0);
+    for (vxr_view* v : b->views) vxr_view_end_frame(v);
+    if (e != cudaSuccess) return cuda_error(e, "vxr_batch_render");
+    b->slotUsed[slot] = true;
+    b->timed = true;
+    b->frames++;
+    return VXR_OK;
+}
+
+int vxr_batch_wait(vxr_batch* b, float* ms) {
+    VXR_CHECK_ARG(b, "vxr_batch_wait: null batch");
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_error(e, "vxr_batch_wait");
+    if (ms) {
+        *ms = 0.0f;
+        if (b->timed && cudaEventElapsedTime(ms, b->t0, b->t1) != cudaSuccess) *ms = 0.0f;
+    }
+    uint32_t any = 0;
+    for (vxr_view* v : b->views) {
+        uint32_t err = 0;
+        e = cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_error(e, "vxr_batch_wait: read device error flags");
+        if (err) {
+            cudaMemset(v->buf.err, 0, sizeof(uint32_t));
+            any |= err;
+        }
+    }
+    if (any)
+        return vxr::set_error(VXR_E_DEVICE, "device error flags 0x" + std::to_string(any) +
+                                                " (2: temporal light index, 4: spatial light index, 8: shading light index)");
+    return VXR_OK;
+}
+
+}  // extern "C"

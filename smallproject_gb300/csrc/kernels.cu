@@ -7,24 +7,29 @@
 //   reservoirs C, H   uint4 + float4 planes (see Res in device.cuh), 32 B/pixel each:
 //              C = candidate+temporal output, H = spatial output = temporal history
 //   frame      float4 (rgb, dist); accum float4 (running mean, the output image)
-//   hits       uint32 list of the pixels whose primary ray hit a voxel
-//   queue      float4 x 2 per entry: shadow-ray requests (origin | pixel, dir | light)
-//   counters   uint32[8]: hit count, request count / fetch cursor of the two queues
+// and per batch of views:
+//   hits       uint32 list of (view << 27 | pixel) whose primary ray hit a voxel
+//   queue      float4 x 2 per entry: shadow-ray requests (origin | entry, dir | light)
+//   counters   uint32[kCounters]: list lengths and work-queue cursors (kernels.hpp)
 // The reference cycles two 80-byte reservoir buffers through three roles per frame
 // (world.cpp:2209-2219) and copies the shaded reservoir at the end of shading
 // (ris.cl:412). Here the spatial pass writes H in place of the previous history,
 // which the candidate pass has finished reading, and shading patches H on a failed
 // visibility test; H is then next frame's history without any copy.
 //
-// Work decomposition (wavefront): the reference runs one work item per pixel through
-// each whole kernel, so sky pixels idle beside terrain pixels and every warp waits for
-// its longest shadow ray. Here (1) hit pixels are compacted into a list, (2) the
-// candidate loop, the temporal step and the shading request run over that list, and
-// (3) every shadow ray goes through one persistent tracer whose lanes take a new ray
-// as soon as theirs ends. Each pixel's arithmetic is unchanged, so results are the
-// same bit for bit whatever order pixels and rays are processed in.
+// Work decomposition: the reference runs one work item per pixel through each whole
+// kernel, so sky pixels idle beside terrain pixels and every warp waits for its
+// longest shadow ray. Here every stage is one launch over a table of views (one view,
+// or a batch of up to 16 independent views with their own worlds, resolutions and
+// light models): pixel stages are persistent blocks pulling screen tiles from a work queue;
+// the candidate loop, the temporal step and the shading request run over a compacted
+// list of hit pixels; and every shadow ray goes through one persistent tracer whose
+// lanes take a new ray as soon as theirs ends. Each pixel's arithmetic is unchanged,
+// so results are the same bit for bit whatever order pixels and rays are processed in.
 #include <algorithm>
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -66,10 +71,67 @@ __global__ void build_uber_kernel(const uint32_t* __restrict__ grid, uint8_t* ub
     uber[x + z * 32 + y * 1024] = empty ? 0 : 1;
 }
 
+
+// ---- work distribution --------------------------------------------------------------------
+// VARIANT of a launch: 0 one view with area lights, 1 one view with point lights (the
+// view is read from the kernel parameter), 2 a table of views in device memory, light
+// model per view.
+constexpr uint32_t kPixMask = (1u << 27) - 1u;
+
+template <int VARIANT>
+__device__ __forceinline__ const ViewDev* view_of(const BatchDev& bd, uint32_t v) {
+    if (VARIANT < 2) return &bd.one;
+    return bd.views + v;
+}
+// pixel of a hit-list or request entry (a single view's entries are the bare pixel index,
+// so a single view may hold more than 2^27 pixels)
+template <int VARIANT>
+__device__ __forceinline__ uint32_t pix_of(uint32_t e) {
+    return VARIANT < 2 ? e : (e & kPixMask);
+}
+template <int VARIANT>
+__device__ __forceinline__ bool point_of(const ViewDev* V) {
+    return VARIANT == 1 || (VARIANT == 2 && V->point);
+}
+
+// warp-aggregated append to a list: one atomic per group of lanes that call it together
+__device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+// next tile of the batch for this block (tile-queue cursor `ctr`); false when drained
+__device__ __forceinline__ bool next_tile(const BatchDev& bd, uint32_t* ctr, uint32_t* tile) {
+    __shared__ uint32_t s_tile;
+    __syncthreads();
+    if (threadIdx.x == 0) s_tile = atomicAdd(ctr, 1u);
+    __syncthreads();
+    *tile = s_tile;
+    return s_tile < bd.totalTiles;
+}
+
+// view of a batch tile and the pixel of this thread in it
+template <int VARIANT>
+__device__ __forceinline__ const ViewDev* tile_pixel(const BatchDev& bd, uint32_t tile, int* x, int* y) {
+    uint32_t v = 0;
+    if (VARIANT == 2)
+        while (v + 1 < bd.nviews && bd.views[v + 1].tileBase <= tile) v++;
+    const ViewDev* V = view_of<VARIANT>(bd, v);
+    const uint32_t lt = tile - V->tileBase;
+    const uint32_t tx = lt % V->tilesX, ty = lt / V->tilesX;
+    *x = (int)(tx * (uint32_t)bd.tx + threadIdx.x % (uint32_t)bd.tx);
+    *y = (int)(ty * (uint32_t)bd.ty + threadIdx.x / (uint32_t)bd.tx);
+    return V;
+}
+
 // ---- stage 1: primary rays / G-buffer (renderAlbedo, ris.cl:295-389) --------------------
-__global__ void __launch_bounds__(128) albedo_kernel(World w, Frame k, uint2* __restrict__ vd, uint32_t* __restrict__ seeds) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= k.W || y >= k.H) return;
+__device__ __forceinline__ void albedo_px(const World& w, const Frame& k, uint2* __restrict__ vd, uint32_t* __restrict__ seeds,
+                                          int x, int y) {
     const uint32_t seed = wang_hash((uint32_t)x * 171u + (uint32_t)y * 1773u + k.R0);
     const float3 D = camera_ray(k, x, y);
     uint32_t side = 0;
@@ -103,26 +165,33 @@ __global__ void __launch_bounds__(128) albedo_kernel(World w, Frame k, uint2* __
     seeds[i] = seed;
 }
 
-// warp-aggregated append to a list: one atomic per group of lanes that call it together
-__device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
-    const unsigned m = __activemask();
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
-    base = __shfl_sync(m, base, leader);
-    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+template <int VARIANT>
+__global__ void __launch_bounds__(128) albedo_kernel(const __grid_constant__ BatchDev bd) {
+    uint32_t tile;
+    while (next_tile(bd, bd.counters + kCtrAlbedo, &tile)) {
+        int x, y;
+        const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
+        const Frame& k = V->k;
+        if (x < k.W && y < k.H) {
+            const World w = V->w;
+            albedo_px(w, k, V->b.vd[V->cur], V->b.seed, x, y);
+        }
+    }
 }
 
-// Hit list for the frame; pixels without a hit get the empty reservoir (ris.cl:34,123).
-__global__ void __launch_bounds__(256) compact_hits_kernel(Frame k, const uint2* __restrict__ vd, uint32_t* __restrict__ hits,
-                                                           uint32_t* counters, uint4* __restrict__ cA,
-                                                           float4* __restrict__ cB) {
-    const uint32_t n = (uint32_t)k.W * (uint32_t)k.H;
+// Hit list of the frame over every view (blockIdx.y = view); pixels without a hit get
+// the empty reservoir (ris.cl:34,123).
+template <int VARIANT>
+__global__ void __launch_bounds__(256) compact_hits_kernel(const __grid_constant__ BatchDev bd) {
+    const ViewDev* V = view_of<VARIANT>(bd, blockIdx.y);
+    const uint32_t n = (uint32_t)V->k.W * (uint32_t)V->k.H;
+    const uint2* vd = V->b.vd[V->cur];
+    uint4* cA = V->b.cA;
+    float4* cB = V->b.cB;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t voxel = vd[i].x & 0x00FFFFFFu;
         if (voxel != 0u) {
-            hits[append_slot(&counters[0])] = i;
+            bd.hits[append_slot(bd.counters + kCtrHits)] = (blockIdx.y << 27) | i;
         } else {
             cA[i] = make_uint4(0u, 6u << 29, 0u, 0u);
             cB[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -172,15 +241,16 @@ __device__ __forceinline__ float phat(float3 pos, uint32_t ncode, float3 sp, uin
 }
 
 // ---- visibility (isLightOccluded, ris.cl:1-17) -----------------------------------------
-// Persistent shadow tracer. Requests: qA = (origin, bits(pixel)), qB = (dir, bits(light)).
-// Budget GRIDWIDTH = 128 steps (ris.cl:10); a miss leaves dist/side at 0 (the fixed
-// convention for the reference's uninitialised locals); visible iff the hit voxel
-// (hit point - 0.1 N, truncated) lies in the emitter cube [pos, pos + size)
-// (GridCoordinatesFromHit / Uint3CubeEquals, tools.cl:452-472). An occluded request
-// zeroes sumOfWeights of its pixel in `plane` (W follows: ris.cl:79-80, 248-250).
-// Lanes refill from the queue as soon as enough of them are idle.
-__device__ __forceinline__ void shadow_finish(const World& w, int st, const Walker& wk, float3 o, float3 L, uint32_t pix,
-                                              uint32_t li, uint32_t* plane) {
+// Persistent shadow tracer over the batch's request queue. Requests:
+// qA = (origin, bits(view << 27 | pixel)), qB = (dir, bits(light)). Budget GRIDWIDTH = 128
+// steps (ris.cl:10); a miss leaves dist/side at 0 (the fixed convention for the
+// reference's uninitialised locals); visible iff the hit voxel (hit point - 0.1 N,
+// truncated) lies in the emitter cube [pos, pos + size) (GridCoordinatesFromHit /
+// Uint3CubeEquals, tools.cl:452-472). An occluded request zeroes sumOfWeights of its
+// pixel in reservoir plane C (plane 0) or H (plane 1) of its view (W follows:
+// ris.cl:79-80, 248-250). Lanes refill from the queue as soon as enough are idle.
+__device__ __forceinline__ void shadow_finish(const World& w, int st, const Walker& wk, float3 o, float3 L, uint32_t* plane,
+                                              uint32_t pix, uint32_t li) {
     const float d2 = st == WALK_HIT ? wk.dist : 0.0f;
     const uint32_t s2 = st == WALK_HIT ? wk.side : 0u;
     const float ns = side_sign(s2, L);
@@ -195,12 +265,15 @@ __device__ __forceinline__ void shadow_finish(const World& w, int st, const Walk
     if (!inside) plane[(size_t)pix * 4u + 2u] = 0u;
 }
 
-__global__ void __launch_bounds__(128) shadow_kernel(World w, const float4* __restrict__ qA, const float4* __restrict__ qB,
-                                                     const uint32_t* count, uint32_t* fetch, uint32_t* plane,
-                                                     int refill) {
-    const uint32_t n = *count;
+template <int VARIANT>
+__global__ void __launch_bounds__(128) shadow_kernel(const __grid_constant__ BatchDev bd, int countIdx, int fetchIdx,
+                                                     int planeSel, int refill) {
+    const uint32_t n = bd.counters[countIdx];
+    uint32_t* fetch = bd.counters + fetchIdx;
     const int lane = threadIdx.x & 31;
     Walker wk;
+    World w;
+    uint32_t* plane = nullptr;
     bool active = false, exhausted = false;
     float3 o = f3(0.0f, 0.0f, 0.0f), L = f3(0.0f, 0.0f, 0.0f);
     uint32_t pix = 0, li = 0;
@@ -214,14 +287,18 @@ __global__ void __launch_bounds__(128) shadow_kernel(World w, const float4* __re
             if (!active) {
                 const uint32_t r = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (r < n) {
-                    const float4 a = __ldg(qA + r), b = __ldg(qB + r);
+                    const float4 a = __ldg(bd.qA + r), b = __ldg(bd.qB + r);
                     o = f3(a.x, a.y, a.z);
                     L = f3(b.x, b.y, b.z);
-                    pix = __float_as_uint(a.w);
+                    const uint32_t e = __float_as_uint(a.w);
+                    const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
+                    pix = pix_of<VARIANT>(e);
                     li = __float_as_uint(b.w);
+                    w = V->w;
+                    plane = reinterpret_cast<uint32_t*>(planeSel ? V->b.hA : V->b.cA);
                     const int st = walk_init(wk, w, o.x, o.y, o.z, L.x, L.y, L.z, 128);
                     if (st == WALK_CONTINUE) active = true;
-                    else shadow_finish(w, st, wk, o, L, pix, li, plane);
+                    else shadow_finish(w, st, wk, o, L, plane, pix, li);
                 }
             }
         }
@@ -234,7 +311,7 @@ __global__ void __launch_bounds__(128) shadow_kernel(World w, const float4* __re
             for (int s = 0; s < 4; s++) {
                 const int st = walk_step(wk, w);
                 if (st != WALK_CONTINUE) {
-                    shadow_finish(w, st, wk, o, L, pix, li, plane);
+                    shadow_finish(w, st, wk, o, L, plane, pix, li);
                     active = false;
                     break;
                 }
@@ -318,141 +395,144 @@ __device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32
 // LEARNED: the light index comes from the learned proposal instead of
 // GenerateLightCandidate: cluster c with probability q(c) (drawn by the inference kernel),
 // then a member of c uniformly; the source pdf p = q(c) / |c| replaces 1 / N.
-struct LearnedLists {
-    const uint2* cand;          // [hit][kMaxCand] (cluster, bits(q))
-    const uint32_t* clOff;      // cluster c members: clMembers[clOff[c] .. clOff[c+1])
-    const uint32_t* clMembers;
-};
-
 template <bool POINT, bool LEARNED>
-__global__ void __launch_bounds__(128) ris_kernel(World w, Frame k, const uint2* __restrict__ vd,
-                                                  uint32_t* __restrict__ seeds, const uint32_t* __restrict__ hits,
-                                                  uint32_t* counters, uint4* __restrict__ cA, float4* __restrict__ cB,
-                                                  float4* __restrict__ qA, float4* __restrict__ qB, LearnedLists ll) {
-    const uint32_t nh = counters[0];
+__device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, uint32_t e, uint32_t i, uint32_t j) {
+    const World w = V->w;
+    const Frame& k = V->k;
+    const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
+    const uint2 g = V->b.vd[V->cur][i];
+    const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
+    const float dist = __uint_as_float(g.y);
+    Res res = res_zero();
+    uint32_t seed = V->b.seed[i];
+    const float3 D = camera_ray(k, x, y);
+    const float nsign = side_sign(side, D);
+    const float3 brdf = mul(to_rgb(voxel), 0.31830988618379067153777f);
+    const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+    const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
+                          sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
+    const uint32_t nL = k.nlights;
+    const float puni = 1.0f / (float)nL;
+    for (uint32_t c = 0; c < k.ncand; c++) {
+        int li;
+        float p = puni;
+        if (LEARNED) {
+            const uint2 cq = __ldg(V->ll.cand + (size_t)j * prop::kMaxCand + c);
+            const uint32_t off = __ldg(V->ll.clOff + cq.x), sz = __ldg(V->ll.clOff + cq.x + 1) - off;
+            const uint32_t mi = min((uint32_t)f2i(rnd(seed) * (float)sz), sz - 1u);
+            li = (int)__ldg(V->ll.clMembers + off + mi);
+            p = __uint_as_float(cq.y) / (float)sz;
+        } else {
+            // GenerateLightCandidate (tools.cl:593-598)
+            li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
+        }
+        const float4 lg = __ldg(w.lgeom + li);
+        const float4 le = __ldg(w.lemit + li);
+        float3 pos;
+        float inv;
+        uint32_t nc;
+        if (POINT) {
+            pos = f3(lg.x, lg.y, lg.z);
+            inv = 1.0f;
+            nc = 6;
+        } else {
+            pos = sample_area_light(lg, spo, seed, &inv, &nc);
+        }
+        const float ph = phat<POINT>(pos, nc, sp, side, nsign, brdf, le, lg.w) * inv;
+        res_update(res, ph / p, ph, (uint32_t)li, rnd(seed), pos, inv, nc);
+    }
+    if (k.ncand > 0 && res.sumW > 0.0f) {
+        const float3 L = normalize3(sub(res.pos, spo));
+        const uint32_t slot = append_slot(bd.counters + kCtrQ1);
+        bd.qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(e));
+        bd.qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(res.idx));
+    }
+    res_store(V->b.cA, V->b.cB, i, res);
+    V->b.seed[i] = seed;
+}
+
+template <int VARIANT, bool LEARNED>
+__global__ void __launch_bounds__(128) ris_kernel(const __grid_constant__ BatchDev bd) {
+    const uint32_t nh = bd.counters[kCtrHits];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
-        const uint32_t i = hits[j];
-        const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
-        const uint2 g = vd[i];
-        const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
-        const float dist = __uint_as_float(g.y);
-        Res res = res_zero();
-        uint32_t seed = seeds[i];
-        const float3 D = camera_ray(k, x, y);
-        const float nsign = side_sign(side, D);
-        const float3 brdf = mul(to_rgb(voxel), 0.31830988618379067153777f);
-        const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
-        const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
-                              sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
-        const uint32_t nL = k.nlights;
-        const float puni = 1.0f / (float)nL;
-        for (uint32_t c = 0; c < k.ncand; c++) {
-            int li;
-            float p = puni;
-            if (LEARNED) {
-                const uint2 cq = __ldg(ll.cand + (size_t)j * prop::kMaxCand + c);
-                const uint32_t off = __ldg(ll.clOff + cq.x), sz = __ldg(ll.clOff + cq.x + 1) - off;
-                const uint32_t mi = min((uint32_t)f2i(rnd(seed) * (float)sz), sz - 1u);
-                li = (int)__ldg(ll.clMembers + off + mi);
-                p = __uint_as_float(cq.y) / (float)sz;
-            } else {
-                // GenerateLightCandidate (tools.cl:593-598)
-                li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
-            }
-            const float4 lg = __ldg(w.lgeom + li);
-            const float4 le = __ldg(w.lemit + li);
-            float3 pos;
-            float inv;
-            uint32_t nc;
-            if (POINT) {
-                pos = f3(lg.x, lg.y, lg.z);
-                inv = 1.0f;
-                nc = 6;
-            } else {
-                pos = sample_area_light(lg, spo, seed, &inv, &nc);
-            }
-            const float ph = phat<POINT>(pos, nc, sp, side, nsign, brdf, le, lg.w) * inv;
-            res_update(res, ph / p, ph, (uint32_t)li, rnd(seed), pos, inv, nc);
-        }
-        if (k.ncand > 0 && res.sumW > 0.0f) {
-            const float3 L = normalize3(sub(res.pos, spo));
-            const uint32_t slot = append_slot(&counters[1]);
-            qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(i));
-            qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(res.idx));
-        }
-        res_store(cA, cB, i, res);
-        seeds[i] = seed;
+        const uint32_t e = bd.hits[j];
+        const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
+        if (point_of<VARIANT>(V)) ris_item<true, LEARNED>(bd, V, e, pix_of<VARIANT>(e), j);
+        else ris_item<false, LEARNED>(bd, V, e, pix_of<VARIANT>(e), j);
     }
 }
 
 // ---- stage 2c: temporal reuse (ris.cl:84-119) over the hit list, after visibility ------------
 template <bool POINT>
-__global__ void __launch_bounds__(128) temporal_kernel(World w, Frame k, const uint2* __restrict__ vd,
-                                                       const uint2* __restrict__ vdPrev, uint32_t* __restrict__ seeds,
-                                                       const uint32_t* __restrict__ hits, const uint32_t* counters,
-                                                       const uint4* __restrict__ hA, const float4* __restrict__ hB,
-                                                       uint4* __restrict__ cA, float4* __restrict__ cB, uint32_t* err) {
-    const uint32_t nh = counters[0];
+__device__ __forceinline__ void temporal_item(const ViewDev* V, uint32_t i) {
+    const Frame& k = V->k;
+    if (!(k.restirtemporalframe > 0 && k.temporal)) return;
+    const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
+    const uint2 g = V->b.vd[V->cur][i];
+    const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
+    const float dist = __uint_as_float(g.y);
+    const float3 D = camera_ray(k, x, y);
+    const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+    const float dl = ((sp.x * k.Nl.x + sp.y * k.Nl.y) + sp.z * k.Nl.z) - k.Nl.w;
+    const float dr = ((sp.x * k.Nr.x + sp.y * k.Nr.y) + sp.z * k.Nr.z) - k.Nr.w;
+    const float dt = ((sp.x * k.Nt.x + sp.y * k.Nt.y) + sp.z * k.Nt.z) - k.Nt.w;
+    const float db = ((sp.x * k.Nb.x + sp.y * k.Nb.y) + sp.z * k.Nb.z) - k.Nb.w;
+    const float up = (float)k.W * (dl / (dl + dr));
+    const float vp = (float)k.H * (dt / (dt + db));
+    const float ru = roundf(up), rv = roundf(vp);
+    if (!(ru == ru && rv == rv)) return;
+    const int px = f2i(ru), py = f2i(rv);
+    if (px < 0 || py < 0 || px >= k.W || py >= k.H) return;
+    const size_t jp = (size_t)py * k.W + px;
+    const uint2 pg = __ldg(V->b.vd[V->cur ^ 1] + jp);
+    const float pdist = __uint_as_float(pg.y);
+    if ((pg.x >> 24) != side || !(fabsf(dist - pdist) <= 0.1f * dist)) return;
+    Res prev = res_load(V->b.hA, V->b.hB, jp);
+    const uint32_t pm = min(k.maxTemporal * k.ncand, prev.M);
+    if (pm == 0u) return;
+    uint32_t pli = prev.idx;
+    if (pli >= k.nlights) { raise_error(V->b.err, 2u); pli = 0; }
+    const float nsign = side_sign(side, D);
+    const float3 brdf = mul(to_rgb(voxel), 0.31830988618379067153777f);
+    const float4 pg4 = __ldg(V->w.lgeom + pli), pe4 = __ldg(V->w.lemit + pli);
+    const float pph = phat<POINT>(prev.pos, prev.ncode, sp, side, nsign, brdf, pe4, pg4.w) * prev.inv;
+    const float W = res_W(prev);
+    res_reweigh(prev, W, pph, pm);
+    Res res = res_load(V->b.cA, V->b.cB, i);
+    uint32_t seed = V->b.seed[i];
+    res_combine(res, prev, rnd(seed));
+    // AdjustWeight(res, pHat of the selected sample here) equals res.pHat
+    res_store(V->b.cA, V->b.cB, i, res);
+    V->b.seed[i] = seed;
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(128) temporal_kernel(const __grid_constant__ BatchDev bd) {
+    const uint32_t nh = bd.counters[kCtrHits];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
-        const uint32_t i = hits[j];
-        const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
-        const uint2 g = vd[i];
-        const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
-        const float dist = __uint_as_float(g.y);
-        const float3 D = camera_ray(k, x, y);
-        const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
-        const float dl = ((sp.x * k.Nl.x + sp.y * k.Nl.y) + sp.z * k.Nl.z) - k.Nl.w;
-        const float dr = ((sp.x * k.Nr.x + sp.y * k.Nr.y) + sp.z * k.Nr.z) - k.Nr.w;
-        const float dt = ((sp.x * k.Nt.x + sp.y * k.Nt.y) + sp.z * k.Nt.z) - k.Nt.w;
-        const float db = ((sp.x * k.Nb.x + sp.y * k.Nb.y) + sp.z * k.Nb.z) - k.Nb.w;
-        const float up = (float)k.W * (dl / (dl + dr));
-        const float vp = (float)k.H * (dt / (dt + db));
-        const float ru = roundf(up), rv = roundf(vp);
-        if (!(ru == ru && rv == rv)) continue;
-        const int px = f2i(ru), py = f2i(rv);
-        if (px < 0 || py < 0 || px >= k.W || py >= k.H) continue;
-        const size_t jp = (size_t)py * k.W + px;
-        const uint2 pg = __ldg(vdPrev + jp);
-        const float pdist = __uint_as_float(pg.y);
-        if ((pg.x >> 24) != side || !(fabsf(dist - pdist) <= 0.1f * dist)) continue;
-        Res prev = res_load(hA, hB, jp);
-        const uint32_t pm = min(k.maxTemporal * k.ncand, prev.M);
-        if (pm == 0u) continue;
-        uint32_t pli = prev.idx;
-        if (pli >= k.nlights) { raise_error(err, 2u); pli = 0; }
-        const float nsign = side_sign(side, D);
-        const float3 brdf = mul(to_rgb(voxel), 0.31830988618379067153777f);
-        const float4 pg4 = __ldg(w.lgeom + pli), pe4 = __ldg(w.lemit + pli);
-        const float pph = phat<POINT>(prev.pos, prev.ncode, sp, side, nsign, brdf, pe4, pg4.w) * prev.inv;
-        const float W = res_W(prev);
-        res_reweigh(prev, W, pph, pm);
-        Res res = res_load(cA, cB, i);
-        uint32_t seed = seeds[i];
-        res_combine(res, prev, rnd(seed));
-        // AdjustWeight(res, pHat of the selected sample here) equals res.pHat
-        res_store(cA, cB, i, res);
-        seeds[i] = seed;
+        const uint32_t e = bd.hits[j];
+        const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
+        if (point_of<VARIANT>(V)) temporal_item<true>(V, pix_of<VARIANT>(e));
+        else temporal_item<false>(V, pix_of<VARIANT>(e));
     }
 }
 
 // ---- stage 3: spatial reuse (perPixelSpatialResampling, ris.cl:126-151,
 //      spatialSampling.cl:2-66) -------------------------------------------------------
-
 template <bool POINT>
-__global__ void __launch_bounds__(128) spatial_kernel(World w, Frame k, const uint2* __restrict__ vd,
-                                                      uint32_t* __restrict__ seeds, const uint4* __restrict__ cA,
-                                                      const float4* __restrict__ cB, uint4* __restrict__ hA,
-                                                      float4* __restrict__ hB, uint32_t* err) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= k.W || y >= k.H) return;
+__device__ __forceinline__ void spatial_px(const ViewDev* V, int x, int y) {
+    const Frame& k = V->k;
     const size_t i = (size_t)y * k.W + x;
+    const uint4* cA = V->b.cA;
+    const float4* cB = V->b.cB;
+    const uint2* vd = V->b.vd[V->cur];
     Res res = res_load(cA, cB, i);
     const uint2 g = vd[i];
     const uint32_t voxel = g.x & 0x00FFFFFFu;
     if (voxel != 0u && k.spatial) {
         const uint32_t side = g.x >> 24;
         const float dist = __uint_as_float(g.y);
-        uint32_t seed = seeds[i];
+        uint32_t seed = V->b.seed[i];
         const float3 D = camera_ray(k, x, y);
         const float nsign = side_sign(side, D);
         const float3 brdf = mul(to_rgb(voxel), 0.31830988618379067153777f);
@@ -472,8 +552,8 @@ __global__ void __launch_bounds__(128) spatial_kernel(World w, Frame k, const ui
                 const float ndist = __uint_as_float(ng.y);
                 if ((ng.x >> 24) == side && fabsf(dist - ndist) <= 0.1f * dist) {
                     uint32_t nli = nb.idx;
-                    if (nli >= k.nlights) { raise_error(err, 4u); nli = 0; }
-                    const float4 lg = __ldg(w.lgeom + nli), le = __ldg(w.lemit + nli);
+                    if (nli >= k.nlights) { raise_error(V->b.err, 4u); nli = 0; }
+                    const float4 lg = __ldg(V->w.lgeom + nli), le = __ldg(V->w.lemit + nli);
                     const float ph = phat<POINT>(nb.pos, nb.ncode, sp, side, nsign, brdf, le, lg.w) * nb.inv;
                     const float W = res_W(nb);
                     res_reweigh(nb, W, ph, nb.M);
@@ -482,26 +562,40 @@ __global__ void __launch_bounds__(128) spatial_kernel(World w, Frame k, const ui
             }
         }
         // AdjustWeight(res, res.pHat): implied by the stored (sumW, pHat, M)
-        seeds[i] = seed;
+        V->b.seed[i] = seed;
     }
-    res_store(hA, hB, i, res);
+    res_store(V->b.hA, V->b.hB, i, res);
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(128) spatial_kernel(const __grid_constant__ BatchDev bd) {
+    uint32_t tile;
+    while (next_tile(bd, bd.counters + kCtrSpatial, &tile)) {
+        int x, y;
+        const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
+        if (x < V->k.W && y < V->k.H) {
+            if (point_of<VARIANT>(V)) spatial_px<true>(V, x, y);
+            else spatial_px<false>(V, x, y);
+        }
+    }
 }
 
 // ---- stage 4: shading (renderRIS / render_di_ris, ris.cl:155-293, 391-413) ------------------
 // 4a: a shadow-ray request for every hit pixel whose reservoir has W > 0 and M > 0.
-__global__ void __launch_bounds__(128) shade_request_kernel(Frame k, const uint2* __restrict__ vd,
-                                                            const uint32_t* __restrict__ hits, uint32_t* counters,
-                                                            const uint4* __restrict__ hA, const float4* __restrict__ hB,
-                                                            float4* __restrict__ qA, float4* __restrict__ qB, uint32_t* err) {
-    const uint32_t nh = counters[0];
+template <int VARIANT>
+__global__ void __launch_bounds__(128) shade_request_kernel(const __grid_constant__ BatchDev bd) {
+    const uint32_t nh = bd.counters[kCtrHits];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
-        const uint32_t i = hits[j];
-        const uint4 qa = hA[i];
+        const uint32_t e = bd.hits[j];
+        const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
+        const Frame& k = V->k;
+        const uint32_t i = pix_of<VARIANT>(e);
+        const uint4 qa = V->b.hA[i];
         const uint32_t M = qa.y & 0x1FFFFFFFu;
         const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, __uint_as_float(qa.w) * (float)M);
         if (!(W > 0.0f && M > 0u)) continue;
         const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
-        const uint2 g = vd[i];
+        const uint2 g = V->b.vd[V->cur][i];
         const uint32_t side = g.x >> 24;
         const float dist = __uint_as_float(g.y);
         const float3 D = camera_ray(k, x, y);
@@ -510,26 +604,33 @@ __global__ void __launch_bounds__(128) shade_request_kernel(Frame k, const uint2
         const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
                               sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
         uint32_t li = qa.x;
-        if (li >= k.nlights) { raise_error(err, 8u); li = 0; }
-        const float4 qb = __ldg(hB + i);
+        if (li >= k.nlights) { raise_error(V->b.err, 8u); li = 0; }
+        const float4 qb = __ldg(V->b.hB + i);
         const float3 L = normalize3(sub(f3(qb.x, qb.y, qb.z), spo));
-        const uint32_t slot = append_slot(&counters[3]);
-        qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(i));
-        qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(li));
+        const uint32_t slot = append_slot(bd.counters + kCtrQ2);
+        bd.qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(e));
+        bd.qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(li));
     }
 }
 
+// accumulatorFinalizer (kernels.cl:304-326): running mean over `framecount` frames
+__device__ __forceinline__ void accumulate_px(const ViewDev* V, size_t i, float4 px) {
+    const Frame& k = V->k;
+    const int n = (int)k.framecount * k.accumulate;
+    float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (n > 0) prev = V->b.accum[i];
+    const float cw = 1.0f / (float)(1 + n);
+    V->b.accum[i] = make_float4((1.0f - cw) * prev.x + cw * px.x, (1.0f - cw) * prev.y + cw * px.y,
+                                (1.0f - cw) * prev.z + cw * px.z, 1.0f);
+}
+
 // 4c: colour per pixel once visibility has zeroed the occluded reservoirs; optionally
-// fused with the accumulator (accumulatorFinalizer, kernels.cl:304-326).
+// fused with the accumulator.
 template <bool POINT>
-__global__ void __launch_bounds__(128) shade_finish_kernel(World w, Frame k, const uint2* __restrict__ vd,
-                                                           const uint4* __restrict__ hA, const float4* __restrict__ hB,
-                                                           float4* __restrict__ frame, float4* __restrict__ accum,
-                                                           int fuse_accumulate) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= k.W || y >= k.H) return;
+__device__ __forceinline__ void shade_finish_px(const ViewDev* V, int x, int y, int fuse) {
+    const Frame& k = V->k;
     const size_t i = (size_t)y * k.W + x;
-    const uint2 g = vd[i];
+    const uint2 g = V->b.vd[V->cur][i];
     const uint32_t voxel = g.x & 0x00FFFFFFu;
     const float dist = __uint_as_float(g.y);
     float3 color = f3(0.0f, 0.0f, 0.0f);
@@ -540,17 +641,17 @@ __global__ void __launch_bounds__(128) shade_finish_kernel(World w, Frame k, con
             const float m = strength(voxel);
             color = add(color, f3((c.x * m) * INVPI, (c.y * m) * INVPI, (c.z * m) * INVPI));
         }
-        const uint4 qa = hA[i];
+        const uint4 qa = V->b.hA[i];
         const uint32_t M = qa.y & 0x1FFFFFFFu;
         const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, __uint_as_float(qa.w) * (float)M);
         if (W > 0.0f && M > 0u) {   // visible: occluded reservoirs were zeroed by the tracer
             const uint32_t side = g.x >> 24;
-            const float4 qb = __ldg(hB + i);
+            const float4 qb = __ldg(V->b.hB + i);
             const float3 D = camera_ray(k, x, y);
             const float nsign = side_sign(side, D);
             const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
             const uint32_t li = qa.x < k.nlights ? qa.x : 0u;
-            const float4 lg = __ldg(w.lgeom + li), le = __ldg(w.lemit + li);
+            const float4 lg = __ldg(V->w.lgeom + li), le = __ldg(V->w.lemit + li);
             const float3 brdf = mul(to_rgb(voxel), INVPI);
             bool zero;
             const float3 inc = phat_full<POINT>(f3(qb.x, qb.y, qb.z), qa.y >> 29, sp, side, nsign, brdf, le, lg.w, &zero);
@@ -561,29 +662,35 @@ __global__ void __launch_bounds__(128) shade_finish_kernel(World w, Frame k, con
                    color.z + ((a * color.z) + ((1.0f - a) * 0.0f)));
     }
     const float4 px = make_float4(color.x, color.y, color.z, dist);
-    frame[i] = px;
-    if (fuse_accumulate) {
-        const int n = (int)k.framecount * k.accumulate;
-        float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (n > 0) prev = accum[i];
-        const float cw = 1.0f / (float)(1 + n);
-        accum[i] = make_float4((1.0f - cw) * prev.x + cw * px.x, (1.0f - cw) * prev.y + cw * px.y,
-                               (1.0f - cw) * prev.z + cw * px.z, 1.0f);
+    V->b.frame[i] = px;
+    if (fuse) accumulate_px(V, i, px);
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(128) shade_finish_kernel(const __grid_constant__ BatchDev bd) {
+    uint32_t tile;
+    while (next_tile(bd, bd.counters + kCtrFinish, &tile)) {
+        int x, y;
+        const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
+        if (x < V->k.W && y < V->k.H) {
+            if (point_of<VARIANT>(V)) shade_finish_px<true>(V, x, y, bd.fuse);
+            else shade_finish_px<false>(V, x, y, bd.fuse);
+        }
     }
 }
 
-// stage 5 on its own (accumulatorFinalizer, kernels.cl:304-326)
-__global__ void __launch_bounds__(256) accumulate_kernel(Frame k, const float4* __restrict__ frame, float4* __restrict__ accum) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= k.W || y >= k.H) return;
-    const size_t i = (size_t)y * k.W + x;
-    const float4 px = frame[i];
-    const int n = (int)k.framecount * k.accumulate;
-    float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (n > 0) prev = accum[i];
-    const float cw = 1.0f / (float)(1 + n);
-    accum[i] = make_float4((1.0f - cw) * prev.x + cw * px.x, (1.0f - cw) * prev.y + cw * px.y,
-                           (1.0f - cw) * prev.z + cw * px.z, 1.0f);
+// stage 5 on its own
+template <int VARIANT>
+__global__ void __launch_bounds__(128) accumulate_kernel(const __grid_constant__ BatchDev bd) {
+    uint32_t tile;
+    while (next_tile(bd, bd.counters + kCtrAccum, &tile)) {
+        int x, y;
+        const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
+        if (x < V->k.W && y < V->k.H) {
+            const size_t i = (size_t)y * V->k.W + x;
+            accumulate_px(V, i, V->b.frame[i]);
+        }
+    }
 }
 
 }  // namespace dev
@@ -591,10 +698,6 @@ __global__ void __launch_bounds__(256) accumulate_kernel(Frame k, const float4* 
 
 // ---- launchers -------------------------------------------------------------------------
 namespace vxr {
-
-static dim3 grid_for(const dev::Frame& k, LaunchShape sh) {
-    return dim3((unsigned)((k.W + sh.bx - 1) / sh.bx), (unsigned)((k.H + sh.by - 1) / sh.by), 1);
-}
 
 static int g_sms = 0;
 static int sm_count() {
@@ -612,6 +715,48 @@ static unsigned list_blocks(size_t n, int threads, int per_sm) {
     const size_t cap = (size_t)sm_count() * per_sm;
     return (unsigned)std::max<size_t>(1, std::min(need, cap));
 }
+// Persistent kernels: as many blocks as fit on the machine at once (occupancy query per
+// kernel and block size, cached), never more than there are tiles.
+static unsigned resident_blocks(const void* kernel, int threads) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find({kernel, threads});
+    if (it == cache.end()) {
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0) != cudaSuccess || per < 1) per = 1;
+        it = cache.emplace(std::make_pair(kernel, threads), per).first;
+    }
+    return (unsigned)(sm_count() * it->second);
+}
+template <class K>
+static void launch_tiles(K kernel, const BatchDev& bd, int ctr, cudaStream_t s) {
+    const int threads = bd.tx * bd.ty;
+    cudaMemsetAsync(bd.counters + ctr, 0, sizeof(uint32_t), s);
+    const unsigned nb = std::max(1u, std::min(resident_blocks((const void*)kernel, threads), bd.totalTiles));
+    kernel<<<nb, threads, 0, s>>>(bd);
+}
+
+BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, LaunchShape sh) {
+    BatchDev bd;
+    bd.one.w = w;
+    bd.one.k = k;
+    bd.one.b = b;
+    bd.one.cur = cur;
+    bd.one.point = point ? 1 : 0;
+    bd.one.tileBase = 0;
+    bd.one.tilesX = (uint32_t)((k.W + sh.bx - 1) / sh.bx);
+    bd.nviews = 1;
+    bd.totalPixels = (uint32_t)k.W * (uint32_t)k.H;
+    bd.totalTiles = bd.one.tilesX * (uint32_t)((k.H + sh.by - 1) / sh.by);
+    bd.tx = sh.bx;
+    bd.ty = sh.by;
+    bd.hits = b.hits;
+    bd.qA = b.qA;
+    bd.qB = b.qB;
+    bd.counters = b.counters;
+    return bd;
+}
 
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s) {
     if (n == 0) return;
@@ -622,88 +767,83 @@ void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s) {
     dev::build_uber_kernel<<<(32 * 32 * 32 + 255) / 256, 256, 0, s>>>(grid, uber);
 }
 
-void launch_albedo(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh, cudaStream_t s) {
-    dev::albedo_kernel<<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.seed);
+void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {
+    if (variant == 2) launch_tiles(dev::albedo_kernel<2>, bd, kCtrAlbedo, s);
+    else launch_tiles(dev::albedo_kernel<0>, bd, kCtrAlbedo, s);
 }
 
-static int g_shadow_per_sm = 0;
-static void launch_shadow(const dev::World& w, const ViewBuffers& b, const uint32_t* count, uint32_t* fetch,
-                          uint32_t* plane, size_t max_rays, cudaStream_t s) {
-    // persistent: exactly the blocks that fit on the machine at once, never more than the rays
-    if (!g_shadow_per_sm) {
-        int per = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dev::shadow_kernel, 128, 0) != cudaSuccess || per < 1) per = 4;
-        g_shadow_per_sm = per;
-    }
-    dev::shadow_kernel<<<list_blocks(max_rays, 128, g_shadow_per_sm), 128, 0, s>>>(w, b.qA, b.qB, count, fetch, plane, 8);
+template <int VARIANT>
+static void launch_shadow(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
+    const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT>, 128);
+    const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 127) / 128));
+    dev::shadow_kernel<VARIANT><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel, 8);
 }
 
-void launch_candidates(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh,
-                       cudaStream_t s, const LearnedHook* learned) {
-    (void)sh;
-    const size_t n = (size_t)k.W * k.H;
-    cudaMemsetAsync(b.counters, 0, 8 * sizeof(uint32_t), s);
-    dev::compact_hits_kernel<<<list_blocks(n, 256, 8), 256, 0, s>>>(k, b.vd[cur], b.hits, b.counters, b.cA, b.cB);
+template <int VARIANT>
+static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStream_t s) {
+    const size_t n = bd.totalPixels;
+    cudaMemsetAsync(bd.counters + kCtrHits, 0, 3 * sizeof(uint32_t), s);   // hits, q1 requests, q1 fetch
+    uint32_t maxPx = VARIANT < 2 ? bd.totalPixels : 0;
+    if (VARIANT == 2) maxPx = (uint32_t)(n / bd.nviews + 1);
+    dev::compact_hits_kernel<VARIANT><<<dim3(list_blocks(maxPx, 256, 8), bd.nviews), 256, 0, s>>>(bd);
     const unsigned nb = list_blocks(n, 128, 16);
-    dev::LearnedLists ll{nullptr, nullptr, nullptr};
-    if (learned && k.ncand > 0) {
-        prop::InferArgs ia = learned->infer;
-        ia.k = k;
-        ia.vd = b.vd[cur];
-        ia.hits = b.hits;
-        ia.count = b.counters;
-        ia.ncand = k.ncand;
-        ia.cand = learned->cand;
-        ia.samples = nullptr;
-        ia.probs = nullptr;
-        prop::launch_infer(ia, (uint32_t)n, s);
-        ll = dev::LearnedLists{learned->cand, learned->clOff, learned->clMembers};
-        if (point)
-            dev::ris_kernel<true, true><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
-        else
-            dev::ris_kernel<false, true><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
-    } else if (point) {
-        dev::ris_kernel<true, false><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
-    } else {
-        dev::ris_kernel<false, false><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.seed, b.hits, b.counters, b.cA, b.cB, b.qA, b.qB, ll);
+    bool learnedDone = false;
+    if constexpr (VARIANT < 2) {
+        if (learned) {
+            BatchDev lb = bd;
+            lb.one.ll.cand = learned->cand;
+            lb.one.ll.clOff = learned->clOff;
+            lb.one.ll.clMembers = learned->clMembers;
+            prop::InferArgs ia = learned->infer;
+            ia.k = bd.one.k;
+            ia.vd = bd.one.b.vd[bd.one.cur];
+            ia.hits = bd.hits;
+            ia.count = bd.counters + kCtrHits;
+            ia.ncand = bd.one.k.ncand;
+            ia.cand = learned->cand;
+            ia.samples = nullptr;
+            ia.probs = nullptr;
+            if (bd.one.k.ncand > 0) prop::launch_infer(ia, (uint32_t)n, s);
+            dev::ris_kernel<VARIANT, true><<<nb, 128, 0, s>>>(lb);
+            learnedDone = true;
+        }
     }
-    launch_shadow(w, b, &b.counters[1], &b.counters[2], (uint32_t*)b.cA, n, s);
-    if (k.restirtemporalframe > 0 && k.temporal) {
-        if (point)
-            dev::temporal_kernel<true><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.vd[cur ^ 1], b.seed, b.hits, b.counters, b.hA,
-                                                          b.hB, b.cA, b.cB, b.err);
-        else
-            dev::temporal_kernel<false><<<nb, 128, 0, s>>>(w, k, b.vd[cur], b.vd[cur ^ 1], b.seed, b.hits, b.counters,
-                                                           b.hA, b.hB, b.cA, b.cB, b.err);
-    }
+    if (!learnedDone) dev::ris_kernel<VARIANT, false><<<nb, 128, 0, s>>>(bd);
+    launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ1, 0, s);
+    // a single view without temporal reuse this frame skips the launch (a table checks per view)
+    if (VARIANT == 2 || (bd.one.k.restirtemporalframe > 0 && bd.one.k.temporal))
+        dev::temporal_kernel<VARIANT><<<nb, 128, 0, s>>>(bd);
 }
 
-void launch_spatial(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh,
-                    cudaStream_t s) {
-    if (point)
-        dev::spatial_kernel<true><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.seed, b.cA, b.cB, b.hA,
-                                                                               b.hB, b.err);
-    else
-        dev::spatial_kernel<false><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.seed, b.cA, b.cB, b.hA,
-                                                                                b.hB, b.err);
+void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s) {
+    if (variant == 0) candidates_v<0>(bd, learned, s);
+    else if (variant == 1) candidates_v<1>(bd, learned, s);
+    else candidates_v<2>(bd, nullptr, s);
 }
 
-void launch_shade(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool fuse_accumulate,
-                  LaunchShape sh, cudaStream_t s) {
-    const size_t n = (size_t)k.W * k.H;
-    dev::shade_request_kernel<<<list_blocks(n, 128, 16), 128, 0, s>>>(k, b.vd[cur], b.hits, b.counters, b.hA, b.hB, b.qA,
-                                                                      b.qB, b.err);
-    launch_shadow(w, b, &b.counters[3], &b.counters[4], (uint32_t*)b.hA, n, s);
-    if (point)
-        dev::shade_finish_kernel<true><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.hA, b.hB, b.frame,
-                                                                                    b.accum, fuse_accumulate ? 1 : 0);
-    else
-        dev::shade_finish_kernel<false><<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(w, k, b.vd[cur], b.hA, b.hB, b.frame,
-                                                                                     b.accum, fuse_accumulate ? 1 : 0);
+void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s) {
+    if (variant == 0) launch_tiles(dev::spatial_kernel<0>, bd, kCtrSpatial, s);
+    else if (variant == 1) launch_tiles(dev::spatial_kernel<1>, bd, kCtrSpatial, s);
+    else launch_tiles(dev::spatial_kernel<2>, bd, kCtrSpatial, s);
 }
 
-void launch_accumulate(const dev::Frame& k, const ViewBuffers& b, LaunchShape sh, cudaStream_t s) {
-    dev::accumulate_kernel<<<grid_for(k, sh), dim3(sh.bx, sh.by), 0, s>>>(k, b.frame, b.accum);
+template <int VARIANT>
+static void shade_v(const BatchDev& bd, cudaStream_t s) {
+    cudaMemsetAsync(bd.counters + kCtrQ2, 0, 2 * sizeof(uint32_t), s);   // q2 requests, q2 fetch
+    dev::shade_request_kernel<VARIANT < 2 ? 0 : 2><<<list_blocks(bd.totalPixels, 128, 16), 128, 0, s>>>(bd);
+    launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ2, 1, s);
+    launch_tiles(dev::shade_finish_kernel<VARIANT>, bd, kCtrFinish, s);
+}
+
+void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s) {
+    if (variant == 0) shade_v<0>(bd, s);
+    else if (variant == 1) shade_v<1>(bd, s);
+    else shade_v<2>(bd, s);
+}
+
+void launch_batch_accumulate(const BatchDev& bd, int variant, cudaStream_t s) {
+    if (variant == 2) launch_tiles(dev::accumulate_kernel<2>, bd, kCtrAccum, s);
+    else launch_tiles(dev::accumulate_kernel<0>, bd, kCtrAccum, s);
 }
 
 }  // namespace vxr

@@ -19,11 +19,59 @@ struct ViewBuffers {
     float4* frame = nullptr;
     float4* accum = nullptr;
     uint32_t* err = nullptr;              // device error flags (bit set per fault kind)
-    uint32_t* hits = nullptr;             // hit-pixel list (one entry per pixel at most)
-    float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(pixel))
+    uint32_t* hits = nullptr;             // work lists of a single-view batch (BatchDev)
+    float4* qA = nullptr;
+    float4* qB = nullptr;
+    uint32_t* counters = nullptr;         // kCounters words
+};
+
+// Work-list counters of a batch: list lengths and work-queue cursors.
+enum : int {
+    kCtrHits = 0,       // hit-list length
+    kCtrQ1 = 1,         // candidate shadow queue: [1] requests, [2] fetch cursor
+    kCtrQ2 = 3,         // shading shadow queue:   [3] requests, [4] fetch cursor
+    kCtrFinish = 5,     // tile cursors of the persistent pixel stages
+    kCtrAlbedo = 6,
+    kCtrSpatial = 7,
+    kCtrAccum = 8,
+    kCounters = 16
+};
+
+// learned-proposal lists read by the candidate loop (all null = uniform source pdf)
+struct LearnedLists {
+    const uint2* cand = nullptr;          // [hit][kMaxCand] (cluster, bits(q(cluster)))
+    const uint32_t* clOff = nullptr;      // cluster CSR
+    const uint32_t* clMembers = nullptr;
+};
+
+// Everything a kernel needs about one view of a batch.
+struct ViewDev {
+    dev::World w;
+    dev::Frame k;
+    ViewBuffers b;
+    int cur = 0;                          // current G-buffer plane
+    int point = 0;                        // point-light model
+    LearnedLists ll;
+    uint32_t tileBase = 0;                // first tile of this view in the batch's tile space
+    uint32_t tilesX = 0;
+};
+
+// One launch's work: a single view (read from the kernel parameter `one`) or a table of
+// views in device memory. Hit-list entries are (view << 27 | pixel), at most 16 views
+// of at most 2^27 pixels each.
+constexpr uint32_t kMaxBatchViews = 16;
+struct BatchDev {
+    ViewDev one;
+    const ViewDev* views = nullptr;       // device table when nviews > 1
+    uint32_t nviews = 1;
+    uint32_t totalPixels = 0;
+    uint32_t totalTiles = 0;
+    int tx = 16, ty = 8;                  // tile = block shape of the pixel stages
+    int fuse = 0;                         // shading also accumulates
+    uint32_t* hits = nullptr;             // hit list over all views
+    float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(entry))
     float4* qB = nullptr;                 //                      (direction, bits(light))
-    uint32_t* counters = nullptr;         // [0] hits, [1] requests / [2] fetch of the candidate
-                                          // queue, [3] requests / [4] fetch of the shading queue
+    uint32_t* counters = nullptr;         // kCounters words
 };
 
 struct LaunchShape {
@@ -33,22 +81,25 @@ struct LaunchShape {
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s);
 void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s);
 
-// cur: index (0/1) of the current G-buffer plane
-void launch_albedo(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh, cudaStream_t s);
-// learned proposal inputs of the candidate stage (nullptr = uniform source pdf)
+// learned proposal inputs of the candidate stage
 struct LearnedHook {
     prop::InferArgs infer;      // dims, layout, params, BF16 weights
     uint2* cand;                // [pixels][kMaxCand] scratch for drawn clusters
     const uint32_t* clOff;      // cluster CSR on the device
     const uint32_t* clMembers;
 };
-void launch_candidates(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh,
-                       cudaStream_t s, const LearnedHook* learned = nullptr);
-void launch_spatial(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, LaunchShape sh,
-                    cudaStream_t s);
-void launch_shade(bool point, const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool fuse_accumulate,
-                  LaunchShape sh, cudaStream_t s);
-void launch_accumulate(const dev::Frame& k, const ViewBuffers& b, LaunchShape sh, cudaStream_t s);
+
+// A batch of one view over its own list buffers.
+BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, LaunchShape sh);
+
+// Stage launchers over a batch. variant: 0 single view / area lights, 1 single view /
+// point lights, 2 view table (light model per view). A learned proposal needs variant 0/1.
+void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s);
+void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s);
+void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s);
+void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s);
+void launch_batch_accumulate(const BatchDev& bd, int variant, cudaStream_t s);
+
 // converged reference (FP64 running sum of shaded frames) and the MSE / MAE metric
 void launch_sum64_add(const float4* frame, double* sum, uint32_t n, cudaStream_t s);
 void launch_error(const float4* img, const double* sum, double inv_count, uint32_t n, double* out, cudaStream_t s);

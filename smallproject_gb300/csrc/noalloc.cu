@@ -39,7 +39,7 @@ constexpr size_t kOffRaw = kOffEmit + 16 * kMaxLights;         // uint4 [kMaxLig
 constexpr size_t kOffHits = kOffRaw + 16 * kMaxLights;         // uint32 [kMaxPx] hit list
 constexpr size_t kOffQA = kOffHits + 4 * kMaxPx;               // float4 [kMaxPx] shadow requests
 constexpr size_t kOffQB = kOffQA + 16 * kMaxPx;                // float4 [kMaxPx]
-constexpr size_t kOffErr = kOffQB + 16 * kMaxPx;               // uint32 error word, then 8 counters
+constexpr size_t kOffErr = kOffQB + 16 * kMaxPx;               // uint32 error word, then the work-list counters
 constexpr size_t kScratchBytes = kOffErr + 256;
 static_assert(kScratchBytes == VXR_NOALLOC_SCRATCH_BYTES, "scratch size must match the header");
 static_assert(kOffSeed % 256 == 0 && kOffCA % 256 == 0 && kOffUber % 256 == 0 && kOffGeom % 256 == 0 &&
@@ -189,10 +189,12 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     b.counters = (uint32_t*)(s + kOffErr + 64);
     const bool point = light_model == VXR_LIGHTS_POINT;
     const vxr::LaunchShape sh;
-    vxr::launch_albedo(w, f, b, 0, sh, st);
-    vxr::launch_candidates(point, w, f, b, 0, sh, st);
-    vxr::launch_spatial(point, w, f, b, 0, sh, st);
-    vxr::launch_shade(point, w, f, b, 0, false, sh, st);
+    const vxr::BatchDev bd = vxr::single_batch(w, f, b, 0, point, sh);
+    const int variant = point ? 1 : 0;
+    vxr::launch_batch_albedo(bd, variant, st);
+    vxr::launch_batch_candidates(bd, variant, nullptr, st);
+    vxr::launch_batch_spatial(bd, variant, st);
+    vxr::launch_batch_shade(bd, variant, st);
     CUN(cudaGetLastError(), "stage kernels");
     CUN(cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "read error word");
     CUN(cudaStreamSynchronize(st), "vxr_render_frame_noalloc");

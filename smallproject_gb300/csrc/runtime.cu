@@ -283,7 +283,7 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     alloc((void**)&b.hits, n * sizeof(uint32_t));
     alloc((void**)&b.qA, n * sizeof(float4));
     alloc((void**)&b.qB, n * sizeof(float4));
-    alloc((void**)&b.counters, 8 * sizeof(uint32_t));
+    alloc((void**)&b.counters, vxr::kCounters * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking);
     v->ringS.assign(vxr_view::kRing * 6, nullptr);
     v->ringE.assign(vxr_view::kRing * 6, nullptr);
@@ -395,17 +395,20 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     const int ri = (int)(v->frameSerial % vxr_view::kRing) * 6 + stage;
     CUV(cudaEventRecord(v->evs[stage], v->stream), "cudaEventRecord");
     CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");
+    vxr::BatchDev bd = vxr::single_batch(w, k, v->buf, v->cur, point, sh);
+    bd.fuse = fuse ? 1 : 0;
+    const int variant = point ? 1 : 0;
     switch (stage) {
-    case VXR_STAGE_ALBEDO: vxr::launch_albedo(w, k, v->buf, v->cur, sh, v->stream); break;
+    case VXR_STAGE_ALBEDO: vxr::launch_batch_albedo(bd, variant, v->stream); break;
     case VXR_STAGE_CANDIDATES: {
         vxr::LearnedHook hook;
         const bool learned = vxr::learned_hook(v, &hook);
-        vxr::launch_candidates(point, w, k, v->buf, v->cur, sh, v->stream, learned ? &hook : nullptr);
+        vxr::launch_batch_candidates(bd, variant, learned ? &hook : nullptr, v->stream);
         break;
     }
-    case VXR_STAGE_SPATIAL: vxr::launch_spatial(point, w, k, v->buf, v->cur, sh, v->stream); break;
-    case VXR_STAGE_SHADE: vxr::launch_shade(point, w, k, v->buf, v->cur, fuse, sh, v->stream); break;
-    case VXR_STAGE_ACCUMULATE: vxr::launch_accumulate(k, v->buf, sh, v->stream); break;
+    case VXR_STAGE_SPATIAL: vxr::launch_batch_spatial(bd, variant, v->stream); break;
+    case VXR_STAGE_SHADE: vxr::launch_batch_shade(bd, variant, v->stream); break;
+    case VXR_STAGE_ACCUMULATE: vxr::launch_batch_accumulate(bd, variant, v->stream); break;
     default: return set_error(VXR_E_INVALID, "vxr_view_stage: unknown stage");
     }
     CUV(cudaGetLastError(), "kernel launch");

@@ -130,6 +130,8 @@ _SIGS = {
     "vxr_view_proposal_grad": [_P, C.c_uint32, _F3, C.POINTER(C.c_uint32), _F3, C.POINTER(C.c_float), _F3],
     "vxr_view_proposal_probs": [_P, C.c_uint32, _F3, _F3],
     "vxr_view_proposal_save": [_P, C.c_char_p], "vxr_view_proposal_load": [_P, C.c_char_p],
+    "vxr_batch_create": [C.POINTER(_P), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(_P)],
+    "vxr_batch_destroy": [_P], "vxr_batch_render": [_P], "vxr_batch_wait": [_P, C.POINTER(C.c_float)],
     "vxr_render_frame_noalloc": [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts), _P, _P],
 }
 _RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
@@ -465,6 +467,42 @@ class View:
     def render_to_host(self, pos, target, out):
         assert out.dtype == np.float32 and out.size == self.n * 4 and out.flags.c_contiguous
         check(self._lib.vxr_view_render_to_host(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3)))
+
+
+BATCH_MAX_VIEWS = 16
+BATCH_GRAPH = 1
+
+
+class Batch:
+    """Several views rendered as one frame (vxr_batch): each stage is one launch over all."""
+
+    def __init__(self, views, tile=(0, 0), graph=False):
+        self._lib = load()
+        self.views = list(views)
+        arr = (_P * len(self.views))(*[v.h for v in self.views])
+        self.h = _P()
+        check(self._lib.vxr_batch_create(arr, len(self.views), tile[0], tile[1], BATCH_GRAPH if graph else 0,
+                                         C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self._lib.vxr_batch_destroy(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self):
+        check(self._lib.vxr_batch_render(self.h))
+
+    def wait(self):
+        """Wait for the batch; returns the GPU time of the last frame in ms."""
+        ms = C.c_float()
+        check(self._lib.vxr_batch_wait(self.h, C.byref(ms)))
+        return ms.value
 
 
 class Camera:
