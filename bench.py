@@ -177,6 +177,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile", type=str, default="", help="threads per block, e.g. 16x8")
+    ap.add_argument("--no-tune", action="store_true", help="library default launch tuning instead of the autotuner")
     args = ap.parse_args()
     W, H = args.width, args.height
     warmup = max(args.warmup, 3)
@@ -213,8 +214,19 @@ def main():
     if args.tile:
         tx, ty = args.tile.split("x")
         tile = dict(tile_x=int(tx), tile_y=int(ty))
-    view = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, **tile))
+    vdesc = vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, **tile)
     nfr = 300
+    tuning_report = None
+    if not args.no_tune and not tile:
+        # launch parameters only (results are identical for every tuning); untimed setup
+        from smallproject_gb300 import autotune as at
+        cache = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "_build",
+                             "vxr_tuning.json")
+        t, tuning_report = at.autotune(world, vdesc, lambda f: vx.camera_path(desc, 1, (1000 + f) % nfr, nfr),
+                                       frames=4, rounds=2, cache_path=cache)
+    view = vx.View(world, vdesc)
+    if tuning_report is not None:
+        view.set_tuning(t)
 
     def frame(f):
         pos, tgt = vx.camera_path(desc, 1, f % nfr, nfr)
@@ -282,7 +294,8 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
                     "d2h_bytes_per_step": npx * 16, "image_ok": img_ok},
-            "gpu_launches": 4 * args.steps, "clocks": clk}
+            "gpu_launches": 4 * args.steps, "clocks": clk,
+            "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report}
     print(json.dumps(line))
     view.close()
 

@@ -368,6 +368,25 @@ int vxr_view_sum64_mean(vxr_view* v, uint32_t* count, double* mean);
  * shaded frame, 1 the accumulator. Same resolution required. FP64 accumulation. */
 int vxr_view_error(vxr_view* img, int which, vxr_view* ref, double* mse, double* mae);
 
+/* ---- launch tuning ---------------------------------------------------------------------
+ * No counterpart in the reference (its work-group size is fixed, template.cpp:1700-1754).
+ * Parameters that change speed but never results: every setting renders the same bits.
+ * The autotuner (smallproject_gb300/autotune.py) times them per configuration. */
+typedef struct vxr_tuning {
+    uint32_t tile_x, tile_y;       /* threads of a pixel-stage block; tile_x * tile_y a multiple of 32, <= 1024 */
+    uint32_t persistent;           /* pixel stages: 1 = resident blocks pull tiles from a queue, 0 = one block per tile */
+    uint32_t shadow_refill;        /* shadow tracer: idle lanes of a warp (1..32) that trigger a refill from the queue */
+    uint32_t shadow_burst;         /* shadow tracer: cell visits per lane between refill checks (1..64) */
+    uint32_t list_blocks_per_sm;   /* hit-list kernels (candidates, temporal, shading requests): blocks per SM (1..64) */
+} vxr_tuning;
+int vxr_default_tuning(vxr_tuning* t);
+/* Current CUDA device: name (NUL-terminated, truncated to n bytes), SM count and compute
+ * capability; the autotuner's cache key. */
+int vxr_device_info(char* name, size_t n, int* sms, int* cc_major, int* cc_minor);
+/* Replaces the view's launch parameters (including vxr_view_desc tile_x / tile_y). */
+int vxr_view_set_tuning(vxr_view* v, const vxr_tuning* t);
+int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t);
+
 /* ---- batches: several views rendered as one frame -------------------------------------
  * No counterpart in the reference: World::Render (world.cpp:2127-2340) draws one camera
  * per call, so several views are rendered one after another. A batch renders one frame of
@@ -393,6 +412,9 @@ int vxr_batch_render(vxr_batch* b);
 /* Wait for the batch's frames. ms (may be NULL): GPU time of the last frame. A device
  * error flag raised in any view -> VXR_E_DEVICE. */
 int vxr_batch_wait(vxr_batch* b, float* ms);
+/* Replaces the batch's launch parameters (tile shape included); recorded graphs are
+ * re-recorded on the next frame. */
+int vxr_batch_set_tuning(vxr_batch* b, const vxr_tuning* t);
 
 /* ---- rendering without allocation ---------------------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc - an

@@ -111,8 +111,10 @@ int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32
     bd.nviews = n;
     bd.totalPixels = (uint32_t)total;
     bd.totalTiles = (uint32_t)tiles;
-    bd.tx = (int)tx;
-    bd.ty = (int)ty;
+    vxr::Tuning tu;
+    tu.bx = (int)tx;
+    tu.by = (int)ty;
+    vxr::apply_tuning(bd, tu);
     bd.fuse = 1;
     cudaError_t e = cudaSuccess;
     auto dalloc = [&](void** p, size_t bytes) {
@@ -216,6 +218,24 @@ int vxr_batch_render(vxr_batch* b) {
     b->slotUsed[slot] = true;
     b->timed = true;
     b->frames++;
+    return VXR_OK;
+}
+
+int vxr_batch_set_tuning(vxr_batch* b, const vxr_tuning* t) {
+    VXR_CHECK_ARG(b, "vxr_batch_set_tuning: null batch");
+    if (int r = vxr::check_tuning(t, "vxr_batch_set_tuning")) return r;
+    cudaError_t e = cudaStreamSynchronize(b->stream);   // recorded graphs may still run
+    if (e != cudaSuccess) return cuda_error(e, "vxr_batch_set_tuning");
+    uint64_t tiles = 0;
+    for (vxr_view* v : b->views)
+        tiles += (uint64_t)((v->desc.width + t->tile_x - 1) / t->tile_x) * ((v->desc.height + t->tile_y - 1) / t->tile_y);
+    VXR_CHECK_ARG(tiles < (1ull << 32), "vxr_batch_set_tuning: batch too large");
+    vxr::apply_tuning(b->bd, vxr::to_tuning(*t));
+    b->bd.totalTiles = (uint32_t)tiles;
+    for (int i = 0; i < 2; i++) {
+        if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+        b->graph[i] = nullptr;
+    }
     return VXR_OK;
 }
 

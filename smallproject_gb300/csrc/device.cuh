@@ -250,13 +250,14 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
 // Every float op, the step budget accounting and the exit cascade (brick -> grid step
 // -> uber step) follow trace<MODE> exactly; the oracle checks the two for equality.
 struct Walker {
-    float ax, ay, az, vx, vy, vz, rx, ry, rz, to, tdx, tdy, tdz;
+    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;   // per-axis cell step in t: |r| (= sign(v) * r)
     float t, tmx, tmy, tmz;        // current level
-    float umx, umy, umz;           // saved uber-level crossings
-    float gmx, gmy, gmz;           // saved grid-level crossings
-    int ux, uy, uz, gx, gy, gz, lx, ly, lz;
+    float umx, umy, umz;           // saved uber-level crossings (while below the uber level)
+    float gmx, gmy, gmz;           // saved grid-level crossings (while in a brick)
+    int cx, cy, cz;                // current cell: uber / grid (absolute) or brick-local voxel
+    int ux, uy, uz, gx, gy, gz;    // saved uber cell, saved grid cell
     int steps, level, bi;
-    uint32_t o, brick, last, dirbits;   // dirbits: bit a set = positive direction on axis a
+    uint32_t o, brick, last, dirbits;   // o: content of the current cell; dirbits: bit a = positive on axis a
     float dist;                    // result
     uint32_t side, voxel;
     __device__ __forceinline__ int sx() const { return (dirbits & 1u) ? 1 : -1; }
@@ -267,6 +268,15 @@ struct Walker {
     __device__ __forceinline__ int oz() const { return (int)((dirbits >> 2) & 1u); }
 };
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
+
+// content of cell (cx, cy, cz) at the walker's level: uber occupancy byte, grid cell, or
+// brick voxel
+__device__ __forceinline__ uint32_t walk_load(const Walker& k, const World& w) {
+    if (k.level == 0) return __ldg(w.uber + k.cx + k.cz * 32 + k.cy * 1024);
+    const uint32_t* base = k.level == 1 ? w.grid : w.bricks + (size_t)k.brick * 512u;
+    const int sy = k.level == 1 ? 16384 : 8, sz = k.level == 1 ? 128 : 64;
+    return __ldg(base + k.cx + k.cz * sz + k.cy * sy);
+}
 
 // TraceOpaqueRay prologue (trace.cl:219-243); returns WALK_MISS when the ray misses the map
 __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, float ay, float az, float vx, float vy,
@@ -298,119 +308,98 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
         if (az < 0.01f || az > hi) k.last = 2;
     }
     k.ax = ax; k.ay = ay; k.az = az;
-    k.ux = (int)min(f2u(ax) >> 5, 31u);
-    k.uy = (int)min(f2u(ay) >> 5, 31u);
-    k.uz = (int)min(f2u(az) >> 5, 31u);
-    k.tmx = ((float)(uint32_t)(k.ux + k.ox()) - ax * 0.03125f) * k.rx;
-    k.tmy = ((float)(uint32_t)(k.uy + k.oy()) - ay * 0.03125f) * k.ry;
-    k.tmz = ((float)(uint32_t)(k.uz + k.oz()) - az * 0.03125f) * k.rz;
-    k.tdx = (float)k.sx() * k.rx;
-    k.tdy = (float)k.sy() * k.ry;
-    k.tdz = (float)k.sz() * k.rz;
+    k.cx = (int)min(f2u(ax) >> 5, 31u);
+    k.cy = (int)min(f2u(ay) >> 5, 31u);
+    k.cz = (int)min(f2u(az) >> 5, 31u);
+    k.tmx = ((float)(uint32_t)(k.cx + k.ox()) - ax * 0.03125f) * k.rx;
+    k.tmy = ((float)(uint32_t)(k.cy + k.oy()) - ay * 0.03125f) * k.ry;
+    k.tmz = ((float)(uint32_t)(k.cz + k.oz()) - az * 0.03125f) * k.rz;
     k.t = 0.0f;
     k.steps = steps;
     k.level = 0;
-    k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
+    k.o = walk_load(k, w);
     return WALK_CONTINUE;
 }
 
-// uber-level step (trace.cl:274-279); returns false when the ray leaves the map
-__device__ __forceinline__ bool walk_uber_step(Walker& k, const World& w) {
-    k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-    k.last = 0;
-    if (k.t == k.tmx) { k.tmx += k.tdx; k.ux += k.sx(); }
-    if (k.t == k.tmy) { k.tmy += k.tdy; k.uy += k.sy(); k.last = 1; }
-    if (k.t == k.tmz) { k.tmz += k.tdz; k.uz += k.sz(); k.last = 2; }
-    if ((k.ux | k.uy | k.uz) & ~31) return false;
-    k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
-    return true;
-}
-
-// grid-level step (GRIDSTEP tail, trace.cl:105-110); continues into the uber step
-// when the ray leaves the current uber cell
-__device__ __forceinline__ int walk_grid_step(Walker& k, const World& w) {
-    k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-    k.last = 0;
-    if (k.t == k.tmx) { k.tmx += k.tdx; k.gx += k.sx(); }
-    if (k.t == k.tmy) { k.tmy += k.tdy; k.gy += k.sy(); k.last = 1; }
-    if (k.t == k.tmz) { k.tmz += k.tdz; k.gz += k.sz(); k.last = 2; }
-    if (((k.gx >> 2) != k.ux) | ((k.gy >> 2) != k.uy) | ((k.gz >> 2) != k.uz)) {
-        k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
-        k.level = 0;
-        return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
-    }
-    k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
-    return WALK_CONTINUE;
-}
-
-// one cell visit at the current level
+// One cell visit. The three levels of the reference's DDA (uber 32^3 cells of 4^3 grid
+// cells, grid 128^3 cells, bricks of 8^3 voxels; trace.cl:59-117, 219-285) run the same
+// code with per-level constants, so lanes of a warp at different levels stay converged
+// through the cell step, the only part every visit executes:
+//   examine  uber: budget -4, occupied -> descend; grid: budget -1, solid -> hit test,
+//            brick -> descend; brick voxel: hit test (bricks are free of budget)
+//   descend  entry cell of the child level from the ray point at the current t
+//   advance  t = min crossing, every tied axis steps, `last` = the highest tied axis;
+//            leaving the parent cell (or 24 brick steps) ascends and advances there
+// Arithmetic per level is the reference's: 1.0f and 0-offset factors stand in where a
+// level has no scale, and multiplying by 1.0f or adding 0 is exact.
 __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
-    if (k.level == 2) {
-        const uint32_t v = __ldg(w.bricks + (size_t)k.brick * 512u + k.lx + k.ly * 8 + k.lz * 64);
-        if (((v & 0xf000u) >> 12) == 15u) {
-            k.dist = k.t + k.to;
-            k.side = k.last;
-            k.voxel = v;
-            return WALK_HIT;
+    const int L = k.level;
+    const int cost = L == 0 ? 4 : (L == 1 ? 1 : 0);
+    k.steps -= cost;
+    if (cost != 0 && k.steps <= 0) return WALK_MISS;   // budget (a grid step that empties it always misses)
+    const uint32_t o = k.o;
+    const uint32_t v = L == 1 ? (o >> 1) : o;
+    if ((L == 2 || (L == 1 && (o & 1u) == 0u)) && ((v & 0xf000u) >> 12) == 15u) {
+        k.dist = (L == 1 ? k.t * 8.0f : k.t) + k.to;
+        k.side = k.last;
+        k.voxel = v;
+        return WALK_HIT;
+    }
+    if ((L == 0 && o != 0u) || (L == 1 && (o & 1u))) {
+        // descend: uber -> grid (trace.cl:247-255), grid -> brick (trace.cl:65-74)
+        const bool toGrid = L == 0;
+        const float as = toGrid ? 0.125f : 1.0f;
+        const uint32_t span = toGrid ? 4u : 8u;
+        if (toGrid) {
+            k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
+            k.ux = k.cx; k.uy = k.cy; k.uz = k.cz;
+        } else {
+            k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
+            k.gx = k.cx; k.gy = k.cy; k.gz = k.cz;
+            k.brick = o >> 1;
+            k.bi = 0;
         }
+        k.t *= toGrid ? 4.0f : 8.0f;
+        const uint32_t px = f2u(as * k.ax + k.vx * k.t), py = f2u(as * k.ay + k.vy * k.t), pz = f2u(as * k.az + k.vz * k.t);
+        const uint32_t bx = (uint32_t)k.cx * span, by = (uint32_t)k.cy * span, bz = (uint32_t)k.cz * span;
+        const uint32_t qx = min(max(px, bx), bx + span - 1u), qy = min(max(py, by), by + span - 1u),
+                       qz = min(max(pz, bz), bz + span - 1u);
+        k.tmx = ((float)(qx + (uint32_t)k.ox()) - k.ax * as) * k.rx;
+        k.tmy = ((float)(qy + (uint32_t)k.oy()) - k.ay * as) * k.ry;
+        k.tmz = ((float)(qz + (uint32_t)k.oz()) - k.az * as) * k.rz;
+        const uint32_t lo = toGrid ? 0u : span;   // brick coordinates are local
+        k.cx = (int)(qx - (lo ? bx : 0u));
+        k.cy = (int)(qy - (lo ? by : 0u));
+        k.cz = (int)(qz - (lo ? bz : 0u));
+        k.level = L + 1;
+        k.o = walk_load(k, w);
+        return WALK_CONTINUE;
+    }
+    // advance; ascend while the ray leaves the parent cell
+    for (;;) {
         k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
         k.last = 0;
-        if (k.t == k.tmx) { k.tmx += k.tdx; k.lx += k.sx(); }
-        if (k.t == k.tmy) { k.tmy += k.tdy; k.ly += k.sy(); k.last = 1; }
-        if (k.t == k.tmz) { k.tmz += k.tdz; k.lz += k.sz(); k.last = 2; }
-        if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
+        if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.cx += k.sx(); }
+        if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.cy += k.sy(); k.last = 1; }
+        if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.cz += k.sz(); k.last = 2; }
+        const int lv = k.level;
+        const int lx = lv == 1 ? 4 * k.ux : 0, ly = lv == 1 ? 4 * k.uy : 0, lz = lv == 1 ? 4 * k.uz : 0;
+        const int mask = lv == 0 ? ~31 : (lv == 1 ? ~3 : ~7);
+        bool out = (((k.cx - lx) | (k.cy - ly) | (k.cz - lz)) & mask) != 0;
+        if (!out && lv == 2) out = ++k.bi == 24;
+        if (!out) break;
+        if (lv == 0) return WALK_MISS;   // left the map
+        if (lv == 2) {
             k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
-            k.level = 1;
-            return walk_grid_step(k, w);
+            k.cx = k.gx; k.cy = k.gy; k.cz = k.gz;
+        } else {
+            k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
+            k.cx = k.ux; k.cy = k.uy; k.cz = k.uz;
         }
-        return WALK_CONTINUE;
+        k.level = lv - 1;
     }
-    if (k.level == 1) {
-        // a grid step with the budget exhausted always ends as a miss (the uber loop
-        // re-checks the budget before any further cell is visited)
-        if (!--k.steps) return WALK_MISS;
-        if ((k.o & 1u) == 0u) {
-            const uint32_t v = k.o >> 1;
-            if (((v & 0xf000u) >> 12) == 15u) {
-                k.dist = k.t * 8.0f + k.to;
-                k.side = k.last;
-                k.voxel = v;
-                return WALK_HIT;
-            }
-            return walk_grid_step(k, w);
-        }
-        k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
-        k.t *= 8.0f;
-        const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
-        const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
-        const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u), cz = min(max(pz, bz0), bz0 + 7u);
-        k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
-        k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
-        k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
-        k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
-        k.brick = k.o >> 1;
-        k.bi = 0;
-        k.level = 2;
-        return WALK_CONTINUE;
-    }
-    // uber level
-    if ((k.steps -= 4) <= 0) return WALK_MISS;
-    if (k.o != 0u) {
-        k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
-        k.t *= 4.0f;
-        const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
-                       qz = f2u(0.125f * k.az + k.vz * k.t);
-        k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
-        k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
-        k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
-        k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
-        k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
-        k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
-        k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
-        k.level = 1;
-        return WALK_CONTINUE;
-    }
-    return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
+    k.o = walk_load(k, w);
+    return WALK_CONTINUE;
 }
 
 // ---- reservoirs --------------------------------------------------------------------

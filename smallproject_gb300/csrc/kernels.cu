@@ -105,8 +105,14 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
     return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
 }
 
-// next tile of the batch for this block (tile-queue cursor `ctr`); false when drained
-__device__ __forceinline__ bool next_tile(const BatchDev& bd, uint32_t* ctr, uint32_t* tile) {
+// Next tile of the batch for this block: with bd.persistent, resident blocks pull tiles
+// from the queue cursor `ctr` until it is drained; otherwise the launch has one block per
+// tile and the hardware block scheduler balances them. `round` counts calls (starts at 0).
+__device__ __forceinline__ bool next_tile(const BatchDev& bd, uint32_t* ctr, uint32_t* tile, uint32_t& round) {
+    if (!bd.persistent) {
+        *tile = blockIdx.x;
+        return round++ == 0;
+    }
     __shared__ uint32_t s_tile;
     __syncthreads();
     if (threadIdx.x == 0) s_tile = atomicAdd(ctr, 1u);
@@ -167,8 +173,8 @@ __device__ __forceinline__ void albedo_px(const World& w, const Frame& k, uint2*
 
 template <int VARIANT>
 __global__ void __launch_bounds__(128) albedo_kernel(const __grid_constant__ BatchDev bd) {
-    uint32_t tile;
-    while (next_tile(bd, bd.counters + kCtrAlbedo, &tile)) {
+    uint32_t tile, round = 0;
+    while (next_tile(bd, bd.counters + kCtrAlbedo, &tile, round)) {
         int x, y;
         const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
         const Frame& k = V->k;
@@ -267,7 +273,8 @@ __device__ __forceinline__ void shadow_finish(const World& w, int st, const Walk
 
 template <int VARIANT>
 __global__ void __launch_bounds__(128) shadow_kernel(const __grid_constant__ BatchDev bd, int countIdx, int fetchIdx,
-                                                     int planeSel, int refill) {
+                                                     int planeSel) {
+    const int refill = bd.refill, burst = bd.burst;
     const uint32_t n = bd.counters[countIdx];
     uint32_t* fetch = bd.counters + fetchIdx;
     const int lane = threadIdx.x & 31;
@@ -308,7 +315,7 @@ __global__ void __launch_bounds__(128) shadow_kernel(const __grid_constant__ Bat
         }
         if (active) {
 #pragma unroll 1
-            for (int s = 0; s < 4; s++) {
+            for (int s = 0; s < burst; s++) {
                 const int st = walk_step(wk, w);
                 if (st != WALK_CONTINUE) {
                     shadow_finish(w, st, wk, o, L, plane, pix, li);
@@ -569,8 +576,8 @@ __device__ __forceinline__ void spatial_px(const ViewDev* V, int x, int y) {
 
 template <int VARIANT>
 __global__ void __launch_bounds__(128) spatial_kernel(const __grid_constant__ BatchDev bd) {
-    uint32_t tile;
-    while (next_tile(bd, bd.counters + kCtrSpatial, &tile)) {
+    uint32_t tile, round = 0;
+    while (next_tile(bd, bd.counters + kCtrSpatial, &tile, round)) {
         int x, y;
         const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
         if (x < V->k.W && y < V->k.H) {
@@ -668,8 +675,8 @@ __device__ __forceinline__ void shade_finish_px(const ViewDev* V, int x, int y, 
 
 template <int VARIANT>
 __global__ void __launch_bounds__(128) shade_finish_kernel(const __grid_constant__ BatchDev bd) {
-    uint32_t tile;
-    while (next_tile(bd, bd.counters + kCtrFinish, &tile)) {
+    uint32_t tile, round = 0;
+    while (next_tile(bd, bd.counters + kCtrFinish, &tile, round)) {
         int x, y;
         const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
         if (x < V->k.W && y < V->k.H) {
@@ -682,8 +689,8 @@ __global__ void __launch_bounds__(128) shade_finish_kernel(const __grid_constant
 // stage 5 on its own
 template <int VARIANT>
 __global__ void __launch_bounds__(128) accumulate_kernel(const __grid_constant__ BatchDev bd) {
-    uint32_t tile;
-    while (next_tile(bd, bd.counters + kCtrAccum, &tile)) {
+    uint32_t tile, round = 0;
+    while (next_tile(bd, bd.counters + kCtrAccum, &tile, round)) {
         int x, y;
         const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
         if (x < V->k.W && y < V->k.H) {
@@ -732,12 +739,24 @@ static unsigned resident_blocks(const void* kernel, int threads) {
 template <class K>
 static void launch_tiles(K kernel, const BatchDev& bd, int ctr, cudaStream_t s) {
     const int threads = bd.tx * bd.ty;
-    cudaMemsetAsync(bd.counters + ctr, 0, sizeof(uint32_t), s);
-    const unsigned nb = std::max(1u, std::min(resident_blocks((const void*)kernel, threads), bd.totalTiles));
+    unsigned nb = std::max(1u, bd.totalTiles);
+    if (bd.persistent) {
+        cudaMemsetAsync(bd.counters + ctr, 0, sizeof(uint32_t), s);
+        nb = std::max(1u, std::min(resident_blocks((const void*)kernel, threads), bd.totalTiles));
+    }
     kernel<<<nb, threads, 0, s>>>(bd);
 }
 
-BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, LaunchShape sh) {
+void apply_tuning(BatchDev& bd, const Tuning& tu) {
+    bd.tx = tu.bx;
+    bd.ty = tu.by;
+    bd.persistent = tu.persistent;
+    bd.refill = tu.refill;
+    bd.burst = tu.burst;
+    bd.listPerSm = tu.listPerSm;
+}
+
+BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, const Tuning& tu) {
     BatchDev bd;
     bd.one.w = w;
     bd.one.k = k;
@@ -745,12 +764,11 @@ BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffer
     bd.one.cur = cur;
     bd.one.point = point ? 1 : 0;
     bd.one.tileBase = 0;
-    bd.one.tilesX = (uint32_t)((k.W + sh.bx - 1) / sh.bx);
+    bd.one.tilesX = (uint32_t)((k.W + tu.bx - 1) / tu.bx);
     bd.nviews = 1;
     bd.totalPixels = (uint32_t)k.W * (uint32_t)k.H;
-    bd.totalTiles = bd.one.tilesX * (uint32_t)((k.H + sh.by - 1) / sh.by);
-    bd.tx = sh.bx;
-    bd.ty = sh.by;
+    bd.totalTiles = bd.one.tilesX * (uint32_t)((k.H + tu.by - 1) / tu.by);
+    apply_tuning(bd, tu);
     bd.hits = b.hits;
     bd.qA = b.qA;
     bd.qB = b.qB;
@@ -776,7 +794,7 @@ template <int VARIANT>
 static void launch_shadow(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
     const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT>, 128);
     const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 127) / 128));
-    dev::shadow_kernel<VARIANT><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel, 8);
+    dev::shadow_kernel<VARIANT><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel);
 }
 
 template <int VARIANT>
@@ -786,7 +804,7 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
     uint32_t maxPx = VARIANT < 2 ? bd.totalPixels : 0;
     if (VARIANT == 2) maxPx = (uint32_t)(n / bd.nviews + 1);
     dev::compact_hits_kernel<VARIANT><<<dim3(list_blocks(maxPx, 256, 8), bd.nviews), 256, 0, s>>>(bd);
-    const unsigned nb = list_blocks(n, 128, 16);
+    const unsigned nb = list_blocks(n, 128, bd.listPerSm);
     bool learnedDone = false;
     if constexpr (VARIANT < 2) {
         if (learned) {
@@ -830,7 +848,7 @@ void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s) {
 template <int VARIANT>
 static void shade_v(const BatchDev& bd, cudaStream_t s) {
     cudaMemsetAsync(bd.counters + kCtrQ2, 0, 2 * sizeof(uint32_t), s);   // q2 requests, q2 fetch
-    dev::shade_request_kernel<VARIANT < 2 ? 0 : 2><<<list_blocks(bd.totalPixels, 128, 16), 128, 0, s>>>(bd);
+    dev::shade_request_kernel<VARIANT < 2 ? 0 : 2><<<list_blocks(bd.totalPixels, 128, bd.listPerSm), 128, 0, s>>>(bd);
     launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ2, 1, s);
     launch_tiles(dev::shade_finish_kernel<VARIANT>, bd, kCtrFinish, s);
 }

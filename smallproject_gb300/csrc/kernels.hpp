@@ -67,6 +67,10 @@ struct BatchDev {
     uint32_t totalPixels = 0;
     uint32_t totalTiles = 0;
     int tx = 16, ty = 8;                  // tile = block shape of the pixel stages
+    int persistent = 0;                   // pixel stages: resident blocks pull tiles from a queue
+    int refill = 8;                       // shadow tracer: idle lanes of a warp that trigger a refill
+    int burst = 4;                        // shadow tracer: cell visits per lane between refill checks
+    int listPerSm = 16;                   // blocks per SM of the hit-list kernels
     int fuse = 0;                         // shading also accumulates
     uint32_t* hits = nullptr;             // hit list over all views
     float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(entry))
@@ -74,8 +78,13 @@ struct BatchDev {
     uint32_t* counters = nullptr;         // kCounters words
 };
 
-struct LaunchShape {
-    int bx = 16, by = 8;                  // threads per block (tile)
+// Launch parameters that change speed but never results (autotuned per configuration).
+struct Tuning {
+    int bx = 16, by = 8;                  // threads per block (tile) of the pixel stages
+    int persistent = 0;
+    int refill = 8;
+    int burst = 4;
+    int listPerSm = 16;
 };
 
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s);
@@ -90,7 +99,8 @@ struct LearnedHook {
 };
 
 // A batch of one view over its own list buffers.
-BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, LaunchShape sh);
+BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, const Tuning& tu);
+void apply_tuning(BatchDev& bd, const Tuning& tu);
 
 // Stage launchers over a batch. variant: 0 single view / area lights, 1 single view /
 // point lights, 2 view table (light model per view). A learned proposal needs variant 0/1.

@@ -188,7 +188,7 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     b.qB = (float4*)(s + kOffQB);
     b.counters = (uint32_t*)(s + kOffErr + 64);
     const bool point = light_model == VXR_LIGHTS_POINT;
-    const vxr::LaunchShape sh;
+    const vxr::Tuning sh;
     const vxr::BatchDev bd = vxr::single_batch(w, f, b, 0, point, sh);
     const int variant = point ? 1 : 0;
     vxr::launch_batch_albedo(bd, variant, st);

@@ -193,8 +193,8 @@ void harvest(vxr_view* v) {
     v->harvested = v->frameSerial;
 }
 
-vxr::LaunchShape shape(const vxr_view* v) {
-    vxr::LaunchShape s;
+vxr::Tuning shape(const vxr_view* v) {
+    vxr::Tuning s = v->tuning;
     if (v->desc.tile_x) s.bx = (int)v->desc.tile_x;
     if (v->desc.tile_y) s.by = (int)v->desc.tile_y;
     return s;
@@ -391,7 +391,7 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     const vxr::dev::World w = dev_world(v);
     const vxr::dev::Frame k = dev_frame(v->k);
     const bool point = v->desc.light_model == VXR_LIGHTS_POINT;
-    const vxr::LaunchShape sh = shape(v);
+    const vxr::Tuning sh = shape(v);
     const int ri = (int)(v->frameSerial % vxr_view::kRing) * 6 + stage;
     CUV(cudaEventRecord(v->evs[stage], v->stream), "cudaEventRecord");
     CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");
@@ -660,6 +660,81 @@ int vxr_view_timer_end(vxr_view* v, float* ms) {
 }
 
 }  // extern "C"
+
+namespace vxr {
+int check_tuning(const vxr_tuning* t, const char* fn) {
+    if (!t) return set_error(VXR_E_INVALID, std::string(fn) + ": null tuning");
+    const uint32_t n = t->tile_x * t->tile_y;
+    if (t->tile_x < 1 || t->tile_y < 1 || t->tile_x > 1024 || t->tile_y > 1024 || n > 1024 || n % 32 != 0)
+        return set_error(VXR_E_INVALID, std::string(fn) + ": tile must hold a multiple of 32 threads, at most 1024");
+    if (t->persistent > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": persistent must be 0 or 1");
+    if (t->shadow_refill < 1 || t->shadow_refill > 32)
+        return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_refill out of range [1, 32]");
+    if (t->shadow_burst < 1 || t->shadow_burst > 64)
+        return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_burst out of range [1, 64]");
+    if (t->list_blocks_per_sm < 1 || t->list_blocks_per_sm > 64)
+        return set_error(VXR_E_INVALID, std::string(fn) + ": list_blocks_per_sm out of range [1, 64]");
+    return VXR_OK;
+}
+Tuning to_tuning(const vxr_tuning& t) {
+    Tuning u;
+    u.bx = (int)t.tile_x;
+    u.by = (int)t.tile_y;
+    u.persistent = (int)t.persistent;
+    u.refill = (int)t.shadow_refill;
+    u.burst = (int)t.shadow_burst;
+    u.listPerSm = (int)t.list_blocks_per_sm;
+    return u;
+}
+}  // namespace vxr
+
+extern "C" int vxr_default_tuning(vxr_tuning* t) {
+    VXR_CHECK_ARG(t, "vxr_default_tuning: null tuning");
+    const vxr::Tuning u;
+    t->tile_x = (uint32_t)u.bx;
+    t->tile_y = (uint32_t)u.by;
+    t->persistent = (uint32_t)u.persistent;
+    t->shadow_refill = (uint32_t)u.refill;
+    t->shadow_burst = (uint32_t)u.burst;
+    t->list_blocks_per_sm = (uint32_t)u.listPerSm;
+    return VXR_OK;
+}
+
+extern "C" int vxr_device_info(char* name, size_t n, int* sms, int* cc_major, int* cc_minor) {
+    VXR_CHECK_ARG(name && n > 0 && sms && cc_major && cc_minor, "vxr_device_info: null argument");
+    int dev = 0;
+    cudaDeviceProp p;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess)
+        return set_error(VXR_E_NODEVICE, "vxr_device_info: no CUDA device visible");
+    std::strncpy(name, p.name, n - 1);
+    name[n - 1] = '\0';
+    *sms = p.multiProcessorCount;
+    *cc_major = p.major;
+    *cc_minor = p.minor;
+    return VXR_OK;
+}
+
+extern "C" int vxr_view_set_tuning(vxr_view* v, const vxr_tuning* t) {
+    if (int r = check_view(v, "vxr_view_set_tuning")) return r;
+    if (int r = vxr::check_tuning(t, "vxr_view_set_tuning")) return r;
+    v->tuning = vxr::to_tuning(*t);
+    v->desc.tile_x = t->tile_x;
+    v->desc.tile_y = t->tile_y;
+    return VXR_OK;
+}
+
+extern "C" int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t) {
+    if (int r = check_view(v, "vxr_view_get_tuning")) return r;
+    VXR_CHECK_ARG(t, "vxr_view_get_tuning: null tuning");
+    const vxr::Tuning u = shape(v);
+    t->tile_x = (uint32_t)u.bx;
+    t->tile_y = (uint32_t)u.by;
+    t->persistent = (uint32_t)u.persistent;
+    t->shadow_refill = (uint32_t)u.refill;
+    t->shadow_burst = (uint32_t)u.burst;
+    t->list_blocks_per_sm = (uint32_t)u.listPerSm;
+    return VXR_OK;
+}
 
 extern "C" int vxr_view_stage_stats(vxr_view* v, double sum_ms[5], uint32_t count[5], int reset) {
     if (int r = check_view(v, "vxr_view_stage_stats")) return r;

@@ -33,6 +33,7 @@ struct vxr_view {
     vxr_view_desc desc{};
     vxr::CameraState cam;
     vxr::ViewBuffers buf;
+    vxr::Tuning tuning;                               // launch parameters (vxr_view_set_tuning)
     int cur = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t evs[6] = {}, eve[6] = {};            // [0]: vxr_view_timer_*, [1..5]: last frame's stages
@@ -64,5 +65,7 @@ dev::Frame dev_frame(const vxr_frame_consts& c);
 int ensure_world(vxr_view* v);
 void free_view(vxr_view* v);
 void harvest(vxr_view* v);
-LaunchShape shape(const vxr_view* v);
+Tuning shape(const vxr_view* v);
+int check_tuning(const vxr_tuning* t, const char* fn);
+Tuning to_tuning(const vxr_tuning& t);
 }  // namespace vxr

@@ -65,6 +65,14 @@ class ProposalDesc(C.Structure):
                 ("epsilon", C.c_float), ("learning_rate", C.c_float), ("batch", C.c_uint32), ("seed", C.c_uint32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("tile_x", C.c_uint32), ("tile_y", C.c_uint32), ("persistent", C.c_uint32),
+                ("shadow_refill", C.c_uint32), ("shadow_burst", C.c_uint32), ("list_blocks_per_sm", C.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class ViewDesc(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("light_model", C.c_uint32),
                 ("num_candidates", C.c_uint32), ("spatial_taps", C.c_uint32), ("spatial_radius", C.c_uint32),
@@ -131,7 +139,10 @@ _SIGS = {
     "vxr_view_proposal_probs": [_P, C.c_uint32, _F3, _F3],
     "vxr_view_proposal_save": [_P, C.c_char_p], "vxr_view_proposal_load": [_P, C.c_char_p],
     "vxr_batch_create": [C.POINTER(_P), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(_P)],
-    "vxr_batch_destroy": [_P], "vxr_batch_render": [_P], "vxr_batch_wait": [_P, C.POINTER(C.c_float)],
+    "vxr_batch_destroy": [_P], "vxr_batch_set_tuning": [_P, C.POINTER(Tuning)],
+    "vxr_default_tuning": [C.POINTER(Tuning)], "vxr_view_set_tuning": [_P, C.POINTER(Tuning)],
+    "vxr_view_get_tuning": [_P, C.POINTER(Tuning)],
+    "vxr_device_info": [C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], "vxr_batch_render": [_P], "vxr_batch_wait": [_P, C.POINTER(C.c_float)],
     "vxr_render_frame_noalloc": [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts), _P, _P],
 }
 _RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
@@ -281,6 +292,23 @@ def camera_path(desc, seed, f, n):
     p, t = (C.c_float * 3)(), (C.c_float * 3)()
     check(load().vxr_camera_path(C.byref(desc), seed, f, n, p, t))
     return list(p), list(t)
+
+
+def device_info():
+    """(name, SM count, (major, minor)) of the current CUDA device."""
+    buf = C.create_string_buffer(256)
+    sms, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    check(load().vxr_device_info(buf, 256, C.byref(sms), C.byref(ma), C.byref(mi)))
+    return buf.value.decode(), sms.value, (ma.value, mi.value)
+
+
+def tuning(**kw):
+    """A vxr_tuning with library defaults, fields overridden by keyword."""
+    t = Tuning()
+    check(load().vxr_default_tuning(C.byref(t)))
+    for k, v in kw.items():
+        setattr(t, k, v)
+    return t
 
 
 def view_desc(width, height, light_model=LIGHTS_AREA, **kw):
@@ -456,6 +484,14 @@ class View:
     def proposal_load(self, path):
         check(self._lib.vxr_view_proposal_load(self.h, str(path).encode()))
 
+    def set_tuning(self, t):
+        check(self._lib.vxr_view_set_tuning(self.h, C.byref(t)))
+
+    def get_tuning(self):
+        t = Tuning()
+        check(self._lib.vxr_view_get_tuning(self.h, C.byref(t)))
+        return t
+
     def timer_begin(self):
         check(self._lib.vxr_view_timer_begin(self.h))
 
@@ -497,6 +533,9 @@ class Batch:
 
     def render(self):
         check(self._lib.vxr_batch_render(self.h))
+
+    def set_tuning(self, t):
+        check(self._lib.vxr_batch_set_tuning(self.h, C.byref(t)))
 
     def wait(self):
         """Wait for the batch; returns the GPU time of the last frame in ms."""

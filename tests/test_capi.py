@@ -52,6 +52,41 @@ def test_invalid_arguments_return_status(lib):
     h = C.c_void_p()
     assert L.vxr_view_create(w.h, C.byref(vd), C.byref(h)) == lib.vxr.VXR_E_INVALID
     assert L.vxr_view_stage(None, 1) == lib.vxr.VXR_E_INVALID
+    # batches and tuning: argument checks that need no device
+    assert L.vxr_batch_create(None, 1, 0, 0, 0, C.byref(h)) == lib.vxr.VXR_E_INVALID
+    arr = (C.c_void_p * 1)(None)
+    assert L.vxr_batch_create(arr, 0, 0, 0, 0, C.byref(h)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_create(arr, 17, 0, 0, 0, C.byref(h)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_create(arr, 1, 0, 0, 2, C.byref(h)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_create(arr, 1, 5, 5, 0, C.byref(h)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_create(arr, 1, 0, 0, 0, C.byref(h)) == lib.vxr.VXR_E_INVALID   # null view
+    assert L.vxr_batch_render(None) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_wait(None, None) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_destroy(None) == lib.vxr.VXR_OK
+    t = lib.tuning()
+    assert (t.tile_x, t.tile_y, t.persistent, t.shadow_refill, t.shadow_burst, t.list_blocks_per_sm) == (16, 8, 0, 8, 4, 16)
+    assert L.vxr_view_set_tuning(None, C.byref(t)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_batch_set_tuning(None, C.byref(t)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_default_tuning(None) == lib.vxr.VXR_E_INVALID
+
+
+def test_autotune_cache_roundtrip(tmp_path):
+    from smallproject_gb300 import autotune as at
+    from smallproject_gb300 import vxr as V
+    d = {"tile": [32, 4], "persistent": 1, "shadow_refill": 16, "shadow_burst": 2, "list_blocks_per_sm": 8}
+    t = at._to_tuning(d)
+    assert isinstance(t, V.Tuning) and at._from_tuning(t) == {**d, "tile": (32, 4)}
+    path = str(tmp_path / "c.json")
+    assert at.load_cache(path) == {}
+    at.save_cache({"k": {"tuning": d, "ms": 1.0}}, path)
+    assert at.load_cache(path)["k"]["tuning"] == d
+    # every candidate of the search space is a valid tuning
+    for name, values in at.SPACE:
+        for val in values:
+            dd = dict(d)
+            dd[name] = list(val) if isinstance(val, tuple) else val
+            tt = at._to_tuning(dd)
+            assert (tt.tile_x * tt.tile_y) % 32 == 0 and tt.tile_x * tt.tile_y <= 1024
 
 
 def test_out_of_map_set_is_ignored(lib):
