@@ -246,7 +246,7 @@ typedef struct vxr_view_desc {
     uint32_t temporal_max_importance;      /* TEMPORALMAXIMPORTANCE, default 20 */
     int32_t  spatial, temporal, accumulate;/* RenderParams toggles (defaults 1, 1, 0) */
     uint32_t rng_seed;                     /* host RandomUInt seed for R0, default 0x12345678 */
-    uint32_t tile_x, tile_y;               /* threads per block; 0 = library default */
+    uint32_t tile_x, tile_y;               /* threads per pixel-stage block (<= 256); 0 = library default */
 } vxr_view_desc;
 
 int vxr_view_default_desc(vxr_view_desc* d);
@@ -373,7 +373,7 @@ int vxr_view_error(vxr_view* img, int which, vxr_view* ref, double* mse, double*
  * Parameters that change speed but never results: every setting renders the same bits.
  * The autotuner (smallproject_gb300/autotune.py) times them per configuration. */
 typedef struct vxr_tuning {
-    uint32_t tile_x, tile_y;       /* threads of a pixel-stage block; tile_x * tile_y a multiple of 32, <= 1024 */
+    uint32_t tile_x, tile_y;       /* threads of a pixel-stage block; tile_x * tile_y a multiple of 32, <= 256 */
     uint32_t persistent;           /* pixel stages: 1 = resident blocks pull tiles from a queue, 0 = one block per tile */
     uint32_t shadow_refill;        /* shadow tracer: idle lanes of a warp (1..32) that trigger a refill from the queue */
     uint32_t shadow_burst;         /* shadow tracer: cell visits per lane between refill checks (1..64) */
@@ -397,7 +397,7 @@ int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t);
  * G-buffers and reservoirs are bit-identical to rendering it alone with vxr_view_render.
  * Views must be on one device, hold at most 2^27 - 1 pixels each and not use a learned
  * proposal. tile_x * tile_y = threads of a pixel-stage block (0, 0 = 16 x 8), a multiple
- * of 32 up to 1024. flags: VXR_BATCH_GRAPH records the frame once as a CUDA graph and
+ * of 32 up to 256. flags: VXR_BATCH_GRAPH records the frame once as a CUDA graph and
  * replays it: one graph launch per frame. */
 #define VXR_BATCH_MAX_VIEWS 16u
 #define VXR_BATCH_GRAPH     1u

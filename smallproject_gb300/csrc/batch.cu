@@ -89,8 +89,8 @@ int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32
     VXR_CHECK_ARG(n >= 1 && n <= VXR_BATCH_MAX_VIEWS, "vxr_batch_create: view count out of range [1, VXR_BATCH_MAX_VIEWS]");
     VXR_CHECK_ARG((flags & ~VXR_BATCH_GRAPH) == 0, "vxr_batch_create: unknown flags");
     const uint32_t tx = tile_x ? tile_x : 16, ty = tile_y ? tile_y : 8;
-    VXR_CHECK_ARG(tx * ty >= 32 && tx * ty <= 1024 && (tx * ty) % 32 == 0,
-                  "vxr_batch_create: tile must hold a multiple of 32 threads, at most 1024");
+    VXR_CHECK_ARG(tx <= 256 && ty <= 256 && tx * ty >= 32 && tx * ty <= 256 && (tx * ty) % 32 == 0,
+                  "vxr_batch_create: tile must hold a multiple of 32 threads, at most 256");
     uint64_t total = 0, tiles = 0;
     for (uint32_t i = 0; i < n; i++) {
         VXR_CHECK_ARG(views[i], "vxr_batch_create: null view");

@@ -97,6 +97,96 @@ __device__ __forceinline__ float3 camera_ray(const Frame& k, int x, int y) {
     return normalize3(sub(P, k.E));
 }
 
+// ---- area-light sample (RandomPointOnVoxel, tools.cl:499-577) ---------------------------
+// One random point per face of the emitter cube (two draws per face, faces in the order
+// +x +y +z -x -y -z, all twelve draws always taken), faces weighted by the solid angle
+// they subtend from the shading point, a CDF pick with one more draw, weight = 1/pdf.
+// A face contributes only when its outward normal points toward the shading point, and
+// along each axis at most one of the two faces does: the point is beyond the +a face or
+// beyond the -a face or between them. So the solid angles are computed once per axis for
+// that axis' facing face, with the same operations the per-face form uses; faces that do
+// not face the point have solid angle +0, and adding +0 to the running total (which is
+// never -0) changes nothing.
+__device__ __forceinline__ float rnd_of(uint32_t u) { return __uint2float_rn(u) * 2.3283064365387e-10f; }
+
+// point on face `face` at (r0, r1): center + 0.5 size N - 0.5 size T - 0.5 size B + r0 size T
+// + r1 size B, with T, B the two following axes (tools.cl:502-515, 540-546)
+__device__ __forceinline__ float3 face_point(float4 g, uint32_t face, float r0, float r1) {
+    const float size = g.w, h = 0.5f * size;
+    const float s = face < 3 ? 1.0f : -1.0f;
+    const uint32_t an = face % 3, at = (an + 1) % 3, ab = (an + 2) % 3;
+    float c[3] = {g.x, g.y, g.z}, p[3];
+    p[an] = c[an] + h * s;
+    p[at] = (c[at] - h * s) + (r0 * size) * s;
+    p[ab] = (c[ab] - h * s) + (r1 * size) * s;
+    return f3(p[0], p[1], p[2]);
+}
+
+// lg = (centre, size); spo = offset shading point. Returns the point, *invp = 1/pdf
+// (NaN/Inf -> 0), *ncode = face index (Nlight = normals[face]).
+__device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32_t& seed, float* invp, uint32_t* ncode) {
+    uint32_t u[12];
+#pragma unroll
+    for (int i = 0; i < 12; i++) u[i] = xs32(seed);
+    const float size = g.w, h = 0.5f * size, area = size * size;
+    const float c[3] = {g.x, g.y, g.z}, sp[3] = {spo.x, spo.y, spo.z};
+    float sa[6];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int at = (a + 1) % 3, ab = (a + 2) % 3;
+        const bool plus = (sp[a] - (c[a] + h)) > 0.0f;      // s (sp - (c + h s)) > 0, s = +1
+        const bool minus = -(sp[a] - (c[a] + (-h))) > 0.0f;  // s = -1
+        const float s = plus ? 1.0f : -1.0f;
+        const float r0 = rnd_of(plus ? u[2 * a] : u[2 * a + 6]), r1 = rnd_of(plus ? u[2 * a + 1] : u[2 * a + 7]);
+        float P[3];
+        P[a] = c[a] + h * s;
+        P[at] = (c[at] - h * s) + (r0 * size) * s;
+        P[ab] = (c[ab] - h * s) + (r1 * size) * s;
+        const float3 R = f3(P[0] - spo.x, P[1] - spo.y, P[2] - spo.z);
+        const float dd = dot3(R, R);
+        const float inv = 1.0f / sqrtf(dd);
+        const float nl = -(s * (comp(R, a) * inv));
+        const float d = fmaxf(1e-5f, dd);
+        const float val = (nl * area) / d;
+        sa[a] = plus ? val : 0.0f;
+        sa[a + 3] = minus ? val : 0.0f;
+    }
+    float total = 0.0f;
+#pragma unroll
+    for (int f = 0; f < 6; f++) total += sa[f];
+    const float r2 = rnd(seed);
+    uint32_t index = 0;
+    float pdf;
+    if (total == 0.0f) {
+        pdf = __int_as_float(0x7fffffff);   // 0/0: NaN -> weight 0
+    } else {
+        // +0 / a positive finite total is +0: skip those divisions
+        const bool fin = total > 0.0f && total < __int_as_float(0x7f800000);
+        pdf = (fin && __float_as_uint(sa[0]) == 0u) ? 0.0f : sa[0] / total;
+        float cdf = pdf;
+        if (cdf < r2) {
+#pragma unroll
+            for (int i = 1; i < 6; i++) {
+                const float p = (fin && __float_as_uint(sa[i]) == 0u) ? 0.0f : sa[i] / total;
+                cdf = cdf + p;
+                index = i;
+                pdf = p;
+                if (cdf >= r2) break;
+            }
+        }
+    }
+    float wgt = 1.0f / pdf;
+    if (isinf(wgt) || isnan(wgt)) wgt = 0.0f;
+    *invp = wgt;
+    *ncode = index;
+    // the two draws of the chosen face
+    uint32_t d0 = u[0], d1 = u[1];
+#pragma unroll
+    for (int i = 1; i < 6; i++)
+        if (index == (uint32_t)i) { d0 = u[2 * i]; d1 = u[2 * i + 1]; }
+    return face_point(g, index, rnd_of(d0), rnd_of(d1));
+}
+
 // ---- sin/cos for the spatial tap offsets (spatialSampling.cl:24-27) -----------------
 // OpenCL leaves cos/sin accuracy to the implementation; the oracle fixes this one:
 // Cody-Waite reduction by pi/2 (three-part constant, exact products for |q| <= 4) and

@@ -172,7 +172,7 @@ __device__ __forceinline__ void albedo_px(const World& w, const Frame& k, uint2*
 }
 
 template <int VARIANT>
-__global__ void __launch_bounds__(128) albedo_kernel(const __grid_constant__ BatchDev bd) {
+__global__ void __launch_bounds__(kMaxTileThreads) albedo_kernel(const __grid_constant__ BatchDev bd) {
     uint32_t tile, round = 0;
     while (next_tile(bd, bd.counters + kCtrAlbedo, &tile, round)) {
         int x, y;
@@ -325,74 +325,6 @@ __global__ void __launch_bounds__(128) shadow_kernel(const __grid_constant__ Bat
             }
         }
     }
-}
-
-// Area-light sample (RandomPointOnVoxel, tools.cl:499-577): one random point per face
-// (2 draws each, all six faces always drawn), faces weighted by their solid angle,
-// CDF pick with one more draw, weight = 1/pdf. Only faces whose normal points toward
-// the shading point get a non-zero solid angle, so only those are normalised.
-__device__ __forceinline__ float3 face_point(float4 g, uint32_t face, float r0, float r1) {
-    // N = normals[face], T = normals[(face / 3) * 3 + (face + 1) % 3], B = ... + (face + 2) % 3
-    const float size = g.w, h = 0.5f * size;
-    const float s = face < 3 ? 1.0f : -1.0f;
-    const uint32_t an = face % 3, at = (an + 1) % 3, ab = (an + 2) % 3;
-    float c[3] = {g.x, g.y, g.z}, p[3];
-    p[an] = c[an] + h * s;                                // center + 0.5*size*N
-    p[at] = (c[at] - h * s) + (r0 * size) * s;            // - 0.5*size*T + r0*size*T
-    p[ab] = (c[ab] - h * s) + (r1 * size) * s;            // - 0.5*size*B + r1*size*B
-    return f3(p[0], p[1], p[2]);
-}
-
-__device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32_t& seed, float* invp, uint32_t* ncode) {
-    const uint32_t seed0 = seed;
-    float sa[6];
-    float total = 0.0f;
-    const float area = g.w * g.w, h = 0.5f * g.w;
-#pragma unroll
-    for (int f = 0; f < 6; f++) {
-        const float r0 = rnd(seed), r1 = rnd(seed);
-        const float s = f < 3 ? 1.0f : -1.0f;
-        const uint32_t an = f % 3;
-        const float pa = comp(f3(g.x, g.y, g.z), an) + h * s;
-        sa[f] = 0.0f;
-        if (s * (comp(spo, an) - pa) > 0.0f) {       // dot(N, -L) > 0 <=> s * R[an] < 0
-            const float3 P = face_point(g, f, r0, r1);
-            const float3 R = sub(P, spo);
-            const float dd = dot3(R, R);
-            const float inv = 1.0f / sqrtf(dd);
-            const float nl = -(s * (comp(R, an) * inv));
-            const float d = fmaxf(1e-5f, dd);
-            sa[f] = (nl * area) / d;
-            total += sa[f];
-        }
-    }
-    const float r2 = rnd(seed);
-    uint32_t index = 0;
-    float pdf;
-    if (total == 0.0f) {
-        pdf = __int_as_float(0x7fffffff);   // 0/0: NaN -> weight 0
-    } else {
-        pdf = sa[0] / total;
-        float cdf = pdf;
-        if (cdf < r2) {
-            for (int i = 1; i < 6; i++) {
-                const float p = sa[i] / total;
-                cdf = cdf + p;
-                index = i;
-                if (cdf >= r2) break;
-            }
-            pdf = sa[index] / total;
-        }
-    }
-    float wgt = 1.0f / pdf;
-    if (isinf(wgt) || isnan(wgt)) wgt = 0.0f;
-    *invp = wgt;
-    *ncode = index;
-    // regenerate the two draws of the chosen face
-    uint32_t s2 = seed0;
-    for (uint32_t i = 0; i < 2 * index; i++) xs32(s2);
-    const float r0 = rnd(s2), r1 = rnd(s2);
-    return face_point(g, index, r0, r1);
 }
 
 // ---- stage 2a: candidates (perPixelInitialSampling, ris.cl:20-82) ---------------------------
@@ -575,7 +507,7 @@ __device__ __forceinline__ void spatial_px(const ViewDev* V, int x, int y) {
 }
 
 template <int VARIANT>
-__global__ void __launch_bounds__(128) spatial_kernel(const __grid_constant__ BatchDev bd) {
+__global__ void __launch_bounds__(kMaxTileThreads) spatial_kernel(const __grid_constant__ BatchDev bd) {
     uint32_t tile, round = 0;
     while (next_tile(bd, bd.counters + kCtrSpatial, &tile, round)) {
         int x, y;
@@ -674,7 +606,7 @@ __device__ __forceinline__ void shade_finish_px(const ViewDev* V, int x, int y, 
 }
 
 template <int VARIANT>
-__global__ void __launch_bounds__(128) shade_finish_kernel(const __grid_constant__ BatchDev bd) {
+__global__ void __launch_bounds__(kMaxTileThreads) shade_finish_kernel(const __grid_constant__ BatchDev bd) {
     uint32_t tile, round = 0;
     while (next_tile(bd, bd.counters + kCtrFinish, &tile, round)) {
         int x, y;
@@ -688,7 +620,7 @@ __global__ void __launch_bounds__(128) shade_finish_kernel(const __grid_constant
 
 // stage 5 on its own
 template <int VARIANT>
-__global__ void __launch_bounds__(128) accumulate_kernel(const __grid_constant__ BatchDev bd) {
+__global__ void __launch_bounds__(kMaxTileThreads) accumulate_kernel(const __grid_constant__ BatchDev bd) {
     uint32_t tile, round = 0;
     while (next_tile(bd, bd.counters + kCtrAccum, &tile, round)) {
         int x, y;

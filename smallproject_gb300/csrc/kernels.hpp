@@ -60,6 +60,7 @@ struct ViewDev {
 // views in device memory. Hit-list entries are (view << 27 | pixel), at most 16 views
 // of at most 2^27 pixels each.
 constexpr uint32_t kMaxBatchViews = 16;
+constexpr int kMaxTileThreads = 256;      // threads of a pixel-stage block (tile_x * tile_y)
 struct BatchDev {
     ViewDev one;
     const ViewDev* views = nullptr;       // device table when nviews > 1

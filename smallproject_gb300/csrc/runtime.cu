@@ -254,7 +254,7 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     VXR_CHECK_ARG(d->light_model == VXR_LIGHTS_AREA || d->light_model == VXR_LIGHTS_POINT,
                   "vxr_view_create: unknown light model");
     VXR_CHECK_ARG(d->spatial_radius >= 1, "vxr_view_create: spatial_radius must be >= 1");
-    VXR_CHECK_ARG(d->tile_x * d->tile_y <= 1024, "vxr_view_create: tile larger than 1024 threads");
+    VXR_CHECK_ARG(d->tile_x <= 256 && d->tile_y <= 256 && d->tile_x * d->tile_y <= 256, "vxr_view_create: tile larger than 256 threads");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(VXR_E_NODEVICE, "no CUDA device visible");
     vxr_view* v = new (std::nothrow) vxr_view();
@@ -341,7 +341,7 @@ int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d) {
     VXR_CHECK_ARG(d->width == v->desc.width && d->height == v->desc.height && d->light_model == v->desc.light_model,
                   "vxr_view_set_params: resolution and light model are fixed at creation");
     VXR_CHECK_ARG(d->spatial_radius >= 1, "vxr_view_set_params: spatial_radius must be >= 1");
-    VXR_CHECK_ARG(d->tile_x * d->tile_y <= 1024, "vxr_view_set_params: tile larger than 1024 threads");
+    VXR_CHECK_ARG(d->tile_x <= 256 && d->tile_y <= 256 && d->tile_x * d->tile_y <= 256, "vxr_view_set_params: tile larger than 256 threads");
     const uint32_t seed = v->desc.rng_seed;
     v->desc = *d;
     v->desc.rng_seed = seed;
@@ -665,8 +665,8 @@ namespace vxr {
 int check_tuning(const vxr_tuning* t, const char* fn) {
     if (!t) return set_error(VXR_E_INVALID, std::string(fn) + ": null tuning");
     const uint32_t n = t->tile_x * t->tile_y;
-    if (t->tile_x < 1 || t->tile_y < 1 || t->tile_x > 1024 || t->tile_y > 1024 || n > 1024 || n % 32 != 0)
-        return set_error(VXR_E_INVALID, std::string(fn) + ": tile must hold a multiple of 32 threads, at most 1024");
+    if (t->tile_x < 1 || t->tile_y < 1 || t->tile_x > 256 || t->tile_y > 256 || n > 256 || n % 32 != 0)
+        return set_error(VXR_E_INVALID, std::string(fn) + ": tile must hold a multiple of 32 threads, at most 256");
     if (t->persistent > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": persistent must be 0 or 1");
     if (t->shadow_refill < 1 || t->shadow_refill > 32)
         return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_refill out of range [1, 32]");

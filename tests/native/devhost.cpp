@@ -24,7 +24,10 @@ static inline int __float2int_rz(float f) {
 static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
 static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 static inline float __uint2float_rn(unsigned u) { return (float)u; }
+static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 template <class T> static inline T __ldg(const T* p) { return *p; }
+using std::isinf;
+using std::isnan;
 using std::max;
 using std::min;
 #ifndef __noinline__
@@ -40,6 +43,75 @@ static World make_world(const uint32_t* grid, const uint8_t* uber, const uint32_
     w.grid = grid; w.uber = uber; w.bricks = bricks; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
     return w;
 }
+
+// The per-face form of the area-light sample (RandomPointOnVoxel, tools.cl:499-577) that
+// the GPU path used before its per-axis form, kept here as a second restatement to
+// check the per-axis form against, bit for bit (the GPU parity tests pin both to the
+// oracle through whole frames).
+__device__ __forceinline__ float3 face_point_perface(float4 g, uint32_t face, float r0, float r1) {
+    // N = normals[face], T = normals[(face / 3) * 3 + (face + 1) % 3], B = ... + (face + 2) % 3
+    const float size = g.w, h = 0.5f * size;
+    const float s = face < 3 ? 1.0f : -1.0f;
+    const uint32_t an = face % 3, at = (an + 1) % 3, ab = (an + 2) % 3;
+    float c[3] = {g.x, g.y, g.z}, p[3];
+    p[an] = c[an] + h * s;                                // center + 0.5*size*N
+    p[at] = (c[at] - h * s) + (r0 * size) * s;            // - 0.5*size*T + r0*size*T
+    p[ab] = (c[ab] - h * s) + (r1 * size) * s;            // - 0.5*size*B + r1*size*B
+    return f3(p[0], p[1], p[2]);
+}
+
+__device__ __forceinline__ float3 sample_area_light_perface(float4 g, float3 spo, uint32_t& seed, float* invp, uint32_t* ncode) {
+    const uint32_t seed0 = seed;
+    float sa[6];
+    float total = 0.0f;
+    const float area = g.w * g.w, h = 0.5f * g.w;
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+        const float r0 = rnd(seed), r1 = rnd(seed);
+        const float s = f < 3 ? 1.0f : -1.0f;
+        const uint32_t an = f % 3;
+        const float pa = comp(f3(g.x, g.y, g.z), an) + h * s;
+        sa[f] = 0.0f;
+        if (s * (comp(spo, an) - pa) > 0.0f) {       // dot(N, -L) > 0 <=> s * R[an] < 0
+            const float3 P = face_point_perface(g, f, r0, r1);
+            const float3 R = sub(P, spo);
+            const float dd = dot3(R, R);
+            const float inv = 1.0f / sqrtf(dd);
+            const float nl = -(s * (comp(R, an) * inv));
+            const float d = fmaxf(1e-5f, dd);
+            sa[f] = (nl * area) / d;
+            total += sa[f];
+        }
+    }
+    const float r2 = rnd(seed);
+    uint32_t index = 0;
+    float pdf;
+    if (total == 0.0f) {
+        pdf = __int_as_float(0x7fffffff);   // 0/0: NaN -> weight 0
+    } else {
+        pdf = sa[0] / total;
+        float cdf = pdf;
+        if (cdf < r2) {
+            for (int i = 1; i < 6; i++) {
+                const float p = sa[i] / total;
+                cdf = cdf + p;
+                index = i;
+                if (cdf >= r2) break;
+            }
+            pdf = sa[index] / total;
+        }
+    }
+    float wgt = 1.0f / pdf;
+    if (isinf(wgt) || isnan(wgt)) wgt = 0.0f;
+    *invp = wgt;
+    *ncode = index;
+    // regenerate the two draws of the chosen face
+    uint32_t s2 = seed0;
+    for (uint32_t i = 0; i < 2 * index; i++) xs32(s2);
+    const float r0 = rnd(s2), r1 = rnd(s2);
+    return face_point_perface(g, index, r0, r1);
+}
+
 
 extern "C" {
 
@@ -81,5 +153,17 @@ uint32_t dh_walk(const uint32_t* grid, const uint8_t* uber, const uint32_t* bric
 }
 
 void dh_sincos(float a, float* s, float* c) { sincos_vx(a, s, c); }
+
+// area-light sample, per-axis form (device.cuh) and per-face form (above); out = point xyz, inv, face, seed
+void dh_area_sample(int which, const float* lg, const float* spo, uint32_t seed, float* out) {
+    const float4 g = make_float4(lg[0], lg[1], lg[2], lg[3]);
+    const float3 p = f3(spo[0], spo[1], spo[2]);
+    float inv = 0.0f;
+    uint32_t nc = 0;
+    const float3 q = which ? sample_area_light_perface(g, p, seed, &inv, &nc) : sample_area_light(g, p, seed, &inv, &nc);
+    out[0] = q.x; out[1] = q.y; out[2] = q.z; out[3] = inv;
+    std::memcpy(out + 4, &nc, 4);
+    std::memcpy(out + 5, &seed, 4);
+}
 
 }  // extern "C"

@@ -32,6 +32,7 @@ def dh():
     lib.dh_walk.restype = C.c_uint32
     lib.dh_walk.argtypes = [P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.dh_sincos.argtypes = [C.c_float, F, F]
+    lib.dh_area_sample.argtypes = [C.c_int, F, F, C.c_uint32, F]
     return lib
 
 
@@ -96,3 +97,38 @@ def test_device_sincos_matches_oracle(dh):
         dh.dh_sincos(float(x), C.byref(sn), C.byref(cs))
         osn, ocs = ob.sincos(float(x))
         assert np.float32(sn.value) == np.float32(osn) and np.float32(cs.value) == np.float32(ocs), x
+
+
+def test_area_sample_per_axis_matches_per_face(dh):
+    """The per-axis area-light sample (one facing face per axis) against the per-face
+    form, bit for bit: point, weight, face and the advanced RNG state. Shading points
+    far away, near the cube, inside its slabs, on its face planes, and inside it."""
+    rng = np.random.default_rng(11)
+    n = 60000
+    out_a = np.zeros(6, np.float32)
+    out_b = np.zeros(6, np.float32)
+    pa = out_a.ctypes.data_as(C.POINTER(C.c_float))
+    pb = out_b.ctypes.data_as(C.POINTER(C.c_float))
+    for i in range(n):
+        size = float(rng.choice([1.0, 8.0]))
+        c = np.floor(rng.uniform(0, 1000, 3)).astype(np.float32) + np.float32(0.5 * size)
+        mode = i % 5
+        if mode == 0:
+            sp = rng.uniform(0, 1024, 3)
+        elif mode == 1:
+            sp = c + rng.normal(0, 3 * size, 3)
+        elif mode == 2:      # inside one or two slabs
+            sp = c + rng.uniform(-0.5 * size, 0.5 * size, 3) * (rng.random(3) < 0.5) + rng.normal(0, 5, 3) * (rng.random(3) < 0.5)
+        elif mode == 3:      # exactly on a face plane
+            sp = c + rng.normal(0, 4, 3)
+            ax = rng.integers(3)
+            sp[ax] = c[ax] + rng.choice([-0.5, 0.5]) * size
+        else:                # inside the cube
+            sp = c + rng.uniform(-0.5 * size, 0.5 * size, 3)
+        sp = sp.astype(np.float32)
+        lg = (C.c_float * 4)(float(c[0]), float(c[1]), float(c[2]), size)
+        spo = _f3(sp)
+        seed = int(rng.integers(1, 2 ** 32))
+        dh.dh_area_sample(0, lg, spo, seed, pa)
+        dh.dh_area_sample(1, lg, spo, seed, pb)
+        assert out_a.view(np.uint32).tolist() == out_b.view(np.uint32).tolist(), (i, c, size, sp, seed, out_a, out_b)

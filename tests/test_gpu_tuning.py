@@ -51,7 +51,7 @@ def test_tuning_does_not_change_results(lib, cuda_device, scene0, model):
 def test_tuning_rejects_bad_values(lib, cuda_device, scene0):
     v = lib.View(scene0[0], lib.view_desc(32, 32))
     try:
-        for bad in (dict(tile_x=5, tile_y=5), dict(tile_x=64, tile_y=32), dict(persistent=2), dict(shadow_refill=0),
+        for bad in (dict(tile_x=5, tile_y=5), dict(tile_x=64, tile_y=32), dict(tile_x=32, tile_y=16), dict(persistent=2), dict(shadow_refill=0),
                     dict(shadow_refill=33), dict(shadow_burst=0), dict(shadow_burst=65), dict(list_blocks_per_sm=0)):
             with pytest.raises(lib.VxrError):
                 v.set_tuning(lib.tuning(**bad))
