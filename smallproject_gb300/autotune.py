@@ -3,7 +3,7 @@ work-group size is fixed, template/template.cpp:1700-1754).
 
 Tunes the launch parameters of vxr_tuning - pixel-stage tile shape, persistent tile
 queue on/off, shadow-tracer refill threshold and burst length, blocks per SM of the
-hit-list kernels - per configuration, by timing whole frames on the GPU, and caches the
+hit-list kernels, register cap of the shadow tracer and candidate kernels - per configuration, by timing whole frames on the GPU, and caches the
 winner in a JSON file keyed by device, resolution, light model, candidate count and the
 world's size class. Every setting renders the same bits (the kernels' per-pixel
 arithmetic does not depend on them), so tuning changes speed only.
@@ -29,6 +29,7 @@ SPACE = [
     ("shadow_refill", [4, 8, 16, 24]),
     ("shadow_burst", [2, 4, 8, 16]),
     ("list_blocks_per_sm", [4, 8, 16, 32]),
+    ("occupancy", [0, 1]),
 ]
 
 
@@ -60,14 +61,14 @@ def config_key(world, desc):
 def _to_tuning(d):
     t = _v.tuning()
     t.tile_x, t.tile_y = d["tile"]
-    for k in ("persistent", "shadow_refill", "shadow_burst", "list_blocks_per_sm"):
+    for k in ("persistent", "shadow_refill", "shadow_burst", "list_blocks_per_sm", "occupancy"):
         setattr(t, k, d[k])
     return t
 
 
 def _from_tuning(t):
     return {"tile": (t.tile_x, t.tile_y), "persistent": t.persistent, "shadow_refill": t.shadow_refill,
-            "shadow_burst": t.shadow_burst, "list_blocks_per_sm": t.list_blocks_per_sm}
+            "shadow_burst": t.shadow_burst, "list_blocks_per_sm": t.list_blocks_per_sm, "occupancy": t.occupancy}
 
 
 def time_view(view, t, cams, frames, start=0):

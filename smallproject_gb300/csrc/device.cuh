@@ -340,32 +340,34 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
 // Every float op, the step budget accounting and the exit cascade (brick -> grid step
 // -> uber step) follow trace<MODE> exactly; the oracle checks the two for equality.
 struct Walker {
-    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;   // per-axis cell step in t: |r| (= sign(v) * r)
-    float t, tmx, tmy, tmz;        // current level
-    float umx, umy, umz;           // saved uber-level crossings (while below the uber level)
-    float gmx, gmy, gmz;           // saved grid-level crossings (while in a brick)
-    int cx, cy, cz;                // current cell: uber / grid (absolute) or brick-local voxel
-    int ux, uy, uz, gx, gy, gz;    // saved uber cell, saved grid cell
+    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;
+    float t, tmx, tmy, tmz;        // crossings at the current level
+    float umx, umy, umz;           // saved uber-level crossings (below the uber level)
+    float gmx, gmy, gmz;           // saved grid-level crossings (inside a brick)
+    int cx, cy, cz;                // current cell relative to its parent cell (uber: absolute)
+    int ux, uy, uz;                // saved uber cell (absolute)
+    int gx, gy, gz;                // saved grid cell relative to its uber cell
+    int sx, sy, sz;                // axis steps (+-1)
+    uint32_t lin, ulin, glin;      // element index of the current / saved uber / saved grid cell
+    int dly, dlz;                  // lin step for a y / z cell step at the current level
+    int mask;                      // ~(cells per parent cell - 1) at the current level
     int steps, level, bi;
-    uint32_t o, brick, last, dirbits;   // o: content of the current cell; dirbits: bit a = positive on axis a
+    uint32_t o, last;
     float dist;                    // result
     uint32_t side, voxel;
-    __device__ __forceinline__ int sx() const { return (dirbits & 1u) ? 1 : -1; }
-    __device__ __forceinline__ int sy() const { return (dirbits & 2u) ? 1 : -1; }
-    __device__ __forceinline__ int sz() const { return (dirbits & 4u) ? 1 : -1; }
-    __device__ __forceinline__ int ox() const { return (int)(dirbits & 1u); }
-    __device__ __forceinline__ int oy() const { return (int)((dirbits >> 1) & 1u); }
-    __device__ __forceinline__ int oz() const { return (int)((dirbits >> 2) & 1u); }
 };
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
 
-// content of cell (cx, cy, cz) at the walker's level: uber occupancy byte, grid cell, or
-// brick voxel
+__device__ __forceinline__ void walk_level_consts(Walker& k) {
+    // uber x + z*32 + y*1024, grid x + z*128 + y*16384, brick x + y*8 + z*64
+    k.dly = k.sy * (k.level == 0 ? 1024 : (k.level == 1 ? 16384 : 8));
+    k.dlz = k.sz * (k.level == 0 ? 32 : (k.level == 1 ? 128 : 64));
+    k.mask = k.level == 0 ? ~31 : (k.level == 1 ? ~3 : ~7);
+}
+
 __device__ __forceinline__ uint32_t walk_load(const Walker& k, const World& w) {
-    if (k.level == 0) return __ldg(w.uber + k.cx + k.cz * 32 + k.cy * 1024);
-    const uint32_t* base = k.level == 1 ? w.grid : w.bricks + (size_t)k.brick * 512u;
-    const int sy = k.level == 1 ? 16384 : 8, sz = k.level == 1 ? 128 : 64;
-    return __ldg(base + k.cx + k.cz * sz + k.cy * sy);
+    if (k.level == 0) return __ldg(w.uber + k.lin);
+    return __ldg((k.level == 1 ? w.grid : w.bricks) + k.lin);
 }
 
 // TraceOpaqueRay prologue (trace.cl:219-243); returns WALK_MISS when the ray misses the map
@@ -376,7 +378,9 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
     if (fabsf(vz) < 1e-8f) vz = vz < 0.0f ? -1e-8f : 1e-8f;
     k.vx = vx; k.vy = vy; k.vz = vz;
     k.rx = 1.0f / vx; k.ry = 1.0f / vy; k.rz = 1.0f / vz;
-    k.dirbits = (vx > 0.0f ? 1u : 0u) | (vy > 0.0f ? 2u : 0u) | (vz > 0.0f ? 4u : 0u);
+    k.sx = vx > 0.0f ? 1 : -1;
+    k.sy = vy > 0.0f ? 1 : -1;
+    k.sz = vz > 0.0f ? 1 : -1;
     k.to = 0.0f;
     k.last = 0;
     if (ax < 0.0f || ay < 0.0f || az < 0.0f || ax > 1024.0f || ay > 1024.0f || az > 1024.0f) {
@@ -401,67 +405,77 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
     k.cx = (int)min(f2u(ax) >> 5, 31u);
     k.cy = (int)min(f2u(ay) >> 5, 31u);
     k.cz = (int)min(f2u(az) >> 5, 31u);
-    k.tmx = ((float)(uint32_t)(k.cx + k.ox()) - ax * 0.03125f) * k.rx;
-    k.tmy = ((float)(uint32_t)(k.cy + k.oy()) - ay * 0.03125f) * k.ry;
-    k.tmz = ((float)(uint32_t)(k.cz + k.oz()) - az * 0.03125f) * k.rz;
+    const uint32_t ox = k.sx > 0 ? 1u : 0u, oy = k.sy > 0 ? 1u : 0u, oz = k.sz > 0 ? 1u : 0u;
+    k.tmx = ((float)((uint32_t)k.cx + ox) - ax * 0.03125f) * k.rx;
+    k.tmy = ((float)((uint32_t)k.cy + oy) - ay * 0.03125f) * k.ry;
+    k.tmz = ((float)((uint32_t)k.cz + oz) - az * 0.03125f) * k.rz;
     k.t = 0.0f;
     k.steps = steps;
     k.level = 0;
+    k.lin = (uint32_t)(k.cx + k.cz * 32 + k.cy * 1024);
+    walk_level_consts(k);
     k.o = walk_load(k, w);
     return WALK_CONTINUE;
 }
 
-// One cell visit. The three levels of the reference's DDA (uber 32^3 cells of 4^3 grid
-// cells, grid 128^3 cells, bricks of 8^3 voxels; trace.cl:59-117, 219-285) run the same
-// code with per-level constants, so lanes of a warp at different levels stay converged
-// through the cell step, the only part every visit executes:
+// One cell visit of the reference's three-level DDA (trace.cl:59-117, 219-285: uber 32^3
+// cells of 4^3 grid cells, grid 128^3 cells, bricks of 8^3 voxels). Every level runs the
+// same cell step on coordinates relative to the parent cell (bounds = one mask test) and
+// an element index advanced with the coordinates, so lanes of a warp at different levels
+// stay converged through it; only the examine and the rare level changes differ.
 //   examine  uber: budget -4, occupied -> descend; grid: budget -1, solid -> hit test,
 //            brick -> descend; brick voxel: hit test (bricks are free of budget)
-//   descend  entry cell of the child level from the ray point at the current t
 //   advance  t = min crossing, every tied axis steps, `last` = the highest tied axis;
 //            leaving the parent cell (or 24 brick steps) ascends and advances there
-// Arithmetic per level is the reference's: 1.0f and 0-offset factors stand in where a
-// level has no scale, and multiplying by 1.0f or adding 0 is exact.
+// Per level the float operations are the reference's (factors of 1 and offsets of 0 are
+// exact where a level has no scale).
 __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
     const int L = k.level;
-    const int cost = L == 0 ? 4 : (L == 1 ? 1 : 0);
-    k.steps -= cost;
-    if (cost != 0 && k.steps <= 0) return WALK_MISS;   // budget (a grid step that empties it always misses)
     const uint32_t o = k.o;
+    if (L != 2) {
+        k.steps -= L == 0 ? 4 : 1;
+        if (k.steps <= 0) return WALK_MISS;   // a grid step that empties the budget always misses
+    }
     const uint32_t v = L == 1 ? (o >> 1) : o;
-    if ((L == 2 || (L == 1 && (o & 1u) == 0u)) && ((v & 0xf000u) >> 12) == 15u) {
+    if (((v & 0xf000u) == 0xf000u) && !(L == 1 && (o & 1u))) {   // uber content is 0/1: never a hit
         k.dist = (L == 1 ? k.t * 8.0f : k.t) + k.to;
         k.side = k.last;
         k.voxel = v;
         return WALK_HIT;
     }
-    if ((L == 0 && o != 0u) || (L == 1 && (o & 1u))) {
+    if (L != 2 && (o & 1u)) {
         // descend: uber -> grid (trace.cl:247-255), grid -> brick (trace.cl:65-74)
         const bool toGrid = L == 0;
         const float as = toGrid ? 0.125f : 1.0f;
         const uint32_t span = toGrid ? 4u : 8u;
+        uint32_t bx, by, bz;
         if (toGrid) {
             k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
             k.ux = k.cx; k.uy = k.cy; k.uz = k.cz;
+            k.ulin = k.lin;
+            bx = (uint32_t)k.cx * 4u; by = (uint32_t)k.cy * 4u; bz = (uint32_t)k.cz * 4u;
         } else {
             k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
             k.gx = k.cx; k.gy = k.cy; k.gz = k.cz;
-            k.brick = o >> 1;
+            k.glin = k.lin;
+            bx = ((uint32_t)k.ux * 4u + (uint32_t)k.cx) * 8u;
+            by = ((uint32_t)k.uy * 4u + (uint32_t)k.cy) * 8u;
+            bz = ((uint32_t)k.uz * 4u + (uint32_t)k.cz) * 8u;
             k.bi = 0;
         }
         k.t *= toGrid ? 4.0f : 8.0f;
         const uint32_t px = f2u(as * k.ax + k.vx * k.t), py = f2u(as * k.ay + k.vy * k.t), pz = f2u(as * k.az + k.vz * k.t);
-        const uint32_t bx = (uint32_t)k.cx * span, by = (uint32_t)k.cy * span, bz = (uint32_t)k.cz * span;
         const uint32_t qx = min(max(px, bx), bx + span - 1u), qy = min(max(py, by), by + span - 1u),
                        qz = min(max(pz, bz), bz + span - 1u);
-        k.tmx = ((float)(qx + (uint32_t)k.ox()) - k.ax * as) * k.rx;
-        k.tmy = ((float)(qy + (uint32_t)k.oy()) - k.ay * as) * k.ry;
-        k.tmz = ((float)(qz + (uint32_t)k.oz()) - k.az * as) * k.rz;
-        const uint32_t lo = toGrid ? 0u : span;   // brick coordinates are local
-        k.cx = (int)(qx - (lo ? bx : 0u));
-        k.cy = (int)(qy - (lo ? by : 0u));
-        k.cz = (int)(qz - (lo ? bz : 0u));
+        k.tmx = ((float)(qx + (k.sx > 0 ? 1u : 0u)) - k.ax * as) * k.rx;
+        k.tmy = ((float)(qy + (k.sy > 0 ? 1u : 0u)) - k.ay * as) * k.ry;
+        k.tmz = ((float)(qz + (k.sz > 0 ? 1u : 0u)) - k.az * as) * k.rz;
+        k.cx = (int)(qx - bx);
+        k.cy = (int)(qy - by);
+        k.cz = (int)(qz - bz);
+        k.lin = toGrid ? qx + qz * 128u + qy * 16384u : (o >> 1) * 512u + (uint32_t)(k.cx + k.cy * 8 + k.cz * 64);
         k.level = L + 1;
+        walk_level_consts(k);
         k.o = walk_load(k, w);
         return WALK_CONTINUE;
     }
@@ -469,24 +483,24 @@ __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
     for (;;) {
         k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
         k.last = 0;
-        if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.cx += k.sx(); }
-        if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.cy += k.sy(); k.last = 1; }
-        if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.cz += k.sz(); k.last = 2; }
-        const int lv = k.level;
-        const int lx = lv == 1 ? 4 * k.ux : 0, ly = lv == 1 ? 4 * k.uy : 0, lz = lv == 1 ? 4 * k.uz : 0;
-        const int mask = lv == 0 ? ~31 : (lv == 1 ? ~3 : ~7);
-        bool out = (((k.cx - lx) | (k.cy - ly) | (k.cz - lz)) & mask) != 0;
-        if (!out && lv == 2) out = ++k.bi == 24;
+        if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.cx += k.sx; k.lin += (uint32_t)k.sx; }
+        if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.cy += k.sy; k.lin += (uint32_t)k.dly; k.last = 1; }
+        if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.cz += k.sz; k.lin += (uint32_t)k.dlz; k.last = 2; }
+        bool out = ((k.cx | k.cy | k.cz) & k.mask) != 0;
+        if (k.level == 2 && !out) out = ++k.bi == 24;
         if (!out) break;
-        if (lv == 0) return WALK_MISS;   // left the map
-        if (lv == 2) {
+        if (k.level == 0) return WALK_MISS;   // left the map
+        if (k.level == 2) {
             k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
             k.cx = k.gx; k.cy = k.gy; k.cz = k.gz;
+            k.lin = k.glin;
         } else {
             k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
             k.cx = k.ux; k.cy = k.uy; k.cz = k.uz;
+            k.lin = k.ulin;
         }
-        k.level = lv - 1;
+        k.level -= 1;
+        walk_level_consts(k);
     }
     k.o = walk_load(k, w);
     return WALK_CONTINUE;

@@ -271,15 +271,18 @@ __device__ __forceinline__ void shadow_finish(const World& w, int st, const Walk
     if (!inside) plane[(size_t)pix * 4u + 2u] = 0u;
 }
 
-template <int VARIANT>
-__global__ void __launch_bounds__(128) shadow_kernel(const __grid_constant__ BatchDev bd, int countIdx, int fetchIdx,
+// MINB > 0 caps registers so that MINB blocks of 128 threads fit on an SM (more warps to
+// hide L2 latency, at the price of a few spills); chosen by the launch tuning.
+template <int VARIANT, int MINB>
+__global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant__ BatchDev bd, int countIdx, int fetchIdx,
                                                      int planeSel) {
     const int refill = bd.refill, burst = bd.burst;
     const uint32_t n = bd.counters[countIdx];
     uint32_t* fetch = bd.counters + fetchIdx;
     const int lane = threadIdx.x & 31;
     Walker wk;
-    World w;
+    World wt;   // a table batch: the world of this lane's ray; one view: the parameter's
+    const World& w = VARIANT < 2 ? bd.one.w : wt;
     uint32_t* plane = nullptr;
     bool active = false, exhausted = false;
     float3 o = f3(0.0f, 0.0f, 0.0f), L = f3(0.0f, 0.0f, 0.0f);
@@ -301,7 +304,7 @@ __global__ void __launch_bounds__(128) shadow_kernel(const __grid_constant__ Bat
                     const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
                     pix = pix_of<VARIANT>(e);
                     li = __float_as_uint(b.w);
-                    w = V->w;
+                    if (VARIANT == 2) wt = V->w;
                     plane = reinterpret_cast<uint32_t*>(planeSel ? V->b.hA : V->b.cA);
                     const int st = walk_init(wk, w, o.x, o.y, o.z, L.x, L.y, L.z, 128);
                     if (st == WALK_CONTINUE) active = true;
@@ -390,8 +393,8 @@ __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, u
     V->b.seed[i] = seed;
 }
 
-template <int VARIANT, bool LEARNED>
-__global__ void __launch_bounds__(128) ris_kernel(const __grid_constant__ BatchDev bd) {
+template <int VARIANT, bool LEARNED, int MINB>
+__global__ void __launch_bounds__(128, MINB) ris_kernel(const __grid_constant__ BatchDev bd) {
     const uint32_t nh = bd.counters[kCtrHits];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
         const uint32_t e = bd.hits[j];
@@ -686,6 +689,7 @@ void apply_tuning(BatchDev& bd, const Tuning& tu) {
     bd.refill = tu.refill;
     bd.burst = tu.burst;
     bd.listPerSm = tu.listPerSm;
+    bd.occupancy = tu.occupancy;
 }
 
 BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, const Tuning& tu) {
@@ -722,11 +726,21 @@ void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {
     else launch_tiles(dev::albedo_kernel<0>, bd, kCtrAlbedo, s);
 }
 
+template <int VARIANT, int MINB>
+static void launch_shadow_k(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
+    const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT, MINB>, 128);
+    const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 127) / 128));
+    dev::shadow_kernel<VARIANT, MINB><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel);
+}
 template <int VARIANT>
 static void launch_shadow(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
-    const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT>, 128);
-    const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 127) / 128));
-    dev::shadow_kernel<VARIANT><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel);
+    if (bd.occupancy) launch_shadow_k<VARIANT, 8>(bd, countIdx, planeSel, s);
+    else launch_shadow_k<VARIANT, 0>(bd, countIdx, planeSel, s);
+}
+template <int VARIANT, bool LEARNED>
+static void launch_ris(const BatchDev& bd, unsigned nb, cudaStream_t s) {
+    if (bd.occupancy) dev::ris_kernel<VARIANT, LEARNED, 7><<<nb, 128, 0, s>>>(bd);
+    else dev::ris_kernel<VARIANT, LEARNED, 0><<<nb, 128, 0, s>>>(bd);
 }
 
 template <int VARIANT>
@@ -754,11 +768,11 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
             ia.samples = nullptr;
             ia.probs = nullptr;
             if (bd.one.k.ncand > 0) prop::launch_infer(ia, (uint32_t)n, s);
-            dev::ris_kernel<VARIANT, true><<<nb, 128, 0, s>>>(lb);
+            launch_ris<VARIANT, true>(lb, nb, s);
             learnedDone = true;
         }
     }
-    if (!learnedDone) dev::ris_kernel<VARIANT, false><<<nb, 128, 0, s>>>(bd);
+    if (!learnedDone) launch_ris<VARIANT, false>(bd, nb, s);
     launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ1, 0, s);
     // a single view without temporal reuse this frame skips the launch (a table checks per view)
     if (VARIANT == 2 || (bd.one.k.restirtemporalframe > 0 && bd.one.k.temporal))

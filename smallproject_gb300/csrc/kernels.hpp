@@ -72,6 +72,7 @@ struct BatchDev {
     int refill = 8;                       // shadow tracer: idle lanes of a warp that trigger a refill
     int burst = 4;                        // shadow tracer: cell visits per lane between refill checks
     int listPerSm = 16;                   // blocks per SM of the hit-list kernels
+    int occupancy = 0;                    // 1: register-capped shadow / RIS kernels (more warps per SM)
     int fuse = 0;                         // shading also accumulates
     uint32_t* hits = nullptr;             // hit list over all views
     float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(entry))
@@ -86,6 +87,7 @@ struct Tuning {
     int refill = 8;
     int burst = 4;
     int listPerSm = 16;
+    int occupancy = 0;
 };
 
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s);

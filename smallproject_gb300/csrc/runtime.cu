@@ -674,6 +674,7 @@ int check_tuning(const vxr_tuning* t, const char* fn) {
         return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_burst out of range [1, 64]");
     if (t->list_blocks_per_sm < 1 || t->list_blocks_per_sm > 64)
         return set_error(VXR_E_INVALID, std::string(fn) + ": list_blocks_per_sm out of range [1, 64]");
+    if (t->occupancy > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": occupancy must be 0 or 1");
     return VXR_OK;
 }
 Tuning to_tuning(const vxr_tuning& t) {
@@ -684,6 +685,7 @@ Tuning to_tuning(const vxr_tuning& t) {
     u.refill = (int)t.shadow_refill;
     u.burst = (int)t.shadow_burst;
     u.listPerSm = (int)t.list_blocks_per_sm;
+    u.occupancy = (int)t.occupancy;
     return u;
 }
 }  // namespace vxr
@@ -697,6 +699,7 @@ extern "C" int vxr_default_tuning(vxr_tuning* t) {
     t->shadow_refill = (uint32_t)u.refill;
     t->shadow_burst = (uint32_t)u.burst;
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
+    t->occupancy = (uint32_t)u.occupancy;
     return VXR_OK;
 }
 
@@ -733,6 +736,7 @@ extern "C" int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t) {
     t->shadow_refill = (uint32_t)u.refill;
     t->shadow_burst = (uint32_t)u.burst;
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
+    t->occupancy = (uint32_t)u.occupancy;
     return VXR_OK;
 }
 
