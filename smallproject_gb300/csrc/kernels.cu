@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
 // sumW, pHat, M) and a shadow-ray request for the selected sample when sumW > 0 (when
 // sumW == 0 the discard of ris.cl:79-80 changes nothing).
 // LEARNED: the light index comes from the learned proposal instead of
-// GenerateLightCandidate: cluster c with probability q(c) (drawn by the inference kernel),
-// then a member of c uniformly; the source pdf p = q(c) / |c| replaces 1 / N.
+// GenerateLightCandidate (drawn by the inference kernel: cluster c with probability q(c),
+// then a member of c uniformly); its source pdf p = q(c) / |c| replaces 1 / N.
 template <bool POINT, bool LEARNED>
 __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, uint32_t e, uint32_t i, uint32_t j) {
     const World w = V->w;
@@ -360,10 +360,8 @@ __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, u
         float p = puni;
         if (LEARNED) {
             const uint2 cq = __ldg(V->ll.cand + (size_t)j * prop::kMaxCand + c);
-            const uint32_t off = __ldg(V->ll.clOff + cq.x), sz = __ldg(V->ll.clOff + cq.x + 1) - off;
-            const uint32_t mi = min((uint32_t)f2i(rnd(seed) * (float)sz), sz - 1u);
-            li = (int)__ldg(V->ll.clMembers + off + mi);
-            p = __uint_as_float(cq.y) / (float)sz;
+            li = (int)cq.x;
+            p = __uint_as_float(cq.y);
         } else {
             // GenerateLightCandidate (tools.cl:593-598)
             li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
@@ -756,8 +754,6 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
         if (learned) {
             BatchDev lb = bd;
             lb.one.ll.cand = learned->cand;
-            lb.one.ll.clOff = learned->clOff;
-            lb.one.ll.clMembers = learned->clMembers;
             prop::InferArgs ia = learned->infer;
             ia.k = bd.one.k;
             ia.vd = bd.one.b.vd[bd.one.cur];
@@ -765,6 +761,8 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
             ia.count = bd.counters + kCtrHits;
             ia.ncand = bd.one.k.ncand;
             ia.cand = learned->cand;
+            ia.clOff = learned->clOff;
+            ia.clMembers = learned->clMembers;
             ia.samples = nullptr;
             ia.probs = nullptr;
             if (bd.one.k.ncand > 0) prop::launch_infer(ia, (uint32_t)n, s);

@@ -37,11 +37,9 @@ enum : int {
     kCounters = 16
 };
 
-// learned-proposal lists read by the candidate loop (all null = uniform source pdf)
+// learned-proposal candidates read by the candidate loop (null = uniform source pdf)
 struct LearnedLists {
-    const uint2* cand = nullptr;          // [hit][kMaxCand] (cluster, bits(q(cluster)))
-    const uint32_t* clOff = nullptr;      // cluster CSR
-    const uint32_t* clMembers = nullptr;
+    const uint2* cand = nullptr;          // [hit][kMaxCand] (emitter, bits(p_src))
 };
 
 // Everything a kernel needs about one view of a batch.

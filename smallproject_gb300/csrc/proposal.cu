@@ -4,9 +4,10 @@
 // hash-grid encoding is built in shared memory, the MLP runs on the tensor cores with
 // BF16 mma.sync.m16n8k16 (FP32 accumulation, hidden layers kept in registers: the
 // accumulator fragment of one layer is the A fragment of the next), the K logits land
-// in shared memory as FP16, and every lane draws its pixel's candidate clusters from
-// q = (1 - eps) softmax + eps / K with a two-level (16 groups) inverse CDF. Output per
-// pixel: kMaxCand (cluster, q(cluster)) pairs that the candidate kernel consumes.
+// in shared memory as FP16, and every lane draws its pixel's candidates: a cluster from
+// q = (1 - eps) softmax + eps / K with a two-level (16 groups) inverse CDF, then one of
+// its emitters uniformly. Output per pixel: kMaxCand (emitter, p_src = q(c) / |c|) pairs
+// that the candidate kernel consumes.
 //
 // Training (FP32 CUDA cores): batch gather from the reservoirs, encoding, a tiled
 // strided GEMM with fused epilogues for every forward / backward product, softmax
@@ -262,22 +263,49 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
         }
         __syncwarp();
         if (valid) {
-            // softmax over the lane's row, summed in 16 groups
-            const __half* row = Ls + lane * ldl;
-            const int G = 16, gs = K / 16;
+            // Softmax of the lane's row, stored for sampling as 16-bit fixed-point prefix sums
+            // inside each group of K/16 clusters (fraction of the group total, last = 65535),
+            // overwriting the logits; FP32 prefix sums P over the 16 group totals. Every
+            // probability the sampler reports comes from these stored numbers: group q has
+            // weight P[q] - P[q-1], cluster c inside it (fp[c] - fp[c-1]) / 65535 of that, so
+            // the pdf returned with a sample is the pdf it was drawn with (up to FP32
+            // rounding) and small clusters keep a resolution of 1/65535 of their group.
+            __half* row = Ls + lane * ldl;
+            uint16_t* fp = reinterpret_cast<uint16_t*>(row);
+            const int gs = K / 16;
             float mx = -INFINITY;
             for (int c = 0; c < K; c++) mx = fmaxf(mx, __half2float(row[c]));
-            float S[16];
+            float P[16];
             float Z = 0.0f;
 #pragma unroll
-            for (int q = 0; q < G; q++) {
-                float s = 0.0f;
-                for (int c = q * gs; c < (q + 1) * gs; c++) s += __expf(__half2float(row[c]) - mx);
-                S[q] = s;
-                Z += s;
+            for (int q = 0; q < 16; q++) {
+                float T = 0.0f;
+                for (int c = q * gs; c < (q + 1) * gs; c++) {
+                    const __half h = __float2half_rn(__expf(__half2float(row[c]) - mx));
+                    row[c] = h;
+                    T += __half2float(h);
+                }
+                const float sc = T > 0.0f ? 65535.0f / T : 0.0f;
+                float acc = 0.0f;
+                for (int c = q * gs; c < (q + 1) * gs; c++) {
+                    acc += __half2float(row[c]);
+                    fp[c] = c == (q + 1) * gs - 1 ? (uint16_t)65535u : (uint16_t)min((uint32_t)(acc * sc), 65535u);
+                }
+                Z += T;
+                P[q] = Z;
             }
+            const float invZ = 1.0f / Z;
+            // fraction of its group held by cluster c
+            auto frac = [&](int c) {
+                const uint32_t hi = fp[c], lo = (c % gs) ? fp[c - 1] : 0u;
+                return (float)(hi - lo) * (1.0f / 65535.0f);
+            };
             if (a.probs) {
-                for (int c = 0; c < K; c++) a.probs[(size_t)j * K + c] = __expf(__half2float(row[c]) - mx) / Z;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const float gw = q ? P[q] - P[q - 1] : P[0];
+                    for (int c = q * gs; c < (q + 1) * gs; c++) a.probs[(size_t)j * K + c] = (gw * frac(c)) * invZ;
+                }
             } else {
                 uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
                 const float eps = d.eps, invK = 1.0f / (float)K;
@@ -285,22 +313,38 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
                 for (uint32_t m = 0; m < a.ncand; m++) {
                     const float u = dev::rnd(s);
                     const float v = dev::rnd(s);
+                    const float w = dev::rnd(s);
                     int c;
+                    float gw;   // weight of the chosen cluster's group
                     if (u < eps) {
                         c = min((int)(v * (float)K), K - 1);
+                        const int q = c / gs;
+                        float lo = 0.0f, hi = P[0];
+#pragma unroll
+                        for (int i = 1; i < 16; i++)
+                            if (q == i) { lo = P[i - 1]; hi = P[i]; }
+                        gw = hi - lo;
                     } else {
-                        float target = v * Z;
+                        // group: count of prefix sums <= target (branch-free)
+                        const float target = v * Z;
                         int q = 0;
-                        while (q < G - 1 && target >= S[q]) { target -= S[q]; q++; }
-                        c = q * gs + gs - 1;
-                        for (int cc = q * gs; cc < (q + 1) * gs; cc++) {
-                            const float e = __expf(__half2float(row[cc]) - mx);
-                            if (target < e) { c = cc; break; }
-                            target -= e;
-                        }
+                        float base = 0.0f, top = P[0];
+#pragma unroll
+                        for (int i = 0; i < 15; i++)
+                            if (target >= P[i]) { q = i + 1; base = P[i]; top = P[i + 1]; }
+                        // cluster inside the group: count of in-group prefix fractions <= the
+                        // target's fraction of the group
+                        gw = top - base;
+                        const float x = gw > 0.0f ? (target - base) * (65535.0f / gw) : 0.0f;
+                        int in = 0;
+                        for (int i = 0; i < gs - 1; i++) in += x >= (float)fp[q * gs + i] ? 1 : 0;
+                        c = q * gs + in;
                     }
-                    const float qc = (1.0f - eps) * (__expf(__half2float(row[c]) - mx) / Z) + eps * invK;
-                    out[m] = make_uint2((uint32_t)c, __float_as_uint(qc));
+                    const float qc = (1.0f - eps) * ((gw * frac(c)) * invZ) + eps * invK;
+                    // an emitter of cluster c, uniformly: p_src = q(c) / |c|
+                    const uint32_t off = __ldg(a.clOff + c), sz = __ldg(a.clOff + c + 1) - off;
+                    const uint32_t mi = min((uint32_t)(w * (float)sz), sz - 1u);
+                    out[m] = make_uint2(__ldg(a.clMembers + off + mi), __float_as_uint(qc / (float)sz));
                 }
             }
         }

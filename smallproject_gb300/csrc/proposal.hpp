@@ -20,7 +20,9 @@ struct InferArgs {
     const uint32_t* hits;
     const uint32_t* count;            // device hit count (render mode)
     uint32_t ncand;                   // candidates per pixel (<= kMaxCand)
-    uint2* cand;                      // out: [hit][kMaxCand] (cluster, bits(q))
+    const uint32_t* clOff;            // cluster c = emitters clMembers[clOff[c] .. clOff[c+1])
+    const uint32_t* clMembers;
+    uint2* cand;                      // out: [hit][kMaxCand] (emitter, bits(p_src))
     // sample mode (tests): explicit inputs (x, y, z, bits(side code)) and softmax output
     const float4* samples;
     uint32_t n;
