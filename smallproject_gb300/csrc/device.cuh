@@ -340,35 +340,23 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
 // Every float op, the step budget accounting and the exit cascade (brick -> grid step
 // -> uber step) follow trace<MODE> exactly; the oracle checks the two for equality.
 struct Walker {
-    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;
-    float t, tmx, tmy, tmz;        // crossings at the current level
-    float umx, umy, umz;           // saved uber-level crossings (below the uber level)
-    float gmx, gmy, gmz;           // saved grid-level crossings (inside a brick)
-    int cx, cy, cz;                // current cell relative to its parent cell (uber: absolute)
-    int ux, uy, uz;                // saved uber cell (absolute)
-    int gx, gy, gz;                // saved grid cell relative to its uber cell
-    int sx, sy, sz;                // axis steps (+-1)
-    uint32_t lin, ulin, glin;      // element index of the current / saved uber / saved grid cell
-    int dly, dlz;                  // lin step for a y / z cell step at the current level
-    int mask;                      // ~(cells per parent cell - 1) at the current level
+    float ax, ay, az, vx, vy, vz, rx, ry, rz, to, tdx, tdy, tdz;
+    float t, tmx, tmy, tmz;        // current level
+    float umx, umy, umz;           // saved uber-level crossings
+    float gmx, gmy, gmz;           // saved grid-level crossings
+    int ux, uy, uz, gx, gy, gz, lx, ly, lz;
     int steps, level, bi;
-    uint32_t o, last;
+    uint32_t o, brick, last, dirbits;   // dirbits: bit a set = positive direction on axis a
     float dist;                    // result
     uint32_t side, voxel;
+    __device__ __forceinline__ int sx() const { return (dirbits & 1u) ? 1 : -1; }
+    __device__ __forceinline__ int sy() const { return (dirbits & 2u) ? 1 : -1; }
+    __device__ __forceinline__ int sz() const { return (dirbits & 4u) ? 1 : -1; }
+    __device__ __forceinline__ int ox() const { return (int)(dirbits & 1u); }
+    __device__ __forceinline__ int oy() const { return (int)((dirbits >> 1) & 1u); }
+    __device__ __forceinline__ int oz() const { return (int)((dirbits >> 2) & 1u); }
 };
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
-
-__device__ __forceinline__ void walk_level_consts(Walker& k) {
-    // uber x + z*32 + y*1024, grid x + z*128 + y*16384, brick x + y*8 + z*64
-    k.dly = k.sy * (k.level == 0 ? 1024 : (k.level == 1 ? 16384 : 8));
-    k.dlz = k.sz * (k.level == 0 ? 32 : (k.level == 1 ? 128 : 64));
-    k.mask = k.level == 0 ? ~31 : (k.level == 1 ? ~3 : ~7);
-}
-
-__device__ __forceinline__ uint32_t walk_load(const Walker& k, const World& w) {
-    if (k.level == 0) return __ldg(w.uber + k.lin);
-    return __ldg((k.level == 1 ? w.grid : w.bricks) + k.lin);
-}
 
 // TraceOpaqueRay prologue (trace.cl:219-243); returns WALK_MISS when the ray misses the map
 __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, float ay, float az, float vx, float vy,
@@ -378,9 +366,7 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
     if (fabsf(vz) < 1e-8f) vz = vz < 0.0f ? -1e-8f : 1e-8f;
     k.vx = vx; k.vy = vy; k.vz = vz;
     k.rx = 1.0f / vx; k.ry = 1.0f / vy; k.rz = 1.0f / vz;
-    k.sx = vx > 0.0f ? 1 : -1;
-    k.sy = vy > 0.0f ? 1 : -1;
-    k.sz = vz > 0.0f ? 1 : -1;
+    k.dirbits = (vx > 0.0f ? 1u : 0u) | (vy > 0.0f ? 2u : 0u) | (vz > 0.0f ? 4u : 0u);
     k.to = 0.0f;
     k.last = 0;
     if (ax < 0.0f || ay < 0.0f || az < 0.0f || ax > 1024.0f || ay > 1024.0f || az > 1024.0f) {
@@ -402,108 +388,119 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
         if (az < 0.01f || az > hi) k.last = 2;
     }
     k.ax = ax; k.ay = ay; k.az = az;
-    k.cx = (int)min(f2u(ax) >> 5, 31u);
-    k.cy = (int)min(f2u(ay) >> 5, 31u);
-    k.cz = (int)min(f2u(az) >> 5, 31u);
-    const uint32_t ox = k.sx > 0 ? 1u : 0u, oy = k.sy > 0 ? 1u : 0u, oz = k.sz > 0 ? 1u : 0u;
-    k.tmx = ((float)((uint32_t)k.cx + ox) - ax * 0.03125f) * k.rx;
-    k.tmy = ((float)((uint32_t)k.cy + oy) - ay * 0.03125f) * k.ry;
-    k.tmz = ((float)((uint32_t)k.cz + oz) - az * 0.03125f) * k.rz;
+    k.ux = (int)min(f2u(ax) >> 5, 31u);
+    k.uy = (int)min(f2u(ay) >> 5, 31u);
+    k.uz = (int)min(f2u(az) >> 5, 31u);
+    k.tmx = ((float)(uint32_t)(k.ux + k.ox()) - ax * 0.03125f) * k.rx;
+    k.tmy = ((float)(uint32_t)(k.uy + k.oy()) - ay * 0.03125f) * k.ry;
+    k.tmz = ((float)(uint32_t)(k.uz + k.oz()) - az * 0.03125f) * k.rz;
+    k.tdx = (float)k.sx() * k.rx;
+    k.tdy = (float)k.sy() * k.ry;
+    k.tdz = (float)k.sz() * k.rz;
     k.t = 0.0f;
     k.steps = steps;
     k.level = 0;
-    k.lin = (uint32_t)(k.cx + k.cz * 32 + k.cy * 1024);
-    walk_level_consts(k);
-    k.o = walk_load(k, w);
+    k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
     return WALK_CONTINUE;
 }
 
-// One cell visit of the reference's three-level DDA (trace.cl:59-117, 219-285: uber 32^3
-// cells of 4^3 grid cells, grid 128^3 cells, bricks of 8^3 voxels). Every level runs the
-// same cell step on coordinates relative to the parent cell (bounds = one mask test) and
-// an element index advanced with the coordinates, so lanes of a warp at different levels
-// stay converged through it; only the examine and the rare level changes differ.
-//   examine  uber: budget -4, occupied -> descend; grid: budget -1, solid -> hit test,
-//            brick -> descend; brick voxel: hit test (bricks are free of budget)
-//   advance  t = min crossing, every tied axis steps, `last` = the highest tied axis;
-//            leaving the parent cell (or 24 brick steps) ascends and advances there
-// Per level the float operations are the reference's (factors of 1 and offsets of 0 are
-// exact where a level has no scale).
+// uber-level step (trace.cl:274-279); returns false when the ray leaves the map
+__device__ __forceinline__ bool walk_uber_step(Walker& k, const World& w) {
+    k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
+    k.last = 0;
+    if (k.t == k.tmx) { k.tmx += k.tdx; k.ux += k.sx(); }
+    if (k.t == k.tmy) { k.tmy += k.tdy; k.uy += k.sy(); k.last = 1; }
+    if (k.t == k.tmz) { k.tmz += k.tdz; k.uz += k.sz(); k.last = 2; }
+    if ((k.ux | k.uy | k.uz) & ~31) return false;
+    k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
+    return true;
+}
+
+// grid-level step (GRIDSTEP tail, trace.cl:105-110); continues into the uber step
+// when the ray leaves the current uber cell
+__device__ __forceinline__ int walk_grid_step(Walker& k, const World& w) {
+    k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
+    k.last = 0;
+    if (k.t == k.tmx) { k.tmx += k.tdx; k.gx += k.sx(); }
+    if (k.t == k.tmy) { k.tmy += k.tdy; k.gy += k.sy(); k.last = 1; }
+    if (k.t == k.tmz) { k.tmz += k.tdz; k.gz += k.sz(); k.last = 2; }
+    if (((k.gx >> 2) != k.ux) | ((k.gy >> 2) != k.uy) | ((k.gz >> 2) != k.uz)) {
+        k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
+        k.level = 0;
+        return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
+    }
+    k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
+    return WALK_CONTINUE;
+}
+
+// one cell visit at the current level
 __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
-    const int L = k.level;
-    const uint32_t o = k.o;
-    if (L != 2) {
-        k.steps -= L == 0 ? 4 : 1;
-        if (k.steps <= 0) return WALK_MISS;   // a grid step that empties the budget always misses
-    }
-    const uint32_t v = L == 1 ? (o >> 1) : o;
-    if (((v & 0xf000u) == 0xf000u) && !(L == 1 && (o & 1u))) {   // uber content is 0/1: never a hit
-        k.dist = (L == 1 ? k.t * 8.0f : k.t) + k.to;
-        k.side = k.last;
-        k.voxel = v;
-        return WALK_HIT;
-    }
-    if (L != 2 && (o & 1u)) {
-        // descend: uber -> grid (trace.cl:247-255), grid -> brick (trace.cl:65-74)
-        const bool toGrid = L == 0;
-        const float as = toGrid ? 0.125f : 1.0f;
-        const uint32_t span = toGrid ? 4u : 8u;
-        uint32_t bx, by, bz;
-        if (toGrid) {
-            k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
-            k.ux = k.cx; k.uy = k.cy; k.uz = k.cz;
-            k.ulin = k.lin;
-            bx = (uint32_t)k.cx * 4u; by = (uint32_t)k.cy * 4u; bz = (uint32_t)k.cz * 4u;
-        } else {
-            k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
-            k.gx = k.cx; k.gy = k.cy; k.gz = k.cz;
-            k.glin = k.lin;
-            bx = ((uint32_t)k.ux * 4u + (uint32_t)k.cx) * 8u;
-            by = ((uint32_t)k.uy * 4u + (uint32_t)k.cy) * 8u;
-            bz = ((uint32_t)k.uz * 4u + (uint32_t)k.cz) * 8u;
-            k.bi = 0;
+    if (k.level == 2) {
+        const uint32_t v = __ldg(w.bricks + (size_t)k.brick * 512u + k.lx + k.ly * 8 + k.lz * 64);
+        if (((v & 0xf000u) >> 12) == 15u) {
+            k.dist = k.t + k.to;
+            k.side = k.last;
+            k.voxel = v;
+            return WALK_HIT;
         }
-        k.t *= toGrid ? 4.0f : 8.0f;
-        const uint32_t px = f2u(as * k.ax + k.vx * k.t), py = f2u(as * k.ay + k.vy * k.t), pz = f2u(as * k.az + k.vz * k.t);
-        const uint32_t qx = min(max(px, bx), bx + span - 1u), qy = min(max(py, by), by + span - 1u),
-                       qz = min(max(pz, bz), bz + span - 1u);
-        k.tmx = ((float)(qx + (k.sx > 0 ? 1u : 0u)) - k.ax * as) * k.rx;
-        k.tmy = ((float)(qy + (k.sy > 0 ? 1u : 0u)) - k.ay * as) * k.ry;
-        k.tmz = ((float)(qz + (k.sz > 0 ? 1u : 0u)) - k.az * as) * k.rz;
-        k.cx = (int)(qx - bx);
-        k.cy = (int)(qy - by);
-        k.cz = (int)(qz - bz);
-        k.lin = toGrid ? qx + qz * 128u + qy * 16384u : (o >> 1) * 512u + (uint32_t)(k.cx + k.cy * 8 + k.cz * 64);
-        k.level = L + 1;
-        walk_level_consts(k);
-        k.o = walk_load(k, w);
-        return WALK_CONTINUE;
-    }
-    // advance; ascend while the ray leaves the parent cell
-    for (;;) {
         k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
         k.last = 0;
-        if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.cx += k.sx; k.lin += (uint32_t)k.sx; }
-        if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.cy += k.sy; k.lin += (uint32_t)k.dly; k.last = 1; }
-        if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.cz += k.sz; k.lin += (uint32_t)k.dlz; k.last = 2; }
-        bool out = ((k.cx | k.cy | k.cz) & k.mask) != 0;
-        if (k.level == 2 && !out) out = ++k.bi == 24;
-        if (!out) break;
-        if (k.level == 0) return WALK_MISS;   // left the map
-        if (k.level == 2) {
+        if (k.t == k.tmx) { k.tmx += k.tdx; k.lx += k.sx(); }
+        if (k.t == k.tmy) { k.tmy += k.tdy; k.ly += k.sy(); k.last = 1; }
+        if (k.t == k.tmz) { k.tmz += k.tdz; k.lz += k.sz(); k.last = 2; }
+        if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
             k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
-            k.cx = k.gx; k.cy = k.gy; k.cz = k.gz;
-            k.lin = k.glin;
-        } else {
-            k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
-            k.cx = k.ux; k.cy = k.uy; k.cz = k.uz;
-            k.lin = k.ulin;
+            k.level = 1;
+            return walk_grid_step(k, w);
         }
-        k.level -= 1;
-        walk_level_consts(k);
+        return WALK_CONTINUE;
     }
-    k.o = walk_load(k, w);
-    return WALK_CONTINUE;
+    if (k.level == 1) {
+        // a grid step with the budget exhausted always ends as a miss (the uber loop
+        // re-checks the budget before any further cell is visited)
+        if (!--k.steps) return WALK_MISS;
+        if ((k.o & 1u) == 0u) {
+            const uint32_t v = k.o >> 1;
+            if (((v & 0xf000u) >> 12) == 15u) {
+                k.dist = k.t * 8.0f + k.to;
+                k.side = k.last;
+                k.voxel = v;
+                return WALK_HIT;
+            }
+            return walk_grid_step(k, w);
+        }
+        k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
+        k.t *= 8.0f;
+        const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
+        const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
+        const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u), cz = min(max(pz, bz0), bz0 + 7u);
+        k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
+        k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
+        k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
+        k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
+        k.brick = k.o >> 1;
+        k.bi = 0;
+        k.level = 2;
+        return WALK_CONTINUE;
+    }
+    // uber level
+    if ((k.steps -= 4) <= 0) return WALK_MISS;
+    if (k.o != 0u) {
+        k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
+        k.t *= 4.0f;
+        const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
+                       qz = f2u(0.125f * k.az + k.vz * k.t);
+        k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
+        k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
+        k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
+        k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
+        k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
+        k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
+        k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
+        k.level = 1;
+        return WALK_CONTINUE;
+    }
+    return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
 }
 
 // ---- reservoirs --------------------------------------------------------------------

@@ -135,7 +135,7 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][H / 16][4],
 // ---- inference --------------------------------------------------------------------------
 // Shared memory (per CTA of 8 warps): W1 [H][kIn+8], W2,W3 [H][H+8], W4 [K][H+8] (BF16,
 // rows padded against bank conflicts), biases (FP32), per warp X [32][kIn+8] (BF16) and
-// logits [32][K+2] (FP16).
+// logits [32][K+2] (FP16, then the sampling tables), cluster offsets [K+1].
 template <int H>
 __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
     float* bs = reinterpret_cast<float*>(W4s + (size_t)K * ldh);           // b1 | b2 | b3 | b4
     __nv_bfloat16* Xall = reinterpret_cast<__nv_bfloat16*>(bs + 3 * H + K);
     __half* Lall = reinterpret_cast<__half*>(Xall + 8 * 32 * ldx);
+    uint32_t* offs = reinterpret_cast<uint32_t*>(Lall + (size_t)8 * 32 * ldl);   // cluster offsets [K + 1]
     // weights -> shared memory
     {
         const __nv_bfloat16* wg = a.wbf;   // W1 [H][kIn] | W2 [H][H] | W3 [H][H] | W4 [K][H]
@@ -166,6 +167,8 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
             bs[2 * H + e] = p[a.L.b3 + e];
         }
         for (int e = threadIdx.x; e < K; e += blockDim.x) bs[3 * H + e] = p[a.L.b4 + e];
+        if (a.clOff)
+            for (int e = threadIdx.x; e <= K; e += blockDim.x) offs[e] = a.clOff[e];
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -310,6 +313,8 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
                 uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
                 const float eps = d.eps, invK = 1.0f / (float)K;
                 uint2* out = a.cand + (size_t)j * kMaxCand;
+                // unrolled so that the member loads of several candidates are in flight together
+#pragma unroll 4
                 for (uint32_t m = 0; m < a.ncand; m++) {
                     const float u = dev::rnd(s);
                     const float v = dev::rnd(s);
@@ -342,7 +347,7 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
                     }
                     const float qc = (1.0f - eps) * ((gw * frac(c)) * invZ) + eps * invK;
                     // an emitter of cluster c, uniformly: p_src = q(c) / |c|
-                    const uint32_t off = __ldg(a.clOff + c), sz = __ldg(a.clOff + c + 1) - off;
+                    const uint32_t off = offs[c], sz = offs[c + 1] - off;
                     const uint32_t mi = min((uint32_t)(w * (float)sz), sz - 1u);
                     out[m] = make_uint2(__ldg(a.clMembers + off + mi), __float_as_uint(qc / (float)sz));
                 }
@@ -561,7 +566,7 @@ static int sms() {
 size_t infer_smem_bytes(const Dims& d) {
     const int H = d.H, K = d.K;
     return (size_t)H * (kIn + 8) * 2 + 2 * (size_t)H * (H + 8) * 2 + (size_t)K * (H + 8) * 2 + (3 * H + K) * 4 +
-           8 * 32 * (kIn + 8) * 2 + 8 * 32 * (size_t)(K + 2) * 2;
+           8 * 32 * (kIn + 8) * 2 + 8 * 32 * (size_t)(K + 2) * 2 + (size_t)(K + 1) * 4;
 }
 
 bool infer_supported(const Dims& d) {
