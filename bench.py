@@ -1,10 +1,21 @@
-"""Benchmark: ms/frame of the Voxel ReSTIR render path on one GB300.
+"""Benchmark: ms/frame at 1080p at equal MSE against the converged render, learned
+candidate proposal vs plain uniform-source RIS, on one GB300.
 
-Workload (config 3 of the benchmark set, plain uniform-source method): 1024^3 fBm
-terrain (seed 4), 65,536 emitter voxels (70% in 32 Gaussian blobs, sigma 24),
-1920x1080, area lights with solid-angle side sampling, 32 candidates, temporal reuse
-(20x M clamp) and 5-tap / 30-px spatial reuse, camera on a seeded Catmull-Rom path.
-A step is one frame: albedo -> candidates+temporal -> spatial -> shading+accumulate.
+Workload (config 3 of the benchmark set): 1024^3 fBm terrain (seed 4), 65,536 emitter
+voxels (70% in 32 Gaussian blobs, sigma 24) grouped in 256 clusters, 1920x1080, area
+lights with solid-angle side sampling, temporal reuse (20x M clamp) and 5-tap / 30-px
+spatial reuse, camera on a seeded 300-frame Catmull-Rom path. A step is one frame:
+albedo -> candidates (+ proposal inference) + temporal -> spatial -> shading+accumulate.
+
+Quality protocol (untimed setup, --quality full): a converged render (FP64 mean of
+--conv-frames frames of the unbiased estimator: spatial and temporal reuse off) at path
+frame 150; the proposal trained online for --train-frames frames along the path on the
+plain method's reservoirs; then for each method and candidate count in CANDS, seeds x
+frames at the static pose: device ms/frame and MSE against the converged render. The
+plain method's reference point is 32 candidates (the reference's NUMBEROFCANDIDATES).
+The timed configuration is the learned method at the smallest candidate count whose mean
+MSE is at most the plain method's (equal MSE), else plain at 32; `value` is its device
+ms/frame over the timed steps along the camera path.
 
 Arms:
   --impl ours       the CUDA path (libvxr.so) - the JSON line's `value` is device time
@@ -164,6 +175,86 @@ def cpu_arm(args, desc, world, steps, warmup, W, H):
                                 "desc": f"{rows} rows x {W} px of each {W}x{H} frame, scaled by {H}/{rows}"}
 
 
+CANDS = (4, 8, 12, 16, 24, 32)
+POSE = 150
+NFR = 300
+# DRAM bytes per launch of the dominant kernel from the ncu capture of the 960x540 case
+# (profiles/), scaled by 4 to 1920x1080 (the ray count grows with the pixel count)
+NCU_TRAFFIC_1080P = {"shadow_candidates": 4 * (123.28e6 + 6.81e6), "shadow_shading": 4 * (89.91e6 + 3.95e6)}
+
+
+def quality_eval(vx, world, desc, W, H, tuning, args):
+    """Converged render, online training, and the MSE / ms table of both methods."""
+    pos, tgt = vx.camera_path(desc, 1, POSE, NFR)
+    ref = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=77))
+    ref.set_tuning(tuning)
+    ref.lookat(pos, tgt)
+    ref.sum64_reset()
+    t0 = time.perf_counter()
+    for _ in range(args.conv_frames):
+        ref.render()
+        ref.sum64_add()
+    ref.wait()
+    conv_s = time.perf_counter() - t0
+    trainer = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5))
+    trainer.set_tuning(tuning)
+    trainer.proposal_enable(seed=2, batch=65536)
+    t0 = time.perf_counter()
+    losses = []
+    for f in range(args.train_frames):
+        p, t = vx.camera_path(desc, 1, f % NFR, NFR)
+        trainer.lookat(p, t)
+        trainer.render()
+        losses.append(trainer.proposal_train(1))
+    trainer.wait()
+    train_s = time.perf_counter() - t0
+    params = trainer.proposal_params()
+    trainer.close()
+    table = {}
+    for method in ("plain", "learned"):
+        for c in CANDS:
+            ms_l, mse_l = [], []
+            for seed in range(args.mse_seeds):
+                v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, num_candidates=c, rng_seed=1000 + seed))
+                v.set_tuning(tuning)
+                v.lookat(pos, tgt)
+                if method == "learned":
+                    v.proposal_enable(seed=2, batch=65536)
+                    v.proposal_set_params(params)
+                    v.proposal_use(True)
+                for _ in range(8):
+                    v.render()
+                v.wait()
+                v.timer_begin()
+                for _ in range(8):
+                    v.render()
+                ms_l.append(v.timer_end() / 8)
+                v.wait()
+                for _ in range(args.mse_frames):
+                    v.render()
+                    mse_l.append(v.error_vs(ref, 0)[0])
+                v.close()
+            table[f"{method}_{c}"] = {"method": method, "candidates": c, "ms": float(np.median(ms_l)),
+                                      "mse": float(np.mean(mse_l)), "mse_median": float(np.median(mse_l)),
+                                      "frames": len(mse_l)}
+    ref.close()
+    p32 = table["plain_32"]
+    eq = None
+    for c in CANDS:
+        if table[f"learned_{c}"]["mse"] <= p32["mse"]:
+            eq = table[f"learned_{c}"]
+            break
+    # equal time: the learned configuration with the largest ms/frame not above plain's
+    at = [table[f"learned_{c}"] for c in CANDS if table[f"learned_{c}"]["ms"] <= p32["ms"]]
+    et = max(at, key=lambda r: r["ms"]) if at else None
+    return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s,
+            "train_frames": args.train_frames, "train_s": train_s, "train_batch": 65536,
+            "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
+            "frames_per_point": args.mse_seeds * args.mse_frames, "table": table,
+            "plain_reference": p32, "learned_at_equal_mse": eq,
+            "equal_time": None if et is None else {"learned": et, "mse_ratio": et["mse"] / p32["mse"]}}, params
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -176,17 +267,22 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=96, help="rows of the frame timed on the CPU per step")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--tile", type=str, default="", help="threads per block, e.g. 16x8")
     ap.add_argument("--no-tune", action="store_true", help="library default launch tuning instead of the autotuner")
+    ap.add_argument("--quality", choices=["full", "off"], default="full",
+                    help="off: no converged render / training; time the plain method at 32 candidates")
+    ap.add_argument("--conv-frames", type=int, default=4096)
+    ap.add_argument("--train-frames", type=int, default=200)
+    ap.add_argument("--mse-seeds", type=int, default=4)
+    ap.add_argument("--mse-frames", type=int, default=8)
     args = ap.parse_args()
     W, H = args.width, args.height
     warmup = max(args.warmup, 3)
 
     dist, rank, ws = dist_init(args)
-    config = {"workload": f"config{args.config}: plain Voxel ReSTIR, {W}x{H}, area lights, 32 candidates, "
-                          "temporal 20x clamp, 5 taps / 30 px spatial, 1024^3 fBm terrain seed 4, "
-                          "65,536 emitters (70% in 32 blobs), Catmull-Rom camera path",
-              "resolution": [W, H], "scene_config": args.config, "method": "plain uniform-source RIS",
+    config = {"workload": f"config{args.config}: Voxel ReSTIR {W}x{H}, area lights, temporal 20x clamp, 5 taps / "
+                          "30 px spatial, 1024^3 fBm terrain seed 4, 65,536 emitters (70% in 32 blobs) in 256 "
+                          "clusters, Catmull-Rom camera path",
+              "resolution": [W, H], "scene_config": args.config,
               "l2": "per-frame working set (G-buffers, reservoirs, frame, accumulator: 237 MB at 1080p) exceeds "
                     "the 129 MB L2; no flush between frames"}
 
@@ -197,6 +293,7 @@ def main():
         B.build()
         vx, desc, world = make_scene(args.config)
         ms, kind, sample = cpu_arm(args, desc, world, args.steps, min(args.warmup, 1), W, H)
+        config["method"] = "plain uniform-source RIS, 32 candidates"
         line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms/frame", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
@@ -210,57 +307,111 @@ def main():
     from smallproject_gb300 import build as B
     B.build()
     vx, desc, world = make_scene(args.config)
-    tile = {}
-    if args.tile:
-        tx, ty = args.tile.split("x")
-        tile = dict(tile_x=int(tx), tile_y=int(ty))
-    vdesc = vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, **tile)
-    nfr = 300
-    tuning_report = None
-    if not args.no_tune and not tile:
+    world.cluster_lights(256, seed=1, iters=8)
+    vdesc = vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0)
+
+    def cams(f):
+        return vx.camera_path(desc, 1, f % NFR, NFR)
+
+    tuning, tuning_report = vx.tuning(), None
+    if not args.no_tune:
         # launch parameters only (results are identical for every tuning); untimed setup
         from smallproject_gb300 import autotune as at
         cache = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "_build",
                              "vxr_tuning.json")
-        t, tuning_report = at.autotune(world, vdesc, lambda f: vx.camera_path(desc, 1, (1000 + f) % nfr, nfr),
-                                       frames=4, rounds=2, cache_path=cache)
-    view = vx.View(world, vdesc)
-    if tuning_report is not None:
-        view.set_tuning(t)
+        tuning, tuning_report = at.autotune(world, vdesc, lambda f: cams(1000 + f), frames=4, rounds=2,
+                                            cache_path=cache)
 
-    def frame(f):
-        pos, tgt = vx.camera_path(desc, 1, f % nfr, nfr)
+    quality, params = None, None
+    if args.quality == "full" and rank == 0:
+        quality, params = quality_eval(vx, world, desc, W, H, tuning, args)
+    if dist is not None:
+        obj = [quality, params]
+        dist.broadcast_object_list(obj, src=0)
+        quality, params = obj
+    eq = quality["learned_at_equal_mse"] if quality else None
+    learned = eq is not None
+    cand = eq["candidates"] if learned else 32
+    config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32)" if learned
+                        else "plain uniform-source RIS, 32 candidates")
+
+    def make_view(learned_view, c):
+        v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, num_candidates=c))
+        v.set_tuning(tuning)
+        if learned_view:
+            v.proposal_enable(seed=2, batch=65536)
+            v.proposal_set_params(params)
+            v.proposal_use(True)
+        return v
+
+    def timed(view, steps, start):
+        for f in range(warmup):
+            pos, tgt = cams(start + f)
+            view.lookat(pos, tgt)
+            view.render()
+        view.wait()
+        view.stage_stats(reset=True)
+        view.kernel_timing(True)
+        view.kernel_stats(reset=True)
+        barrier(dist)
+        view.timer_begin()
+        for f in range(steps):
+            pos, tgt = cams(start + warmup + f)
+            view.lookat(pos, tgt)
+            view.render()
+        ms = view.timer_end()
+        view.wait()
+        barrier(dist)
+        view.kernel_timing(False)
+        return ms
+
+    # the plain method at 32 candidates for context (same path, same tuning)
+    plain_ms = None
+    if learned:
+        pv = make_view(False, 32)
+        plain_ms = max_over_ranks(dist, timed(pv, args.steps, 0)) / args.steps
+        pv.close()
+
+    view = make_view(learned, cand)
+    clocks = None
+    for f in range(warmup):
+        pos, tgt = cams(f)
         view.lookat(pos, tgt)
         view.render()
-
-    for f in range(warmup):
-        frame(f)
     view.wait()
     view.stage_stats(reset=True)
-
+    view.kernel_timing(True)
+    view.kernel_stats(reset=True)
     barrier(dist)
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if rank == 0 else None
     view.timer_begin()
     for f in range(args.steps):
-        frame(warmup + f)
+        pos, tgt = cams(warmup + f)
+        view.lookat(pos, tgt)
+        view.render()
     ms_total = view.timer_end()
     view.wait()
     barrier(dist)
     clk = clocks.stop() if clocks else None
+    view.kernel_timing(False)
     ms_total = max_over_ranks(dist, ms_total)
     ms_frame = ms_total / args.steps
     sums, counts = view.stage_stats(reset=True)
     stage_ms = {STAGES[i]: (sums[i] / counts[i] if counts[i] else 0.0) for i in range(5)}
+    kstats = view.kernel_stats(reset=True)
+    kernel_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in kstats.items()}
+    launches = sum(v[1] for v in kstats.values())
+    hits, rays_c, rays_s = view.work_counts()
 
     # end to end through the C ABI with a page-locked host image
     pinned = vx.PinnedBuffer(W * H * 4)
     e2e_steps = max(5, min(args.steps, 30))
     for f in range(3):
-        pos, tgt = vx.camera_path(desc, 1, f, nfr)
+        pos, tgt = cams(f)
         view.render_to_host(pos, tgt, pinned.array)
     t0 = time.perf_counter()
     for f in range(e2e_steps):
-        pos, tgt = vx.camera_path(desc, 1, f, nfr)
+        pos, tgt = cams(f)
         view.render_to_host(pos, tgt, pinned.array)
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / e2e_steps
     e2e_ms = max_over_ranks(dist, e2e_ms)
@@ -271,17 +422,26 @@ def main():
         return
     hbm, peak_kind = peaks()
     npx = W * H
-    # dominant kernel = the slowest stage
-    dom = max(("albedo", "candidates", "spatial", "shade"), key=lambda s: stage_ms[s])
-    achieved = BYTES_PER_PX[dom] * npx / (stage_ms[dom] * 1e-3) / 1e9 if stage_ms[dom] > 0 else 0.0
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_kind": f"of {peak_kind}", "traffic": None,
-                "bytes_per_launch": BYTES_PER_PX[dom] * npx}
     stage_rooflines = {s: {"ms": stage_ms[s], "GB/s": BYTES_PER_PX[s] * npx / (stage_ms[s] * 1e-3) / 1e9
                            if stage_ms[s] > 0 else 0.0, "frac": (BYTES_PER_PX[s] * npx / (stage_ms[s] * 1e-3) / 1e9)
                            / hbm if stage_ms[s] > 0 else 0.0}
                        for s in ("albedo", "candidates", "spatial", "shade")}
-    rays_per_s = 3.0 * npx / (ms_frame * 1e-3)
+    # dominant kernel (largest share of the timed frames); algorithmic bytes per launch:
+    # shadow tracers read the 32-byte request and write at most a 4-byte flag per ray
+    dom = max(kernel_ms, key=lambda k: kernel_ms[k] * (kstats[k][1] or 0))
+    per_launch_bytes = {"shadow_candidates": 36.0 * rays_c, "shadow_shading": 36.0 * rays_s,
+                        "ris_candidates": 80.0 * hits, "albedo": 12.0 * npx, "spatial": 80.0 * npx,
+                        "proposal_infer": 8.0 * hits + 8.0 * 32 * hits, "temporal": 48.0 * hits,
+                        "shade_finish": 72.0 * npx, "shade_request": 72.0 * hits, "compact_hits": 12.0 * npx,
+                        "accumulate": 48.0 * npx}
+    ab = per_launch_bytes.get(dom, 0.0)
+    achieved = ab / (kernel_ms[dom] * 1e-3) / 1e9 if kernel_ms[dom] > 0 else 0.0
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": f"of {peak_kind}",
+                "traffic": NCU_TRAFFIC_1080P.get(dom) if (W, H) == (1920, 1080) else None,
+                "bytes_per_launch": ab,
+                "note": "the DDA is latency / ALU bound (L2-resident bricks), not HBM bound: see rays_per_s"}
+    rays = hits + rays_c + rays_s
     cpu = None
     if not args.no_cpu_baseline:
         cms, kind, sample = cpu_arm(args, desc, world, args.cpu_steps, 1, W, H)
@@ -290,11 +450,13 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "ms/frame", "n_gpus": ws, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms_frame, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": config, "stage_ms": stage_ms, "stage_roofline": stage_rooflines, "rays_per_s": rays_per_s,
-            "roofline": roofline, "cpu_baseline": cpu,
+            "config": config, "plain_ms_per_frame": plain_ms if learned else ms_frame,
+            "stage_ms": stage_ms, "kernel_ms": kernel_ms, "stage_roofline": stage_rooflines,
+            "rays_per_frame": rays, "rays_per_s": rays / (ms_frame * 1e-3),
+            "roofline": roofline, "cpu_baseline": cpu, "quality": quality,
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
                     "d2h_bytes_per_step": npx * 16, "image_ok": img_ok},
-            "gpu_launches": 4 * args.steps, "clocks": clk,
+            "gpu_launches": launches, "clocks": clk,
             "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report}
     print(json.dumps(line))
     view.close()

@@ -308,6 +308,18 @@ int vxr_view_stage_stats(vxr_view* v, double sum_ms[5], uint32_t count[5], int r
  * enqueued in between; vxr_view_timer_end waits and returns the elapsed milliseconds. */
 int vxr_view_timer_begin(vxr_view* v);
 int vxr_view_timer_end(vxr_view* v, float* ms);
+/* Per-kernel timing (no reference counterpart): CUDA events around every kernel the
+ * view launches, while on. Kernel ids 0..VXR_KERNEL_COUNT-1 (names from
+ * vxr_kernel_name): albedo, compact_hits, proposal_infer, ris_candidates,
+ * shadow_candidates, temporal, spatial, shade_request, shadow_shading, shade_finish,
+ * accumulate. Stats: summed milliseconds and launch counts since the last reset. */
+#define VXR_KERNEL_COUNT 11
+int vxr_view_kernel_timing(vxr_view* v, int on);
+int vxr_view_kernel_stats(vxr_view* v, double sum_ms[VXR_KERNEL_COUNT], uint32_t count[VXR_KERNEL_COUNT], int reset);
+const char* vxr_kernel_name(int id);
+/* Work of the view's last frame (waits for it): counts[0] hit pixels, counts[1] shadow
+ * rays of the candidate stage, counts[2] shadow rays of shading. */
+int vxr_view_work_counts(vxr_view* v, uint32_t counts[3]);
 /* End-to-end frame through host memory: LookAt(pos, target), render, copy the
  * accumulated image into host_rgba (W*H float4; page-locked memory is fastest), wait. */
 int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba);

@@ -669,14 +669,28 @@ static unsigned resident_blocks(const void* kernel, int threads) {
     }
     return (unsigned)(sm_count() * it->second);
 }
+// brackets one kernel launch with the attached timer's events
+struct Timed {
+    const BatchDev& bd;
+    int id;
+    cudaStream_t s;
+    Timed(const BatchDev& b, int i, cudaStream_t st) : bd(b), id(i), s(st) {
+        if (bd.timer) bd.timer->mark(id, false, s);
+    }
+    ~Timed() {
+        if (bd.timer) bd.timer->mark(id, true, s);
+    }
+};
+
 template <class K>
-static void launch_tiles(K kernel, const BatchDev& bd, int ctr, cudaStream_t s) {
+static void launch_tiles(K kernel, const BatchDev& bd, int ctr, cudaStream_t s, int id) {
     const int threads = bd.tx * bd.ty;
     unsigned nb = std::max(1u, bd.totalTiles);
     if (bd.persistent) {
         cudaMemsetAsync(bd.counters + ctr, 0, sizeof(uint32_t), s);
         nb = std::max(1u, std::min(resident_blocks((const void*)kernel, threads), bd.totalTiles));
     }
+    Timed tm(bd, id, s);
     kernel<<<nb, threads, 0, s>>>(bd);
 }
 
@@ -720,14 +734,15 @@ void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s) {
 }
 
 void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {
-    if (variant == 2) launch_tiles(dev::albedo_kernel<2>, bd, kCtrAlbedo, s);
-    else launch_tiles(dev::albedo_kernel<0>, bd, kCtrAlbedo, s);
+    if (variant == 2) launch_tiles(dev::albedo_kernel<2>, bd, kCtrAlbedo, s, K_ALBEDO);
+    else launch_tiles(dev::albedo_kernel<0>, bd, kCtrAlbedo, s, K_ALBEDO);
 }
 
 template <int VARIANT, int MINB>
 static void launch_shadow_k(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
     const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT, MINB>, 128);
     const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 127) / 128));
+    Timed tm(bd, planeSel ? K_SHADOW_SHADE : K_SHADOW_CAND, s);
     dev::shadow_kernel<VARIANT, MINB><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel);
 }
 template <int VARIANT>
@@ -737,6 +752,7 @@ static void launch_shadow(const BatchDev& bd, int countIdx, int planeSel, cudaSt
 }
 template <int VARIANT, bool LEARNED>
 static void launch_ris(const BatchDev& bd, unsigned nb, cudaStream_t s) {
+    Timed tm(bd, K_RIS, s);
     if (bd.occupancy) dev::ris_kernel<VARIANT, LEARNED, 7><<<nb, 128, 0, s>>>(bd);
     else dev::ris_kernel<VARIANT, LEARNED, 0><<<nb, 128, 0, s>>>(bd);
 }
@@ -747,7 +763,10 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
     cudaMemsetAsync(bd.counters + kCtrHits, 0, 3 * sizeof(uint32_t), s);   // hits, q1 requests, q1 fetch
     uint32_t maxPx = VARIANT < 2 ? bd.totalPixels : 0;
     if (VARIANT == 2) maxPx = (uint32_t)(n / bd.nviews + 1);
-    dev::compact_hits_kernel<VARIANT><<<dim3(list_blocks(maxPx, 256, 8), bd.nviews), 256, 0, s>>>(bd);
+    {
+        Timed tm(bd, K_COMPACT, s);
+        dev::compact_hits_kernel<VARIANT><<<dim3(list_blocks(maxPx, 256, 8), bd.nviews), 256, 0, s>>>(bd);
+    }
     const unsigned nb = list_blocks(n, 128, bd.listPerSm);
     bool learnedDone = false;
     if constexpr (VARIANT < 2) {
@@ -765,7 +784,10 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
             ia.clMembers = learned->clMembers;
             ia.samples = nullptr;
             ia.probs = nullptr;
-            if (bd.one.k.ncand > 0) prop::launch_infer(ia, (uint32_t)n, s);
+            if (bd.one.k.ncand > 0) {
+                Timed tm(bd, K_INFER, s);
+                prop::launch_infer(ia, (uint32_t)n, s);
+            }
             launch_ris<VARIANT, true>(lb, nb, s);
             learnedDone = true;
         }
@@ -773,8 +795,10 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
     if (!learnedDone) launch_ris<VARIANT, false>(bd, nb, s);
     launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ1, 0, s);
     // a single view without temporal reuse this frame skips the launch (a table checks per view)
-    if (VARIANT == 2 || (bd.one.k.restirtemporalframe > 0 && bd.one.k.temporal))
+    if (VARIANT == 2 || (bd.one.k.restirtemporalframe > 0 && bd.one.k.temporal)) {
+        Timed tm(bd, K_TEMPORAL, s);
         dev::temporal_kernel<VARIANT><<<nb, 128, 0, s>>>(bd);
+    }
 }
 
 void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s) {
@@ -784,17 +808,20 @@ void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook*
 }
 
 void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s) {
-    if (variant == 0) launch_tiles(dev::spatial_kernel<0>, bd, kCtrSpatial, s);
-    else if (variant == 1) launch_tiles(dev::spatial_kernel<1>, bd, kCtrSpatial, s);
-    else launch_tiles(dev::spatial_kernel<2>, bd, kCtrSpatial, s);
+    if (variant == 0) launch_tiles(dev::spatial_kernel<0>, bd, kCtrSpatial, s, K_SPATIAL);
+    else if (variant == 1) launch_tiles(dev::spatial_kernel<1>, bd, kCtrSpatial, s, K_SPATIAL);
+    else launch_tiles(dev::spatial_kernel<2>, bd, kCtrSpatial, s, K_SPATIAL);
 }
 
 template <int VARIANT>
 static void shade_v(const BatchDev& bd, cudaStream_t s) {
     cudaMemsetAsync(bd.counters + kCtrQ2, 0, 2 * sizeof(uint32_t), s);   // q2 requests, q2 fetch
-    dev::shade_request_kernel<VARIANT < 2 ? 0 : 2><<<list_blocks(bd.totalPixels, 128, bd.listPerSm), 128, 0, s>>>(bd);
+    {
+        Timed tm(bd, K_SHADE_REQ, s);
+        dev::shade_request_kernel<VARIANT < 2 ? 0 : 2><<<list_blocks(bd.totalPixels, 128, bd.listPerSm), 128, 0, s>>>(bd);
+    }
     launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ2, 1, s);
-    launch_tiles(dev::shade_finish_kernel<VARIANT>, bd, kCtrFinish, s);
+    launch_tiles(dev::shade_finish_kernel<VARIANT>, bd, kCtrFinish, s, K_SHADE_FINISH);
 }
 
 void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s) {
@@ -804,8 +831,8 @@ void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s) {
 }
 
 void launch_batch_accumulate(const BatchDev& bd, int variant, cudaStream_t s) {
-    if (variant == 2) launch_tiles(dev::accumulate_kernel<2>, bd, kCtrAccum, s);
-    else launch_tiles(dev::accumulate_kernel<0>, bd, kCtrAccum, s);
+    if (variant == 2) launch_tiles(dev::accumulate_kernel<2>, bd, kCtrAccum, s, K_ACCUM);
+    else launch_tiles(dev::accumulate_kernel<0>, bd, kCtrAccum, s, K_ACCUM);
 }
 
 }  // namespace vxr

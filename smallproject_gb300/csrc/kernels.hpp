@@ -54,6 +54,17 @@ struct ViewDev {
     uint32_t tilesX = 0;
 };
 
+// Optional per-kernel CUDA-event timing: the launchers bracket every kernel they launch
+// with mark(id, false, s) / mark(id, true, s) when a timer is attached (runtime.cu).
+enum KernelId : int {
+    K_ALBEDO = 0, K_COMPACT, K_INFER, K_RIS, K_SHADOW_CAND, K_TEMPORAL, K_SPATIAL, K_SHADE_REQ, K_SHADOW_SHADE,
+    K_SHADE_FINISH, K_ACCUM, K_COUNT
+};
+struct KernelTimer {
+    virtual void mark(int id, bool end, cudaStream_t s) = 0;
+    virtual ~KernelTimer() = default;
+};
+
 // One launch's work: a single view (read from the kernel parameter `one`) or a table of
 // views in device memory. Hit-list entries are (view << 27 | pixel), at most 16 views
 // of at most 2^27 pixels each.
@@ -76,6 +87,7 @@ struct BatchDev {
     float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(entry))
     float4* qB = nullptr;                 //                      (direction, bits(light))
     uint32_t* counters = nullptr;         // kCounters words
+    KernelTimer* timer = nullptr;         // host object (never dereferenced on the device)
 };
 
 // Launch parameters that change speed but never results (autotuned per configuration).

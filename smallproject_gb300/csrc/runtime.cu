@@ -1,6 +1,7 @@
 // runtime.cu - device world copies, views (one camera on one world) and the render
 // orchestration behind the C ABI: the GB300 counterpart of World::Render/Commit
 // (template/world.cpp:2127-2483) on one CUDA stream per view.
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -164,6 +165,8 @@ void free_view(vxr_view* v) {
     cudaFree(v->sum64); cudaFree(v->errOut);
     if (v->prop) vxr::destroy_proposal(v->prop);
     v->prop = nullptr;
+    delete v->ktimer;
+    v->ktimer = nullptr;
     for (int i = 0; i < 6; i++) {
         if (v->evs[i]) cudaEventDestroy(v->evs[i]);
         if (v->eve[i]) cudaEventDestroy(v->eve[i]);
@@ -191,6 +194,36 @@ void harvest(vxr_view* v) {
         }
     }
     v->harvested = v->frameSerial;
+}
+
+void ViewKernelTimer::mark(int k, bool end, cudaStream_t s) {
+    if (!end) {
+        const int slot = (int)(next % kPairs);
+        open[k] = slot;
+        id[slot] = k;
+        next++;
+        cudaEventRecord(ev[2 * slot], s);
+    } else {
+        cudaEventRecord(ev[2 * open[k] + 1], s);
+    }
+}
+
+void ViewKernelTimer::harvest() {
+    const uint64_t from = next > (uint64_t)kPairs ? std::max(harvested, next - kPairs) : harvested;
+    for (uint64_t i = from; i < next; i++) {
+        const int slot = (int)(i % kPairs);
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev[2 * slot], ev[2 * slot + 1]) == cudaSuccess) {
+            sum[id[slot]] += ms;
+            count[id[slot]]++;
+        }
+    }
+    harvested = next;
+}
+
+ViewKernelTimer::~ViewKernelTimer() {
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
 }
 
 vxr::Tuning shape(const vxr_view* v) {
@@ -397,6 +430,7 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");
     vxr::BatchDev bd = vxr::single_batch(w, k, v->buf, v->cur, point, sh);
     bd.fuse = fuse ? 1 : 0;
+    bd.timer = v->ktimerOn ? v->ktimer : nullptr;
     const int variant = point ? 1 : 0;
     switch (stage) {
     case VXR_STAGE_ALBEDO: vxr::launch_batch_albedo(bd, variant, v->stream); break;
@@ -452,6 +486,7 @@ int vxr_view_wait(vxr_view* v) {
         v->times[s - 1] = ms;
     }
     harvest(v);
+    if (v->ktimer) v->ktimer->harvest();
     uint32_t err = 0;
     CUV(cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost), "read device error flags");
     if (err) {
@@ -738,6 +773,67 @@ extern "C" int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t) {
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
     t->occupancy = (uint32_t)u.occupancy;
     return VXR_OK;
+}
+
+extern "C" int vxr_view_kernel_timing(vxr_view* v, int on) {
+    if (int r = check_view(v, "vxr_view_kernel_timing")) return r;
+    if (on && !v->ktimer) {
+        vxr::ViewKernelTimer* t = new (std::nothrow) vxr::ViewKernelTimer();
+        if (!t) return set_error(VXR_E_NOMEM, "vxr_view_kernel_timing: out of host memory");
+        t->ev.assign(2 * vxr::ViewKernelTimer::kPairs, nullptr);
+        t->id.assign(vxr::ViewKernelTimer::kPairs, 0);
+        for (cudaEvent_t& e : t->ev) {
+            const cudaError_t ce = cudaEventCreate(&e);
+            if (ce != cudaSuccess) {
+                delete t;
+                return set_error(VXR_E_CUDA, std::string("vxr_view_kernel_timing: ") + cudaGetErrorString(ce));
+            }
+        }
+        v->ktimer = t;
+    }
+    v->ktimerOn = on != 0;
+    return VXR_OK;
+}
+
+extern "C" int vxr_view_kernel_stats(vxr_view* v, double sum_ms[VXR_KERNEL_COUNT], uint32_t count[VXR_KERNEL_COUNT],
+                                     int reset) {
+    if (int r = check_view(v, "vxr_view_kernel_stats")) return r;
+    VXR_CHECK_ARG(sum_ms && count, "vxr_view_kernel_stats: null argument");
+    CUV(cudaStreamSynchronize(v->stream), "vxr_view_kernel_stats");
+    for (int i = 0; i < VXR_KERNEL_COUNT; i++) {
+        sum_ms[i] = 0.0;
+        count[i] = 0;
+    }
+    if (!v->ktimer) return VXR_OK;
+    v->ktimer->harvest();
+    for (int i = 0; i < VXR_KERNEL_COUNT; i++) {
+        sum_ms[i] = v->ktimer->sum[i];
+        count[i] = v->ktimer->count[i];
+        if (reset) {
+            v->ktimer->sum[i] = 0.0;
+            v->ktimer->count[i] = 0;
+        }
+    }
+    return VXR_OK;
+}
+
+extern "C" int vxr_view_work_counts(vxr_view* v, uint32_t counts[3]) {
+    if (int r = check_view(v, "vxr_view_work_counts")) return r;
+    VXR_CHECK_ARG(counts, "vxr_view_work_counts: null argument");
+    uint32_t c[vxr::kCounters];
+    CUV(cudaMemcpyAsync(c, v->buf.counters, sizeof(c), cudaMemcpyDeviceToHost, v->stream), "read counters");
+    CUV(cudaStreamSynchronize(v->stream), "vxr_view_work_counts");
+    counts[0] = c[vxr::kCtrHits];
+    counts[1] = c[vxr::kCtrQ1];
+    counts[2] = c[vxr::kCtrQ2];
+    return VXR_OK;
+}
+
+extern "C" const char* vxr_kernel_name(int id) {
+    static const char* names[VXR_KERNEL_COUNT] = {"albedo", "compact_hits", "proposal_infer", "ris_candidates",
+                                                  "shadow_candidates", "temporal", "spatial", "shade_request",
+                                                  "shadow_shading", "shade_finish", "accumulate"};
+    return id >= 0 && id < VXR_KERNEL_COUNT ? names[id] : "";
 }
 
 extern "C" int vxr_view_stage_stats(vxr_view* v, double sum_ms[5], uint32_t count[5], int reset) {

@@ -25,6 +25,20 @@ struct DeviceWorld {
     int device = -1;
 };
 struct Proposal;   // learned candidate proposal state (proposal_api.cu)
+// Per-kernel CUDA-event timing of one view: event pairs from a ring, harvested after a
+// wait into per-kernel sums (runtime.cu).
+struct ViewKernelTimer : KernelTimer {
+    static constexpr int kPairs = 4096;
+    std::vector<cudaEvent_t> ev;          // 2 * kPairs
+    std::vector<int> id;                  // kernel of each pair
+    uint64_t next = 0, harvested = 0;
+    int open[K_COUNT];                    // pair index of an open mark per kernel
+    double sum[K_COUNT] = {};
+    uint32_t count[K_COUNT] = {};
+    void mark(int k, bool end, cudaStream_t s) override;
+    void harvest();
+    ~ViewKernelTimer() override;
+};
 void destroy_proposal(Proposal* p);
 }  // namespace vxr
 
@@ -49,6 +63,8 @@ struct vxr_view {
     uint32_t sum64Count = 0;
     double* errOut = nullptr;                         // [mse sum, mae sum]
     vxr::Proposal* prop = nullptr;                    // learned proposal (optional)
+    vxr::ViewKernelTimer* ktimer = nullptr;           // per-kernel timing (vxr_view_kernel_timing)
+    bool ktimerOn = false;
     bool useProposal = false;
     bool frameOpen = false;
     vxr_frame_consts k{};

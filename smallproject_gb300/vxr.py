@@ -143,10 +143,13 @@ _SIGS = {
     "vxr_batch_destroy": [_P], "vxr_batch_set_tuning": [_P, C.POINTER(Tuning)],
     "vxr_default_tuning": [C.POINTER(Tuning)], "vxr_view_set_tuning": [_P, C.POINTER(Tuning)],
     "vxr_view_get_tuning": [_P, C.POINTER(Tuning)],
+    "vxr_view_kernel_timing": [_P, C.c_int],
+    "vxr_view_kernel_stats": [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.c_int],
+    "vxr_kernel_name": [C.c_int], "vxr_view_work_counts": [_P, C.POINTER(C.c_uint32)],
     "vxr_device_info": [C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], "vxr_batch_render": [_P], "vxr_batch_wait": [_P, C.POINTER(C.c_float)],
     "vxr_render_frame_noalloc": [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.POINTER(FrameConsts), _P, _P],
 }
-_RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p}
+_RESTYPES = {"vxr_last_error": C.c_char_p, "vxr_version": C.c_char_p, "vxr_kernel_name": C.c_char_p}
 
 _lib = None
 
@@ -485,6 +488,22 @@ class View:
     def proposal_load(self, path):
         check(self._lib.vxr_view_proposal_load(self.h, str(path).encode()))
 
+    def kernel_timing(self, on=True):
+        check(self._lib.vxr_view_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_stats(self, reset=False):
+        """{kernel name: (summed ms, launches)} since the last reset."""
+        n = KERNEL_COUNT
+        sums, counts = (C.c_double * n)(), (C.c_uint32 * n)()
+        check(self._lib.vxr_view_kernel_stats(self.h, sums, counts, 1 if reset else 0))
+        return {self._lib.vxr_kernel_name(i).decode(): (sums[i], counts[i]) for i in range(n)}
+
+    def work_counts(self):
+        """(hit pixels, candidate shadow rays, shading shadow rays) of the last frame."""
+        c = (C.c_uint32 * 3)()
+        check(self._lib.vxr_view_work_counts(self.h, c))
+        return tuple(c)
+
     def set_tuning(self, t):
         check(self._lib.vxr_view_set_tuning(self.h, C.byref(t)))
 
@@ -506,6 +525,7 @@ class View:
         check(self._lib.vxr_view_render_to_host(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3)))
 
 
+KERNEL_COUNT = 11
 BATCH_MAX_VIEWS = 16
 BATCH_GRAPH = 1
 
