@@ -213,7 +213,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
     table = {}
     for method in ("plain", "learned"):
         for c in CANDS:
-            ms_l, mse_l = [], []
+            ms_l, mse_l, kms_l = [], [], {}
             for seed in range(args.mse_seeds):
                 v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, num_candidates=c, rng_seed=1000 + seed))
                 v.set_tuning(tuning)
@@ -225,18 +225,24 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
                 for _ in range(8):
                     v.render()
                 v.wait()
+                v.kernel_timing(True)
                 v.timer_begin()
                 for _ in range(8):
                     v.render()
                 ms_l.append(v.timer_end() / 8)
                 v.wait()
+                v.kernel_timing(False)
+                ks = v.kernel_stats(reset=True)
+                for k in ("proposal_infer", "ris_candidates"):
+                    kms_l.setdefault(k, []).append(ks[k][0] / max(ks[k][1], 1))
                 for _ in range(args.mse_frames):
                     v.render()
                     mse_l.append(v.error_vs(ref, 0)[0])
                 v.close()
             table[f"{method}_{c}"] = {"method": method, "candidates": c, "ms": float(np.median(ms_l)),
                                       "mse": float(np.mean(mse_l)), "mse_median": float(np.median(mse_l)),
-                                      "frames": len(mse_l)}
+                                      "frames": len(mse_l),
+                                      "kernel_ms": {k: float(np.median(v)) for k, v in kms_l.items()}}
     ref.close()
     p32 = table["plain_32"]
     eq = None

@@ -328,16 +328,17 @@ int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[
  * Replaces the uniform source pdf of RIS (GenerateLightCandidate, tools.cl:593-598) by a
  * small network over the world's emitter clusters (vxr_world_cluster_lights): input =
  * 2-level hash-grid encoding of the shading point + one-hot voxel side, 3 hidden ReLU
- * layers, softmax over K clusters. A candidate draws cluster c from
- * q(c) = (1 - epsilon) softmax_c + epsilon / K, then an emitter of c uniformly, and RIS
- * weighs it with p_hat / (q(c) / |c|). Inference: BF16 tensor cores, FP32 accumulation.
+ * layers, softmax over K clusters. A candidate is, with probability epsilon, an emitter
+ * drawn uniformly, else an emitter drawn uniformly from a cluster c ~ softmax; RIS weighs
+ * it with p_hat / p_src, p_src(e) = (1 - epsilon) softmax_c(e) / |c(e)| + epsilon / N.
+ * Inference: BF16 tensor cores, FP32 accumulation.
  * Training: online, weighted cross-entropy towards the cluster of each final reservoir's
  * emitter (weight W * p_hat), Adam; FP32 kernels. */
 typedef struct vxr_proposal_desc {
     uint32_t hidden;          /* hidden width (64) */
     uint32_t table_log2;      /* hash-table entries per level, log2 (16) */
     uint32_t res0, res1;      /* grid resolution of the two levels over the 1024^3 map (32, 128) */
-    float    epsilon;         /* weight of the uniform cluster mixture (0.1) */
+    float    epsilon;         /* weight of the uniform (defensive) emitter mixture (0.1) */
     float    learning_rate;   /* Adam (1e-3) */
     uint32_t batch;           /* training samples per step (65536) */
     uint32_t seed;            /* parameter initialisation */

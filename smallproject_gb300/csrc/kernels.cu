@@ -334,9 +334,8 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
 // Over the hit list. Ends with AdjustWeight(res, res.pHat) (implied by the stored
 // sumW, pHat, M) and a shadow-ray request for the selected sample when sumW > 0 (when
 // sumW == 0 the discard of ris.cl:79-80 changes nothing).
-// LEARNED: the light index comes from the learned proposal instead of
-// GenerateLightCandidate (drawn by the inference kernel: cluster c with probability q(c),
-// then a member of c uniformly); its source pdf p = q(c) / |c| replaces 1 / N.
+// LEARNED: the light index and its source pdf p come from the learned proposal (drawn
+// by the inference kernel) instead of GenerateLightCandidate's uniform 1 / N.
 template <bool POINT, bool LEARNED>
 __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, uint32_t e, uint32_t i, uint32_t j) {
     const World w = V->w;
@@ -359,7 +358,7 @@ __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, u
         int li;
         float p = puni;
         if (LEARNED) {
-            const uint2 cq = __ldg(V->ll.cand + (size_t)j * prop::kMaxCand + c);
+            const uint2 cq = __ldg(V->ll.cand + (size_t)c * V->ll.stride + j);
             li = (int)cq.x;
             p = __uint_as_float(cq.y);
         } else {
@@ -773,6 +772,7 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
         if (learned) {
             BatchDev lb = bd;
             lb.one.ll.cand = learned->cand;
+            lb.one.ll.stride = (uint32_t)n;
             prop::InferArgs ia = learned->infer;
             ia.k = bd.one.k;
             ia.vd = bd.one.b.vd[bd.one.cur];
@@ -782,6 +782,9 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
             ia.cand = learned->cand;
             ia.clOff = learned->clOff;
             ia.clMembers = learned->clMembers;
+            ia.lightCluster = learned->lightCluster;
+            ia.nlights = bd.one.k.nlights;
+            ia.candStride = (uint32_t)n;
             ia.samples = nullptr;
             ia.probs = nullptr;
             if (bd.one.k.ncand > 0) {

@@ -39,7 +39,8 @@ enum : int {
 
 // learned-proposal candidates read by the candidate loop (null = uniform source pdf)
 struct LearnedLists {
-    const uint2* cand = nullptr;          // [hit][kMaxCand] (emitter, bits(p_src))
+    const uint2* cand = nullptr;          // [candidate][stride] (emitter, bits(p_src)), hit j at column j
+    uint32_t stride = 0;
 };
 
 // Everything a kernel needs about one view of a batch.
@@ -106,9 +107,10 @@ void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s);
 // learned proposal inputs of the candidate stage
 struct LearnedHook {
     prop::InferArgs infer;      // dims, layout, params, BF16 weights
-    uint2* cand;                // [pixels][kMaxCand] scratch for drawn clusters
+    uint2* cand;                // [kMaxCand][pixels] scratch for the drawn candidates
     const uint32_t* clOff;      // cluster CSR on the device
     const uint32_t* clMembers;
+    const uint32_t* lightCluster;
 };
 
 // A batch of one view over its own list buffers.

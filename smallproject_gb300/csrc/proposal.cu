@@ -4,10 +4,11 @@
 // hash-grid encoding is built in shared memory, the MLP runs on the tensor cores with
 // BF16 mma.sync.m16n8k16 (FP32 accumulation, hidden layers kept in registers: the
 // accumulator fragment of one layer is the A fragment of the next), the K logits land
-// in shared memory as FP16, and every lane draws its pixel's candidates: a cluster from
-// q = (1 - eps) softmax + eps / K with a two-level (16 groups) inverse CDF, then one of
-// its emitters uniformly. Output per pixel: kMaxCand (emitter, p_src = q(c) / |c|) pairs
-// that the candidate kernel consumes.
+// in shared memory as FP16, and every lane draws its pixel's candidates from
+// p_src(e) = (1 - eps) softmax(c(e)) / |c(e)| + eps / N: with probability eps an emitter
+// uniformly, else a cluster through a two-level (16 groups) inverse CDF and one of its
+// emitters uniformly. Output: (emitter, p_src) per candidate, candidate-major so that
+// both this kernel's stores and the candidate kernel's loads are coalesced.
 //
 // Training (FP32 CUDA cores): batch gather from the reservoirs, encoding, a tiled
 // strided GEMM with fused epilogues for every forward / backward product, softmax
@@ -98,59 +99,81 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// one hidden layer on register fragments: out = relu(in * W^T + b); in/out as A fragments
-// act[mt][kt][4] for 2 m-tiles (32 rows) and H/16 k-tiles
+// one hidden layer on register fragments: out = relu(in * W^T + b); in/out are the A
+// fragments of one m-tile (16 rows), H/16 k-tiles
 template <int H>
-__device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][H / 16][4], uint32_t (&out)[2][H / 16][4],
+__device__ __forceinline__ void hidden_layer(const uint32_t (&in)[H / 16][4], uint32_t (&out)[H / 16][4],
                                              const __nv_bfloat16* Ws, int ldw, const float* bs, int g, int t) {
-    float c[2][H / 8][4];
+    float c[H / 8][4];
 #pragma unroll
     for (int nt = 0; nt < H / 8; nt++) {
         const float b0 = bs[nt * 8 + 2 * t], b1 = bs[nt * 8 + 2 * t + 1];
-#pragma unroll
-        for (int mt = 0; mt < 2; mt++) { c[mt][nt][0] = b0; c[mt][nt][1] = b1; c[mt][nt][2] = b0; c[mt][nt][3] = b1; }
+        c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
     }
 #pragma unroll
     for (int kt = 0; kt < H / 16; kt++) {
 #pragma unroll
         for (int nt = 0; nt < H / 8; nt++) {
             const __nv_bfloat16* row = Ws + (size_t)(nt * 8 + g) * ldw + kt * 16 + 2 * t;
-            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
-            mma16816(c[0][nt], in[0][kt], b0, b1);
-            mma16816(c[1][nt], in[1][kt], b0, b1);
+            mma16816(c[nt], in[kt], *reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8));
         }
     }
 #pragma unroll
-    for (int mt = 0; mt < 2; mt++)
+    for (int kt = 0; kt < H / 16; kt++) {
+        out[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+        out[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+        out[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+        out[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+    }
+}
+
+// the 8 hash-grid features of one level at point p (trilinear over the cell's corners)
+__device__ __forceinline__ void level_features(const float* __restrict__ enc, const Dims& d, float px, float py, float pz,
+                                               int l, float* a) {
+    const uint32_t mask = (1u << d.tableLog2) - 1u;
+    const int R = l == 0 ? d.res0 : d.res1;
+    const float s = (float)R * (1.0f / 1024.0f);
+    const float ux = fminf(fmaxf(px * s, 0.0f), (float)R), uy = fminf(fmaxf(py * s, 0.0f), (float)R),
+                uz = fminf(fmaxf(pz * s, 0.0f), (float)R);
+    const int ix = min((int)ux, R - 1), iy = min((int)uy, R - 1), iz = min((int)uz, R - 1);
+    const float fx = ux - (float)ix, fy = uy - (float)iy, fz = uz - (float)iz;
 #pragma unroll
-        for (int kt = 0; kt < H / 16; kt++) {
-            out[mt][kt][0] = pack_bf16(fmaxf(c[mt][2 * kt][0], 0.f), fmaxf(c[mt][2 * kt][1], 0.f));
-            out[mt][kt][1] = pack_bf16(fmaxf(c[mt][2 * kt][2], 0.f), fmaxf(c[mt][2 * kt][3], 0.f));
-            out[mt][kt][2] = pack_bf16(fmaxf(c[mt][2 * kt + 1][0], 0.f), fmaxf(c[mt][2 * kt + 1][1], 0.f));
-            out[mt][kt][3] = pack_bf16(fmaxf(c[mt][2 * kt + 1][2], 0.f), fmaxf(c[mt][2 * kt + 1][3], 0.f));
-        }
+    for (int f = 0; f < 8; f++) a[f] = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
+        const uint32_t idx = (uint32_t)l * (mask + 1u) + grid_hash((uint32_t)(ix + ox), (uint32_t)(iy + oy), (uint32_t)(iz + oz), mask);
+        const float w = (ox ? fx : 1.0f - fx) * (oy ? fy : 1.0f - fy) * (oz ? fz : 1.0f - fz);
+        const float4* e = reinterpret_cast<const float4*>(enc + (size_t)idx * kFeat);
+        const float4 e0 = __ldg(e), e1 = __ldg(e + 1);
+        a[0] += w * e0.x; a[1] += w * e0.y; a[2] += w * e0.z; a[3] += w * e0.w;
+        a[4] += w * e1.x; a[5] += w * e1.y; a[6] += w * e1.z; a[7] += w * e1.w;
+    }
 }
 
 // ---- inference --------------------------------------------------------------------------
-// Shared memory (per CTA of 8 warps): W1 [H][kIn+8], W2,W3 [H][H+8], W4 [K][H+8] (BF16,
-// rows padded against bank conflicts), biases (FP32), per warp X [32][kIn+8] (BF16) and
-// logits [32][K+2] (FP16, then the sampling tables), cluster offsets [K+1].
+// A warp handles 16 pixels (one m16 tile): two lanes per pixel (lane = half * 16 + row)
+// split the encoding (one hash-grid level each), the softmax tables (8 groups each) and
+// the candidates (every other one each). 16 pixels per warp keep the MLP within 128
+// registers per thread, so 16 warps share one copy of the weights per SM.
+// Shared memory: W1 [H][kIn+8], W2,W3 [H][H+8], W4 [K][H+8] (BF16, rows padded against
+// bank conflicts), biases (FP32), cluster offsets [K+1], then per warp X [16][kIn+8]
+// (BF16) and logits [16][K+2] (FP16, then the sampling tables).
 template <int H>
-__global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
+__global__ void __launch_bounds__(512) infer_kernel(InferArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Dims d = a.dims;
     const int K = d.K;
     const int ld1 = kIn + 8, ldh = H + 8, ldl = K + 2, ldx = kIn + 8;
+    const int nwarps = blockDim.x >> 5;
     __nv_bfloat16* W1s = reinterpret_cast<__nv_bfloat16*>(smem);
     __nv_bfloat16* W2s = W1s + H * ld1;
     __nv_bfloat16* W3s = W2s + H * ldh;
     __nv_bfloat16* W4s = W3s + H * ldh;
     float* bs = reinterpret_cast<float*>(W4s + (size_t)K * ldh);           // b1 | b2 | b3 | b4
-    __nv_bfloat16* Xall = reinterpret_cast<__nv_bfloat16*>(bs + 3 * H + K);
-    __half* Lall = reinterpret_cast<__half*>(Xall + 8 * 32 * ldx);
-    uint32_t* offs = reinterpret_cast<uint32_t*>(Lall + (size_t)8 * 32 * ldl);   // cluster offsets [K + 1]
-    // weights -> shared memory
+    uint32_t* offs = reinterpret_cast<uint32_t*>(bs + 3 * H + K);          // cluster offsets [K + 1]
+    __nv_bfloat16* Xall = reinterpret_cast<__nv_bfloat16*>(offs + ((K + 1 + 3) & ~3));
+    __half* Lall = reinterpret_cast<__half*>(Xall + (size_t)nwarps * 16 * ldx);
     {
         const __nv_bfloat16* wg = a.wbf;   // W1 [H][kIn] | W2 [H][H] | W3 [H][H] | W4 [K][H]
         for (int e = threadIdx.x; e < H * kIn; e += blockDim.x) W1s[(e / kIn) * ld1 + e % kIn] = wg[e];
@@ -172,12 +195,14 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __nv_bfloat16* Xs = Xall + warp * 32 * ldx;
-    __half* Ls = Lall + (size_t)warp * 32 * ldl;
+    const int r = lane & 15, half = lane >> 4;
+    __nv_bfloat16* Xs = Xall + (size_t)warp * 16 * ldx;
+    __half* Ls = Lall + (size_t)warp * 16 * ldl;
     const float* enc = a.params + a.L.enc;
     const uint32_t n = a.count ? *a.count : a.n;
-    for (uint32_t base = (blockIdx.x * 8 + warp) * 32; base < n; base += gridDim.x * 8 * 32) {
-        const uint32_t j = base + lane;
+    const int gs = K / 16;
+    for (uint32_t base = (blockIdx.x * nwarps + warp) * 16; base < n; base += gridDim.x * nwarps * 16) {
+        const uint32_t j = base + r;
         const bool valid = j < n;
         float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
         uint32_t pix = 0;
@@ -196,92 +221,93 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
                                   __uint_as_float(side_code(side, ns)));
             }
         }
-        float xr[kIn];
-        input_row(enc, d, pin, xr);
+        // input row: this lane's hash-grid level; the first half also the one-hot side
+        {
+            float f[8];
+            level_features(enc, d, pin.x, pin.y, pin.z, half, f);
+            __nv_bfloat16* xr = Xs + r * ldx;
 #pragma unroll
-        for (int f = 0; f < kIn; f += 2)
-            *reinterpret_cast<uint32_t*>(Xs + lane * ldx + f) = valid ? pack_bf16(xr[f], xr[f + 1]) : 0u;
+            for (int q = 0; q < 8; q += 2)
+                *reinterpret_cast<uint32_t*>(xr + half * 8 + q) = valid ? pack_bf16(f[q], f[q + 1]) : 0u;
+            if (half == 0) {
+                const uint32_t code = __float_as_uint(pin.w);
+#pragma unroll
+                for (int q = 16; q < kIn; q += 2)
+                    *reinterpret_cast<uint32_t*>(xr + q) =
+                        valid ? pack_bf16(code == (uint32_t)(q - 16) ? 1.f : 0.f, code == (uint32_t)(q - 15) ? 1.f : 0.f) : 0u;
+            }
+        }
         __syncwarp();
         // layer 1 (kIn = 32 -> H) from shared memory
-        uint32_t act[2][H / 16][4], act2[2][H / 16][4];
+        uint32_t act[H / 16][4], act2[H / 16][4];
         {
-            uint32_t xa[2][2][4];
+            uint32_t xa[2][4];
 #pragma unroll
-            for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-                for (int kt = 0; kt < 2; kt++) {
-                    const __nv_bfloat16* r0 = Xs + (mt * 16 + g) * ldx + kt * 16 + 2 * t;
-                    const __nv_bfloat16* r1 = r0 + 8 * ldx;
-                    xa[mt][kt][0] = *reinterpret_cast<const uint32_t*>(r0);
-                    xa[mt][kt][1] = *reinterpret_cast<const uint32_t*>(r1);
-                    xa[mt][kt][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
-                    xa[mt][kt][3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
-                }
-            float c[2][H / 8][4];
+            for (int kt = 0; kt < 2; kt++) {
+                const __nv_bfloat16* r0 = Xs + g * ldx + kt * 16 + 2 * t;
+                const __nv_bfloat16* r1 = r0 + 8 * ldx;
+                xa[kt][0] = *reinterpret_cast<const uint32_t*>(r0);
+                xa[kt][1] = *reinterpret_cast<const uint32_t*>(r1);
+                xa[kt][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+                xa[kt][3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+            }
+            float c[H / 8][4];
 #pragma unroll
             for (int nt = 0; nt < H / 8; nt++) {
                 const float b0 = bs[nt * 8 + 2 * t], b1 = bs[nt * 8 + 2 * t + 1];
-#pragma unroll
-                for (int mt = 0; mt < 2; mt++) { c[mt][nt][0] = b0; c[mt][nt][1] = b1; c[mt][nt][2] = b0; c[mt][nt][3] = b1; }
+                c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
             }
 #pragma unroll
             for (int kt = 0; kt < 2; kt++)
 #pragma unroll
                 for (int nt = 0; nt < H / 8; nt++) {
                     const __nv_bfloat16* row = W1s + (nt * 8 + g) * ld1 + kt * 16 + 2 * t;
-                    const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
-                    const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
-                    mma16816(c[0][nt], xa[0][kt], b0, b1);
-                    mma16816(c[1][nt], xa[1][kt], b0, b1);
+                    mma16816(c[nt], xa[kt], *reinterpret_cast<const uint32_t*>(row),
+                             *reinterpret_cast<const uint32_t*>(row + 8));
                 }
 #pragma unroll
-            for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-                for (int kt = 0; kt < H / 16; kt++) {
-                    act[mt][kt][0] = pack_bf16(fmaxf(c[mt][2 * kt][0], 0.f), fmaxf(c[mt][2 * kt][1], 0.f));
-                    act[mt][kt][1] = pack_bf16(fmaxf(c[mt][2 * kt][2], 0.f), fmaxf(c[mt][2 * kt][3], 0.f));
-                    act[mt][kt][2] = pack_bf16(fmaxf(c[mt][2 * kt + 1][0], 0.f), fmaxf(c[mt][2 * kt + 1][1], 0.f));
-                    act[mt][kt][3] = pack_bf16(fmaxf(c[mt][2 * kt + 1][2], 0.f), fmaxf(c[mt][2 * kt + 1][3], 0.f));
-                }
+            for (int kt = 0; kt < H / 16; kt++) {
+                act[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+                act[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+                act[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+                act[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+            }
         }
         hidden_layer<H>(act, act2, W2s, ldh, bs + H, g, t);
         hidden_layer<H>(act2, act, W3s, ldh, bs + 2 * H, g, t);
         // output layer: K logits, 8 columns at a time, to shared memory as FP16
         for (int nt = 0; nt < K / 8; nt++) {
             const float b0 = bs[3 * H + nt * 8 + 2 * t], b1 = bs[3 * H + nt * 8 + 2 * t + 1];
-            float c0[4] = {b0, b1, b0, b1}, c1[4] = {b0, b1, b0, b1};
+            float c0[4] = {b0, b1, b0, b1};
 #pragma unroll
             for (int kt = 0; kt < H / 16; kt++) {
                 const __nv_bfloat16* row = W4s + (size_t)(nt * 8 + g) * ldh + kt * 16 + 2 * t;
-                const uint32_t bb0 = *reinterpret_cast<const uint32_t*>(row);
-                const uint32_t bb1 = *reinterpret_cast<const uint32_t*>(row + 8);
-                mma16816(c0, act[0][kt], bb0, bb1);
-                mma16816(c1, act[1][kt], bb0, bb1);
+                mma16816(c0, act[kt], *reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8));
             }
             const int col = nt * 8 + 2 * t;
             *reinterpret_cast<__half2*>(Ls + g * ldl + col) = __floats2half2_rn(c0[0], c0[1]);
             *reinterpret_cast<__half2*>(Ls + (g + 8) * ldl + col) = __floats2half2_rn(c0[2], c0[3]);
-            *reinterpret_cast<__half2*>(Ls + (16 + g) * ldl + col) = __floats2half2_rn(c1[0], c1[1]);
-            *reinterpret_cast<__half2*>(Ls + (24 + g) * ldl + col) = __floats2half2_rn(c1[2], c1[3]);
         }
         __syncwarp();
-        if (valid) {
-            // Softmax of the lane's row, stored for sampling as 16-bit fixed-point prefix sums
-            // inside each group of K/16 clusters (fraction of the group total, last = 65535),
-            // overwriting the logits; FP32 prefix sums P over the 16 group totals. Every
-            // probability the sampler reports comes from these stored numbers: group q has
-            // weight P[q] - P[q-1], cluster c inside it (fp[c] - fp[c-1]) / 65535 of that, so
-            // the pdf returned with a sample is the pdf it was drawn with (up to FP32
-            // rounding) and small clusters keep a resolution of 1/65535 of their group.
-            __half* row = Ls + lane * ldl;
-            uint16_t* fp = reinterpret_cast<uint16_t*>(row);
-            const int gs = K / 16;
-            float mx = -INFINITY;
-            for (int c = 0; c < K; c++) mx = fmaxf(mx, __half2float(row[c]));
-            float P[16];
-            float Z = 0.0f;
+        // Softmax of row r, stored for sampling as 16-bit fixed-point prefix sums inside
+        // each group of K/16 clusters (fraction of the group total, last = 65535),
+        // overwriting the logits; FP32 prefix sums P over the 16 group totals. Every
+        // probability the sampler reports comes from these stored numbers: group q has
+        // weight P[q] - P[q-1], cluster c inside it (fp[c] - fp[c-1]) / 65535 of that, so
+        // the pdf returned with a sample is the pdf it was drawn with (up to FP32
+        // rounding) and small clusters keep a resolution of 1/65535 of their group.
+        // The two lanes of the row take 8 groups each.
+        __half* row = Ls + r * ldl;
+        uint16_t* fp = reinterpret_cast<uint16_t*>(row);
+        float mx = -INFINITY;
+        for (int c = half * (K / 2); c < (half + 1) * (K / 2); c++) mx = fmaxf(mx, __half2float(row[c]));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+        float Pl[8];   // prefix sums over this lane's 8 groups
+        {
+            float Zl = 0.0f;
 #pragma unroll
-            for (int q = 0; q < 16; q++) {
+            for (int q8 = 0; q8 < 8; q8++) {
+                const int q = half * 8 + q8;
                 float T = 0.0f;
                 for (int c = q * gs; c < (q + 1) * gs; c++) {
                     const __half h = __float2half_rn(__expf(__half2float(row[c]) - mx));
@@ -294,35 +320,55 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
                     acc += __half2float(row[c]);
                     fp[c] = c == (q + 1) * gs - 1 ? (uint16_t)65535u : (uint16_t)min((uint32_t)(acc * sc), 65535u);
                 }
-                Z += T;
-                P[q] = Z;
+                Zl += T;
+                Pl[q8] = Zl;
             }
-            const float invZ = 1.0f / Z;
-            // fraction of its group held by cluster c
-            auto frac = [&](int c) {
-                const uint32_t hi = fp[c], lo = (c % gs) ? fp[c - 1] : 0u;
-                return (float)(hi - lo) * (1.0f / 65535.0f);
-            };
+        }
+        float P[16];
+        {
+            float lowZ = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const float o = __shfl_xor_sync(0xffffffffu, Pl[i], 16);
+                P[i] = half ? o : Pl[i];
+                P[8 + i] = half ? Pl[i] : o;   // high half, relative to its own start
+            }
+            lowZ = P[7];
+#pragma unroll
+            for (int i = 8; i < 16; i++) P[i] += lowZ;
+        }
+        __syncwarp();
+        const float Z = P[15], invZ = 1.0f / Z;
+        // fraction of its group held by cluster c
+        auto frac = [&](int c) {
+            const uint32_t hi = fp[c], lo = (c % gs) ? fp[c - 1] : 0u;
+            return (float)(hi - lo) * (1.0f / 65535.0f);
+        };
+        if (valid) {
             if (a.probs) {
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
+                    if ((q >> 3) != half) continue;
                     const float gw = q ? P[q] - P[q - 1] : P[0];
                     for (int c = q * gs; c < (q + 1) * gs; c++) a.probs[(size_t)j * K + c] = (gw * frac(c)) * invZ;
                 }
             } else {
-                uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
-                const float eps = d.eps, invK = 1.0f / (float)K;
-                uint2* out = a.cand + (size_t)j * kMaxCand;
-                // unrolled so that the member loads of several candidates are in flight together
+                uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u + (uint32_t)half * 0x68E31DA4u);
+                const float eps = d.eps, invN = 1.0f / (float)a.nlights;
+                uint2* out = a.cand + j;
+                // unrolled so that the emitter loads of several candidates are in flight together
 #pragma unroll 4
-                for (uint32_t m = 0; m < a.ncand; m++) {
+                for (uint32_t m = (uint32_t)half; m < a.ncand; m += 2) {
                     const float u = dev::rnd(s);
                     const float v = dev::rnd(s);
                     const float w = dev::rnd(s);
                     int c;
+                    uint32_t e;
                     float gw;   // weight of the chosen cluster's group
                     if (u < eps) {
-                        c = min((int)(v * (float)K), K - 1);
+                        // defensive part: an emitter uniformly
+                        e = min((uint32_t)(v * (float)a.nlights), a.nlights - 1u);
+                        c = (int)__ldg(a.lightCluster + e);
                         const int q = c / gs;
                         float lo = 0.0f, hi = P[0];
 #pragma unroll
@@ -333,23 +379,25 @@ __global__ void __launch_bounds__(256) infer_kernel(InferArgs a) {
                         // group: count of prefix sums <= target (branch-free)
                         const float target = v * Z;
                         int q = 0;
-                        float base = 0.0f, top = P[0];
+                        float lo = 0.0f, hi = P[0];
 #pragma unroll
                         for (int i = 0; i < 15; i++)
-                            if (target >= P[i]) { q = i + 1; base = P[i]; top = P[i + 1]; }
+                            if (target >= P[i]) { q = i + 1; lo = P[i]; hi = P[i + 1]; }
                         // cluster inside the group: count of in-group prefix fractions <= the
                         // target's fraction of the group
-                        gw = top - base;
-                        const float x = gw > 0.0f ? (target - base) * (65535.0f / gw) : 0.0f;
+                        gw = hi - lo;
+                        const float x = gw > 0.0f ? (target - lo) * (65535.0f / gw) : 0.0f;
                         int in = 0;
                         for (int i = 0; i < gs - 1; i++) in += x >= (float)fp[q * gs + i] ? 1 : 0;
                         c = q * gs + in;
+                        // an emitter of cluster c, uniformly
+                        const uint32_t off = offs[c], sz = offs[c + 1] - off;
+                        e = __ldg(a.clMembers + off + min((uint32_t)(w * (float)sz), sz - 1u));
                     }
-                    const float qc = (1.0f - eps) * ((gw * frac(c)) * invZ) + eps * invK;
-                    // an emitter of cluster c, uniformly: p_src = q(c) / |c|
-                    const uint32_t off = offs[c], sz = offs[c + 1] - off;
-                    const uint32_t mi = min((uint32_t)(w * (float)sz), sz - 1u);
-                    out[m] = make_uint2(__ldg(a.clMembers + off + mi), __float_as_uint(qc / (float)sz));
+                    // p_src(e) = (1 - eps) softmax(c(e)) / |c(e)| + eps / N
+                    const float sz = (float)(offs[c + 1] - offs[c]);
+                    const float pe = (1.0f - eps) * (((gw * frac(c)) * invZ) / sz) + eps * invN;
+                    out[(size_t)m * a.candStride] = make_uint2(e, __float_as_uint(pe));
                 }
             }
         }
@@ -563,22 +611,33 @@ static int sms() {
     return n > 0 ? n : 1;
 }
 
-size_t infer_smem_bytes(const Dims& d) {
+static size_t infer_fixed_bytes(const Dims& d) {
     const int H = d.H, K = d.K;
     return (size_t)H * (kIn + 8) * 2 + 2 * (size_t)H * (H + 8) * 2 + (size_t)K * (H + 8) * 2 + (3 * H + K) * 4 +
-           8 * 32 * (kIn + 8) * 2 + 8 * 32 * (size_t)(K + 2) * 2 + (size_t)(K + 1) * 4;
+           (size_t)((K + 1 + 3) & ~3) * 4;
+}
+static size_t infer_warp_bytes(const Dims& d) { return 16 * (kIn + 8) * 2 + 16 * (size_t)(d.K + 2) * 2; }
+// warps per block: as many as the shared memory holds, at most 16
+static int infer_warps(const Dims& d) {
+    const size_t fixed = infer_fixed_bytes(d), per = infer_warp_bytes(d), cap = 227 * 1024;
+    if (fixed + per > cap) return 0;
+    return (int)std::min<size_t>(16, (cap - fixed) / per);
 }
 
+size_t infer_smem_bytes(const Dims& d) { return infer_fixed_bytes(d) + (size_t)std::max(infer_warps(d), 1) * infer_warp_bytes(d); }
+
 bool infer_supported(const Dims& d) {
-    return d.H == 64 && d.K >= 16 && d.K % 16 == 0 && d.K <= 1024 && infer_smem_bytes(d) <= 227 * 1024;
+    return d.H == 64 && d.K >= 16 && d.K % 16 == 0 && d.K <= 1024 && infer_warps(d) >= 1;
 }
 
 cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s) {
-    const size_t sm = infer_smem_bytes(a.dims);
+    const int nw = infer_warps(a.dims);
+    const size_t sm = infer_fixed_bytes(a.dims) + (size_t)nw * infer_warp_bytes(a.dims);
     cudaError_t e = cudaFuncSetAttribute(infer_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((max_items + 255) / 256, (uint32_t)sms() * 2));
-    infer_kernel<64><<<blocks, 256, sm, s>>>(a);
+    const uint32_t per = (uint32_t)nw * 16;
+    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((max_items + per - 1) / per, (uint32_t)sms()));
+    infer_kernel<64><<<blocks, nw * 32, sm, s>>>(a);
     return cudaGetLastError();
 }
 

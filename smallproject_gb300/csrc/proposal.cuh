@@ -2,10 +2,12 @@
 //
 // A small network replaces the uniform source pdf of RIS (GenerateLightCandidate,
 // tools.cl:593-598, p = 1/N): given the shading point and its voxel side it predicts a
-// distribution over K spatial emitter clusters. Sampling: cluster c ~ q, then an emitter
-// uniformly inside c, with
-//   q(c) = (1 - eps) * softmax(z)_c + eps / K,        p_src(e) = q(c(e)) / |c(e)|,
-// so every emitter keeps p_src > 0 and the RIS weight p_hat / p_src stays consistent.
+// distribution over K spatial emitter clusters. Sampling: with probability eps an emitter
+// uniformly (the defensive part), else cluster c ~ softmax(z) and an emitter uniformly
+// inside c, so
+//   p_src(e) = (1 - eps) * softmax(z)_c(e) / |c(e)| + eps / N,
+// every emitter keeps p_src >= eps / N (RIS weights at most 1/eps times the uniform
+// method's) and the RIS weight p_hat / p_src stays consistent.
 //
 // Network: input 32 = hash-grid encoding (2 levels x 8 features, trilinear, 2^16-entry
 // tables, spatial hash of Teschner et al. as used by Instant-NGP) + one-hot voxel side

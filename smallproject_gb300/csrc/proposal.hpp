@@ -22,7 +22,10 @@ struct InferArgs {
     uint32_t ncand;                   // candidates per pixel (<= kMaxCand)
     const uint32_t* clOff;            // cluster c = emitters clMembers[clOff[c] .. clOff[c+1])
     const uint32_t* clMembers;
-    uint2* cand;                      // out: [hit][kMaxCand] (emitter, bits(p_src))
+    const uint32_t* lightCluster;     // cluster of every emitter
+    uint32_t nlights;
+    uint32_t candStride;              // hits per candidate row of `cand`
+    uint2* cand;                      // out: [candidate][candStride] (emitter, bits(p_src))
     // sample mode (tests): explicit inputs (x, y, z, bits(side code)) and softmax output
     const float4* samples;
     uint32_t n;

@@ -28,7 +28,7 @@ struct Proposal {
     uint32_t* clMembers = nullptr;
     uint32_t* lightCluster = nullptr;
     uint64_t clusterVersion = 0;
-    uint2* cand = nullptr;         // [pixels][kMaxCand]
+    uint2* cand = nullptr;         // [kMaxCand][pixels]
     // training batch
     uint32_t B = 0;
     float4* samples = nullptr;
@@ -215,6 +215,7 @@ bool learned_hook(vxr_view* v, LearnedHook* h) {
     h->cand = p->cand;
     h->clOff = p->clOff;
     h->clMembers = p->clMembers;
+    h->lightCluster = p->lightCluster;
     return true;
 }
 }  // namespace vxr
