@@ -158,13 +158,14 @@ __device__ __forceinline__ void level_features(const float* __restrict__ enc, co
 // registers per thread, so 16 warps share one copy of the weights per SM.
 // Shared memory: W1 [H][kIn+8], W2,W3 [H][H+8], W4 [K][H+8] (BF16, rows padded against
 // bank conflicts), biases (FP32), cluster offsets [K+1], then per warp X [16][kIn+8]
-// (BF16) and logits [16][K+2] (FP16, then the sampling tables).
+// (BF16; later the rows' group prefix sums [16][16] FP32) and logits [16][K+8] (FP16, then
+// the sampling tables; rows 16-byte aligned).
 template <int H>
-__global__ void __launch_bounds__(512) infer_kernel(InferArgs a) {
+__global__ void __launch_bounds__(512, 1) infer_kernel(InferArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Dims d = a.dims;
     const int K = d.K;
-    const int ld1 = kIn + 8, ldh = H + 8, ldl = K + 2, ldx = kIn + 8;
+    const int ld1 = kIn + 8, ldh = H + 8, ldl = K + 8, ldx = kIn + 8;
     const int nwarps = blockDim.x >> 5;
     __nv_bfloat16* W1s = reinterpret_cast<__nv_bfloat16*>(smem);
     __nv_bfloat16* W2s = W1s + H * ld1;
@@ -289,21 +290,69 @@ __global__ void __launch_bounds__(512) infer_kernel(InferArgs a) {
             *reinterpret_cast<__half2*>(Ls + (g + 8) * ldl + col) = __floats2half2_rn(c0[2], c0[3]);
         }
         __syncwarp();
-        // Softmax of row r, stored for sampling as 16-bit fixed-point prefix sums inside
+        // Softmax of each row, stored for sampling as 16-bit fixed-point prefix sums inside
         // each group of K/16 clusters (fraction of the group total, last = 65535),
-        // overwriting the logits; FP32 prefix sums P over the 16 group totals. Every
+        // overwriting the logits, and FP32 prefix sums Prow over the 16 group totals. Every
         // probability the sampler reports comes from these stored numbers: group q has
         // weight P[q] - P[q-1], cluster c inside it (fp[c] - fp[c-1]) / 65535 of that, so
         // the pdf returned with a sample is the pdf it was drawn with (up to FP32
         // rounding) and small clusters keep a resolution of 1/65535 of their group.
-        // The two lanes of the row take 8 groups each.
-        __half* row = Ls + r * ldl;
-        uint16_t* fp = reinterpret_cast<uint16_t*>(row);
-        float mx = -INFINITY;
-        for (int c = half * (K / 2); c < (half + 1) * (K / 2); c++) mx = fmaxf(mx, __half2float(row[c]));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-        float Pl[8];   // prefix sums over this lane's 8 groups
-        {
+        float* Prow = reinterpret_cast<float*>(Xs);   // X is dead after layer 1
+        if (K == 256) {
+            // one row at a time by the whole warp: lane l holds columns 8l .. 8l+7 (half a
+            // group), 16-byte loads and stores, reductions by shuffles
+            for (int rr = 0; rr < 16; rr++) {
+                uint4* rowv = reinterpret_cast<uint4*>(Ls + rr * ldl) + lane;
+                const uint4 raw = *rowv;
+                const __half2* h2 = reinterpret_cast<const __half2*>(&raw);
+                float z[8];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float2 f = __half22float2(h2[i]);
+                    z[2 * i] = f.x;
+                    z[2 * i + 1] = f.y;
+                }
+                float m = z[0];
+#pragma unroll
+                for (int i = 1; i < 8; i++) m = fmaxf(m, z[i]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+                float pre[8];
+                float acc = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    acc += __expf(z[i] - m);
+                    pre[i] = acc;
+                }
+                const float other = __shfl_xor_sync(0xffffffffu, acc, 1);
+                const float T = (lane & 1) ? other + acc : acc + other;   // same order in both lanes
+                const float base = (lane & 1) ? other : 0.0f;
+                const float sc = T > 0.0f ? 65535.0f / T : 0.0f;
+                uint32_t pk[4];
+#pragma unroll
+                for (int i = 0; i < 8; i += 2) {
+                    const uint32_t lo = min((uint32_t)((base + pre[i]) * sc), 65535u);
+                    const uint32_t hi = (i == 6 && (lane & 1)) ? 65535u : min((uint32_t)((base + pre[i + 1]) * sc), 65535u);
+                    pk[i / 2] = lo | (hi << 16);
+                }
+                *rowv = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                // inclusive scan of the group totals over the even lanes
+                float v = (lane & 1) ? 0.0f : T;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float u = __shfl_up_sync(0xffffffffu, v, o);
+                    if (lane >= o) v += u;
+                }
+                if (!(lane & 1)) Prow[rr * 16 + (lane >> 1)] = v;
+            }
+        } else {
+            // generic K: the two lanes of a row take 8 groups each
+            __half* row = Ls + r * ldl;
+            uint16_t* fpw = reinterpret_cast<uint16_t*>(row);
+            float mx = -INFINITY;
+            for (int c = half * (K / 2); c < (half + 1) * (K / 2); c++) mx = fmaxf(mx, __half2float(row[c]));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+            float Pl[8];
             float Zl = 0.0f;
 #pragma unroll
             for (int q8 = 0; q8 < 8; q8++) {
@@ -318,26 +367,23 @@ __global__ void __launch_bounds__(512) infer_kernel(InferArgs a) {
                 float acc = 0.0f;
                 for (int c = q * gs; c < (q + 1) * gs; c++) {
                     acc += __half2float(row[c]);
-                    fp[c] = c == (q + 1) * gs - 1 ? (uint16_t)65535u : (uint16_t)min((uint32_t)(acc * sc), 65535u);
+                    fpw[c] = c == (q + 1) * gs - 1 ? (uint16_t)65535u : (uint16_t)min((uint32_t)(acc * sc), 65535u);
                 }
                 Zl += T;
                 Pl[q8] = Zl;
             }
-        }
-        float P[16];
-        {
-            float lowZ = 0.0f;
+            const float lowZ = __shfl_xor_sync(0xffffffffu, Pl[7], 16);
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const float o = __shfl_xor_sync(0xffffffffu, Pl[i], 16);
-                P[i] = half ? o : Pl[i];
-                P[8 + i] = half ? Pl[i] : o;   // high half, relative to its own start
-            }
-            lowZ = P[7];
-#pragma unroll
-            for (int i = 8; i < 16; i++) P[i] += lowZ;
+            for (int i = 0; i < 8; i++) Prow[r * 16 + half * 8 + i] = half ? Pl[i] + lowZ : Pl[i];
         }
         __syncwarp();
+        const uint16_t* fp = reinterpret_cast<const uint16_t*>(Ls + r * ldl);
+        float P[16];
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+            const float4 p4 = *reinterpret_cast<const float4*>(Prow + r * 16 + i);
+            P[i] = p4.x; P[i + 1] = p4.y; P[i + 2] = p4.z; P[i + 3] = p4.w;
+        }
         const float Z = P[15], invZ = 1.0f / Z;
         // fraction of its group held by cluster c
         auto frac = [&](int c) {
@@ -388,7 +434,16 @@ __global__ void __launch_bounds__(512) infer_kernel(InferArgs a) {
                         gw = hi - lo;
                         const float x = gw > 0.0f ? (target - lo) * (65535.0f / gw) : 0.0f;
                         int in = 0;
-                        for (int i = 0; i < gs - 1; i++) in += x >= (float)fp[q * gs + i] ? 1 : 0;
+                        if (gs == 16) {
+                            const uint4 a0 = *reinterpret_cast<const uint4*>(fp + q * 16);
+                            const uint4 a1 = *reinterpret_cast<const uint4*>(fp + q * 16 + 8);
+                            const uint32_t wv[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+                            for (int i = 0; i < 15; i++)
+                                in += x >= (float)((wv[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu) ? 1 : 0;
+                        } else {
+                            for (int i = 0; i < gs - 1; i++) in += x >= (float)fp[q * gs + i] ? 1 : 0;
+                        }
                         c = q * gs + in;
                         // an emitter of cluster c, uniformly
                         const uint32_t off = offs[c], sz = offs[c + 1] - off;
@@ -616,7 +671,7 @@ static size_t infer_fixed_bytes(const Dims& d) {
     return (size_t)H * (kIn + 8) * 2 + 2 * (size_t)H * (H + 8) * 2 + (size_t)K * (H + 8) * 2 + (3 * H + K) * 4 +
            (size_t)((K + 1 + 3) & ~3) * 4;
 }
-static size_t infer_warp_bytes(const Dims& d) { return 16 * (kIn + 8) * 2 + 16 * (size_t)(d.K + 2) * 2; }
+static size_t infer_warp_bytes(const Dims& d) { return 16 * (kIn + 8) * 2 + 16 * (size_t)(d.K + 8) * 2; }
 // warps per block: as many as the shared memory holds, at most 16
 static int infer_warps(const Dims& d) {
     const size_t fixed = infer_fixed_bytes(d), per = infer_warp_bytes(d), cap = 227 * 1024;
