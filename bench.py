@@ -343,8 +343,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="library default launch tuning instead of the autotuner")
-    ap.add_argument("--quality", choices=["full", "off"], default="full",
-                    help="off: no converged render / training; time the plain method at 32 candidates")
+    ap.add_argument("--quality", choices=["full", "train", "off"], default="full",
+                    help="train: train the proposal and time the learned method at --candidates (no converged "
+                         "render, no sweep); off: time the plain method at 32 candidates")
+    ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
     ap.add_argument("--train-frames", type=int, default=200)
     ap.add_argument("--mse-seeds", type=int, default=4)
@@ -403,15 +405,30 @@ def main():
     quality, params = None, None
     if args.quality == "full" and rank == 0:
         quality, params = quality_eval(vx, world, desc, W, H, tuning, args)
+    elif args.quality == "train" and rank == 0:
+        trainer = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5))
+        trainer.set_tuning(tuning)
+        trainer.proposal_enable(seed=2, batch=65536)
+        for f in range(args.train_frames):
+            p, t = cams(f)
+            trainer.lookat(p, t)
+            trainer.render()
+            trainer.proposal_train(1)
+        params = trainer.proposal_params()
+        trainer.close()
     if dist is not None:
         obj = [quality, params]
         dist.broadcast_object_list(obj, src=0)
         quality, params = obj
-    eq = quality["learned_at_equal_mse"] if quality else None
-    learned = eq is not None
-    cand = eq["candidates"] if learned else 32
-    config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32)" if learned
-                        else "plain uniform-source RIS, 32 candidates")
+    if args.quality == "train":
+        learned, cand = True, args.candidates
+        config["method"] = f"learned proposal, {cand} candidates (trained {args.train_frames} frames)"
+    else:
+        eq = quality["learned_at_equal_mse"] if quality else None
+        learned = eq is not None
+        cand = eq["candidates"] if learned else 32
+        config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32)" if learned
+                            else "plain uniform-source RIS, 32 candidates")
 
     def make_view(learned_view, c):
         v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, num_candidates=c))
