@@ -340,21 +340,22 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
 // Every float op, the step budget accounting and the exit cascade (brick -> grid step
 // -> uber step) follow trace<MODE> exactly; the oracle checks the two for equality.
 struct Walker {
-    float ax, ay, az, vx, vy, vz, rx, ry, rz, to, tdx, tdy, tdz;
+    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;   // cell step in t per axis: |r| (= sign(v) * r)
     float t, tmx, tmy, tmz;        // current level
     float umx, umy, umz;           // saved uber-level crossings
     float gmx, gmy, gmz;           // saved grid-level crossings
     int ux, uy, uz, gx, gy, gz, lx, ly, lz;
     int steps, level, bi;
-    uint32_t o, brick, last, dirbits;   // dirbits: bit a set = positive direction on axis a
+    uint32_t o, brick, last;
+    int stx, sty, stz;             // axis steps (+-1)
     float dist;                    // result
     uint32_t side, voxel;
-    __device__ __forceinline__ int sx() const { return (dirbits & 1u) ? 1 : -1; }
-    __device__ __forceinline__ int sy() const { return (dirbits & 2u) ? 1 : -1; }
-    __device__ __forceinline__ int sz() const { return (dirbits & 4u) ? 1 : -1; }
-    __device__ __forceinline__ int ox() const { return (int)(dirbits & 1u); }
-    __device__ __forceinline__ int oy() const { return (int)((dirbits >> 1) & 1u); }
-    __device__ __forceinline__ int oz() const { return (int)((dirbits >> 2) & 1u); }
+    __device__ __forceinline__ int sx() const { return stx; }
+    __device__ __forceinline__ int sy() const { return sty; }
+    __device__ __forceinline__ int sz() const { return stz; }
+    __device__ __forceinline__ int ox() const { return stx > 0 ? 1 : 0; }
+    __device__ __forceinline__ int oy() const { return sty > 0 ? 1 : 0; }
+    __device__ __forceinline__ int oz() const { return stz > 0 ? 1 : 0; }
 };
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
 
@@ -366,7 +367,9 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
     if (fabsf(vz) < 1e-8f) vz = vz < 0.0f ? -1e-8f : 1e-8f;
     k.vx = vx; k.vy = vy; k.vz = vz;
     k.rx = 1.0f / vx; k.ry = 1.0f / vy; k.rz = 1.0f / vz;
-    k.dirbits = (vx > 0.0f ? 1u : 0u) | (vy > 0.0f ? 2u : 0u) | (vz > 0.0f ? 4u : 0u);
+    k.stx = vx > 0.0f ? 1 : -1;
+    k.sty = vy > 0.0f ? 1 : -1;
+    k.stz = vz > 0.0f ? 1 : -1;
     k.to = 0.0f;
     k.last = 0;
     if (ax < 0.0f || ay < 0.0f || az < 0.0f || ax > 1024.0f || ay > 1024.0f || az > 1024.0f) {
@@ -394,9 +397,6 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
     k.tmx = ((float)(uint32_t)(k.ux + k.ox()) - ax * 0.03125f) * k.rx;
     k.tmy = ((float)(uint32_t)(k.uy + k.oy()) - ay * 0.03125f) * k.ry;
     k.tmz = ((float)(uint32_t)(k.uz + k.oz()) - az * 0.03125f) * k.rz;
-    k.tdx = (float)k.sx() * k.rx;
-    k.tdy = (float)k.sy() * k.ry;
-    k.tdz = (float)k.sz() * k.rz;
     k.t = 0.0f;
     k.steps = steps;
     k.level = 0;
@@ -408,9 +408,9 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
 __device__ __forceinline__ bool walk_uber_step(Walker& k, const World& w) {
     k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
     k.last = 0;
-    if (k.t == k.tmx) { k.tmx += k.tdx; k.ux += k.sx(); }
-    if (k.t == k.tmy) { k.tmy += k.tdy; k.uy += k.sy(); k.last = 1; }
-    if (k.t == k.tmz) { k.tmz += k.tdz; k.uz += k.sz(); k.last = 2; }
+    if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.ux += k.sx(); }
+    if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.uy += k.sy(); k.last = 1; }
+    if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.uz += k.sz(); k.last = 2; }
     if ((k.ux | k.uy | k.uz) & ~31) return false;
     k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
     return true;
@@ -421,9 +421,9 @@ __device__ __forceinline__ bool walk_uber_step(Walker& k, const World& w) {
 __device__ __forceinline__ int walk_grid_step(Walker& k, const World& w) {
     k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
     k.last = 0;
-    if (k.t == k.tmx) { k.tmx += k.tdx; k.gx += k.sx(); }
-    if (k.t == k.tmy) { k.tmy += k.tdy; k.gy += k.sy(); k.last = 1; }
-    if (k.t == k.tmz) { k.tmz += k.tdz; k.gz += k.sz(); k.last = 2; }
+    if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.gx += k.sx(); }
+    if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.gy += k.sy(); k.last = 1; }
+    if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.gz += k.sz(); k.last = 2; }
     if (((k.gx >> 2) != k.ux) | ((k.gy >> 2) != k.uy) | ((k.gz >> 2) != k.uz)) {
         k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
         k.level = 0;
@@ -433,75 +433,105 @@ __device__ __forceinline__ int walk_grid_step(Walker& k, const World& w) {
     return WALK_CONTINUE;
 }
 
-// one cell visit at the current level
-__device__ __forceinline__ int walk_step(Walker& k, const World& w) {
-    if (k.level == 2) {
-        const uint32_t v = __ldg(w.bricks + (size_t)k.brick * 512u + k.lx + k.ly * 8 + k.lz * 64);
-        if (((v & 0xf000u) >> 12) == 15u) {
-            k.dist = k.t + k.to;
-            k.side = k.last;
-            k.voxel = v;
-            return WALK_HIT;
-        }
-        k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-        k.last = 0;
-        if (k.t == k.tmx) { k.tmx += k.tdx; k.lx += k.sx(); }
-        if (k.t == k.tmy) { k.tmy += k.tdy; k.ly += k.sy(); k.last = 1; }
-        if (k.t == k.tmz) { k.tmz += k.tdz; k.lz += k.sz(); k.last = 2; }
-        if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
-            k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
-            k.level = 1;
-            return walk_grid_step(k, w);
-        }
-        return WALK_CONTINUE;
-    }
-    if (k.level == 1) {
-        // a grid step with the budget exhausted always ends as a miss (the uber loop
-        // re-checks the budget before any further cell is visited)
-        if (!--k.steps) return WALK_MISS;
-        if ((k.o & 1u) == 0u) {
-            const uint32_t v = k.o >> 1;
-            if (((v & 0xf000u) >> 12) == 15u) {
-                k.dist = k.t * 8.0f + k.to;
-                k.side = k.last;
-                k.voxel = v;
-                return WALK_HIT;
+// hit test of a voxel payload (opaque: alpha nibble 0xF)
+__device__ __forceinline__ bool walk_opaque(uint32_t v) { return ((v & 0xf000u) >> 12) == 15u; }
+
+// Up to n cell visits (each one visit at the walker's level: examine, then descend or
+// step), stopping at a hit or a miss. A lane stays in the inner loop of its level while
+// it does not change level, so the per-visit dispatch is paid only at level changes.
+__device__ __forceinline__ int walk_run(Walker& k, const World& w, int n) {
+    while (true) {
+        if (k.level == 2) {
+            const uint32_t* br = w.bricks + (size_t)k.brick * 512u;
+            while (true) {
+                const uint32_t v = __ldg(br + k.lx + k.ly * 8 + k.lz * 64);
+                if (walk_opaque(v)) {
+                    k.dist = k.t + k.to;
+                    k.side = k.last;
+                    k.voxel = v;
+                    return WALK_HIT;
+                }
+                k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
+                k.last = 0;
+                if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.lx += k.sx(); }
+                if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.ly += k.sy(); k.last = 1; }
+                if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.lz += k.sz(); k.last = 2; }
+                if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
+                    k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
+                    k.level = 1;
+                    const int st = walk_grid_step(k, w);
+                    if (st != WALK_CONTINUE) return st;
+                    break;
+                }
+                if (--n == 0) return WALK_CONTINUE;
             }
-            return walk_grid_step(k, w);
+            if (--n == 0) return WALK_CONTINUE;
+            continue;
         }
-        k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
-        k.t *= 8.0f;
-        const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
-        const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
-        const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u), cz = min(max(pz, bz0), bz0 + 7u);
-        k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
-        k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
-        k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
-        k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
-        k.brick = k.o >> 1;
-        k.bi = 0;
-        k.level = 2;
-        return WALK_CONTINUE;
+        if (k.level == 1) {
+            while (true) {
+                // a grid step with the budget exhausted always ends as a miss (the uber
+                // loop re-checks the budget before any further cell is visited)
+                if (!--k.steps) return WALK_MISS;
+                if ((k.o & 1u) == 0u) {
+                    const uint32_t v = k.o >> 1;
+                    if (walk_opaque(v)) {
+                        k.dist = k.t * 8.0f + k.to;
+                        k.side = k.last;
+                        k.voxel = v;
+                        return WALK_HIT;
+                    }
+                    const int st = walk_grid_step(k, w);
+                    if (st != WALK_CONTINUE) return st;
+                    if (--n == 0) return WALK_CONTINUE;
+                    if (k.level != 1) break;
+                } else {
+                    k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
+                    k.t *= 8.0f;
+                    const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
+                    const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
+                    const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u),
+                                   cz = min(max(pz, bz0), bz0 + 7u);
+                    k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
+                    k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
+                    k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
+                    k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
+                    k.brick = k.o >> 1;
+                    k.bi = 0;
+                    k.level = 2;
+                    if (--n == 0) return WALK_CONTINUE;
+                    break;
+                }
+            }
+            continue;
+        }
+        // uber level
+        while (true) {
+            if ((k.steps -= 4) <= 0) return WALK_MISS;
+            if (k.o != 0u) {
+                k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
+                k.t *= 4.0f;
+                const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
+                               qz = f2u(0.125f * k.az + k.vz * k.t);
+                k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
+                k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
+                k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
+                k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
+                k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
+                k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
+                k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
+                k.level = 1;
+                if (--n == 0) return WALK_CONTINUE;
+                break;
+            }
+            if (!walk_uber_step(k, w)) return WALK_MISS;
+            if (--n == 0) return WALK_CONTINUE;
+        }
     }
-    // uber level
-    if ((k.steps -= 4) <= 0) return WALK_MISS;
-    if (k.o != 0u) {
-        k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
-        k.t *= 4.0f;
-        const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
-                       qz = f2u(0.125f * k.az + k.vz * k.t);
-        k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
-        k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
-        k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
-        k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
-        k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
-        k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
-        k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
-        k.level = 1;
-        return WALK_CONTINUE;
-    }
-    return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
 }
+
+// one cell visit at the current level
+__device__ __forceinline__ int walk_step(Walker& k, const World& w) { return walk_run(k, w, 1); }
 
 // ---- reservoirs --------------------------------------------------------------------
 // In HBM a reservoir is 32 bytes in two SoA planes:

@@ -152,6 +152,24 @@ uint32_t dh_walk(const uint32_t* grid, const uint8_t* uber, const uint32_t* bric
     return 0u;
 }
 
+// the walker run in bursts of `burst` visits (the shadow tracer's form)
+uint32_t dh_walk_burst(const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks, const float* O,
+                       const float* D, int steps, int burst, float* dist, uint32_t* side, int* status) {
+    const World w = make_world(grid, uber, bricks);
+    Walker k;
+    int st = walk_init(k, w, O[0], O[1], O[2], D[0], D[1], D[2], steps);
+    while (st == WALK_CONTINUE) st = walk_run(k, w, burst);
+    *status = st;
+    if (st == WALK_HIT) {
+        *dist = k.dist;
+        *side = k.side;
+        return k.voxel;
+    }
+    *dist = 0.0f;
+    *side = 0;
+    return 0u;
+}
+
 void dh_sincos(float a, float* s, float* c) { sincos_vx(a, s, c); }
 
 // area-light sample, per-axis form (device.cuh) and per-face form (above); out = point xyz, inv, face, seed

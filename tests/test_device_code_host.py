@@ -32,6 +32,8 @@ def dh():
     lib.dh_walk.restype = C.c_uint32
     lib.dh_walk.argtypes = [P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.dh_sincos.argtypes = [C.c_float, F, F]
+    lib.dh_walk_burst.restype = C.c_uint32
+    lib.dh_walk_burst.argtypes = [P, P, P, F, F, C.c_int, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     lib.dh_area_sample.argtypes = [C.c_int, F, F, C.c_uint32, F]
     return lib
 
@@ -86,6 +88,26 @@ def test_walker_matches_recursive_trace(dh, world0_arrays):
         else:
             assert v == 0, (i, o[i], d[i], v)
     assert total_visits > 10000
+
+
+def test_walker_bursts_match_single_visits(dh, world0_arrays):
+    """walk_run(n) (the shadow tracer's bursts) ends exactly like n single visits."""
+    wa = world0_arrays
+    o, d, rng = _rays(4000, 19)
+    for i in range(len(o)):
+        steps = int(rng.choice([128, 999999, 7, 1]))
+        burst = int(rng.choice([1, 2, 3, 4, 8, 16, 64]))
+        dist, side = C.c_float(0), C.c_uint32(0)
+        v = dh.dh_trace(1, wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, _f3(o[i]), _f3(d[i]),
+                        steps, 0, 0, C.byref(dist), C.byref(side))
+        d2, s2, st = C.c_float(0), C.c_uint32(0), C.c_int(0)
+        v2 = dh.dh_walk_burst(wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, _f3(o[i]), _f3(d[i]),
+                              steps, burst, C.byref(d2), C.byref(s2), C.byref(st))
+        if st.value == 1:
+            assert v == v2 and side.value == s2.value and \
+                np.float32(dist.value).view(np.uint32) == np.float32(d2.value).view(np.uint32), (i, burst)
+        else:
+            assert v == 0, (i, burst)
 
 
 def test_device_sincos_matches_oracle(dh):
