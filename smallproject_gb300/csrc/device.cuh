@@ -433,105 +433,75 @@ __device__ __forceinline__ int walk_grid_step(Walker& k, const World& w) {
     return WALK_CONTINUE;
 }
 
-// hit test of a voxel payload (opaque: alpha nibble 0xF)
-__device__ __forceinline__ bool walk_opaque(uint32_t v) { return ((v & 0xf000u) >> 12) == 15u; }
-
-// Up to n cell visits (each one visit at the walker's level: examine, then descend or
-// step), stopping at a hit or a miss. A lane stays in the inner loop of its level while
-// it does not change level, so the per-visit dispatch is paid only at level changes.
-__device__ __forceinline__ int walk_run(Walker& k, const World& w, int n) {
-    while (true) {
-        if (k.level == 2) {
-            const uint32_t* br = w.bricks + (size_t)k.brick * 512u;
-            while (true) {
-                const uint32_t v = __ldg(br + k.lx + k.ly * 8 + k.lz * 64);
-                if (walk_opaque(v)) {
-                    k.dist = k.t + k.to;
-                    k.side = k.last;
-                    k.voxel = v;
-                    return WALK_HIT;
-                }
-                k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-                k.last = 0;
-                if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.lx += k.sx(); }
-                if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.ly += k.sy(); k.last = 1; }
-                if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.lz += k.sz(); k.last = 2; }
-                if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
-                    k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
-                    k.level = 1;
-                    const int st = walk_grid_step(k, w);
-                    if (st != WALK_CONTINUE) return st;
-                    break;
-                }
-                if (--n == 0) return WALK_CONTINUE;
-            }
-            if (--n == 0) return WALK_CONTINUE;
-            continue;
-        }
-        if (k.level == 1) {
-            while (true) {
-                // a grid step with the budget exhausted always ends as a miss (the uber
-                // loop re-checks the budget before any further cell is visited)
-                if (!--k.steps) return WALK_MISS;
-                if ((k.o & 1u) == 0u) {
-                    const uint32_t v = k.o >> 1;
-                    if (walk_opaque(v)) {
-                        k.dist = k.t * 8.0f + k.to;
-                        k.side = k.last;
-                        k.voxel = v;
-                        return WALK_HIT;
-                    }
-                    const int st = walk_grid_step(k, w);
-                    if (st != WALK_CONTINUE) return st;
-                    if (--n == 0) return WALK_CONTINUE;
-                    if (k.level != 1) break;
-                } else {
-                    k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
-                    k.t *= 8.0f;
-                    const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
-                    const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
-                    const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u),
-                                   cz = min(max(pz, bz0), bz0 + 7u);
-                    k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
-                    k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
-                    k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
-                    k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
-                    k.brick = k.o >> 1;
-                    k.bi = 0;
-                    k.level = 2;
-                    if (--n == 0) return WALK_CONTINUE;
-                    break;
-                }
-            }
-            continue;
-        }
-        // uber level
-        while (true) {
-            if ((k.steps -= 4) <= 0) return WALK_MISS;
-            if (k.o != 0u) {
-                k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
-                k.t *= 4.0f;
-                const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
-                               qz = f2u(0.125f * k.az + k.vz * k.t);
-                k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
-                k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
-                k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
-                k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
-                k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
-                k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
-                k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
-                k.level = 1;
-                if (--n == 0) return WALK_CONTINUE;
-                break;
-            }
-            if (!walk_uber_step(k, w)) return WALK_MISS;
-            if (--n == 0) return WALK_CONTINUE;
-        }
-    }
-}
-
 // one cell visit at the current level
-__device__ __forceinline__ int walk_step(Walker& k, const World& w) { return walk_run(k, w, 1); }
+__device__ __forceinline__ int walk_step(Walker& k, const World& w) {
+    if (k.level == 2) {
+        const uint32_t v = __ldg(w.bricks + (size_t)k.brick * 512u + k.lx + k.ly * 8 + k.lz * 64);
+        if (((v & 0xf000u) >> 12) == 15u) {
+            k.dist = k.t + k.to;
+            k.side = k.last;
+            k.voxel = v;
+            return WALK_HIT;
+        }
+        k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
+        k.last = 0;
+        if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.lx += k.sx(); }
+        if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.ly += k.sy(); k.last = 1; }
+        if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.lz += k.sz(); k.last = 2; }
+        if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
+            k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
+            k.level = 1;
+            return walk_grid_step(k, w);
+        }
+        return WALK_CONTINUE;
+    }
+    if (k.level == 1) {
+        // a grid step with the budget exhausted always ends as a miss (the uber loop
+        // re-checks the budget before any further cell is visited)
+        if (!--k.steps) return WALK_MISS;
+        if ((k.o & 1u) == 0u) {
+            const uint32_t v = k.o >> 1;
+            if (((v & 0xf000u) >> 12) == 15u) {
+                k.dist = k.t * 8.0f + k.to;
+                k.side = k.last;
+                k.voxel = v;
+                return WALK_HIT;
+            }
+            return walk_grid_step(k, w);
+        }
+        k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
+        k.t *= 8.0f;
+        const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
+        const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
+        const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u), cz = min(max(pz, bz0), bz0 + 7u);
+        k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
+        k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
+        k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
+        k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
+        k.brick = k.o >> 1;
+        k.bi = 0;
+        k.level = 2;
+        return WALK_CONTINUE;
+    }
+    // uber level
+    if ((k.steps -= 4) <= 0) return WALK_MISS;
+    if (k.o != 0u) {
+        k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
+        k.t *= 4.0f;
+        const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
+                       qz = f2u(0.125f * k.az + k.vz * k.t);
+        k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
+        k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
+        k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
+        k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
+        k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
+        k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
+        k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
+        k.level = 1;
+        return WALK_CONTINUE;
+    }
+    return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
+}
 
 // ---- reservoirs --------------------------------------------------------------------
 // In HBM a reservoir is 32 bytes in two SoA planes:

@@ -317,10 +317,14 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
             continue;
         }
         if (active) {
-            const int st = walk_run(wk, w, burst);
-            if (st != WALK_CONTINUE) {
-                shadow_finish(w, st, wk, o, L, plane, pix, li);
-                active = false;
+#pragma unroll 1
+            for (int s = 0; s < burst; s++) {
+                const int st = walk_step(wk, w);
+                if (st != WALK_CONTINUE) {
+                    shadow_finish(w, st, wk, o, L, plane, pix, li);
+                    active = false;
+                    break;
+                }
             }
         }
     }

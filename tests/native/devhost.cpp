@@ -158,7 +158,9 @@ uint32_t dh_walk_burst(const uint32_t* grid, const uint8_t* uber, const uint32_t
     const World w = make_world(grid, uber, bricks);
     Walker k;
     int st = walk_init(k, w, O[0], O[1], O[2], D[0], D[1], D[2], steps);
-    while (st == WALK_CONTINUE) st = walk_run(k, w, burst);
+    while (st == WALK_CONTINUE) {
+        for (int i = 0; i < burst && st == WALK_CONTINUE; i++) st = walk_step(k, w);
+    }
     *status = st;
     if (st == WALK_HIT) {
         *dist = k.dist;
