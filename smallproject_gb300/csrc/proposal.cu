@@ -299,51 +299,58 @@ __global__ void __launch_bounds__(512, 1) infer_kernel(InferArgs a) {
         // rounding) and small clusters keep a resolution of 1/65535 of their group.
         float* Prow = reinterpret_cast<float*>(Xs);   // X is dead after layer 1
         if (K == 256) {
-            // one row at a time by the whole warp: lane l holds columns 8l .. 8l+7 (half a
-            // group), 16-byte loads and stores, reductions by shuffles
-            for (int rr = 0; rr < 16; rr++) {
-                uint4* rowv = reinterpret_cast<uint4*>(Ls + rr * ldl) + lane;
-                const uint4 raw = *rowv;
-                const __half2* h2 = reinterpret_cast<const __half2*>(&raw);
-                float z[8];
+            // two rows at a time, a half-warp per row: lane l of the half holds group l
+            // (16 columns, 32 bytes), so the group total and its in-group prefix sums stay in
+            // the lane; row maxima and the scan over the 16 groups are half-warp shuffles
+            const int lr = lane & 15;
+            for (int rr = half; rr < 16; rr += 2) {
+                uint4* rowv = reinterpret_cast<uint4*>(Ls + rr * ldl) + 2 * lr;
+                const uint4 raw0 = rowv[0], raw1 = rowv[1];
+                float z[16];
+                {
+                    const __half2* h0 = reinterpret_cast<const __half2*>(&raw0);
+                    const __half2* h1 = reinterpret_cast<const __half2*>(&raw1);
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const float2 f = __half22float2(h2[i]);
-                    z[2 * i] = f.x;
-                    z[2 * i + 1] = f.y;
+                    for (int i = 0; i < 4; i++) {
+                        const float2 f0 = __half22float2(h0[i]), f1 = __half22float2(h1[i]);
+                        z[2 * i] = f0.x; z[2 * i + 1] = f0.y;
+                        z[8 + 2 * i] = f1.x; z[8 + 2 * i + 1] = f1.y;
+                    }
                 }
                 float m = z[0];
 #pragma unroll
-                for (int i = 1; i < 8; i++) m = fmaxf(m, z[i]);
+                for (int i = 1; i < 16; i++) m = fmaxf(m, z[i]);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-                float pre[8];
-                float acc = 0.0f;
+                for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+                // in-group prefix sums as two chains of 8, joined
+                float pa[8], pb[8];
+                float ea = 0.0f, eb = 0.0f;
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
-                    acc += __expf(z[i] - m);
-                    pre[i] = acc;
+                    ea += __expf(z[i] - m);
+                    eb += __expf(z[8 + i] - m);
+                    pa[i] = ea;
+                    pb[i] = eb;
                 }
-                const float other = __shfl_xor_sync(0xffffffffu, acc, 1);
-                const float T = (lane & 1) ? other + acc : acc + other;   // same order in both lanes
-                const float base = (lane & 1) ? other : 0.0f;
+                const float T = ea + eb;
                 const float sc = T > 0.0f ? 65535.0f / T : 0.0f;
-                uint32_t pk[4];
+                uint32_t pk[8];
 #pragma unroll
                 for (int i = 0; i < 8; i += 2) {
-                    const uint32_t lo = min((uint32_t)((base + pre[i]) * sc), 65535u);
-                    const uint32_t hi = (i == 6 && (lane & 1)) ? 65535u : min((uint32_t)((base + pre[i + 1]) * sc), 65535u);
-                    pk[i / 2] = lo | (hi << 16);
+                    pk[i / 2] = min((uint32_t)(pa[i] * sc), 65535u) | (min((uint32_t)(pa[i + 1] * sc), 65535u) << 16);
+                    const uint32_t hi = i == 6 ? 65535u : min((uint32_t)((ea + pb[i + 1]) * sc), 65535u);
+                    pk[4 + i / 2] = min((uint32_t)((ea + pb[i]) * sc), 65535u) | (hi << 16);
                 }
-                *rowv = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                // inclusive scan of the group totals over the even lanes
-                float v = (lane & 1) ? 0.0f : T;
+                rowv[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                rowv[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                // inclusive scan of the group totals over the half-warp
+                float v = T;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const float u = __shfl_up_sync(0xffffffffu, v, o);
-                    if (lane >= o) v += u;
+                for (int o = 1; o < 16; o <<= 1) {
+                    const float u = __shfl_up_sync(0xffffffffu, v, o, 16);
+                    if (lr >= o) v += u;
                 }
-                if (!(lane & 1)) Prow[rr * 16 + (lane >> 1)] = v;
+                Prow[rr * 16 + lr] = v;
             }
         } else {
             // generic K: the two lanes of a row take 8 groups each
