@@ -10,8 +10,8 @@ albedo -> candidates (+ proposal inference) + temporal -> spatial -> shading+acc
 Quality protocol (untimed setup, --quality full): a converged render (FP64 mean of
 --conv-frames frames of the unbiased estimator: spatial and temporal reuse off) at path
 frame 150; the proposal trained online for --train-frames frames along the path on the
-plain method's reservoirs; then for each method and candidate count in CANDS, seeds x
-frames at the static pose: device ms/frame and MSE against the converged render. The
+plain method's reservoirs; then for each method and candidate count in CANDS, 8 seeds x
+16 frames at the static pose: device ms/frame and MSE against the converged render. The
 plain method's reference point is 32 candidates (the reference's NUMBEROFCANDIDATES).
 The timed configuration is the learned method at the smallest candidate count whose mean
 MSE is at most the plain method's (equal MSE), else plain at 32; `value` is its device
@@ -199,7 +199,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
     conv_s = time.perf_counter() - t0
     trainer = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5))
     trainer.set_tuning(tuning)
-    trainer.proposal_enable(seed=2, batch=65536)
+    trainer.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
     t0 = time.perf_counter()
     losses = []
     for f in range(args.train_frames):
@@ -220,7 +220,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
                 v.set_tuning(tuning)
                 v.lookat(pos, tgt)
                 if method == "learned":
-                    v.proposal_enable(seed=2, batch=65536)
+                    v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
                     v.proposal_set_params(params)
                     v.proposal_use(True)
                 for _ in range(8):
@@ -254,7 +254,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
     # equal time: the learned configuration with the largest ms/frame not above plain's
     at = [table[f"learned_{c}"] for c in CANDS if table[f"learned_{c}"]["ms"] <= p32["ms"]]
     et = max(at, key=lambda r: r["ms"]) if at else None
-    return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s,
+    return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s, "epsilon": args.epsilon,
             "train_frames": args.train_frames, "train_s": train_s, "train_batch": 65536,
             "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
             "frames_per_point": args.mse_seeds * args.mse_frames, "table": table,
@@ -350,8 +350,9 @@ def main():
     ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
     ap.add_argument("--train-frames", type=int, default=200)
-    ap.add_argument("--mse-seeds", type=int, default=4)
-    ap.add_argument("--mse-frames", type=int, default=8)
+    ap.add_argument("--mse-seeds", type=int, default=8)
+    ap.add_argument("--mse-frames", type=int, default=16)
+    ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
     args = ap.parse_args()
     W, H = args.width, args.height
     warmup = max(args.warmup, 3)
@@ -409,7 +410,7 @@ def main():
     elif args.quality == "train" and rank == 0:
         trainer = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5))
         trainer.set_tuning(tuning)
-        trainer.proposal_enable(seed=2, batch=65536)
+        trainer.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
         for f in range(args.train_frames):
             p, t = cams(f)
             trainer.lookat(p, t)
@@ -435,7 +436,7 @@ def main():
         v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, num_candidates=c))
         v.set_tuning(tuning)
         if learned_view:
-            v.proposal_enable(seed=2, batch=65536)
+            v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
             v.proposal_set_params(params)
             v.proposal_use(True)
         return v
