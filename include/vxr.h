@@ -342,6 +342,7 @@ typedef struct vxr_proposal_desc {
     float    learning_rate;   /* Adam (1e-3) */
     uint32_t batch;           /* training samples per step (65536) */
     uint32_t seed;            /* parameter initialisation */
+    uint32_t inference;       /* 0 auto (tcgen05 when hidden = 64 and 256 clusters, else mma.sync), 1 mma.sync, 2 tcgen05 */
 } vxr_proposal_desc;
 int vxr_proposal_default_desc(vxr_proposal_desc* d);
 /* Allocate and initialise the network for this view; K = the world's cluster count. */

@@ -785,6 +785,7 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
             ia.lightCluster = learned->lightCluster;
             ia.nlights = bd.one.k.nlights;
             ia.candStride = (uint32_t)n;
+            ia.err = bd.one.b.err;
             ia.samples = nullptr;
             ia.probs = nullptr;
             if (bd.one.k.ncand > 0) {

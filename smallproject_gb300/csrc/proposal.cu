@@ -467,6 +467,343 @@ __global__ void __launch_bounds__(512, 1) infer_kernel(InferArgs a) {
     }
 }
 
+// ---- inference on the 5th-generation tensor cores (tcgen05, TMEM) --------------------------
+// The same network and sampler as infer_kernel for H = 64 and K = 256. A CTA of 256 threads
+// runs two independent tiles of 128 hit pixels (threads 0-127 and 128-255, one pixel per
+// thread = one TMEM lane). Per layer one thread issues tcgen05.mma (M = 128, N = 64 or 256,
+// K = 16 per instruction; A = the tile's activations, B = the weights, both BF16 in shared
+// memory in the K-major no-swizzle core-matrix layout), the accumulator stays in tensor
+// memory (FP32), tcgen05.commit arrives on an mbarrier, and every thread reads its own
+// row back with tcgen05.ld for the epilogue (bias, ReLU, BF16 into the next layer's A) or,
+// after the output layer, for its pixel's softmax tables and candidates. All waits are
+// bounded; on a timeout the kernel raises *a.err, skips its remaining tiles and still
+// frees its tensor memory.
+namespace tc {
+constexpr int kTile = 128;
+constexpr uint32_t kCols = 512;          // TMEM columns: 256 per tile
+constexpr int kRowBytes = 512 + 16;      // a pixel's sampling table (256 x u16), padded
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) in a K-major no-swizzle operand with `kdim` columns:
+// 8-row x 16-byte core matrices, 128 bytes apart along K, kdim * 16 bytes apart along rows
+__device__ __forceinline__ uint32_t core_off(int r, int k, int kdim) {
+    return (uint32_t)((r >> 3) * (kdim * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+// shared-memory matrix descriptor (no swizzle): start address, leading-dimension (K)
+// byte offset, stride-dimension (M/N) byte offset, descriptor version 1
+__device__ __forceinline__ uint64_t desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__device__ __forceinline__ constexpr uint32_t idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bar_half(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+// bounded wait for the mbarrier phase of parity `par`; false when the limit ran out
+__device__ __forceinline__ bool wait(uint32_t mbar, uint32_t par) {
+    for (uint32_t i = 0; i < (1u << 22); i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\tselp.b32 %0, 1, 0, P;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(par)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// 32 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    __syncwarp();
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+// copy a BF16 [rows][kdim] row-major matrix into the core-matrix layout (16-byte chunks)
+__device__ __forceinline__ void stage(const __nv_bfloat16* g, unsigned char* s, int rows, int kdim) {
+    const int chunks = rows * (kdim / 8);
+    for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+        const int r = c / (kdim / 8), k = (c % (kdim / 8)) * 8;
+        *reinterpret_cast<uint4*>(s + core_off(r, k, kdim)) = *reinterpret_cast<const uint4*>(g + (size_t)r * kdim + k);
+    }
+}
+// one thread's row of 64 accumulators -> bias, ReLU, BF16, into the next A operand (K = 64)
+__device__ __forceinline__ void epilogue64(uint32_t taddr, const float* bias, unsigned char* A, int row) {
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        float v[32];
+        ld32(taddr + half * 32, v);
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int k = half * 32 + c * 8 + 2 * q;
+                w[q] = pack_bf16(fmaxf(v[c * 8 + 2 * q] + bias[k], 0.0f), fmaxf(v[c * 8 + 2 * q + 1] + bias[k + 1], 0.0f));
+            }
+            *reinterpret_cast<uint4*>(A + core_off(row, half * 32 + c * 8, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+}  // namespace tc
+
+__global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    constexpr int H = 64, K = 256;
+    unsigned char* W1c = smem;                     // [64][32]
+    unsigned char* W2c = W1c + H * kIn * 2;        // [64][64]
+    unsigned char* W3c = W2c + H * H * 2;
+    unsigned char* W4c = W3c + H * H * 2;          // [256][64]
+    float* bs = reinterpret_cast<float*>(W4c + K * H * 2);   // b1 | b2 | b3 | b4
+    uint32_t* offs = reinterpret_cast<uint32_t*>(bs + 3 * H + K);
+    unsigned char* Abuf = reinterpret_cast<unsigned char*>(offs + 260);            // 2 x [128][64]
+    unsigned char* Tbuf = Abuf + 2 * tc::kTile * H * 2;                             // 2 x 128 table rows
+    uint64_t* mbars = reinterpret_cast<uint64_t*>(Tbuf + 2 * tc::kTile * tc::kRowBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbars + 2);
+    const int warp = threadIdx.x >> 5;
+    {
+        const __nv_bfloat16* wg = a.wbf;
+        tc::stage(wg, W1c, H, kIn);
+        tc::stage(wg + H * kIn, W2c, H, H);
+        tc::stage(wg + H * kIn + H * H, W3c, H, H);
+        tc::stage(wg + H * kIn + 2 * H * H, W4c, K, H);
+        const float* p = a.params;
+        for (int e = threadIdx.x; e < H; e += blockDim.x) {
+            bs[e] = p[a.L.b1 + e];
+            bs[H + e] = p[a.L.b2 + e];
+            bs[2 * H + e] = p[a.L.b3 + e];
+        }
+        for (int e = threadIdx.x; e < K; e += blockDim.x) bs[3 * H + e] = p[a.L.b4 + e];
+        if (a.clOff)
+            for (int e = threadIdx.x; e <= K; e += blockDim.x) offs[e] = a.clOff[e];
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::smem_u32(&mbars[0])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::smem_u32(&mbars[1])));
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        if (warp == 0) {
+            __syncwarp();
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(tslot)),
+                         "r"(tc::kCols));
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        }
+        tc::fence_async_smem();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot;
+    const int h = threadIdx.x >> 7, tid = threadIdx.x & 127, wq = warp & 3, bar = 1 + h;
+    unsigned char* A = Abuf + h * tc::kTile * H * 2;
+    unsigned char* T = Tbuf + h * tc::kTile * tc::kRowBytes;
+    uint16_t* fp = reinterpret_cast<uint16_t*>(T + tid * tc::kRowBytes);
+    const uint32_t mbar = tc::smem_u32(&mbars[h]);
+    const uint32_t dcol = tmem + (uint32_t)(h * 256);                 // this tile's accumulator columns
+    const uint32_t trow = dcol + ((uint32_t)(wq * 32) << 16);         // this warp's lanes
+    const uint32_t aaddr = tc::smem_u32(A);
+    const float* enc = a.params + a.L.enc;
+    const Dims d = a.dims;
+    const uint32_t n = a.count ? *a.count : a.n;
+    const int gs = K / 16;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t tile = blockIdx.x * 2 + h; ok && (size_t)tile * tc::kTile < n; tile += gridDim.x * 2) {
+        const uint32_t j = tile * tc::kTile + tid;
+        const bool valid = j < n;
+        float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
+        uint32_t pix = 0;
+        if (valid) {
+            if (a.samples) {
+                pin = a.samples[j];
+            } else {
+                pix = a.hits[j];
+                const int x = (int)(pix % (uint32_t)a.k.W), y = (int)(pix / (uint32_t)a.k.W);
+                const uint2 gv = a.vd[pix];
+                const uint32_t side = gv.x >> 24;
+                const float dist = __uint_as_float(gv.y);
+                const float3 D = dev::camera_ray(a.k, x, y);
+                const float ns = dev::side_sign(side, D);
+                pin = make_float4(D.x * dist + a.k.E.x, D.y * dist + a.k.E.y, D.z * dist + a.k.E.z,
+                                  __uint_as_float(side_code(side, ns)));
+            }
+        }
+        // input row (K = 32): both hash-grid levels, the one-hot side, zeros
+        {
+            float f[kIn];
+            level_features(enc, d, pin.x, pin.y, pin.z, 0, f);
+            level_features(enc, d, pin.x, pin.y, pin.z, 1, f + 8);
+            const uint32_t code = __float_as_uint(pin.w);
+#pragma unroll
+            for (int q = 16; q < kIn; q++) f[q] = code == (uint32_t)(q - 16) ? 1.0f : 0.0f;
+#pragma unroll
+            for (int c = 0; c < kIn / 8; c++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) w[q] = valid ? pack_bf16(f[c * 8 + 2 * q], f[c * 8 + 2 * q + 1]) : 0u;
+                *reinterpret_cast<uint4*>(A + tc::core_off(tid, c * 8, kIn)) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        // four layers; between them every thread moves its row from TMEM to A
+#pragma unroll 1
+        for (int layer = 0; layer < 4; layer++) {
+            tc::fence_async_smem();
+            tc::fence_before();
+            tc::bar_half(bar);
+            if (tid == 0) {
+                tc::fence_after();
+                const int kdim = layer == 0 ? kIn : H;
+                const unsigned char* W = layer == 0 ? W1c : (layer == 1 ? W2c : (layer == 2 ? W3c : W4c));
+                const int N = layer == 3 ? K : H;
+                const uint32_t id = layer == 3 ? tc::idesc(128, 256) : tc::idesc(128, 64);
+                for (int kk = 0; kk < kdim / 16; kk++)
+                    tc::mma(dcol, tc::desc(aaddr + kk * 256, 128, kdim * 16),
+                            tc::desc(tc::smem_u32(W) + kk * 256, 128, kdim * 16), id, kk > 0 ? 1u : 0u);
+                (void)N;
+                tc::commit(mbar);
+            }
+            if (!tc::wait(mbar, phase)) {
+                ok = false;
+                if (a.err) atomicOr(a.err, 16u);
+                break;
+            }
+            phase ^= 1u;
+            tc::fence_after();
+            if (layer < 3) tc::epilogue64(trow, bs + layer * H, A, tid);
+        }
+        if (!ok) break;
+        // softmax tables of this thread's pixel from its 256 logits in TMEM (see infer_kernel)
+        float mx = -INFINITY;
+#pragma unroll 1
+        for (int ch = 0; ch < K / 32; ch++) {
+            float v[32];
+            tc::ld32(trow + ch * 32, v);
+#pragma unroll
+            for (int i = 0; i < 32; i++) mx = fmaxf(mx, v[i] + bs[3 * H + ch * 32 + i]);
+        }
+        float P[16];
+        float Z = 0.0f;
+#pragma unroll
+        for (int ch = 0; ch < K / 32; ch++) {
+            float v[32];
+            tc::ld32(trow + ch * 32, v);
+#pragma unroll
+            for (int g2 = 0; g2 < 2; g2++) {
+                float pre[16];
+                float acc = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    acc += __expf(v[g2 * 16 + i] + bs[3 * H + ch * 32 + g2 * 16 + i] - mx);
+                    pre[i] = acc;
+                }
+                const float sc = acc > 0.0f ? 65535.0f / acc : 0.0f;
+                uint32_t pk[8];
+#pragma unroll
+                for (int i = 0; i < 16; i += 2) {
+                    const uint32_t lo = min((uint32_t)(pre[i] * sc), 65535u);
+                    const uint32_t hi = i == 14 ? 65535u : min((uint32_t)(pre[i + 1] * sc), 65535u);
+                    pk[i / 2] = lo | (hi << 16);
+                }
+                uint4* dst = reinterpret_cast<uint4*>(fp + (ch * 2 + g2) * 16);
+                dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                Z += acc;
+                P[ch * 2 + g2] = Z;
+            }
+        }
+        tc::fence_before();   // this thread's TMEM reads are complete before the next tile's MMAs
+        const float invZ = 1.0f / Z;
+        auto frac = [&](int c) {
+            const uint32_t hi = fp[c], lo = (c % gs) ? fp[c - 1] : 0u;
+            return (float)(hi - lo) * (1.0f / 65535.0f);
+        };
+        if (!valid) continue;
+        if (a.probs) {
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const float gw = q ? P[q] - P[q - 1] : P[0];
+                for (int c = q * gs; c < (q + 1) * gs; c++) a.probs[(size_t)j * K + c] = (gw * frac(c)) * invZ;
+            }
+            continue;
+        }
+        uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
+        const float eps = d.eps, invN = 1.0f / (float)a.nlights;
+        uint2* out = a.cand + j;
+#pragma unroll 4
+        for (uint32_t m = 0; m < a.ncand; m++) {
+            const float u = dev::rnd(s);
+            const float v = dev::rnd(s);
+            const float w = dev::rnd(s);
+            int c;
+            uint32_t e;
+            float gw;
+            if (u < eps) {
+                e = min((uint32_t)(v * (float)a.nlights), a.nlights - 1u);
+                c = (int)__ldg(a.lightCluster + e);
+                const int q = c / gs;
+                float lo = 0.0f, hi = P[0];
+#pragma unroll
+                for (int i = 1; i < 16; i++)
+                    if (q == i) { lo = P[i - 1]; hi = P[i]; }
+                gw = hi - lo;
+            } else {
+                const float target = v * Z;
+                int q = 0;
+                float lo = 0.0f, hi = P[0];
+#pragma unroll
+                for (int i = 0; i < 15; i++)
+                    if (target >= P[i]) { q = i + 1; lo = P[i]; hi = P[i + 1]; }
+                gw = hi - lo;
+                const float x = gw > 0.0f ? (target - lo) * (65535.0f / gw) : 0.0f;
+                const uint4 a0 = *reinterpret_cast<const uint4*>(fp + q * 16);
+                const uint4 a1 = *reinterpret_cast<const uint4*>(fp + q * 16 + 8);
+                const uint32_t wv[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                int in = 0;
+#pragma unroll
+                for (int i = 0; i < 15; i++) in += x >= (float)((wv[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu) ? 1 : 0;
+                c = q * gs + in;
+                const uint32_t off = offs[c], sz = offs[c + 1] - off;
+                e = __ldg(a.clMembers + off + min((uint32_t)(w * (float)sz), sz - 1u));
+            }
+            const float sz = (float)(offs[c + 1] - offs[c]);
+            const float pe = (1.0f - eps) * (((gw * frac(c)) * invZ) / sz) + eps * invN;
+            out[(size_t)m * a.candStride] = make_uint2(e, __float_as_uint(pe));
+        }
+    }
+    // every MMA of this CTA has completed (each was waited for) unless a wait gave up:
+    // then wait once more, bounded, before the tensor memory is freed
+    if (!ok) tc::wait(mbar, phase);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) {
+        __syncwarp();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc::kCols));
+    }
+}
+
 // ---- training ------------------------------------------------------------------------------
 // training batch from the view's final reservoirs: sample b takes the hit pixel at
 // stratum b of the hit list; target = cluster of the selected emitter, weight = W * pHat
@@ -692,7 +1029,23 @@ bool infer_supported(const Dims& d) {
     return d.H == 64 && d.K >= 16 && d.K % 16 == 0 && d.K <= 1024 && infer_warps(d) >= 1;
 }
 
+bool infer_tc_supported(const Dims& d) { return d.H == 64 && d.K == 256; }
+
+static size_t infer_tc_smem_bytes() {
+    return (size_t)64 * kIn * 2 + 2 * 64 * 64 * 2 + 256 * 64 * 2 + (3 * 64 + 256) * 4 + 260 * 4 + 2 * 128 * 64 * 2 +
+           2 * 128 * (512 + 16) + 2 * 8 + 16;
+}
+
 cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s) {
+    const bool use_tc = a.dims.kernel == 2 || (a.dims.kernel == 0 && infer_tc_supported(a.dims));
+    if (use_tc) {
+        const size_t sm = infer_tc_smem_bytes();
+        cudaError_t e = cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((max_items + 255) / 256, (uint32_t)sms()));
+        infer_tc_kernel<<<blocks, 256, sm, s>>>(a);
+        return cudaGetLastError();
+    }
     const int nw = infer_warps(a.dims);
     const size_t sm = infer_fixed_bytes(a.dims) + (size_t)nw * infer_warp_bytes(a.dims);
     cudaError_t e = cudaFuncSetAttribute(infer_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

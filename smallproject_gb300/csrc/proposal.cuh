@@ -32,6 +32,7 @@ struct Dims {
     int tableLog2 = 16;          // 2^16 entries per level
     int res0 = 32, res1 = 128;   // grid resolution of the two levels over the 1024^3 map
     float eps = 0.1f;            // defensive mixture weight
+    int kernel = 0;              // inference: 0 auto (tcgen05 when supported), 1 mma.sync, 2 tcgen05
 };
 
 // Offsets (in floats) of each tensor inside the parameter vector.

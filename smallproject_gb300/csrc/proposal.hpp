@@ -26,6 +26,7 @@ struct InferArgs {
     uint32_t nlights;
     uint32_t candStride;              // hits per candidate row of `cand`
     uint2* cand;                      // out: [candidate][candStride] (emitter, bits(p_src))
+    uint32_t* err;                    // device error flags (16: a tensor-core wait gave up)
     // sample mode (tests): explicit inputs (x, y, z, bits(side code)) and softmax output
     const float4* samples;
     uint32_t n;
@@ -64,6 +65,7 @@ struct GemmArgs {
 
 size_t infer_smem_bytes(const Dims& d);
 bool infer_supported(const Dims& d);
+bool infer_tc_supported(const Dims& d);   // the tcgen05 kernel (H = 64, K = 256)
 cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s);
 void launch_gather(const GatherArgs& a, cudaStream_t s);
 void launch_encode(const float* params, const Layout& L, const Dims& d, const float4* samples, uint32_t B, float* X,

@@ -242,6 +242,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     VXR_CHECK_ARG(desc->epsilon > 0.0f && desc->epsilon <= 1.0f, "vxr_view_proposal_enable: epsilon must be in (0, 1]");
     VXR_CHECK_ARG(desc->table_log2 >= 8 && desc->table_log2 <= 22, "vxr_view_proposal_enable: table_log2 in [8, 22]");
     VXR_CHECK_ARG(desc->batch >= 1 && desc->batch <= (1u << 22), "vxr_view_proposal_enable: batch in [1, 2^22]");
+    VXR_CHECK_ARG(desc->inference <= 2, "vxr_view_proposal_enable: inference must be 0 (auto), 1 (mma.sync) or 2 (tcgen05)");
     VXR_CHECK_ARG(v->desc.num_candidates <= (uint32_t)vxr::prop::kMaxCand,
                   "vxr_view_proposal_enable: at most 32 candidates per pixel with the learned proposal");
     vxr::prop::Dims d;
@@ -251,10 +252,13 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     d.res0 = (int)desc->res0;
     d.res1 = (int)desc->res1;
     d.eps = desc->epsilon;
+    d.kernel = (int)desc->inference;
     VXR_CHECK_ARG(d.K > 0, "vxr_view_proposal_enable: cluster the world's lights first (vxr_world_cluster_lights)");
     if (!vxr::prop::infer_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: supported shapes are hidden = 64 and 16 <= clusters <= 1024, "
                                         "clusters a multiple of 16");
+    if (d.kernel == 2 && !vxr::prop::infer_tc_supported(d))
+        return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tcgen05 inference needs hidden = 64 and 256 clusters");
     if (v->prop) vxr::destroy_proposal(v->prop);
     vxr::Proposal* p = new (std::nothrow) vxr::Proposal();
     if (!p) return set_error(VXR_E_NOMEM, "vxr_view_proposal_enable: out of host memory");
@@ -404,8 +408,17 @@ int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float
     a.samples = ds;
     a.n = n;
     a.probs = dp;
+    a.err = v->buf.err;
     cudaError_t e = vxr::prop::launch_infer(a, n, v->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(v->stream);
+    uint32_t flags = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&flags, v->buf.err, sizeof(flags), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && (flags & 16u)) {
+        cudaMemset(v->buf.err, 0, sizeof(uint32_t));
+        cudaFree(ds);
+        cudaFree(dp);
+        return set_error(VXR_E_DEVICE, "vxr_view_proposal_probs: a tensor-core wait gave up");
+    }
     if (e == cudaSuccess) e = cudaMemcpy(probs, dp, (size_t)n * p->d.K * sizeof(float), cudaMemcpyDeviceToHost);
     cudaFree(ds);
     cudaFree(dp);

@@ -151,3 +151,56 @@ def test_trained_proposal_beats_uniform(lib, cuda_device):
     assert errs[True] < errs[False], errs
     trainer.close()
     ref.close()
+
+
+@pytest.fixture(scope="module")
+def world256(lib, cuda_device):
+    w = lib.World()
+    w.generate(lib.scene_preset(0, emitters=2048, emitter_mode=1))
+    w.cluster_lights(256, seed=3, iters=6)
+    return w
+
+
+def test_tcgen05_inference_matches_mma_and_fp64(lib, world256):
+    """The tcgen05 / TMEM inference kernel (256 clusters) against the mma.sync kernel with
+    the same parameters and against the FP64 forward pass; 600 samples = 3 tiles of 128
+    per CTA half, the last one partial."""
+    a = lib.View(world256, lib.view_desc(64, 48, lib.LIGHTS_AREA))
+    b = lib.View(world256, lib.view_desc(64, 48, lib.LIGHTS_AREA))
+    try:
+        a.proposal_enable(seed=7, batch=4096, inference=1)
+        b.proposal_enable(seed=7, batch=4096, inference=2)
+        b.proposal_set_params(a.proposal_params())
+        n, K, H = b.proposal_shape()
+        assert K == 256
+        rng = np.random.default_rng(3)
+        s = _samples(rng, 600, 0.0, 1000.0)
+        pa = a.proposal_probs(s)
+        pb = b.proposal_probs(s)
+        ref = pr.softmax(pr.forward(b.proposal_params().astype(np.float64), s, H, K)[-1])
+        assert np.allclose(pb.sum(1), 1.0, atol=1e-3)
+        assert np.abs(pb - ref).max() < 2e-2
+        assert np.abs(pb - pa).max() < 1e-2
+    finally:
+        a.close()
+        b.close()
+
+
+def test_tcgen05_learned_render_runs_clean(lib, world256):
+    """Frames rendered with the tcgen05 inference: no device error flag, finite image."""
+    v = lib.View(world256, lib.view_desc(200, 120, lib.LIGHTS_AREA, num_candidates=12))
+    try:
+        v.proposal_enable(seed=5, batch=8192, inference=2)
+        v.lookat((110.0, 150.0, 10.0), (128.0, 110.0, 128.0))
+        for _ in range(3):
+            v.render()
+            v.proposal_train(1)
+        v.proposal_use(True)
+        for f in range(3):
+            v.lookat((110.0 + f, 150.0, 10.0), (128.0, 110.0, 128.0))
+            v.render()
+        v.wait()
+        img = v.read_frame()
+        assert np.isfinite(img).all() and img[..., :3].max() > 0
+    finally:
+        v.close()
