@@ -393,6 +393,7 @@ typedef struct vxr_tuning {
     uint32_t shadow_burst;         /* shadow tracer: cell visits per lane between refill checks (1..64) */
     uint32_t list_blocks_per_sm;   /* hit-list kernels (candidates, temporal, shading requests): blocks per SM (1..64) */
     uint32_t occupancy;            /* 1: shadow tracer and candidate kernels capped in registers for more warps per SM */
+    uint32_t shadow_schedule;      /* shadow tracer: 0 every lane steps each round, 1 only the lanes at the DDA level most lanes are at */
 } vxr_tuning;
 int vxr_default_tuning(vxr_tuning* t);
 /* Current CUDA device: name (NUL-terminated, truncated to n bytes), SM count and compute

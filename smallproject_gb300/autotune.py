@@ -30,6 +30,7 @@ SPACE = [
     ("shadow_burst", [2, 4, 8, 16]),
     ("list_blocks_per_sm", [4, 8, 16, 32]),
     ("occupancy", [0, 1]),
+    ("shadow_schedule", [0, 1]),
 ]
 
 
@@ -61,14 +62,15 @@ def config_key(world, desc):
 def _to_tuning(d):
     t = _v.tuning()
     t.tile_x, t.tile_y = d["tile"]
-    for k in ("persistent", "shadow_refill", "shadow_burst", "list_blocks_per_sm", "occupancy"):
+    for k in ("persistent", "shadow_refill", "shadow_burst", "list_blocks_per_sm", "occupancy", "shadow_schedule"):
         setattr(t, k, d[k])
     return t
 
 
 def _from_tuning(t):
     return {"tile": (t.tile_x, t.tile_y), "persistent": t.persistent, "shadow_refill": t.shadow_refill,
-            "shadow_burst": t.shadow_burst, "list_blocks_per_sm": t.list_blocks_per_sm, "occupancy": t.occupancy}
+            "shadow_burst": t.shadow_burst, "list_blocks_per_sm": t.list_blocks_per_sm, "occupancy": t.occupancy,
+            "shadow_schedule": t.shadow_schedule}
 
 
 def time_view(view, t, cams, frames, start=0):

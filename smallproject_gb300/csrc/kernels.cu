@@ -276,7 +276,7 @@ __device__ __forceinline__ void shadow_finish(const World& w, int st, const Walk
 template <int VARIANT, int MINB>
 __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant__ BatchDev bd, int countIdx, int fetchIdx,
                                                      int planeSel) {
-    const int refill = bd.refill, burst = bd.burst;
+    const int refill = bd.refill, burst = bd.burst, schedule = bd.schedule;
     const uint32_t n = bd.counters[countIdx];
     uint32_t* fetch = bd.counters + fetchIdx;
     const int lane = threadIdx.x & 31;
@@ -316,7 +316,16 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
             if (exhausted) break;
             continue;
         }
-        if (active) {
+        // schedule 1: only the lanes at the DDA level most lanes are at take this round
+        // (one level's code per round instead of all three), and stop when they leave it
+        int sel = -1;
+        if (schedule) {
+            const int n2 = __popc(__ballot_sync(0xffffffffu, active && wk.level == 2));
+            const int n1 = __popc(__ballot_sync(0xffffffffu, active && wk.level == 1));
+            const int n0 = __popc(__ballot_sync(0xffffffffu, active && wk.level == 0));
+            sel = n2 >= n1 ? (n2 >= n0 ? 2 : 0) : (n1 >= n0 ? 1 : 0);
+        }
+        if (active && (sel < 0 || wk.level == sel)) {
 #pragma unroll 1
             for (int s = 0; s < burst; s++) {
                 const int st = walk_step(wk, w);
@@ -325,6 +334,7 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
                     active = false;
                     break;
                 }
+                if (sel >= 0 && wk.level != sel) break;
             }
         }
     }
@@ -701,6 +711,7 @@ void apply_tuning(BatchDev& bd, const Tuning& tu) {
     bd.burst = tu.burst;
     bd.listPerSm = tu.listPerSm;
     bd.occupancy = tu.occupancy;
+    bd.schedule = tu.schedule;
 }
 
 BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, const Tuning& tu) {

@@ -83,6 +83,7 @@ struct BatchDev {
     int burst = 4;                        // shadow tracer: cell visits per lane between refill checks
     int listPerSm = 16;                   // blocks per SM of the hit-list kernels
     int occupancy = 0;                    // 1: register-capped shadow / RIS kernels (more warps per SM)
+    int schedule = 0;                     // shadow tracer: 1 = one DDA level per round (the majority's)
     int fuse = 0;                         // shading also accumulates
     uint32_t* hits = nullptr;             // hit list over all views
     float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(entry))
@@ -99,6 +100,7 @@ struct Tuning {
     int burst = 4;
     int listPerSm = 16;
     int occupancy = 0;
+    int schedule = 0;
 };
 
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s);

@@ -710,6 +710,7 @@ int check_tuning(const vxr_tuning* t, const char* fn) {
     if (t->list_blocks_per_sm < 1 || t->list_blocks_per_sm > 64)
         return set_error(VXR_E_INVALID, std::string(fn) + ": list_blocks_per_sm out of range [1, 64]");
     if (t->occupancy > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": occupancy must be 0 or 1");
+    if (t->shadow_schedule > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_schedule must be 0 or 1");
     return VXR_OK;
 }
 Tuning to_tuning(const vxr_tuning& t) {
@@ -721,6 +722,7 @@ Tuning to_tuning(const vxr_tuning& t) {
     u.burst = (int)t.shadow_burst;
     u.listPerSm = (int)t.list_blocks_per_sm;
     u.occupancy = (int)t.occupancy;
+    u.schedule = (int)t.shadow_schedule;
     return u;
 }
 }  // namespace vxr
@@ -735,6 +737,7 @@ extern "C" int vxr_default_tuning(vxr_tuning* t) {
     t->shadow_burst = (uint32_t)u.burst;
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
     t->occupancy = (uint32_t)u.occupancy;
+    t->shadow_schedule = (uint32_t)u.schedule;
     return VXR_OK;
 }
 
@@ -772,6 +775,7 @@ extern "C" int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t) {
     t->shadow_burst = (uint32_t)u.burst;
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
     t->occupancy = (uint32_t)u.occupancy;
+    t->shadow_schedule = (uint32_t)u.schedule;
     return VXR_OK;
 }
 

@@ -69,7 +69,7 @@ class ProposalDesc(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("tile_x", C.c_uint32), ("tile_y", C.c_uint32), ("persistent", C.c_uint32),
                 ("shadow_refill", C.c_uint32), ("shadow_burst", C.c_uint32), ("list_blocks_per_sm", C.c_uint32),
-                ("occupancy", C.c_uint32)]
+                ("occupancy", C.c_uint32), ("shadow_schedule", C.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -10,8 +10,10 @@ from conftest import assert_records_equal
 
 pytestmark = pytest.mark.gpu
 
-ODD = dict(tile_x=32, tile_y=4, persistent=1, shadow_refill=16, shadow_burst=16, list_blocks_per_sm=4, occupancy=1)
-ODD2 = dict(tile_x=8, tile_y=16, persistent=1, shadow_refill=1, shadow_burst=1, list_blocks_per_sm=1, occupancy=0)
+ODD = dict(tile_x=32, tile_y=4, persistent=1, shadow_refill=16, shadow_burst=16, list_blocks_per_sm=4, occupancy=1,
+           shadow_schedule=1)
+ODD2 = dict(tile_x=8, tile_y=16, persistent=1, shadow_refill=1, shadow_burst=1, list_blocks_per_sm=1, occupancy=0,
+            shadow_schedule=1)
 
 
 def _cam(f):
@@ -52,7 +54,8 @@ def test_tuning_rejects_bad_values(lib, cuda_device, scene0):
     v = lib.View(scene0[0], lib.view_desc(32, 32))
     try:
         for bad in (dict(tile_x=5, tile_y=5), dict(tile_x=64, tile_y=32), dict(tile_x=32, tile_y=16), dict(persistent=2), dict(shadow_refill=0),
-                    dict(shadow_refill=33), dict(shadow_burst=0), dict(shadow_burst=65), dict(list_blocks_per_sm=0), dict(occupancy=2)):
+                    dict(shadow_refill=33), dict(shadow_burst=0), dict(shadow_burst=65), dict(list_blocks_per_sm=0), dict(occupancy=2),
+                    dict(shadow_schedule=2)):
             with pytest.raises(lib.VxrError):
                 v.set_tuning(lib.tuning(**bad))
     finally:
