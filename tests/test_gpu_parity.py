@@ -72,3 +72,22 @@ def test_stage_parity_inside_world(lib, cuda_device, scene0, world0_arrays):
     # camera inside the map, looking down: primary rays start inside the grid
     _run_parity(lib, scene0, world0_arrays, 128, 96, True, 3,
                 lambda f: ((100.0 + f, 90.0, 100.0), (140.0, 40.0, 150.0)))
+
+
+@pytest.fixture(scope="module")
+def scene_big(lib):
+    """A 1024^3 world (config 1's terrain scaled x4, 4,096 emitters in the air) and its arrays."""
+    w = lib.World()
+    d = lib.scene_preset(1)
+    w.generate(d)
+    g, b, l = w.arrays()
+    return (w, d), ob.WorldArrays(g, b, l)
+
+
+@pytest.mark.parametrize("point", [False, True], ids=["area", "point"])
+def test_stage_parity_1024_world(lib, cuda_device, scene_big, point):
+    """The full 1024^3 map (all 32^3 uber cells, 128^3 grid, ~100k bricks), thousands of
+    emitters, a camera on the config's spline: every stage bit for bit."""
+    scene, arrays = scene_big
+    d = scene[1]
+    _run_parity(lib, scene, arrays, 96, 54, point, 3, lambda f: lib.camera_path(d, 1, 10 + f, 120))
