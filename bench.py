@@ -263,12 +263,25 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
 
 
 def run_batch(args, dist, rank, ws, warmup):
-    """Config 2: eight mixed views rendered as one batch per frame (CUDA graph), autotuned."""
+    """Configs 2 and 4: several views rendered as one batch per frame (CUDA graph), autotuned."""
     import smallproject_gb300 as vx
     from smallproject_gb300 import autotune as at
     from smallproject_gb300 import workloads as wl
-    worlds, views, descs, specs = wl.build_config2(seed=3)
-    cams = wl.config2_cameras(descs, specs, frames=60)
+    if args.config == 2:
+        worlds, views, descs, specs = wl.build_config2(seed=3)
+        cams = wl.config2_cameras(descs, specs, frames=60)
+        metric = "ms/frame, 8-view batch (config 2)"
+        workload = ("config2: 8 views, worlds {256,512,1024}^3, emitters log-uniform [16, 65536], resolutions "
+                    "{360p, 720p, 1080p}, point/area at random, seed 3, one CUDA graph per frame")
+    else:
+        world, views, desc, seeds = wl.build_config4()
+        worlds = [world]
+        specs = [{"width": v.desc.width, "height": v.desc.height, "light_model": "area", "path_seed": sd}
+                 for v, sd in zip(views, seeds)]
+        cams = [lambda f, sd=sd: vx.camera_path(desc, sd, f % 120, 120) for sd in seeds]
+        metric = "ms/frame, 4 x 3840x2160 batch (config 4, plain method)"
+        workload = ("config4: 4 views at 3840x2160, 1024^3 fBm 6 octaves + caves seed 5, 1,048,576 emitters "
+                    "(layer + 10% scattered), area lights, plain method, one CUDA graph per frame")
     batch = vx.Batch(views, graph=True)
     t, rep = at.autotune_batch(batch, cams, frames=2, rounds=1)
     step = [10000]
@@ -316,12 +329,10 @@ def run_batch(args, dist, rank, ws, warmup):
     if rank != 0:
         return
     npx = sum(s["width"] * s["height"] for s in specs)
-    line = {"metric": "ms/frame, 8-view batch (config 2)", "value": ms, "unit": "ms/frame", "n_gpus": ws,
+    line = {"metric": metric, "value": ms, "unit": "ms/frame", "n_gpus": ws,
             "steps": args.steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
-            "config": {"workload": "config2: 8 views, worlds {256,512,1024}^3, emitters log-uniform [16, 65536], "
-                                   "resolutions {360p, 720p, 1080p}, point/area at random, seed 3, one CUDA graph "
-                                   "per frame", "views": specs, "pixels": npx},
+            "config": {"workload": workload, "views": specs, "pixels": npx},
             "pixels_per_s": npx / (ms * 1e-3), "host_ms_per_frame": wall_ms,
             "individual_views_host_ms_per_frame": single_wall_ms,
             "tuning": rep["tuning"], "tuning_search": rep}
@@ -385,7 +396,7 @@ def main():
 
     from smallproject_gb300 import build as B
     B.build()
-    if args.config == 2:
+    if args.config in (2, 4):
         run_batch(args, dist, rank, ws, warmup)
         return
     vx, desc, world = make_scene(args.config)

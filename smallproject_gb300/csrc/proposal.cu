@@ -694,28 +694,28 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
             if (layer < 3) tc::epilogue64(trow, bs + layer * H, A, tid);
         }
         if (!ok) break;
-        // softmax tables of this thread's pixel from its 256 logits in TMEM (see infer_kernel)
-        float mx = -INFINITY;
-#pragma unroll 1
-        for (int ch = 0; ch < K / 32; ch++) {
-            float v[32];
-            tc::ld32(trow + ch * 32, v);
-#pragma unroll
-            for (int i = 0; i < 32; i++) mx = fmaxf(mx, v[i] + bs[3 * H + ch * 32 + i]);
-        }
-        float P[16];
-        float Z = 0.0f;
+        // softmax tables of this thread's pixel from its 256 logits in TMEM, one pass: each
+        // 32-column chunk (two groups) uses its own maximum; the in-group fractions do not
+        // depend on it, and the group totals are rescaled to the row maximum at the end
+        float Tg[16], Mc[8];
 #pragma unroll
         for (int ch = 0; ch < K / 32; ch++) {
             float v[32];
             tc::ld32(trow + ch * 32, v);
+            float m = -INFINITY;
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                v[i] += bs[3 * H + ch * 32 + i];
+                m = fmaxf(m, v[i]);
+            }
+            Mc[ch] = m;
 #pragma unroll
             for (int g2 = 0; g2 < 2; g2++) {
                 float pre[16];
                 float acc = 0.0f;
 #pragma unroll
                 for (int i = 0; i < 16; i++) {
-                    acc += __expf(v[g2 * 16 + i] + bs[3 * H + ch * 32 + g2 * 16 + i] - mx);
+                    acc += __expf(v[g2 * 16 + i] - m);
                     pre[i] = acc;
                 }
                 const float sc = acc > 0.0f ? 65535.0f / acc : 0.0f;
@@ -729,9 +729,18 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
                 uint4* dst = reinterpret_cast<uint4*>(fp + (ch * 2 + g2) * 16);
                 dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
                 dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-                Z += acc;
-                P[ch * 2 + g2] = Z;
+                Tg[ch * 2 + g2] = acc;
             }
+        }
+        float mx = Mc[0];
+#pragma unroll
+        for (int ch = 1; ch < K / 32; ch++) mx = fmaxf(mx, Mc[ch]);
+        float P[16];
+        float Z = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            Z += Tg[q] * __expf(Mc[q >> 1] - mx);
+            P[q] = Z;
         }
         tc::fence_before();   // this thread's TMEM reads are complete before the next tile's MMAs
         const float invZ = 1.0f / Z;

@@ -5,6 +5,10 @@ config 2: eight independent scenes and views rendered as one batch per frame. Fr
 seed: world sizes drawn from {256^3, 512^3, 1024^3}, emitter counts log-uniform in
 [16, 65536], resolutions from {640x360, 1280x720, 1920x1080}, point or area lights at
 random; each view follows its own seeded Catmull-Rom camera path.
+
+config 4 (stress, plain method): four 3840x2160 views of one 1024^3 world (fBm of 6
+octaves with caves, 1,048,576 emitters in a glowing layer plus 10% scattered), area
+lights, each view on its own camera path.
 """
 import numpy as np
 
@@ -49,3 +53,13 @@ def build_config2(seed=3, views=8, scale=1.0):
 def config2_cameras(descs, specs, frames=60):
     """Camera function per view: f -> (pos, target) on the view's own path."""
     return [lambda f, d=d, s=s: _v.camera_path(d, s["path_seed"], f % frames, frames) for d, s in zip(descs, specs)]
+
+
+def build_config4(views=4, scale=1.0):
+    """(world, views, scene desc, path seeds) of config 4 (the plain method)."""
+    d = _v.scene_preset(4)
+    w = _v.World()
+    w.generate(d)
+    W, H = max(16, int(3840 * scale)), max(16, int(2160 * scale))
+    vlist = [_v.View(w, _v.view_desc(W, H, _v.LIGHTS_AREA, rng_seed=5000 + i)) for i in range(views)]
+    return w, vlist, d, [500 + i for i in range(views)]
