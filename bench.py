@@ -10,7 +10,7 @@ albedo -> candidates (+ proposal inference) + temporal -> spatial -> shading+acc
 Quality protocol (untimed setup, --quality full): a converged render (FP64 mean of
 --conv-frames frames of the unbiased estimator: spatial and temporal reuse off) at path
 frame 150; the proposal trained online for --train-frames frames along the path on the
-plain method's reservoirs; then for each method and candidate count in CANDS, 8 seeds x
+plain method's reservoirs; then for each method and candidate count in CANDS, 16 seeds x
 16 frames at the static pose: device ms/frame and MSE against the converged render. The
 plain method's reference point is 32 candidates (the reference's NUMBEROFCANDIDATES).
 The timed configuration is the learned method at the smallest candidate count whose mean
@@ -361,7 +361,7 @@ def main():
     ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
     ap.add_argument("--train-frames", type=int, default=200)
-    ap.add_argument("--mse-seeds", type=int, default=8)
+    ap.add_argument("--mse-seeds", type=int, default=16)
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
     args = ap.parse_args()
