@@ -251,6 +251,12 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
         if table[f"learned_{c}"]["mse"] <= p32["mse"]:
             eq = table[f"learned_{c}"]
             break
+    # the same decision on the median per-frame MSE (single-frame MSE is heavy-tailed)
+    eq_med = None
+    for c in CANDS:
+        if table[f"learned_{c}"]["mse_median"] <= p32["mse_median"]:
+            eq_med = table[f"learned_{c}"]
+            break
     # equal time: the learned configuration with the largest ms/frame not above plain's
     at = [table[f"learned_{c}"] for c in CANDS if table[f"learned_{c}"]["ms"] <= p32["ms"]]
     et = max(at, key=lambda r: r["ms"]) if at else None
@@ -258,8 +264,9 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
             "train_frames": args.train_frames, "train_s": train_s, "train_batch": 65536,
             "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
             "frames_per_point": args.mse_seeds * args.mse_frames, "table": table,
-            "plain_reference": p32, "learned_at_equal_mse": eq,
-            "equal_time": None if et is None else {"learned": et, "mse_ratio": et["mse"] / p32["mse"]}}, params
+            "plain_reference": p32, "learned_at_equal_mse": eq, "learned_at_equal_median_mse": eq_med,
+            "equal_time": None if et is None else {"learned": et, "mse_ratio": et["mse"] / p32["mse"],
+                                                   "median_mse_ratio": et["mse_median"] / p32["mse_median"]}}, params
 
 
 def run_batch(args, dist, rank, ws, warmup):
