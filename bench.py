@@ -209,6 +209,11 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
         losses.append(trainer.proposal_train(1))
     trainer.wait()
     train_s = time.perf_counter() - t0
+    # device time of one training step (gather, forward, backward, Adam) on its own
+    trainer.timer_begin()
+    for _ in range(10):
+        trainer.proposal_train(1)
+    train_step_ms = trainer.timer_end() / 10
     params = trainer.proposal_params()
     trainer.close()
     table = {}
@@ -262,6 +267,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
     et = max(at, key=lambda r: r["ms"]) if at else None
     return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s, "epsilon": args.epsilon,
             "train_frames": args.train_frames, "train_s": train_s, "train_batch": 65536,
+            "train_step_ms": train_step_ms,
             "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
             "frames_per_point": args.mse_seeds * args.mse_frames, "table": table,
             "plain_reference": p32, "learned_at_equal_mse": eq, "learned_at_equal_median_mse": eq_med,
