@@ -1090,7 +1090,8 @@ void launch_sum(const float* v, uint32_t n, float* out, cudaStream_t s) {
 }
 
 void launch_colsum(const float* X, uint32_t B, int N, float* out, cudaStream_t s) {
-    colsum_kernel<<<dim3((N + 127) / 128, std::min<uint32_t>(B, 256)), 128, 0, s>>>(X, B, N, out);
+    // enough row groups that every thread sums only ~16 rows (latency, not bandwidth, bound)
+    colsum_kernel<<<dim3((N + 127) / 128, std::min<uint32_t>(std::max<uint32_t>(B / 16, 1), 8192)), 128, 0, s>>>(X, B, N, out);
 }
 
 void launch_encode_backward(const Dims& d, const Layout& L, const float4* samples, const float* dX, uint32_t B, float* grad,

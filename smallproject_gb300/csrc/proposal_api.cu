@@ -175,7 +175,7 @@ void forward_backward(vxr::Proposal* p, uint32_t B, cudaStream_t s) {
         g.B = Xin; g.sbk = kin; g.sbn = 1;
         g.C = G + wo; g.scm = kin; g.scn = 1;
         g.M = nout; g.N = kin; g.K = (int)B;
-        g.mode = 4; g.kchunk = 512;
+        g.mode = 4; g.kchunk = 128;
         launch_gemm(g, s);
         launch_colsum(dY, B, nout, G + bo, s);
     };
