@@ -105,6 +105,31 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
     return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
 }
 
+// Block-aggregated append: one atomic per block and call instead of one per warp, so a
+// list filled by a short kernel is not serialised on its counter. Every thread of the
+// block calls it (flag = this thread appends); returns this thread's slot when flag.
+__device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool flag) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)((blockDim.x + 31) >> 5);
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0) s_warp[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < nw; w++) {
+            const uint32_t c = s_warp[w];
+            s_warp[w] = tot;
+            tot += c;
+        }
+        s_base = tot ? atomicAdd(counter, tot) : 0u;
+    }
+    __syncthreads();
+    const uint32_t slot = s_base + s_warp[warp] + (uint32_t)__popc(m & ((1u << lane) - 1u));
+    __syncthreads();   // the shared words are reused by the next call
+    return slot;
+}
+
 // Next tile of the batch for this block: with bd.persistent, resident blocks pull tiles
 // from the queue cursor `ctr` until it is drained; otherwise the launch has one block per
 // tile and the hardware block scheduler balances them. `round` counts calls (starts at 0).
@@ -194,11 +219,15 @@ __global__ void __launch_bounds__(256) compact_hits_kernel(const __grid_constant
     const uint2* vd = V->b.vd[V->cur];
     uint4* cA = V->b.cA;
     float4* cB = V->b.cB;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t voxel = vd[i].x & 0x00FFFFFFu;
-        if (voxel != 0u) {
-            bd.hits[append_slot(bd.counters + kCtrHits)] = (blockIdx.y << 27) | i;
-        } else {
+    // every thread of a block runs the same iterations (block_append needs all of them)
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        const bool in = i < n;
+        const bool hit = in && (vd[i].x & 0x00FFFFFFu) != 0u;
+        const uint32_t slot = block_append(bd.counters + kCtrHits, hit);
+        if (hit) {
+            bd.hits[slot] = (blockIdx.y << 27) | i;
+        } else if (in) {
             cA[i] = make_uint4(0u, 6u << 29, 0u, 0u);
             cB[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
@@ -534,31 +563,43 @@ __global__ void __launch_bounds__(kMaxTileThreads) spatial_kernel(const __grid_c
 template <int VARIANT>
 __global__ void __launch_bounds__(128) shade_request_kernel(const __grid_constant__ BatchDev bd) {
     const uint32_t nh = bd.counters[kCtrHits];
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += gridDim.x * blockDim.x) {
-        const uint32_t e = bd.hits[j];
-        const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
-        const Frame& k = V->k;
-        const uint32_t i = pix_of<VARIANT>(e);
-        const uint4 qa = V->b.hA[i];
-        const uint32_t M = qa.y & 0x1FFFFFFFu;
-        const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, __uint_as_float(qa.w) * (float)M);
-        if (!(W > 0.0f && M > 0u)) continue;
-        const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
-        const uint2 g = V->b.vd[V->cur][i];
-        const uint32_t side = g.x >> 24;
-        const float dist = __uint_as_float(g.y);
-        const float3 D = camera_ray(k, x, y);
-        const float nsign = side_sign(side, D);
-        const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
-        const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
-                              sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
-        uint32_t li = qa.x;
-        if (li >= k.nlights) { raise_error(V->b.err, 8u); li = 0; }
-        const float4 qb = __ldg(V->b.hB + i);
-        const float3 L = normalize3(sub(f3(qb.x, qb.y, qb.z), spo));
-        const uint32_t slot = append_slot(bd.counters + kCtrQ2);
-        bd.qA[slot] = make_float4(spo.x, spo.y, spo.z, __uint_as_float(e));
-        bd.qB[slot] = make_float4(L.x, L.y, L.z, __uint_as_float(li));
+    // every thread of a block runs the same iterations (block_append needs all of them)
+    for (uint32_t j0 = blockIdx.x * blockDim.x; j0 < nh; j0 += gridDim.x * blockDim.x) {
+        const uint32_t j = j0 + threadIdx.x;
+        bool want = false;
+        float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f), rb = ra;
+        if (j < nh) {
+            const uint32_t e = bd.hits[j];
+            const ViewDev* V = view_of<VARIANT>(bd, e >> 27);
+            const Frame& k = V->k;
+            const uint32_t i = pix_of<VARIANT>(e);
+            const uint4 qa = V->b.hA[i];
+            const uint32_t M = qa.y & 0x1FFFFFFFu;
+            const float W = __uint_as_float(qa.z) / fmaxf(1e-5f, __uint_as_float(qa.w) * (float)M);
+            if (W > 0.0f && M > 0u) {
+                const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
+                const uint2 g = V->b.vd[V->cur][i];
+                const uint32_t side = g.x >> 24;
+                const float dist = __uint_as_float(g.y);
+                const float3 D = camera_ray(k, x, y);
+                const float nsign = side_sign(side, D);
+                const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+                const float3 spo = f3(sp.x + (side == 0 ? 0.1f * nsign : 0.0f), sp.y + (side == 1 ? 0.1f * nsign : 0.0f),
+                                      sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
+                uint32_t li = qa.x;
+                if (li >= k.nlights) { raise_error(V->b.err, 8u); li = 0; }
+                const float4 qb = __ldg(V->b.hB + i);
+                const float3 L = normalize3(sub(f3(qb.x, qb.y, qb.z), spo));
+                ra = make_float4(spo.x, spo.y, spo.z, __uint_as_float(e));
+                rb = make_float4(L.x, L.y, L.z, __uint_as_float(li));
+                want = true;
+            }
+        }
+        const uint32_t slot = block_append(bd.counters + kCtrQ2, want);
+        if (want) {
+            bd.qA[slot] = ra;
+            bd.qB[slot] = rb;
+        }
     }
 }
 
