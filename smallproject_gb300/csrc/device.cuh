@@ -20,6 +20,10 @@ struct World {
     const uint32_t* __restrict__ grid;    // 128^3 cells, x + z*128 + y*16384
     const uint8_t* __restrict__ uber;     // 32^3 occupancy, x + z*32 + y*1024
     const uint32_t* __restrict__ bricks;  // nbricks * 512 voxels
+    // per brick, or null: the box of its opaque voxels (type 15), corners in voxels from
+    // the brick's corner: low x, y, z in bits 0-2, 3-5, 6-8, high x, y, z (inclusive) in
+    // bits 9-11, 12-14, 15-17; kNoOpaque when the brick has no opaque voxel
+    const uint32_t* __restrict__ bbox;
     const float4* __restrict__ lgeom;
     const float4* __restrict__ lemit;
     uint32_t nlights;
@@ -339,25 +343,67 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
 // soon as its current one ends instead of idling until the warp's longest ray is done.
 // Every float op, the step budget accounting and the exit cascade (brick -> grid step
 // -> uber step) follow trace<MODE> exactly; the oracle checks the two for equality.
+//
+// The three levels share one code for each action (visit, descent, DDA step, ascent,
+// cell load): the current cell (cx, cy, cz) is in uber, grid or voxel units by level,
+// and a lane is inside its parent cell while cell >> sh equals the parent (sh = 5 with
+// parent 0 at the uber level: inside the map). Lanes of a warp at different levels then
+// issue one instruction stream instead of one per level.
 struct Walker {
-    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;   // cell step in t per axis: |r| (= sign(v) * r)
-    float t, tmx, tmy, tmz;        // current level
+    float ax, ay, az, vx, vy, vz, rx, ry, rz, to;
+    float t, tmx, tmy, tmz;        // crossings of the current level
     float umx, umy, umz;           // saved uber-level crossings
     float gmx, gmy, gmz;           // saved grid-level crossings
-    int ux, uy, uz, gx, gy, gz, lx, ly, lz;
-    int steps, level, bi;
-    uint32_t o, brick, last;
+    int cx, cy, cz;                // current cell
+    int px, py, pz;                // parent of the current cell (0 at the uber level)
+    int ux, uy, uz, gx, gy, gz;    // uber cell / grid cell being walked below
+    int sh;                        // 5 (uber), 2 (grid), 3 (brick)
+    int steps, level, cnt;         // cnt: brick steps left (a brick walk ends after 24)
+    uint32_t o, brick, last;       // o: value of the current cell (uber byte, grid cell, voxel)
     int stx, sty, stz;             // axis steps (+-1)
     float dist;                    // result
     uint32_t side, voxel;
-    __device__ __forceinline__ int sx() const { return stx; }
-    __device__ __forceinline__ int sy() const { return sty; }
-    __device__ __forceinline__ int sz() const { return stz; }
     __device__ __forceinline__ int ox() const { return stx > 0 ? 1 : 0; }
     __device__ __forceinline__ int oy() const { return sty > 0 ? 1 : 0; }
     __device__ __forceinline__ int oz() const { return stz > 0 ? 1 : 0; }
 };
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
+constexpr int kWalkNoCap = 1 << 30;   // cnt above the brick level: never runs out
+
+// Brick skipping. A brick walk that ends without a hit leaves the walk exactly where
+// skipping the brick would: the grid-level crossings saved at the descent are restored
+// and the grid step follows, and brick visits cost no budget. So a brick may be skipped
+// (treated as an empty grid cell) when none of the voxels the DDA could visit in it is
+// opaque. The DDA visits only voxels within a few hundredths of a voxel of the ray's
+// line (its crossing times follow the line up to float rounding), so a brick is skipped
+// when the line misses the box of its opaque voxels grown by kBrickSlack = 0.1 voxel on
+// every side (a slab test; its own rounding is far below the slack).
+constexpr float kBrickSlack = 0.1f;
+constexpr uint32_t kNoOpaque = 0xFFFFFFFFu;
+
+__device__ __forceinline__ bool brick_clear(const Walker& k, uint32_t box) {
+    if (box == kNoOpaque) return true;
+    const float bx = (float)(k.cx * 8), by = (float)(k.cy * 8), bz = (float)(k.cz * 8);
+    const float x0 = ((bx + (float)(box & 7u)) - kBrickSlack - k.ax) * k.rx;
+    const float x1 = ((bx + (float)((box >> 9) & 7u)) + (1.0f + kBrickSlack) - k.ax) * k.rx;
+    const float y0 = ((by + (float)((box >> 3) & 7u)) - kBrickSlack - k.ay) * k.ry;
+    const float y1 = ((by + (float)((box >> 12) & 7u)) + (1.0f + kBrickSlack) - k.ay) * k.ry;
+    const float z0 = ((bz + (float)((box >> 6) & 7u)) - kBrickSlack - k.az) * k.rz;
+    const float z1 = ((bz + (float)((box >> 15) & 7u)) + (1.0f + kBrickSlack) - k.az) * k.rz;
+    const float tin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
+    const float tout = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+    return tin > tout;
+}
+
+// value of the current cell at the current level
+__device__ __forceinline__ void walk_load(Walker& k, const World& w) {
+    if (k.level == 0)
+        k.o = __ldg(w.uber + k.cx + k.cz * 32 + k.cy * 1024);
+    else if (k.level == 1)
+        k.o = __ldg(w.grid + k.cx + k.cz * 128 + k.cy * 16384);
+    else
+        k.o = __ldg(w.bricks + (size_t)k.brick * 512u + (uint32_t)((k.cx & 7) | ((k.cy & 7) << 3) | ((k.cz & 7) << 6)));
+}
 
 // TraceOpaqueRay prologue (trace.cl:219-243); returns WALK_MISS when the ray misses the map
 __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, float ay, float az, float vx, float vy,
@@ -391,116 +437,103 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
         if (az < 0.01f || az > hi) k.last = 2;
     }
     k.ax = ax; k.ay = ay; k.az = az;
-    k.ux = (int)min(f2u(ax) >> 5, 31u);
-    k.uy = (int)min(f2u(ay) >> 5, 31u);
-    k.uz = (int)min(f2u(az) >> 5, 31u);
-    k.tmx = ((float)(uint32_t)(k.ux + k.ox()) - ax * 0.03125f) * k.rx;
-    k.tmy = ((float)(uint32_t)(k.uy + k.oy()) - ay * 0.03125f) * k.ry;
-    k.tmz = ((float)(uint32_t)(k.uz + k.oz()) - az * 0.03125f) * k.rz;
+    k.cx = (int)min(f2u(ax) >> 5, 31u);
+    k.cy = (int)min(f2u(ay) >> 5, 31u);
+    k.cz = (int)min(f2u(az) >> 5, 31u);
+    k.tmx = ((float)(uint32_t)(k.cx + k.ox()) - ax * 0.03125f) * k.rx;
+    k.tmy = ((float)(uint32_t)(k.cy + k.oy()) - ay * 0.03125f) * k.ry;
+    k.tmz = ((float)(uint32_t)(k.cz + k.oz()) - az * 0.03125f) * k.rz;
     k.t = 0.0f;
+    k.px = k.py = k.pz = 0;
+    k.sh = 5;
     k.steps = steps;
     k.level = 0;
-    k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
+    k.cnt = kWalkNoCap;
+    walk_load(k, w);
     return WALK_CONTINUE;
 }
 
-// uber-level step (trace.cl:274-279); returns false when the ray leaves the map
-__device__ __forceinline__ bool walk_uber_step(Walker& k, const World& w) {
-    k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-    k.last = 0;
-    if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.ux += k.sx(); }
-    if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.uy += k.sy(); k.last = 1; }
-    if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.uz += k.sz(); k.last = 2; }
-    if ((k.ux | k.uy | k.uz) & ~31) return false;
-    k.o = __ldg(w.uber + k.ux + k.uz * 32 + k.uy * 1024);
-    return true;
-}
-
-// grid-level step (GRIDSTEP tail, trace.cl:105-110); continues into the uber step
-// when the ray leaves the current uber cell
-__device__ __forceinline__ int walk_grid_step(Walker& k, const World& w) {
-    k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-    k.last = 0;
-    if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.gx += k.sx(); }
-    if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.gy += k.sy(); k.last = 1; }
-    if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.gz += k.sz(); k.last = 2; }
-    if (((k.gx >> 2) != k.ux) | ((k.gy >> 2) != k.uy) | ((k.gz >> 2) != k.uz)) {
-        k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
-        k.level = 0;
-        return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
-    }
-    k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
-    return WALK_CONTINUE;
-}
-
-// one cell visit at the current level
+// One cell visit at the current level, then one action: the hit or the budget miss,
+// a descent into the cell (uber -> grid, trace.cl:262-273; grid -> brick, GRIDSTEP,
+// trace.cl:85-104), or a DDA step (BRICKSTEP / GRIDSTEP tail / uber loop,
+// trace.cl:66-80, 105-110, 274-279) that climbs a level each time it leaves the parent
+// cell and ends as a miss when it leaves the map.
 __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
-    if (k.level == 2) {
-        const uint32_t v = __ldg(w.bricks + (size_t)k.brick * 512u + k.lx + k.ly * 8 + k.lz * 64);
-        if (((v & 0xf000u) >> 12) == 15u) {
-            k.dist = k.t + k.to;
-            k.side = k.last;
-            k.voxel = v;
-            return WALK_HIT;
-        }
-        k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
-        k.last = 0;
-        if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.lx += k.sx(); }
-        if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.ly += k.sy(); k.last = 1; }
-        if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.lz += k.sz(); k.last = 2; }
-        if (((k.lx | k.ly | k.lz) & ~7) || ++k.bi == 24) {
-            k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
-            k.level = 1;
-            return walk_grid_step(k, w);
-        }
-        return WALK_CONTINUE;
+    const int lv = k.level;
+    // a grid step with the budget exhausted always ends as a miss (the uber loop
+    // re-checks the budget before any further cell is visited)
+    k.steps -= lv == 0 ? 4 : (lv == 1 ? 1 : 0);
+    if (lv < 2 && k.steps <= 0) return WALK_MISS;
+    // uber: descend into a non-empty cell; grid: descend into a brick, hit an opaque
+    // brick-less cell; brick: hit an opaque voxel
+    const uint32_t hv = lv == 1 ? k.o >> 1 : k.o;
+    const bool brickcell = lv == 1 && (k.o & 1u);
+    bool desc = lv == 0 ? k.o != 0u : brickcell;
+    const bool hit = lv != 0 && !brickcell && ((hv & 0xf000u) >> 12) == 15u;
+    if (brickcell && w.bbox && brick_clear(k, __ldg(w.bbox + (k.o >> 1))))
+        desc = false;   // a brick the ray cannot stop in: step on as over an empty cell
+    if (hit) {
+        k.dist = (lv == 1 ? k.t * 8.0f : k.t) + k.to;
+        k.side = k.last;
+        k.voxel = hv;
+        return WALK_HIT;
     }
-    if (k.level == 1) {
-        // a grid step with the budget exhausted always ends as a miss (the uber loop
-        // re-checks the budget before any further cell is visited)
-        if (!--k.steps) return WALK_MISS;
-        if ((k.o & 1u) == 0u) {
-            const uint32_t v = k.o >> 1;
-            if (((v & 0xf000u) >> 12) == 15u) {
-                k.dist = k.t * 8.0f + k.to;
-                k.side = k.last;
-                k.voxel = v;
-                return WALK_HIT;
+    if (desc) {
+        // uber -> grid: t in grid units (x4), entry cell from 0.125 * a + v * t;
+        // grid -> brick: t in voxel units (x8), entry voxel from a + v * t
+        const bool top = lv == 0;
+        const float S = top ? 4.0f : 8.0f, K = top ? 0.125f : 1.0f;
+        const uint32_t W = top ? 2u : 3u;
+        if (top) {
+            k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
+            k.ux = k.cx; k.uy = k.cy; k.uz = k.cz;
+        } else {
+            k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
+            k.gx = k.cx; k.gy = k.cy; k.gz = k.cz;
+            k.brick = k.o >> 1;
+        }
+        k.t *= S;
+        const uint32_t qx = f2u(K * k.ax + k.vx * k.t), qy = f2u(K * k.ay + k.vy * k.t),
+                       qz = f2u(K * k.az + k.vz * k.t);
+        const uint32_t lx = (uint32_t)k.cx << W, ly = (uint32_t)k.cy << W, lz = (uint32_t)k.cz << W;
+        const uint32_t span = (1u << W) - 1u;
+        k.px = k.cx; k.py = k.cy; k.pz = k.cz;
+        k.cx = (int)min(max(qx, lx), lx + span);
+        k.cy = (int)min(max(qy, ly), ly + span);
+        k.cz = (int)min(max(qz, lz), lz + span);
+        k.tmx = ((float)(uint32_t)(k.cx + k.ox()) - k.ax * K) * k.rx;
+        k.tmy = ((float)(uint32_t)(k.cy + k.oy()) - k.ay * K) * k.ry;
+        k.tmz = ((float)(uint32_t)(k.cz + k.oz()) - k.az * K) * k.rz;
+        k.sh = (int)W;
+        k.cnt = top ? kWalkNoCap : 24;
+        k.level = lv + 1;
+    } else {
+        while (true) {
+            k.t = fminf(k.tmx, fminf(k.tmy, k.tmz));
+            k.last = 0;
+            if (k.t == k.tmx) { k.tmx += fabsf(k.rx); k.cx += k.stx; }
+            if (k.t == k.tmy) { k.tmy += fabsf(k.ry); k.cy += k.sty; k.last = 1; }
+            if (k.t == k.tmz) { k.tmz += fabsf(k.rz); k.cz += k.stz; k.last = 2; }
+            const bool inside = ((k.cx >> k.sh) == k.px) & ((k.cy >> k.sh) == k.py) & ((k.cz >> k.sh) == k.pz);
+            if (inside && --k.cnt != 0) break;
+            if (k.level == 0) return WALK_MISS;
+            if (k.level == 2) {
+                k.tmx = k.gmx; k.tmy = k.gmy; k.tmz = k.gmz;
+                k.cx = k.gx; k.cy = k.gy; k.cz = k.gz;
+                k.px = k.ux; k.py = k.uy; k.pz = k.uz;
+                k.sh = 2;
+                k.cnt = kWalkNoCap;
+            } else {
+                k.tmx = k.umx; k.tmy = k.umy; k.tmz = k.umz;
+                k.cx = k.ux; k.cy = k.uy; k.cz = k.uz;
+                k.px = k.py = k.pz = 0;
+                k.sh = 5;
             }
-            return walk_grid_step(k, w);
+            k.level--;
         }
-        k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
-        k.t *= 8.0f;
-        const uint32_t px = f2u(k.ax + k.vx * k.t), py = f2u(k.ay + k.vy * k.t), pz = f2u(k.az + k.vz * k.t);
-        const uint32_t bx0 = (uint32_t)k.gx * 8u, by0 = (uint32_t)k.gy * 8u, bz0 = (uint32_t)k.gz * 8u;
-        const uint32_t cx = min(max(px, bx0), bx0 + 7u), cy = min(max(py, by0), by0 + 7u), cz = min(max(pz, bz0), bz0 + 7u);
-        k.tmx = ((float)(cx + (uint32_t)k.ox()) - k.ax) * k.rx;
-        k.tmy = ((float)(cy + (uint32_t)k.oy()) - k.ay) * k.ry;
-        k.tmz = ((float)(cz + (uint32_t)k.oz()) - k.az) * k.rz;
-        k.lx = (int)(cx & 7u); k.ly = (int)(cy & 7u); k.lz = (int)(cz & 7u);
-        k.brick = k.o >> 1;
-        k.bi = 0;
-        k.level = 2;
-        return WALK_CONTINUE;
     }
-    // uber level
-    if ((k.steps -= 4) <= 0) return WALK_MISS;
-    if (k.o != 0u) {
-        k.umx = k.tmx; k.umy = k.tmy; k.umz = k.tmz;
-        k.t *= 4.0f;
-        const uint32_t qx = f2u(0.125f * k.ax + k.vx * k.t), qy = f2u(0.125f * k.ay + k.vy * k.t),
-                       qz = f2u(0.125f * k.az + k.vz * k.t);
-        k.gx = (int)min(max(qx, (uint32_t)k.ux * 4u), (uint32_t)k.ux * 4u + 3u);
-        k.gy = (int)min(max(qy, (uint32_t)k.uy * 4u), (uint32_t)k.uy * 4u + 3u);
-        k.gz = (int)min(max(qz, (uint32_t)k.uz * 4u), (uint32_t)k.uz * 4u + 3u);
-        k.tmx = ((float)(uint32_t)(k.gx + k.ox()) - k.ax * 0.125f) * k.rx;
-        k.tmy = ((float)(uint32_t)(k.gy + k.oy()) - k.ay * 0.125f) * k.ry;
-        k.tmz = ((float)(uint32_t)(k.gz + k.oz()) - k.az * 0.125f) * k.rz;
-        k.o = __ldg(w.grid + k.gx + k.gz * 128 + k.gy * 16384);
-        k.level = 1;
-        return WALK_CONTINUE;
-    }
-    return walk_uber_step(k, w) ? WALK_CONTINUE : WALK_MISS;
+    walk_load(k, w);
+    return WALK_CONTINUE;
 }
 
 // ---- reservoirs --------------------------------------------------------------------

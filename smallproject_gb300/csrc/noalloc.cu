@@ -141,6 +141,7 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     w.grid = grid;
     w.uber = s + kOffUber;
     w.bricks = bricks;
+    w.bbox = nullptr;   // no room for brick boxes: visibility walks every brick
     w.lgeom = geom;
     w.lemit = emit;
     w.nlights = nlights;

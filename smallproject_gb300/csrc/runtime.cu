@@ -34,6 +34,7 @@ void release_device_world(World& w) {
     cudaFree(d->grid);
     cudaFree(d->uber);
     cudaFree(d->bricks);
+    cudaFree(d->bbox);
     cudaFree(d->lraw);
     cudaFree(d->lgeom);
     cudaFree(d->lemit);
@@ -62,6 +63,13 @@ static int upload(World& w) {
         CU(cudaMalloc(&d.bricks, bb), "cudaMalloc(bricks)");
         d.brickBytes = bb;
     }
+    const size_t sb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * sizeof(uint32_t);
+    if (sb > d.bboxBytes) {
+        cudaFree(d.bbox);
+        d.bbox = nullptr;
+        CU(cudaMalloc(&d.bbox, sb), "cudaMalloc(brick boxes)");
+        d.bboxBytes = sb;
+    }
     CU(cudaMemcpy(d.grid, w.grid.data(), kGridSize * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload grid");
     if (w.brickHigh)
         CU(cudaMemcpy(d.bricks, w.bricks.data(), (size_t)w.brickHigh * kBrick * sizeof(uint32_t), cudaMemcpyHostToDevice),
@@ -83,6 +91,7 @@ static int upload(World& w) {
     CU(cudaMemcpy(d.lraw, raw.data(), need * sizeof(uint4), cudaMemcpyHostToDevice), "upload lights");
     launch_build_light_table(d.lraw, (uint32_t)need, d.lgeom, d.lemit, 0);
     launch_build_uber(d.grid, d.uber, 0);
+    launch_build_brick_boxes(d.bricks, w.brickHigh, d.bbox, 0);
     CU(cudaGetLastError(), "world kernels launch");
     CU(cudaDeviceSynchronize(), "world kernels");
     d.nl = nl;
@@ -113,6 +122,7 @@ vxr::dev::World dev_world(vxr_view* v) {
     w.grid = d.grid;
     w.uber = d.uber;
     w.bricks = d.bricks;
+    w.bbox = d.bbox;
     w.lgeom = d.lgeom;
     w.lemit = d.lemit;
     w.nlights = d.nl;

@@ -16,6 +16,8 @@ struct DeviceWorld {
     uint8_t* uber = nullptr;
     uint32_t* bricks = nullptr;
     size_t brickBytes = 0;
+    uint32_t* bbox = nullptr;        // box of the opaque voxels per brick (brick skipping)
+    size_t bboxBytes = 0;
     uint4* lraw = nullptr;
     float4* lgeom = nullptr;
     float4* lemit = nullptr;

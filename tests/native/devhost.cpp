@@ -40,7 +40,7 @@ using namespace vxr::dev;
 
 static World make_world(const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks) {
     World w;
-    w.grid = grid; w.uber = uber; w.bricks = bricks; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
+    w.grid = grid; w.uber = uber; w.bricks = bricks; w.bbox = nullptr; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
     return w;
 }
 
@@ -170,6 +170,25 @@ uint32_t dh_walk_burst(const uint32_t* grid, const uint8_t* uber, const uint32_t
     *dist = 0.0f;
     *side = 0;
     return 0u;
+}
+
+// the walker with brick skipping (bbox: per brick the packed box of its opaque voxels);
+// *visits: cells visited
+int dh_walk_skip(const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks, const uint32_t* bbox,
+                 const float* O, const float* D, int steps, float* dist, uint32_t* side, int* visits) {
+    World w = make_world(grid, uber, bricks);
+    w.bbox = bbox;
+    Walker k;
+    int st = walk_init(k, w, O[0], O[1], O[2], D[0], D[1], D[2], steps);
+    int n = 0;
+    while (st == WALK_CONTINUE) {
+        st = walk_step(k, w);
+        n++;
+    }
+    *dist = st == WALK_HIT ? k.dist : 0.0f;
+    *side = st == WALK_HIT ? k.side : 0u;
+    *visits = n;
+    return st;
 }
 
 void dh_sincos(float a, float* s, float* c) { sincos_vx(a, s, c); }

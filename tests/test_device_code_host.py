@@ -35,6 +35,7 @@ def dh():
     lib.dh_walk_burst.restype = C.c_uint32
     lib.dh_walk_burst.argtypes = [P, P, P, F, F, C.c_int, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     lib.dh_area_sample.argtypes = [C.c_int, F, F, C.c_uint32, F]
+    lib.dh_walk_skip.argtypes = [P, P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     return lib
 
 
@@ -108,6 +109,63 @@ def test_walker_bursts_match_single_visits(dh, world0_arrays):
                 np.float32(dist.value).view(np.uint32) == np.float32(d2.value).view(np.uint32), (i, burst)
         else:
             assert v == 0, (i, burst)
+
+
+def brick_boxes(bricks):
+    """Per brick the box of its opaque voxels (type nibble 15), packed as the GPU builds
+    it at upload (build_brick_boxes_kernel): low x, y, z in bits 0-8, high (inclusive)
+    in bits 9-17, 3 bits each; 0xFFFFFFFF when the brick has no opaque voxel."""
+    op = (((bricks.reshape(-1, 8, 8, 8) >> 12) & 15) == 15)        # [n, z, y, x]
+    out = np.full(len(op), 0xFFFFFFFF, np.uint32)
+    for i in np.nonzero(op.any(axis=(1, 2, 3)))[0]:
+        z, y, x = np.nonzero(op[i])
+        lo, hi = (x.min(), y.min(), z.min()), (x.max(), y.max(), z.max())
+        out[i] = sum(int(v) << (3 * a) for a, v in enumerate(lo)) | sum(int(v) << (9 + 3 * a) for a, v in enumerate(hi))
+    return out
+
+
+def _surface_rays(wa, n, seed):
+    """Rays from just above the terrain of world0 towards random points: the shape of
+    shadow rays (they leave a surface and cross bricks near it)."""
+    rng = np.random.default_rng(seed)
+    g = wa.grid.reshape(128, 128, 128)                                   # [y, z, x]
+    occ = g != 0
+    o = np.zeros((n, 3), np.float32)
+    for i in range(n):
+        x, z = int(rng.integers(0, 256)), int(rng.integers(0, 256))
+        col = np.nonzero(occ[:, z // 8, x // 8])[0]
+        top = (int(col.max()) * 8 + 8) if len(col) else 0
+        o[i] = (x + rng.random(), top + rng.uniform(-6.0, 3.0), z + rng.random())
+    tgt = rng.uniform([0, 0, 0], [256, 160, 256], (n, 3)).astype(np.float32)
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o, d.astype(np.float32), rng
+
+
+def test_walker_brick_skipping_is_exact(dh, world0_arrays):
+    """Skipping bricks whose opaque-voxel box the ray's line misses (by more than the
+    slack) changes no walk result (status, distance bits, side), and skips bricks on
+    surface-leaving rays."""
+    wa = world0_arrays
+    boxes = brick_boxes(wa.bricks)
+    assert (boxes != 0xFFFFFFFF).any()
+    o1, d1, rng = _rays(3000, 41)
+    o2, d2, _ = _surface_rays(wa, 3000, 43)
+    o, d = np.concatenate([o1, o2]), np.concatenate([d1, d2])
+    saved = hits = 0
+    for i in range(len(o)):
+        steps = int(rng.choice([128, 128, 999999, 5, 1]))
+        da, sa, sta, nva = C.c_float(0), C.c_uint32(0), C.c_int(0), C.c_int(0)
+        dh.dh_walk(wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, _f3(o[i]), _f3(d[i]), steps,
+                   C.byref(da), C.byref(sa), C.byref(sta), C.byref(nva))
+        db, sb, nvb = C.c_float(0), C.c_uint32(0), C.c_int(0)
+        stb = dh.dh_walk_skip(wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, boxes.ctypes.data,
+                              _f3(o[i]), _f3(d[i]), steps, C.byref(db), C.byref(sb), C.byref(nvb))
+        assert sta.value == stb and sa.value == sb.value and \
+            np.float32(da.value).view(np.uint32) == np.float32(db.value).view(np.uint32), (i, o[i], d[i], steps)
+        saved += nva.value - nvb.value
+        hits += stb == 1
+    assert hits > 500 and saved > 10000
 
 
 def test_device_sincos_matches_oracle(dh):
