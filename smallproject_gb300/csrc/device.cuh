@@ -24,6 +24,8 @@ struct World {
     // the brick's corner: low x, y, z in bits 0-2, 3-5, 6-8, high x, y, z (inclusive) in
     // bits 9-11, 12-14, 15-17; kNoOpaque when the brick has no opaque voxel
     const uint32_t* __restrict__ bbox;
+    // the same for the non-zero voxels (what stops a primary ray), or null
+    const uint32_t* __restrict__ bbox0;
     const float4* __restrict__ lgeom;
     const float4* __restrict__ lemit;
     uint32_t nlights;
@@ -220,6 +222,35 @@ __device__ __forceinline__ void sincos_vx(float a, float* s, float* c) {
 // MODE 0: first non-zero voxel. MODE 1: first opaque voxel (alpha 0xF). MODE 2: first
 // voxel whose masked value differs from `through` (empty space included).
 // dist/side are written only when a voxel is returned (reference behaviour).
+// Brick skipping. A brick walk that ends without a hit leaves the walk exactly where
+// skipping the brick would: the grid-level crossings saved at the descent are restored
+// and the grid step follows, and brick visits cost no budget. So a brick may be skipped
+// (treated as an empty grid cell) when none of the voxels the DDA could visit in it is
+// opaque. The DDA visits only voxels within a few hundredths of a voxel of the ray's
+// line (its crossing times follow the line up to float rounding), so a brick is skipped
+// when the line misses the box of its opaque voxels grown by kBrickSlack = 0.1 voxel on
+// every side (a slab test; its own rounding is far below the slack). Primary rays
+// (trace<0>) skip the same way with the box of the non-zero voxels.
+constexpr float kBrickSlack = 0.1f;
+constexpr uint32_t kNoOpaque = 0xFFFFFFFFu;
+
+// true when the ray a + v t (r = 1 / v) misses the box `box` of the brick at grid cell
+// (gx, gy, gz) grown by the slack
+__device__ __forceinline__ bool brick_clear(float ax, float ay, float az, float rx, float ry, float rz, int gx, int gy,
+                                            int gz, uint32_t box) {
+    if (box == kNoOpaque) return true;
+    const float bx = (float)(gx * 8), by = (float)(gy * 8), bz = (float)(gz * 8);
+    const float x0 = ((bx + (float)(box & 7u)) - kBrickSlack - ax) * rx;
+    const float x1 = ((bx + (float)((box >> 9) & 7u)) + (1.0f + kBrickSlack) - ax) * rx;
+    const float y0 = ((by + (float)((box >> 3) & 7u)) - kBrickSlack - ay) * ry;
+    const float y1 = ((by + (float)((box >> 12) & 7u)) + (1.0f + kBrickSlack) - ay) * ry;
+    const float z0 = ((bz + (float)((box >> 6) & 7u)) - kBrickSlack - az) * rz;
+    const float z1 = ((bz + (float)((box >> 15) & 7u)) + (1.0f + kBrickSlack) - az) * rz;
+    const float tin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
+    const float tout = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+    return tin > tout;
+}
+
 template <int MODE>
 __device__ __forceinline__ bool dda_hit(uint32_t v, uint32_t through, uint32_t mask) {
     if (MODE == 0) return v != 0u;
@@ -287,7 +318,9 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
                         *side = last;
                         return v;
                     }
-                } else {
+                } else if (!(MODE == 0 && w.bbox0 &&
+                             brick_clear(ax, ay, az, rx, ry, rz, gx, gy, gz, __ldg(w.bbox0 + (o >> 1))))) {
+                    // (a skipped brick steps on as an empty cell: no hit, crossings unchanged)
                     const float gx_m = tmx, gy_m = tmy, gz_m = tmz;
                     t *= 8.0f;
                     const uint32_t px = f2u(ax + vx * t), py = f2u(ay + vy * t), pz = f2u(az + vz * t);
@@ -370,31 +403,6 @@ struct Walker {
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
 constexpr int kWalkNoCap = 1 << 30;   // cnt above the brick level: never runs out
 
-// Brick skipping. A brick walk that ends without a hit leaves the walk exactly where
-// skipping the brick would: the grid-level crossings saved at the descent are restored
-// and the grid step follows, and brick visits cost no budget. So a brick may be skipped
-// (treated as an empty grid cell) when none of the voxels the DDA could visit in it is
-// opaque. The DDA visits only voxels within a few hundredths of a voxel of the ray's
-// line (its crossing times follow the line up to float rounding), so a brick is skipped
-// when the line misses the box of its opaque voxels grown by kBrickSlack = 0.1 voxel on
-// every side (a slab test; its own rounding is far below the slack).
-constexpr float kBrickSlack = 0.1f;
-constexpr uint32_t kNoOpaque = 0xFFFFFFFFu;
-
-__device__ __forceinline__ bool brick_clear(const Walker& k, uint32_t box) {
-    if (box == kNoOpaque) return true;
-    const float bx = (float)(k.cx * 8), by = (float)(k.cy * 8), bz = (float)(k.cz * 8);
-    const float x0 = ((bx + (float)(box & 7u)) - kBrickSlack - k.ax) * k.rx;
-    const float x1 = ((bx + (float)((box >> 9) & 7u)) + (1.0f + kBrickSlack) - k.ax) * k.rx;
-    const float y0 = ((by + (float)((box >> 3) & 7u)) - kBrickSlack - k.ay) * k.ry;
-    const float y1 = ((by + (float)((box >> 12) & 7u)) + (1.0f + kBrickSlack) - k.ay) * k.ry;
-    const float z0 = ((bz + (float)((box >> 6) & 7u)) - kBrickSlack - k.az) * k.rz;
-    const float z1 = ((bz + (float)((box >> 15) & 7u)) + (1.0f + kBrickSlack) - k.az) * k.rz;
-    const float tin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
-    const float tout = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
-    return tin > tout;
-}
-
 // value of the current cell at the current level
 __device__ __forceinline__ void walk_load(Walker& k, const World& w) {
     if (k.level == 0)
@@ -470,7 +478,8 @@ __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
     const bool brickcell = lv == 1 && (k.o & 1u);
     bool desc = lv == 0 ? k.o != 0u : brickcell;
     const bool hit = lv != 0 && !brickcell && ((hv & 0xf000u) >> 12) == 15u;
-    if (brickcell && w.bbox && brick_clear(k, __ldg(w.bbox + (k.o >> 1))))
+    if (brickcell && w.bbox &&
+        brick_clear(k.ax, k.ay, k.az, k.rx, k.ry, k.rz, k.cx, k.cy, k.cz, __ldg(w.bbox + (k.o >> 1))))
         desc = false;   // a brick the ray cannot stop in: step on as over an empty cell
     if (hit) {
         k.dist = (lv == 1 ? k.t * 8.0f : k.t) + k.to;

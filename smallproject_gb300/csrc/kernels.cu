@@ -71,29 +71,43 @@ __global__ void build_uber_kernel(const uint32_t* __restrict__ grid, uint8_t* ub
     uber[x + z * 32 + y * 1024] = empty ? 0 : 1;
 }
 
-// Per brick the box of its opaque voxels (type nibble 15), packed as World::bbox
-// describes: one warp per brick, 16 voxels a lane, min / max reductions over the warp.
-__global__ void build_brick_boxes_kernel(const uint32_t* __restrict__ bricks, uint32_t nbricks, uint32_t* __restrict__ bbox) {
-    const size_t brick = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (brick >= nbricks) return;   // whole warps leave together (blockDim a multiple of 32)
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t lo[3] = {7u, 7u, 7u}, hi[3] = {0u, 0u, 0u};
-    bool any = false;
-    for (uint32_t i = 0; i < 16; i++) {
-        const uint32_t e = i * 32u + lane;   // coalesced: a warp reads 32 consecutive voxels
-        if (((__ldg(bricks + brick * 512u + e) & 0xf000u) >> 12) == 15u) {
-            const uint32_t c[3] = {e & 7u, (e >> 3) & 7u, e >> 6};
-            for (int a = 0; a < 3; a++) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
-            any = true;
-        }
-    }
+// Per brick the boxes of its opaque voxels (type nibble 15) and of its non-zero voxels,
+// packed as World::bbox describes: one warp per brick, 16 voxels a lane, min / max
+// reductions over the warp.
+__device__ __forceinline__ uint32_t warp_box(bool any, const uint32_t lo[3], const uint32_t hi[3]) {
     const bool anyw = __any_sync(0xffffffffu, any);
     uint32_t box = 0u;
     for (int a = 0; a < 3; a++) {
         box |= __reduce_min_sync(0xffffffffu, lo[a]) << (3 * a);
         box |= __reduce_max_sync(0xffffffffu, hi[a]) << (9 + 3 * a);
     }
-    if (lane == 0u) bbox[brick] = anyw ? box : kNoOpaque;
+    return anyw ? box : kNoOpaque;
+}
+__global__ void build_brick_boxes_kernel(const uint32_t* __restrict__ bricks, uint32_t nbricks, uint32_t* __restrict__ bbox,
+                                         uint32_t* __restrict__ bbox0) {
+    const size_t brick = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (brick >= nbricks) return;   // whole warps leave together (blockDim a multiple of 32)
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lo[3] = {7u, 7u, 7u}, hi[3] = {0u, 0u, 0u}, lo0[3] = {7u, 7u, 7u}, hi0[3] = {0u, 0u, 0u};
+    bool any = false, any0 = false;
+    for (uint32_t i = 0; i < 16; i++) {
+        const uint32_t e = i * 32u + lane;   // coalesced: a warp reads 32 consecutive voxels
+        const uint32_t v = __ldg(bricks + brick * 512u + e);
+        const uint32_t c[3] = {e & 7u, (e >> 3) & 7u, e >> 6};
+        if (((v & 0xf000u) >> 12) == 15u) {
+            for (int a = 0; a < 3; a++) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
+            any = true;
+        }
+        if (v != 0u) {
+            for (int a = 0; a < 3; a++) { lo0[a] = min(lo0[a], c[a]); hi0[a] = max(hi0[a], c[a]); }
+            any0 = true;
+        }
+    }
+    const uint32_t box = warp_box(any, lo, hi), box0 = warp_box(any0, lo0, hi0);
+    if (lane == 0u) {
+        bbox[brick] = box;
+        bbox0[brick] = box0;
+    }
 }
 
 
@@ -809,9 +823,10 @@ void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s) {
     dev::build_uber_kernel<<<(32 * 32 * 32 + 255) / 256, 256, 0, s>>>(grid, uber);
 }
 
-void launch_build_brick_boxes(const uint32_t* bricks, uint32_t nbricks, uint32_t* bbox, cudaStream_t s) {
+void launch_build_brick_boxes(const uint32_t* bricks, uint32_t nbricks, uint32_t* bbox, uint32_t* bbox0, cudaStream_t s) {
     const size_t threads = (size_t)nbricks * 32u;
-    if (threads) dev::build_brick_boxes_kernel<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(bricks, nbricks, bbox);
+    if (threads)
+        dev::build_brick_boxes_kernel<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(bricks, nbricks, bbox, bbox0);
 }
 
 void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {

@@ -141,7 +141,8 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     w.grid = grid;
     w.uber = s + kOffUber;
     w.bricks = bricks;
-    w.bbox = nullptr;   // no room for brick boxes: visibility walks every brick
+    w.bbox = nullptr;   // no room for brick boxes: rays walk every brick they meet
+    w.bbox0 = nullptr;
     w.lgeom = geom;
     w.lemit = emit;
     w.nlights = nlights;

@@ -63,7 +63,7 @@ static int upload(World& w) {
         CU(cudaMalloc(&d.bricks, bb), "cudaMalloc(bricks)");
         d.brickBytes = bb;
     }
-    const size_t sb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * sizeof(uint32_t);
+    const size_t sb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * 2u * sizeof(uint32_t);
     if (sb > d.bboxBytes) {
         cudaFree(d.bbox);
         d.bbox = nullptr;
@@ -91,7 +91,8 @@ static int upload(World& w) {
     CU(cudaMemcpy(d.lraw, raw.data(), need * sizeof(uint4), cudaMemcpyHostToDevice), "upload lights");
     launch_build_light_table(d.lraw, (uint32_t)need, d.lgeom, d.lemit, 0);
     launch_build_uber(d.grid, d.uber, 0);
-    launch_build_brick_boxes(d.bricks, w.brickHigh, d.bbox, 0);
+    d.bbox0 = d.bbox + std::max<uint32_t>(w.brickHigh, 1u);
+    launch_build_brick_boxes(d.bricks, w.brickHigh, d.bbox, d.bbox0, 0);
     CU(cudaGetLastError(), "world kernels launch");
     CU(cudaDeviceSynchronize(), "world kernels");
     d.nl = nl;
@@ -123,6 +124,7 @@ vxr::dev::World dev_world(vxr_view* v) {
     w.uber = d.uber;
     w.bricks = d.bricks;
     w.bbox = d.bbox;
+    w.bbox0 = d.bbox0;
     w.lgeom = d.lgeom;
     w.lemit = d.lemit;
     w.nlights = d.nl;

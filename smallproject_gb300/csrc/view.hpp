@@ -16,7 +16,8 @@ struct DeviceWorld {
     uint8_t* uber = nullptr;
     uint32_t* bricks = nullptr;
     size_t brickBytes = 0;
-    uint32_t* bbox = nullptr;        // box of the opaque voxels per brick (brick skipping)
+    uint32_t* bbox = nullptr;        // boxes of the opaque voxels per brick (brick skipping),
+    uint32_t* bbox0 = nullptr;       // then those of the non-zero voxels (inside bbox's block)
     size_t bboxBytes = 0;
     uint4* lraw = nullptr;
     float4* lgeom = nullptr;

@@ -40,7 +40,7 @@ using namespace vxr::dev;
 
 static World make_world(const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks) {
     World w;
-    w.grid = grid; w.uber = uber; w.bricks = bricks; w.bbox = nullptr; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
+    w.grid = grid; w.uber = uber; w.bricks = bricks; w.bbox = nullptr; w.bbox0 = nullptr; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
     return w;
 }
 
@@ -118,6 +118,24 @@ extern "C" {
 uint32_t dh_trace(int mode, const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks, const float* O,
                   const float* D, int steps, uint32_t through, uint32_t mask, float* dist, uint32_t* side) {
     const World w = make_world(grid, uber, bricks);
+    float d = 0.0f;
+    uint32_t s = 0;
+    uint32_t v;
+    if (mode == 0) v = trace<0>(w, O[0], O[1], O[2], D[0], D[1], D[2], steps, through, mask, &d, &s);
+    else if (mode == 1) v = trace<1>(w, O[0], O[1], O[2], D[0], D[1], D[2], steps, through, mask, &d, &s);
+    else v = trace<2>(w, O[0], O[1], O[2], D[0], D[1], D[2], steps, through, mask, &d, &s);
+    *dist = d;
+    *side = s;
+    return v;
+}
+
+// trace<mode> with brick skipping (bbox: opaque-voxel boxes, bbox0: non-zero-voxel boxes)
+uint32_t dh_trace_skip(int mode, const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks,
+                       const uint32_t* bbox, const uint32_t* bbox0, const float* O, const float* D, int steps,
+                       uint32_t through, uint32_t mask, float* dist, uint32_t* side) {
+    World w = make_world(grid, uber, bricks);
+    w.bbox = bbox;
+    w.bbox0 = bbox0;
     float d = 0.0f;
     uint32_t s = 0;
     uint32_t v;

@@ -35,6 +35,9 @@ def dh():
     lib.dh_walk_burst.restype = C.c_uint32
     lib.dh_walk_burst.argtypes = [P, P, P, F, F, C.c_int, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     lib.dh_area_sample.argtypes = [C.c_int, F, F, C.c_uint32, F]
+    lib.dh_trace_skip.restype = C.c_uint32
+    lib.dh_trace_skip.argtypes = [C.c_int, P, P, P, P, P, F, F, C.c_int, C.c_uint32, C.c_uint32, F,
+                                  C.POINTER(C.c_uint32)]
     lib.dh_walk_skip.argtypes = [P, P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     return lib
 
@@ -111,11 +114,12 @@ def test_walker_bursts_match_single_visits(dh, world0_arrays):
             assert v == 0, (i, burst)
 
 
-def brick_boxes(bricks):
-    """Per brick the box of its opaque voxels (type nibble 15), packed as the GPU builds
-    it at upload (build_brick_boxes_kernel): low x, y, z in bits 0-8, high (inclusive)
-    in bits 9-17, 3 bits each; 0xFFFFFFFF when the brick has no opaque voxel."""
-    op = (((bricks.reshape(-1, 8, 8, 8) >> 12) & 15) == 15)        # [n, z, y, x]
+def brick_boxes(bricks, nonzero=False):
+    """Per brick the box of its opaque voxels (type nibble 15), or of its non-zero voxels,
+    packed as the GPU builds them at upload (build_brick_boxes_kernel): low x, y, z in
+    bits 0-8, high (inclusive) in bits 9-17, 3 bits each; 0xFFFFFFFF when there is none."""
+    b4 = bricks.reshape(-1, 8, 8, 8)                                   # [n, z, y, x]
+    op = (b4 != 0) if nonzero else (((b4 >> 12) & 15) == 15)
     out = np.full(len(op), 0xFFFFFFFF, np.uint32)
     for i in np.nonzero(op.any(axis=(1, 2, 3)))[0]:
         z, y, x = np.nonzero(op[i])
@@ -166,6 +170,29 @@ def test_walker_brick_skipping_is_exact(dh, world0_arrays):
         saved += nva.value - nvb.value
         hits += stb == 1
     assert hits > 500 and saved > 10000
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_trace_brick_skipping_matches_oracle(dh, world0_arrays, mode):
+    """trace<0> skipping bricks whose non-zero-voxel box the ray misses (primary rays),
+    with both box tables given to every mode, still matches the oracle's DDA bit for bit."""
+    wa = world0_arrays
+    box, box0 = brick_boxes(wa.bricks), brick_boxes(wa.bricks, nonzero=True)
+    assert (box0 != 0xFFFFFFFF).any()
+    port = ob.Renderer("port", wa, 4, 4, False)
+    o1, d1, rng = _rays(2000, 200 + mode)
+    o2, d2, _ = _surface_rays(wa, 2000, 300 + mode)
+    o, d = np.concatenate([o1, o2]), np.concatenate([d1, d2])
+    for i in range(len(o)):
+        steps = int(rng.choice([128, 999999, 9]))
+        through = int(rng.choice([0, 0x7F44, 0xF888]))
+        dist, side = C.c_float(0), C.c_uint32(0)
+        v = dh.dh_trace_skip(mode, wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, box.ctypes.data,
+                             box0.ctypes.data, _f3(o[i]), _f3(d[i]), steps, through, 0xFFFF, C.byref(dist),
+                             C.byref(side))
+        want = port.trace(mode, o[i], d[i], steps, through, 0xFFFF)
+        assert (v, side.value) == (want[0], want[2]) and \
+            np.float32(dist.value).view(np.uint32) == np.float32(want[1]).view(np.uint32), (i, o[i], d[i])
 
 
 def test_device_sincos_matches_oracle(dh):
