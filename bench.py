@@ -180,7 +180,7 @@ POSE = 150
 NFR = 300
 # DRAM bytes per launch of the dominant kernel from the ncu capture of the 960x540 case
 # (profiles/), scaled by 4 to 1920x1080 (the ray count grows with the pixel count)
-NCU_TRAFFIC_1080P = {"shadow_candidates": 4 * (128.29e6 + 6.92e6), "shadow_shading": 4 * (91.09e6 + 3.75e6),
+NCU_TRAFFIC_1080P = {"shadow_candidates": 4 * (71.57e6 + 2.96e6), "shadow_shading": 4 * (62.44e6 + 1.91e6),
                      "ris_candidates": 4 * (10.33e6 + 0.01e6), "albedo": 4 * (33.93e6 + 0.47e6)}
 
 
