@@ -26,6 +26,10 @@ struct World {
     const uint32_t* __restrict__ bbox;
     // the same for the non-zero voxels (what stops a primary ray), or null
     const uint32_t* __restrict__ bbox0;
+    // per uber cell (x + z*32 + y*1024), or null: the box of its non-zero voxels, 5 bits
+    // per corner coordinate in voxels from the cell's corner (low x, y, z in bits 0-14,
+    // high, inclusive, in bits 15-29), kNoOpaque when the cell is empty
+    const uint32_t* __restrict__ ubox0;
     const float4* __restrict__ lgeom;
     const float4* __restrict__ lemit;
     uint32_t nlights;
@@ -230,22 +234,29 @@ __device__ __forceinline__ void sincos_vx(float a, float* s, float* c) {
 // line (its crossing times follow the line up to float rounding), so a brick is skipped
 // when the line misses the box of its opaque voxels grown by kBrickSlack = 0.1 voxel on
 // every side (a slab test; its own rounding is far below the slack). Primary rays
-// (trace<0>) skip the same way with the box of the non-zero voxels.
+// (trace<0>) skip the same way with the box of the non-zero voxels, and, when their step
+// budget cannot run out (kFreeBudget: more than any walk of the map can spend), also
+// whole uber cells whose non-zero box they miss: with no budget to account, an uber
+// cell without a reachable non-zero voxel is walked over like an empty one.
 constexpr float kBrickSlack = 0.1f;
 constexpr uint32_t kNoOpaque = 0xFFFFFFFFu;
+constexpr int kFreeBudget = 4096;   // > 96 uber visits * 4 + 96 * 10 grid visits
 
-// true when the ray a + v t (r = 1 / v) misses the box `box` of the brick at grid cell
-// (gx, gy, gz) grown by the slack
-__device__ __forceinline__ bool brick_clear(float ax, float ay, float az, float rx, float ry, float rz, int gx, int gy,
-                                            int gz, uint32_t box) {
+// true when the ray a + v t (r = 1 / v) misses the box `box` (B bits per corner
+// coordinate, low x, y, z then high x, y, z) of the cell (cx, cy, cz) of 2^SH voxels,
+// grown by the slack
+template <int SH, int B>
+__device__ __forceinline__ bool box_clear(float ax, float ay, float az, float rx, float ry, float rz, int cx, int cy,
+                                          int cz, uint32_t box) {
     if (box == kNoOpaque) return true;
-    const float bx = (float)(gx * 8), by = (float)(gy * 8), bz = (float)(gz * 8);
-    const float x0 = ((bx + (float)(box & 7u)) - kBrickSlack - ax) * rx;
-    const float x1 = ((bx + (float)((box >> 9) & 7u)) + (1.0f + kBrickSlack) - ax) * rx;
-    const float y0 = ((by + (float)((box >> 3) & 7u)) - kBrickSlack - ay) * ry;
-    const float y1 = ((by + (float)((box >> 12) & 7u)) + (1.0f + kBrickSlack) - ay) * ry;
-    const float z0 = ((bz + (float)((box >> 6) & 7u)) - kBrickSlack - az) * rz;
-    const float z1 = ((bz + (float)((box >> 15) & 7u)) + (1.0f + kBrickSlack) - az) * rz;
+    constexpr uint32_t M = (1u << B) - 1u;
+    const float bx = (float)(cx << SH), by = (float)(cy << SH), bz = (float)(cz << SH);
+    const float x0 = ((bx + (float)(box & M)) - kBrickSlack - ax) * rx;
+    const float x1 = ((bx + (float)((box >> (3 * B)) & M)) + (1.0f + kBrickSlack) - ax) * rx;
+    const float y0 = ((by + (float)((box >> B) & M)) - kBrickSlack - ay) * ry;
+    const float y1 = ((by + (float)((box >> (4 * B)) & M)) + (1.0f + kBrickSlack) - ay) * ry;
+    const float z0 = ((bz + (float)((box >> (2 * B)) & M)) - kBrickSlack - az) * rz;
+    const float z1 = ((bz + (float)((box >> (5 * B)) & M)) + (1.0f + kBrickSlack) - az) * rz;
     const float tin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
     const float tout = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
     return tin > tout;
@@ -296,9 +307,12 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
     const float tdx = (float)sx * rx, tdy = (float)sy * ry, tdz = (float)sz * rz;
     float t = 0.0f;
     uint32_t o = __ldg(w.uber + ux + uz * 32 + uy * 1024);
+    const bool nobudget = w.ubox0 && steps > kFreeBudget;
     while (true) {
         if ((steps -= 4) <= 0) break;
-        if (MODE == 2 ? (o != 0u || through != 0u) : (o != 0u)) {
+        if (MODE == 2 ? (o != 0u || through != 0u)
+                      : (o != 0u && !(MODE == 0 && nobudget && box_clear<5, 5>(ax, ay, az, rx, ry, rz, ux, uy, uz,
+                                                                               __ldg(w.ubox0 + ux + uz * 32 + uy * 1024))))) {
             const float ux_m = tmx, uy_m = tmy, uz_m = tmz;
             t *= 4.0f;
             const uint32_t qx = f2u(0.125f * ax + vx * t), qy = f2u(0.125f * ay + vy * t), qz = f2u(0.125f * az + vz * t);
@@ -319,7 +333,7 @@ __device__ __noinline__ uint32_t trace(const World& w, float ax, float ay, float
                         return v;
                     }
                 } else if (!(MODE == 0 && w.bbox0 &&
-                             brick_clear(ax, ay, az, rx, ry, rz, gx, gy, gz, __ldg(w.bbox0 + (o >> 1))))) {
+                             box_clear<3, 3>(ax, ay, az, rx, ry, rz, gx, gy, gz, __ldg(w.bbox0 + (o >> 1))))) {
                     // (a skipped brick steps on as an empty cell: no hit, crossings unchanged)
                     const float gx_m = tmx, gy_m = tmy, gz_m = tmz;
                     t *= 8.0f;
@@ -479,7 +493,7 @@ __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
     bool desc = lv == 0 ? k.o != 0u : brickcell;
     const bool hit = lv != 0 && !brickcell && ((hv & 0xf000u) >> 12) == 15u;
     if (brickcell && w.bbox &&
-        brick_clear(k.ax, k.ay, k.az, k.rx, k.ry, k.rz, k.cx, k.cy, k.cz, __ldg(w.bbox + (k.o >> 1))))
+        box_clear<3, 3>(k.ax, k.ay, k.az, k.rx, k.ry, k.rz, k.cx, k.cy, k.cz, __ldg(w.bbox + (k.o >> 1))))
         desc = false;   // a brick the ray cannot stop in: step on as over an empty cell
     if (hit) {
         k.dist = (lv == 1 ? k.t * 8.0f : k.t) + k.to;

@@ -110,6 +110,34 @@ __global__ void build_brick_boxes_kernel(const uint32_t* __restrict__ bricks, ui
     }
 }
 
+// Per uber cell the box of its non-zero voxels (World::ubox0): brick-less non-zero grid
+// cells count whole, bricks with their non-zero box (bbox0, built before).
+__global__ void build_uber_boxes_kernel(const uint32_t* __restrict__ grid, const uint32_t* __restrict__ bbox0,
+                                        uint32_t* __restrict__ ubox0) {
+    const int task = blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= 32 * 32 * 32) return;
+    const int x = task & 31, z = (task >> 5) & 31, y = task >> 10;
+    uint32_t lo[3] = {31u, 31u, 31u}, hi[3] = {0u, 0u, 0u};
+    bool any = false;
+    for (int b = 0; b < 64; b++) {
+        const uint32_t cx = b & 3, cz = (b >> 2) & 3, cy = b >> 4;
+        const uint32_t c = __ldg(grid + (x * 4 + cx) + (z * 4 + cz) * 128 + (y * 4 + cy) * 16384);
+        if (c == 0u) continue;
+        uint32_t l[3] = {0u, 0u, 0u}, h[3] = {7u, 7u, 7u};
+        if (c & 1u) {
+            const uint32_t bb = __ldg(bbox0 + (c >> 1));
+            if (bb == kNoOpaque) continue;
+            for (int a = 0; a < 3; a++) { l[a] = (bb >> (3 * a)) & 7u; h[a] = (bb >> (9 + 3 * a)) & 7u; }
+        }
+        const uint32_t base[3] = {cx * 8u, cy * 8u, cz * 8u};
+        for (int a = 0; a < 3; a++) { lo[a] = min(lo[a], base[a] + l[a]); hi[a] = max(hi[a], base[a] + h[a]); }
+        any = true;
+    }
+    uint32_t box = 0u;
+    for (int a = 0; a < 3; a++) box |= (lo[a] << (5 * a)) | (hi[a] << (15 + 5 * a));
+    ubox0[task] = any ? box : kNoOpaque;
+}
+
 
 // ---- work distribution --------------------------------------------------------------------
 // VARIANT of a launch: 0 one view with area lights, 1 one view with point lights (the
@@ -827,6 +855,10 @@ void launch_build_brick_boxes(const uint32_t* bricks, uint32_t nbricks, uint32_t
     const size_t threads = (size_t)nbricks * 32u;
     if (threads)
         dev::build_brick_boxes_kernel<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(bricks, nbricks, bbox, bbox0);
+}
+
+void launch_build_uber_boxes(const uint32_t* grid, const uint32_t* bbox0, uint32_t* ubox0, cudaStream_t s) {
+    dev::build_uber_boxes_kernel<<<(32 * 32 * 32 + 255) / 256, 256, 0, s>>>(grid, bbox0, ubox0);
 }
 
 void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {

@@ -143,6 +143,7 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     w.bricks = bricks;
     w.bbox = nullptr;   // no room for brick boxes: rays walk every brick they meet
     w.bbox0 = nullptr;
+    w.ubox0 = nullptr;
     w.lgeom = geom;
     w.lemit = emit;
     w.nlights = nlights;

@@ -35,6 +35,7 @@ void release_device_world(World& w) {
     cudaFree(d->uber);
     cudaFree(d->bricks);
     cudaFree(d->bbox);
+    cudaFree(d->ubox0);
     cudaFree(d->lraw);
     cudaFree(d->lgeom);
     cudaFree(d->lemit);
@@ -56,6 +57,7 @@ static int upload(World& w) {
     d.device = dev;
     if (!d.grid) CU(cudaMalloc(&d.grid, kGridSize * sizeof(uint32_t)), "cudaMalloc(grid)");
     if (!d.uber) CU(cudaMalloc(&d.uber, 32 * 32 * 32), "cudaMalloc(uber)");
+    if (!d.ubox0) CU(cudaMalloc(&d.ubox0, 32 * 32 * 32 * sizeof(uint32_t)), "cudaMalloc(uber boxes)");
     const size_t bb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * kBrick * sizeof(uint32_t);
     if (bb > d.brickBytes) {
         cudaFree(d.bricks);
@@ -93,6 +95,7 @@ static int upload(World& w) {
     launch_build_uber(d.grid, d.uber, 0);
     d.bbox0 = d.bbox + std::max<uint32_t>(w.brickHigh, 1u);
     launch_build_brick_boxes(d.bricks, w.brickHigh, d.bbox, d.bbox0, 0);
+    launch_build_uber_boxes(d.grid, d.bbox0, d.ubox0, 0);
     CU(cudaGetLastError(), "world kernels launch");
     CU(cudaDeviceSynchronize(), "world kernels");
     d.nl = nl;
@@ -125,6 +128,7 @@ vxr::dev::World dev_world(vxr_view* v) {
     w.bricks = d.bricks;
     w.bbox = d.bbox;
     w.bbox0 = d.bbox0;
+    w.ubox0 = d.ubox0;
     w.lgeom = d.lgeom;
     w.lemit = d.lemit;
     w.nlights = d.nl;

@@ -18,6 +18,7 @@ struct DeviceWorld {
     size_t brickBytes = 0;
     uint32_t* bbox = nullptr;        // boxes of the opaque voxels per brick (brick skipping),
     uint32_t* bbox0 = nullptr;       // then those of the non-zero voxels (inside bbox's block)
+    uint32_t* ubox0 = nullptr;       // box of the non-zero voxels per uber cell (32^3)
     size_t bboxBytes = 0;
     uint4* lraw = nullptr;
     float4* lgeom = nullptr;

@@ -40,7 +40,7 @@ using namespace vxr::dev;
 
 static World make_world(const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks) {
     World w;
-    w.grid = grid; w.uber = uber; w.bricks = bricks; w.bbox = nullptr; w.bbox0 = nullptr; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
+    w.grid = grid; w.uber = uber; w.bricks = bricks; w.bbox = nullptr; w.bbox0 = nullptr; w.ubox0 = nullptr; w.lgeom = nullptr; w.lemit = nullptr; w.nlights = 0;
     return w;
 }
 
@@ -130,12 +130,14 @@ uint32_t dh_trace(int mode, const uint32_t* grid, const uint8_t* uber, const uin
 }
 
 // trace<mode> with brick skipping (bbox: opaque-voxel boxes, bbox0: non-zero-voxel boxes)
+// and uber-cell skipping for budget-free primary rays (ubox0, or null)
 uint32_t dh_trace_skip(int mode, const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks,
-                       const uint32_t* bbox, const uint32_t* bbox0, const float* O, const float* D, int steps,
-                       uint32_t through, uint32_t mask, float* dist, uint32_t* side) {
+                       const uint32_t* bbox, const uint32_t* bbox0, const uint32_t* ubox0, const float* O,
+                       const float* D, int steps, uint32_t through, uint32_t mask, float* dist, uint32_t* side) {
     World w = make_world(grid, uber, bricks);
     w.bbox = bbox;
     w.bbox0 = bbox0;
+    w.ubox0 = ubox0;
     float d = 0.0f;
     uint32_t s = 0;
     uint32_t v;

@@ -36,7 +36,7 @@ def dh():
     lib.dh_walk_burst.argtypes = [P, P, P, F, F, C.c_int, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     lib.dh_area_sample.argtypes = [C.c_int, F, F, C.c_uint32, F]
     lib.dh_trace_skip.restype = C.c_uint32
-    lib.dh_trace_skip.argtypes = [C.c_int, P, P, P, P, P, F, F, C.c_int, C.c_uint32, C.c_uint32, F,
+    lib.dh_trace_skip.argtypes = [C.c_int, P, P, P, P, P, P, F, F, C.c_int, C.c_uint32, C.c_uint32, F,
                                   C.POINTER(C.c_uint32)]
     lib.dh_walk_skip.argtypes = [P, P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     return lib
@@ -128,6 +128,33 @@ def brick_boxes(bricks, nonzero=False):
     return out
 
 
+def uber_boxes0(grid, bricks):
+    """Per uber cell (x + z*32 + y*1024) the box of its non-zero voxels (brick-less non-zero
+    grid cells whole, bricks by their non-zero box), 5 bits per corner coordinate: low
+    x, y, z in bits 0-14, high (inclusive) in bits 15-29; 0xFFFFFFFF when empty (the GPU
+    builds the same at upload, build_uber_boxes_kernel)."""
+    g = grid.reshape(128, 128, 128).astype(np.int64)                  # [gy, gz, gx]
+    bb = brick_boxes(bricks, nonzero=True).astype(np.int64)
+    lo = np.full((128, 128, 128, 3), 99, np.int64)
+    hi = np.full((128, 128, 128, 3), -1, np.int64)
+    gy, gz, gx = np.meshgrid(np.arange(128), np.arange(128), np.arange(128), indexing="ij")
+    base = np.stack([(gx & 3) * 8, (gy & 3) * 8, (gz & 3) * 8], -1)    # x, y, z in the uber cell
+    solid = ((g & 1) == 0) & (g != 0)
+    lo[solid] = base[solid]
+    hi[solid] = base[solid] + 7
+    isb = (g & 1) == 1
+    box = bb[g[isb] >> 1]
+    ok = box != 0xFFFFFFFF
+    sel = tuple(a[ok] for a in np.nonzero(isb))
+    box = box[ok]
+    lo[sel] = base[sel] + np.stack([box & 7, (box >> 3) & 7, (box >> 6) & 7], -1)
+    hi[sel] = base[sel] + np.stack([(box >> 9) & 7, (box >> 12) & 7, (box >> 15) & 7], -1)
+    lo = lo.reshape(32, 4, 32, 4, 32, 4, 3).min(axis=(1, 3, 5))       # [uy, uz, ux, 3]
+    hi = hi.reshape(32, 4, 32, 4, 32, 4, 3).max(axis=(1, 3, 5))
+    packed = sum(lo[..., a] << (5 * a) for a in range(3)) + sum(hi[..., a] << (15 + 5 * a) for a in range(3))
+    return np.ascontiguousarray(np.where(hi[..., 0] >= 0, packed, 0xFFFFFFFF).astype(np.uint32).reshape(-1))
+
+
 def _surface_rays(wa, n, seed):
     """Rays from just above the terrain of world0 towards random points: the shape of
     shadow rays (they leave a surface and cross bricks near it)."""
@@ -174,11 +201,13 @@ def test_walker_brick_skipping_is_exact(dh, world0_arrays):
 
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_trace_brick_skipping_matches_oracle(dh, world0_arrays, mode):
-    """trace<0> skipping bricks whose non-zero-voxel box the ray misses (primary rays),
-    with both box tables given to every mode, still matches the oracle's DDA bit for bit."""
+    """trace<0> skipping bricks whose non-zero-voxel box the ray misses, and with a budget
+    that cannot run out whole uber cells likewise (primary rays), with every box table
+    given to every mode, still matches the oracle's DDA bit for bit."""
     wa = world0_arrays
     box, box0 = brick_boxes(wa.bricks), brick_boxes(wa.bricks, nonzero=True)
-    assert (box0 != 0xFFFFFFFF).any()
+    ub0 = uber_boxes0(wa.grid, wa.bricks)
+    assert (box0 != 0xFFFFFFFF).any() and (ub0 != 0xFFFFFFFF).any()
     port = ob.Renderer("port", wa, 4, 4, False)
     o1, d1, rng = _rays(2000, 200 + mode)
     o2, d2, _ = _surface_rays(wa, 2000, 300 + mode)
@@ -188,8 +217,8 @@ def test_trace_brick_skipping_matches_oracle(dh, world0_arrays, mode):
         through = int(rng.choice([0, 0x7F44, 0xF888]))
         dist, side = C.c_float(0), C.c_uint32(0)
         v = dh.dh_trace_skip(mode, wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, box.ctypes.data,
-                             box0.ctypes.data, _f3(o[i]), _f3(d[i]), steps, through, 0xFFFF, C.byref(dist),
-                             C.byref(side))
+                             box0.ctypes.data, ub0.ctypes.data, _f3(o[i]), _f3(d[i]), steps, through, 0xFFFF,
+                             C.byref(dist), C.byref(side))
         want = port.trace(mode, o[i], d[i], steps, through, 0xFFFF)
         assert (v, side.value) == (want[0], want[2]) and \
             np.float32(dist.value).view(np.uint32) == np.float32(want[1]).view(np.uint32), (i, o[i], d[i])
