@@ -512,7 +512,7 @@ __device__ __forceinline__ void commit(uint32_t mbar) {
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void bar_half(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void bar_tile(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
 // bounded wait for the mbarrier phase of parity `par`; false when the limit ran out
 __device__ __forceinline__ bool wait(uint32_t mbar, uint32_t par) {
     for (uint32_t i = 0; i < (1u << 22); i++) {
@@ -550,27 +550,31 @@ __device__ __forceinline__ void stage(const __nv_bfloat16* g, unsigned char* s, 
         *reinterpret_cast<uint4*>(s + core_off(r, k, kdim)) = *reinterpret_cast<const uint4*>(g + (size_t)r * kdim + k);
     }
 }
-// one thread's row of 64 accumulators -> bias, ReLU, BF16, into the next A operand (K = 64)
-__device__ __forceinline__ void epilogue64(uint32_t taddr, const float* bias, unsigned char* A, int row) {
+// columns [32 half, 32 half + 32) of one thread's row of 64 accumulators -> bias, ReLU,
+// BF16, into the next A operand (K = 64)
+__device__ __forceinline__ void epilogue32(uint32_t taddr, const float* bias, unsigned char* A, int row, int half) {
+    float v[32];
+    ld32(taddr + half * 32, v);
 #pragma unroll
-    for (int half = 0; half < 2; half++) {
-        float v[32];
-        ld32(taddr + half * 32, v);
+    for (int c = 0; c < 4; c++) {
+        uint32_t w[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            uint32_t w[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int k = half * 32 + c * 8 + 2 * q;
-                w[q] = pack_bf16(fmaxf(v[c * 8 + 2 * q] + bias[k], 0.0f), fmaxf(v[c * 8 + 2 * q + 1] + bias[k + 1], 0.0f));
-            }
-            *reinterpret_cast<uint4*>(A + core_off(row, half * 32 + c * 8, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
+        for (int q = 0; q < 4; q++) {
+            const int k = half * 32 + c * 8 + 2 * q;
+            w[q] = pack_bf16(fmaxf(v[c * 8 + 2 * q] + bias[k], 0.0f), fmaxf(v[c * 8 + 2 * q + 1] + bias[k + 1], 0.0f));
         }
+        *reinterpret_cast<uint4*>(A + core_off(row, half * 32 + c * 8, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 }  // namespace tc
 
-__global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
+// Two tiles of 128 pixels per CTA, each owned by two warpgroups that split the work of a
+// pixel by columns: warpgroup `half` encodes hash-grid level `half` (half 1 also the
+// one-hot side), moves columns [32 half, 32 half + 32) of each hidden layer from TMEM to
+// the next A operand, builds the sampling tables of cluster groups [8 half, 8 half + 8)
+// and draws the candidates m with m % 2 == half (both advance the pixel's RNG alike).
+// The two halves' group totals meet through shared memory. 16 warps per SM.
+__global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     constexpr int H = 64, K = 256;
     unsigned char* W1c = smem;                     // [64][32]
@@ -616,10 +620,13 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    const int h = threadIdx.x >> 7, tid = threadIdx.x & 127, wq = warp & 3, bar = 1 + h;
+    const int h = threadIdx.x >> 8, t = threadIdx.x & 255, half = t >> 7, tid = t & 127, wq = warp & 3, bar = 1 + h;
     unsigned char* A = Abuf + h * tc::kTile * H * 2;
     unsigned char* T = Tbuf + h * tc::kTile * tc::kRowBytes;
     uint16_t* fp = reinterpret_cast<uint16_t*>(T + tid * tc::kRowBytes);
+    // after the last layer A is free until the next tile's input: the halves' maxima and
+    // group totals, [half][9][128] floats
+    float* X = reinterpret_cast<float*>(A);
     const uint32_t mbar = tc::smem_u32(&mbars[h]);
     const uint32_t dcol = tmem + (uint32_t)(h * 256);                 // this tile's accumulator columns
     const uint32_t trow = dcol + ((uint32_t)(wq * 32) << 16);         // this warp's lanes
@@ -650,20 +657,26 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
                                   __uint_as_float(side_code(side, ns)));
             }
         }
-        // input row (K = 32): both hash-grid levels, the one-hot side, zeros
+        // input row (K = 32): hash-grid level `half` in columns [8 half, 8 half + 8); half 1
+        // also the one-hot side (columns 16-21) and the zero columns 22-31
         {
-            float f[kIn];
-            level_features(enc, d, pin.x, pin.y, pin.z, 0, f);
-            level_features(enc, d, pin.x, pin.y, pin.z, 1, f + 8);
-            const uint32_t code = __float_as_uint(pin.w);
+            float f[8];
+            level_features(enc, d, pin.x, pin.y, pin.z, half, f);
+            uint32_t w[4];
 #pragma unroll
-            for (int q = 16; q < kIn; q++) f[q] = code == (uint32_t)(q - 16) ? 1.0f : 0.0f;
+            for (int q = 0; q < 4; q++) w[q] = valid ? pack_bf16(f[2 * q], f[2 * q + 1]) : 0u;
+            *reinterpret_cast<uint4*>(A + tc::core_off(tid, half * 8, kIn)) = make_uint4(w[0], w[1], w[2], w[3]);
+            if (half) {
+                const uint32_t code = __float_as_uint(pin.w);
 #pragma unroll
-            for (int c = 0; c < kIn / 8; c++) {
-                uint32_t w[4];
+                for (int c = 2; c < kIn / 8; c++) {
 #pragma unroll
-                for (int q = 0; q < 4; q++) w[q] = valid ? pack_bf16(f[c * 8 + 2 * q], f[c * 8 + 2 * q + 1]) : 0u;
-                *reinterpret_cast<uint4*>(A + tc::core_off(tid, c * 8, kIn)) = make_uint4(w[0], w[1], w[2], w[3]);
+                    for (int q = 0; q < 4; q++) {
+                        const uint32_t k = (uint32_t)(c * 8 + 2 * q - 16);
+                        w[q] = valid ? pack_bf16(code == k ? 1.0f : 0.0f, code == k + 1u ? 1.0f : 0.0f) : 0u;
+                    }
+                    *reinterpret_cast<uint4*>(A + tc::core_off(tid, c * 8, kIn)) = make_uint4(w[0], w[1], w[2], w[3]);
+                }
             }
         }
         // four layers; between them every thread moves its row from TMEM to A
@@ -671,8 +684,8 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
         for (int layer = 0; layer < 4; layer++) {
             tc::fence_async_smem();
             tc::fence_before();
-            tc::bar_half(bar);
-            if (tid == 0) {
+            tc::bar_tile(bar);
+            if (t == 0) {
                 tc::fence_after();
                 const int kdim = layer == 0 ? kIn : H;
                 const unsigned char* W = layer == 0 ? W1c : (layer == 1 ? W2c : (layer == 2 ? W3c : W4c));
@@ -691,21 +704,23 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
             }
             phase ^= 1u;
             tc::fence_after();
-            if (layer < 3) tc::epilogue64(trow, bs + layer * H, A, tid);
+            if (layer < 3) tc::epilogue32(trow, bs + layer * H, A, tid, half);
         }
         if (!ok) break;
-        // softmax tables of this thread's pixel from its 256 logits in TMEM, one pass: each
-        // 32-column chunk (two groups) uses its own maximum; the in-group fractions do not
-        // depend on it, and the group totals are rescaled to the row maximum at the end
-        float Tg[16], Mc[8];
+        // softmax tables of this pixel's cluster groups [8 half, 8 half + 8) from its logits
+        // in TMEM, one pass: each 32-column chunk (two groups) uses its own maximum; the
+        // in-group fractions do not depend on it, and the group totals are rescaled to the
+        // half's maximum, then (after the exchange) to the row maximum
+        float Tg[8], Mc[4];
 #pragma unroll
-        for (int ch = 0; ch < K / 32; ch++) {
+        for (int ch = 0; ch < 4; ch++) {
+            const int gc = half * 4 + ch;   // chunk of the row
             float v[32];
-            tc::ld32(trow + ch * 32, v);
+            tc::ld32(trow + gc * 32, v);
             float m = -INFINITY;
 #pragma unroll
             for (int i = 0; i < 32; i++) {
-                v[i] += bs[3 * H + ch * 32 + i];
+                v[i] += bs[3 * H + gc * 32 + i];
                 m = fmaxf(m, v[i]);
             }
             Mc[ch] = m;
@@ -726,23 +741,32 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
                     const uint32_t hi = i == 14 ? 65535u : min((uint32_t)(pre[i + 1] * sc), 65535u);
                     pk[i / 2] = lo | (hi << 16);
                 }
-                uint4* dst = reinterpret_cast<uint4*>(fp + (ch * 2 + g2) * 16);
+                uint4* dst = reinterpret_cast<uint4*>(fp + (gc * 2 + g2) * 16);
                 dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
                 dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
                 Tg[ch * 2 + g2] = acc;
             }
         }
-        float mx = Mc[0];
+        tc::fence_before();   // this thread's TMEM reads are complete before the next tile's MMAs
+        {
+            const float mh = fmaxf(fmaxf(Mc[0], Mc[1]), fmaxf(Mc[2], Mc[3]));
+            X[(half * 9) * tc::kTile + tid] = mh;
 #pragma unroll
-        for (int ch = 1; ch < K / 32; ch++) mx = fmaxf(mx, Mc[ch]);
+            for (int q = 0; q < 8; q++) X[(half * 9 + 1 + q) * tc::kTile + tid] = Tg[q] * __expf(Mc[q >> 1] - mh);
+        }
+        tc::bar_tile(bar);    // both halves' tables and totals are written
         float P[16];
         float Z = 0.0f;
+        {
+            const float m0 = X[tid], m1 = X[9 * tc::kTile + tid];
+            const float mx = fmaxf(m0, m1), s0 = __expf(m0 - mx), s1 = __expf(m1 - mx);
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-            Z += Tg[q] * __expf(Mc[q >> 1] - mx);
-            P[q] = Z;
+            for (int q = 0; q < 16; q++) {
+                Z += X[((q >> 3) * 9 + 1 + (q & 7)) * tc::kTile + tid] * (q < 8 ? s0 : s1);
+                P[q] = Z;
+            }
         }
-        tc::fence_before();   // this thread's TMEM reads are complete before the next tile's MMAs
+        tc::bar_tile(bar);    // every thread has read X before the next tile writes its input
         const float invZ = 1.0f / Z;
         auto frac = [&](int c) {
             const uint32_t hi = fp[c], lo = (c % gs) ? fp[c - 1] : 0u;
@@ -751,7 +775,7 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
         if (!valid) continue;
         if (a.probs) {
 #pragma unroll
-            for (int q = 0; q < 16; q++) {
+            for (int q = half * 8; q < half * 8 + 8; q++) {
                 const float gw = q ? P[q] - P[q - 1] : P[0];
                 for (int c = q * gs; c < (q + 1) * gs; c++) a.probs[(size_t)j * K + c] = (gw * frac(c)) * invZ;
             }
@@ -765,6 +789,7 @@ __global__ void __launch_bounds__(256, 1) infer_tc_kernel(InferArgs a) {
             const float u = dev::rnd(s);
             const float v = dev::rnd(s);
             const float w = dev::rnd(s);
+            if ((int)(m & 1u) != half) continue;   // the other warpgroup's candidate
             int c;
             uint32_t e;
             float gw;
@@ -1052,7 +1077,7 @@ cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s)
         cudaError_t e = cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((max_items + 255) / 256, (uint32_t)sms()));
-        infer_tc_kernel<<<blocks, 256, sm, s>>>(a);
+        infer_tc_kernel<<<blocks, 512, sm, s>>>(a);
         return cudaGetLastError();
     }
     const int nw = infer_warps(a.dims);
