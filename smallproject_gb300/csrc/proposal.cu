@@ -478,6 +478,8 @@ __global__ void __launch_bounds__(512, 1) infer_kernel(InferArgs a) {
 // after the output layer, for its pixel's softmax tables and candidates. All waits are
 // bounded; on a timeout the kernel raises *a.err, skips its remaining tiles and still
 // frees its tensor memory.
+constexpr float kLog2e = 1.44269504088896340736f;   // log2(e)
+
 namespace tc {
 constexpr int kTile = 128;
 constexpr uint32_t kCols = 512;          // TMEM columns: 256 per tile
@@ -513,6 +515,12 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void bar_tile(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
+// 2^x on the special-function unit (PTX ex2.approx.f32)
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 // bounded wait for the mbarrier phase of parity `par`; false when the limit ran out
 __device__ __forceinline__ bool wait(uint32_t mbar, uint32_t par) {
     for (uint32_t i = 0; i < (1u << 22); i++) {
@@ -600,7 +608,8 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
             bs[H + e] = p[a.L.b2 + e];
             bs[2 * H + e] = p[a.L.b3 + e];
         }
-        for (int e = threadIdx.x; e < K; e += blockDim.x) bs[3 * H + e] = p[a.L.b4 + e];
+        // output bias in log2 units: the softmax works with 2^(log2(e) z)
+        for (int e = threadIdx.x; e < K; e += blockDim.x) bs[3 * H + e] = p[a.L.b4 + e] * kLog2e;
         if (a.clOff)
             for (int e = threadIdx.x; e <= K; e += blockDim.x) offs[e] = a.clOff[e];
         if (threadIdx.x == 0) {
@@ -720,7 +729,7 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
             float m = -INFINITY;
 #pragma unroll
             for (int i = 0; i < 32; i++) {
-                v[i] += bs[3 * H + gc * 32 + i];
+                v[i] = v[i] * kLog2e + bs[3 * H + gc * 32 + i];   // log2(e) * logit
                 m = fmaxf(m, v[i]);
             }
             Mc[ch] = m;
@@ -730,7 +739,7 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
                 float acc = 0.0f;
 #pragma unroll
                 for (int i = 0; i < 16; i++) {
-                    acc += __expf(v[g2 * 16 + i] - m);
+                    acc += tc::ex2(v[g2 * 16 + i] - m);
                     pre[i] = acc;
                 }
                 const float sc = acc > 0.0f ? 65535.0f / acc : 0.0f;
@@ -752,14 +761,14 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
             const float mh = fmaxf(fmaxf(Mc[0], Mc[1]), fmaxf(Mc[2], Mc[3]));
             X[(half * 9) * tc::kTile + tid] = mh;
 #pragma unroll
-            for (int q = 0; q < 8; q++) X[(half * 9 + 1 + q) * tc::kTile + tid] = Tg[q] * __expf(Mc[q >> 1] - mh);
+            for (int q = 0; q < 8; q++) X[(half * 9 + 1 + q) * tc::kTile + tid] = Tg[q] * tc::ex2(Mc[q >> 1] - mh);
         }
         tc::bar_tile(bar);    // both halves' tables and totals are written
         float P[16];
         float Z = 0.0f;
         {
             const float m0 = X[tid], m1 = X[9 * tc::kTile + tid];
-            const float mx = fmaxf(m0, m1), s0 = __expf(m0 - mx), s1 = __expf(m1 - mx);
+            const float mx = fmaxf(m0, m1), s0 = tc::ex2(m0 - mx), s1 = tc::ex2(m1 - mx);
 #pragma unroll
             for (int q = 0; q < 16; q++) {
                 Z += X[((q >> 3) * 9 + 1 + (q & 7)) * tc::kTile + tid] * (q < 8 ? s0 : s1);
