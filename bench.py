@@ -10,7 +10,7 @@ albedo -> candidates (+ proposal inference) + temporal -> spatial -> shading+acc
 Quality protocol (untimed setup, --quality full): a converged render (FP64 mean of
 --conv-frames frames of the unbiased estimator: spatial and temporal reuse off) at path
 frame 150; the proposal trained online for --train-frames frames along the path on the
-plain method's reservoirs; then for each method and candidate count in CANDS, 16 seeds x
+plain method's reservoirs; then for each method and candidate count in CANDS, 32 seeds x
 16 frames at the static pose: device ms/frame and MSE against the converged render. The
 plain method's reference point is 32 candidates (the reference's NUMBEROFCANDIDATES).
 The timed configuration is the learned method at the smallest candidate count whose mean
@@ -374,7 +374,7 @@ def main():
     ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
     ap.add_argument("--train-frames", type=int, default=200)
-    ap.add_argument("--mse-seeds", type=int, default=16)
+    ap.add_argument("--mse-seeds", type=int, default=32)
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
     args = ap.parse_args()
@@ -395,10 +395,10 @@ def main():
         from smallproject_gb300 import build as B
         B.build()
         vx, desc, world = make_scene(args.config)
-        ms, kind, sample = cpu_arm(args, desc, world, args.steps, min(args.warmup, 1), W, H)
+        ms, kind, sample = cpu_arm(args, desc, world, args.steps, args.warmup, W, H)
         config["method"] = "plain uniform-source RIS, 32 candidates"
         line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms/frame", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": False,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
                 "config": config,
                 "cpu_baseline": {"value": ms, "unit": "ms/frame", "cores": os.cpu_count(), "kind": kind,
