@@ -228,8 +228,10 @@ int vxr_host_free(void* p);
 /* World::ForceSyncAllBricks + the updateUberGrid kernel + SetupLightBuffer's device copy
  * (world.cpp:639-651, kernels.cl:498-513, world.cpp:563-612): upload the grid, the
  * bricks and the light list to the current CUDA device, build the 32^3 uber grid and
- * the per-light table there. Re-upload after edits; views pick up the new copy at their
- * next frame. Synchronous. */
+ * the per-light table there, and the traversal's skip tables (per brick the boxes of
+ * its opaque and of its non-zero voxels, 8 bytes; per uber cell the box of its non-zero
+ * voxels). Re-upload after edits; views pick up the new copy at their next frame.
+ * Synchronous. */
 int vxr_world_upload(vxr_world* w);
 /* Device bytes held by the world's GPU copy. */
 int vxr_world_device_bytes(const vxr_world* w, uint64_t* bytes);

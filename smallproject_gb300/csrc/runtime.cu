@@ -275,7 +275,8 @@ int vxr_world_upload(vxr_world* w) {
 int vxr_world_device_bytes(const vxr_world* w, uint64_t* bytes) {
     VXR_CHECK_ARG(w && bytes, "vxr_world_device_bytes: null argument");
     const vxr::DeviceWorld* d = w->w.dev;
-    *bytes = d ? (uint64_t)(vxr::kGridSize * 4 + 32768 + d->brickBytes + d->lcap * 48) : 0;
+    // grid, uber grid and its boxes, bricks and their boxes, light tables
+    *bytes = d ? (uint64_t)(vxr::kGridSize * 4 + 32768 + 32768 * 4 + d->brickBytes + d->bboxBytes + d->lcap * 48) : 0;
     return VXR_OK;
 }
 
