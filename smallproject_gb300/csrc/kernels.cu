@@ -460,6 +460,10 @@ __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, u
                           sp.z + (side == 2 ? 0.1f * nsign : 0.0f));
     const uint32_t nL = k.nlights;
     const float puni = 1.0f / (float)nL;
+    // x / (1 / N) is exactly x * N when N is a power of two (1 / N is then exact, and both
+    // are the rounding of the same real number)
+    const bool pow2 = !LEARNED && (nL & (nL - 1u)) == 0u;
+    const float nLf = (float)nL;
     for (uint32_t c = 0; c < k.ncand; c++) {
         int li;
         float p = puni;
@@ -484,7 +488,7 @@ __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, u
             pos = sample_area_light(lg, spo, seed, &inv, &nc);
         }
         const float ph = phat<POINT>(pos, nc, sp, side, nsign, brdf, le, lg.w) * inv;
-        res_update(res, ph / p, ph, (uint32_t)li, rnd(seed), pos, inv, nc);
+        res_update(res, pow2 ? ph * nLf : ph / p, ph, (uint32_t)li, rnd(seed), pos, inv, nc);
     }
     if (k.ncand > 0 && res.sumW > 0.0f) {
         const float3 L = normalize3(sub(res.pos, spo));
@@ -512,6 +516,11 @@ template <bool POINT>
 __device__ __forceinline__ void temporal_item(const ViewDev* V, uint32_t i) {
     const Frame& k = V->k;
     if (!(k.restirtemporalframe > 0 && k.temporal)) return;
+    // loads are issued as early as their addresses are known (before the tests that may
+    // make them unneeded), so the item waits for three rounds of memory instead of five
+    const uint4 ca = __ldg(V->b.cA + i);
+    const float4 cb = __ldg(V->b.cB + i);
+    const uint32_t seed0 = V->b.seed[i];
     const int x = (int)(i % (uint32_t)k.W), y = (int)(i / (uint32_t)k.W);
     const uint2 g = V->b.vd[V->cur][i];
     const uint32_t voxel = g.x & 0x00FFFFFFu, side = g.x >> 24;
@@ -530,9 +539,9 @@ __device__ __forceinline__ void temporal_item(const ViewDev* V, uint32_t i) {
     if (px < 0 || py < 0 || px >= k.W || py >= k.H) return;
     const size_t jp = (size_t)py * k.W + px;
     const uint2 pg = __ldg(V->b.vd[V->cur ^ 1] + jp);
+    Res prev = res_load(V->b.hA, V->b.hB, jp);
     const float pdist = __uint_as_float(pg.y);
     if ((pg.x >> 24) != side || !(fabsf(dist - pdist) <= 0.1f * dist)) return;
-    Res prev = res_load(V->b.hA, V->b.hB, jp);
     const uint32_t pm = min(k.maxTemporal * k.ncand, prev.M);
     if (pm == 0u) return;
     uint32_t pli = prev.idx;
@@ -543,8 +552,15 @@ __device__ __forceinline__ void temporal_item(const ViewDev* V, uint32_t i) {
     const float pph = phat<POINT>(prev.pos, prev.ncode, sp, side, nsign, brdf, pe4, pg4.w) * prev.inv;
     const float W = res_W(prev);
     res_reweigh(prev, W, pph, pm);
-    Res res = res_load(V->b.cA, V->b.cB, i);
-    uint32_t seed = V->b.seed[i];
+    Res res;
+    res.idx = ca.x;
+    res.M = ca.y & 0x1FFFFFFFu;
+    res.ncode = ca.y >> 29;
+    res.sumW = __uint_as_float(ca.z);
+    res.pHat = __uint_as_float(ca.w);
+    res.pos = f3(cb.x, cb.y, cb.z);
+    res.inv = cb.w;
+    uint32_t seed = seed0;
     res_combine(res, prev, rnd(seed));
     // AdjustWeight(res, pHat of the selected sample here) equals res.pHat
     res_store(V->b.cA, V->b.cB, i, res);
@@ -592,13 +608,15 @@ __device__ __forceinline__ void spatial_px(const ViewDev* V, int x, int y) {
             if ((nx == x && ny == y) || nx < 0 || ny < 0 || nx >= k.W || ny >= k.H) continue;
             const size_t j = (size_t)ny * k.W + nx;
             Res nb = res_load(cA, cB, j);
+            const uint2 ng = __ldg(vd + j);
+            // the light record is fetched with the tests still pending (it is needed when
+            // they pass), one round of memory fewer per combined tap
+            const uint32_t nli = nb.idx < k.nlights ? nb.idx : 0u;
+            const float4 lg = __ldg(V->w.lgeom + nli), le = __ldg(V->w.lemit + nli);
             if (nb.M > 0u) {
-                const uint2 ng = __ldg(vd + j);
                 const float ndist = __uint_as_float(ng.y);
                 if ((ng.x >> 24) == side && fabsf(dist - ndist) <= 0.1f * dist) {
-                    uint32_t nli = nb.idx;
-                    if (nli >= k.nlights) { raise_error(V->b.err, 4u); nli = 0; }
-                    const float4 lg = __ldg(V->w.lgeom + nli), le = __ldg(V->w.lemit + nli);
+                    if (nb.idx >= k.nlights) raise_error(V->b.err, 4u);
                     const float ph = phat<POINT>(nb.pos, nb.ncode, sp, side, nsign, brdf, le, lg.w) * nb.inv;
                     const float W = res_W(nb);
                     res_reweigh(nb, W, ph, nb.M);
