@@ -226,13 +226,29 @@ int vxr_host_free(void* p);
 
 /* ---- GPU copy of a world --------------------------------------------------------- */
 /* World::ForceSyncAllBricks + the updateUberGrid kernel + SetupLightBuffer's device copy
- * (world.cpp:639-651, kernels.cl:498-513, world.cpp:563-612): upload the grid, the
+ * (world.cpp:639-651, kernels.cl:498-513, world.cpp:563-612): upload all of the grid, the
  * bricks and the light list to the current CUDA device, build the 32^3 uber grid and
  * the per-light table there, and the traversal's skip tables (per brick the boxes of
  * its opaque and of its non-zero voxels, 8 bytes; per uber cell the box of its non-zero
  * voxels). Re-upload after edits; views pick up the new copy at their next frame.
  * Synchronous. */
 int vxr_world_upload(vxr_world* w);
+/* World::Commit + the commit kernel (world.cpp:2357-2420, kernels.cl:448-477): bring the
+ * device copy up to date with the edits since the last commit. Only the bricks whose
+ * voxels changed are sent (gathered in page-locked memory, copied once, scattered into
+ * the device pool by a kernel), the grid only when it changed, the light table only when
+ * the light list changed; the uber grid and the skip tables are rebuilt for what changed.
+ * Everything is sent when there is no device copy yet, after vxr_world_clear or a scene
+ * build, or when new bricks outgrow the device pool (it is then reallocated with 1/8
+ * headroom). Unlike the reference there is no per-commit brick limit. Waits for all
+ * device work first (frames in flight read these buffers) and is synchronous. Rendering
+ * a view commits its world's pending edits the same way. Optional outputs: bricks sent,
+ * full = 1 when everything was sent. */
+int vxr_world_commit(vxr_world* w, uint32_t* bricks_sent, int* full);
+/* What the next commit would send (no reference counterpart: the reference's dirty
+ * marks, world.h:565-613, are internal): changed bricks (all bricks when everything is
+ * due), whether the grid changed, whether everything is due. Host-only. */
+int vxr_world_pending(const vxr_world* w, uint32_t* dirty_bricks, int* grid_changed, int* full);
 /* Device bytes held by the world's GPU copy. */
 int vxr_world_device_bytes(const vxr_world* w, uint64_t* bytes);
 

@@ -83,10 +83,12 @@ __device__ __forceinline__ uint32_t warp_box(bool any, const uint32_t lo[3], con
     }
     return anyw ? box : kNoOpaque;
 }
-__global__ void build_brick_boxes_kernel(const uint32_t* __restrict__ bricks, uint32_t nbricks, uint32_t* __restrict__ bbox,
-                                         uint32_t* __restrict__ bbox0) {
-    const size_t brick = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (brick >= nbricks) return;   // whole warps leave together (blockDim a multiple of 32)
+// (list: the bricks to do, or null for bricks 0 .. n - 1)
+__global__ void build_brick_boxes_kernel(const uint32_t* __restrict__ bricks, const uint32_t* __restrict__ list,
+                                         uint32_t n, uint32_t* __restrict__ bbox, uint32_t* __restrict__ bbox0) {
+    const size_t item = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (item >= n) return;   // whole warps leave together (blockDim a multiple of 32)
+    const size_t brick = list ? (size_t)__ldg(list + item) : item;
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t lo[3] = {7u, 7u, 7u}, hi[3] = {0u, 0u, 0u}, lo0[3] = {7u, 7u, 7u}, hi0[3] = {0u, 0u, 0u};
     bool any = false, any0 = false;
@@ -108,6 +110,15 @@ __global__ void build_brick_boxes_kernel(const uint32_t* __restrict__ bricks, ui
         bbox[brick] = box;
         bbox0[brick] = box0;
     }
+}
+
+// commit (kernels.cl:448-477): staged brick i (512 voxels after the index list) to its
+// place in the pool; one block of 128 threads per brick, 16 bytes a thread
+__global__ void commit_bricks_kernel(const uint32_t* __restrict__ list, const uint32_t* __restrict__ voxels,
+                                     uint32_t* __restrict__ bricks) {
+    const uint32_t b = __ldg(list + blockIdx.x);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(voxels + (size_t)blockIdx.x * 512u) + threadIdx.x);
+    reinterpret_cast<uint4*>(bricks + (size_t)b * 512u)[threadIdx.x] = v;
 }
 
 // Per uber cell the box of its non-zero voxels (World::ubox0): brick-less non-zero grid
@@ -869,10 +880,15 @@ void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s) {
     dev::build_uber_kernel<<<(32 * 32 * 32 + 255) / 256, 256, 0, s>>>(grid, uber);
 }
 
-void launch_build_brick_boxes(const uint32_t* bricks, uint32_t nbricks, uint32_t* bbox, uint32_t* bbox0, cudaStream_t s) {
-    const size_t threads = (size_t)nbricks * 32u;
+void launch_build_brick_boxes(const uint32_t* bricks, const uint32_t* list, uint32_t n, uint32_t* bbox, uint32_t* bbox0,
+                              cudaStream_t s) {
+    const size_t threads = (size_t)n * 32u;
     if (threads)
-        dev::build_brick_boxes_kernel<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(bricks, nbricks, bbox, bbox0);
+        dev::build_brick_boxes_kernel<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(bricks, list, n, bbox, bbox0);
+}
+
+void launch_commit_bricks(const uint32_t* list, const uint32_t* voxels, uint32_t n, uint32_t* bricks, cudaStream_t s) {
+    if (n) dev::commit_bricks_kernel<<<n, 128, 0, s>>>(list, voxels, bricks);
 }
 
 void launch_build_uber_boxes(const uint32_t* grid, const uint32_t* bbox0, uint32_t* ubox0, cudaStream_t s) {

@@ -105,7 +105,9 @@ struct Tuning {
 
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s);
 void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s);
-void launch_build_brick_boxes(const uint32_t* bricks, uint32_t nbricks, uint32_t* bbox, uint32_t* bbox0, cudaStream_t s);
+void launch_build_brick_boxes(const uint32_t* bricks, const uint32_t* list, uint32_t n, uint32_t* bbox, uint32_t* bbox0,
+                              cudaStream_t s);
+void launch_commit_bricks(const uint32_t* list, const uint32_t* voxels, uint32_t n, uint32_t* bricks, cudaStream_t s);
 void launch_build_uber_boxes(const uint32_t* grid, const uint32_t* bbox0, uint32_t* ubox0, cudaStream_t s);
 
 // learned proposal inputs of the candidate stage

@@ -36,6 +36,8 @@ void release_device_world(World& w) {
     cudaFree(d->bricks);
     cudaFree(d->bbox);
     cudaFree(d->ubox0);
+    cudaFree(d->stageDev);
+    cudaFreeHost(d->stageHost);
     cudaFree(d->lraw);
     cudaFree(d->lgeom);
     cudaFree(d->lemit);
@@ -43,6 +45,13 @@ void release_device_world(World& w) {
     w.dev = nullptr;
 }
 
+// World::Commit (world.cpp:2357-2420) with the commit kernel (kernels.cl:448-477): bring
+// the device copy up to date. Waits for all device work first (frames in flight read the
+// buffers this writes). Sends everything when there is no copy yet, after clear() or a
+// scene build, or when the brick pool outgrew the device pool (which is then reallocated
+// with headroom); otherwise only the bricks marked dirty (their voxels, then a scatter
+// kernel), the grid when it changed, and the lights when they changed, and rebuilds the
+// derived tables of what changed.
 static int upload(World& w) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(VXR_E_NODEVICE, "no CUDA device visible");
@@ -50,57 +59,108 @@ static int upload(World& w) {
     for (uint32_t i = 0; i < kGridSize; i++)
         if ((w.grid[i] & 1u) && (w.grid[i] >> 1) >= w.brickHigh)
             return set_error(VXR_E_STATE, "vxr_world_upload: grid cell references a brick outside the pool");
-    if (!w.dev) w.dev = new DeviceWorld();
-    DeviceWorld& d = *w.dev;
     int dev = 0;
     CU(cudaGetDevice(&dev), "cudaGetDevice");
+    CU(cudaDeviceSynchronize(), "upload: wait for device work");
+    if (!w.dev) w.dev = new DeviceWorld();
+    DeviceWorld& d = *w.dev;
+    const bool full = w.fullDirty || !d.grid || d.device != dev || w.brickHigh > d.cap;
     d.device = dev;
     if (!d.grid) CU(cudaMalloc(&d.grid, kGridSize * sizeof(uint32_t)), "cudaMalloc(grid)");
     if (!d.uber) CU(cudaMalloc(&d.uber, 32 * 32 * 32), "cudaMalloc(uber)");
     if (!d.ubox0) CU(cudaMalloc(&d.ubox0, 32 * 32 * 32 * sizeof(uint32_t)), "cudaMalloc(uber boxes)");
-    const size_t bb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * kBrick * sizeof(uint32_t);
-    if (bb > d.brickBytes) {
-        cudaFree(d.bricks);
-        d.bricks = nullptr;
-        CU(cudaMalloc(&d.bricks, bb), "cudaMalloc(bricks)");
-        d.brickBytes = bb;
+    uint32_t sent = 0;
+    if (full) {
+        if (w.brickHigh > d.cap || !d.bricks) {
+            // headroom for bricks split by later edits without a full upload
+            const uint32_t cap = std::max<uint32_t>(w.brickHigh + w.brickHigh / 8u + 256u, 1u);
+            cudaFree(d.bricks);
+            cudaFree(d.bbox);
+            d.bricks = nullptr;
+            d.bbox = nullptr;
+            d.cap = 0;
+            CU(cudaMalloc(&d.bricks, (size_t)cap * kBrick * sizeof(uint32_t)), "cudaMalloc(bricks)");
+            CU(cudaMalloc(&d.bbox, (size_t)cap * 2u * sizeof(uint32_t)), "cudaMalloc(brick boxes)");
+            d.cap = cap;
+        }
+        d.bbox0 = d.bbox + d.cap;
+        CU(cudaMemcpy(d.grid, w.grid.data(), kGridSize * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload grid");
+        if (w.brickHigh)
+            CU(cudaMemcpy(d.bricks, w.bricks.data(), (size_t)w.brickHigh * kBrick * sizeof(uint32_t), cudaMemcpyHostToDevice),
+               "upload bricks");
+        launch_build_brick_boxes(d.bricks, nullptr, w.brickHigh, d.bbox, d.bbox0, 0);
+        sent = w.brickHigh;
+    } else if (w.dirtyCount) {
+        if (w.dirtyCount > d.stageCap) {
+            cudaFreeHost(d.stageHost);
+            cudaFree(d.stageDev);
+            d.stageHost = nullptr;
+            d.stageDev = nullptr;
+            d.stageCap = 0;
+            const uint32_t cap = std::max<uint32_t>(w.dirtyCount + w.dirtyCount / 2u, 64u);
+            const size_t bytes = (size_t)cap * (kBrick + 1u) * sizeof(uint32_t);
+            CU(cudaMallocHost(&d.stageHost, bytes), "cudaMallocHost(commit staging)");
+            CU(cudaMalloc(&d.stageDev, bytes), "cudaMalloc(commit staging)");
+            d.stageCap = cap;
+        }
+        // staging: the brick indices, then (at a 16-byte aligned offset) their voxels
+        const uint32_t n = w.dirtyCount;
+        const size_t voxOff = ((size_t)n + 3u) & ~(size_t)3u;
+        uint32_t* list = d.stageHost;
+        uint32_t* vox = d.stageHost + voxOff;
+        uint32_t k = 0;
+        for (size_t wd = 0; wd < w.dirty.size() && k < n; wd++) {
+            for (uint32_t m = w.dirty[wd]; m; m &= m - 1u) {
+                const uint32_t b = (uint32_t)(wd * 32u) + (uint32_t)__builtin_ctz(m);
+                if (b >= w.brickHigh) continue;
+                list[k] = b;
+                std::memcpy(vox + (size_t)k * kBrick, &w.bricks[(size_t)b * kBrick], kBrick * sizeof(uint32_t));
+                k++;
+            }
+        }
+        sent = k;
+        if (k) {
+            const size_t bytes = (voxOff + (size_t)k * kBrick) * sizeof(uint32_t);
+            CU(cudaMemcpy(d.stageDev, d.stageHost, bytes, cudaMemcpyHostToDevice), "commit bricks");
+            launch_commit_bricks(d.stageDev, d.stageDev + voxOff, k, d.bricks, 0);
+            launch_build_brick_boxes(d.bricks, d.stageDev, k, d.bbox, d.bbox0, 0);
+        }
     }
-    const size_t sb = (size_t)std::max<uint32_t>(w.brickHigh, 1u) * 2u * sizeof(uint32_t);
-    if (sb > d.bboxBytes) {
-        cudaFree(d.bbox);
-        d.bbox = nullptr;
-        CU(cudaMalloc(&d.bbox, sb), "cudaMalloc(brick boxes)");
-        d.bboxBytes = sb;
+    if (full || w.gridDirty) {
+        if (!full) CU(cudaMemcpy(d.grid, w.grid.data(), kGridSize * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload grid");
+        launch_build_uber(d.grid, d.uber, 0);
     }
-    CU(cudaMemcpy(d.grid, w.grid.data(), kGridSize * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload grid");
-    if (w.brickHigh)
-        CU(cudaMemcpy(d.bricks, w.bricks.data(), (size_t)w.brickHigh * kBrick * sizeof(uint32_t), cudaMemcpyHostToDevice),
-           "upload bricks");
-    const uint32_t nl = (uint32_t)w.lights.size();
-    const size_t need = std::max<uint32_t>(nl, 1u);
-    if (need > d.lcap) {
-        cudaFree(d.lraw);
-        cudaFree(d.lgeom);
-        cudaFree(d.lemit);
-        d.lraw = nullptr; d.lgeom = nullptr; d.lemit = nullptr;
-        CU(cudaMalloc(&d.lraw, need * sizeof(uint4)), "cudaMalloc(lights)");
-        CU(cudaMalloc(&d.lgeom, need * sizeof(float4)), "cudaMalloc(light geom)");
-        CU(cudaMalloc(&d.lemit, need * sizeof(float4)), "cudaMalloc(light emit)");
-        d.lcap = need;
+    if (full || w.gridDirty || sent) launch_build_uber_boxes(d.grid, d.bbox0, d.ubox0, 0);
+    if (full || d.lightVersion != w.lightVersion) {
+        const uint32_t nl = (uint32_t)w.lights.size();
+        const size_t need = std::max<uint32_t>(nl, 1u);
+        if (need > d.lcap) {
+            cudaFree(d.lraw);
+            cudaFree(d.lgeom);
+            cudaFree(d.lemit);
+            d.lraw = nullptr; d.lgeom = nullptr; d.lemit = nullptr;
+            CU(cudaMalloc(&d.lraw, need * sizeof(uint4)), "cudaMalloc(lights)");
+            CU(cudaMalloc(&d.lgeom, need * sizeof(float4)), "cudaMalloc(light geom)");
+            CU(cudaMalloc(&d.lemit, need * sizeof(float4)), "cudaMalloc(light emit)");
+            d.lcap = need;
+        }
+        std::vector<uint4> raw(need, make_uint4(0, 0, 1, 0));
+        for (uint32_t i = 0; i < nl; i++) raw[i] = make_uint4(w.lights[i].position, w.lights[i].voxel, w.lights[i].size, 0);
+        CU(cudaMemcpy(d.lraw, raw.data(), need * sizeof(uint4), cudaMemcpyHostToDevice), "upload lights");
+        launch_build_light_table(d.lraw, (uint32_t)need, d.lgeom, d.lemit, 0);
+        d.nl = nl;
     }
-    std::vector<uint4> raw(need, make_uint4(0, 0, 1, 0));
-    for (uint32_t i = 0; i < nl; i++) raw[i] = make_uint4(w.lights[i].position, w.lights[i].voxel, w.lights[i].size, 0);
-    CU(cudaMemcpy(d.lraw, raw.data(), need * sizeof(uint4), cudaMemcpyHostToDevice), "upload lights");
-    launch_build_light_table(d.lraw, (uint32_t)need, d.lgeom, d.lemit, 0);
-    launch_build_uber(d.grid, d.uber, 0);
-    d.bbox0 = d.bbox + std::max<uint32_t>(w.brickHigh, 1u);
-    launch_build_brick_boxes(d.bricks, w.brickHigh, d.bbox, d.bbox0, 0);
-    launch_build_uber_boxes(d.grid, d.bbox0, d.ubox0, 0);
     CU(cudaGetLastError(), "world kernels launch");
     CU(cudaDeviceSynchronize(), "world kernels");
-    d.nl = nl;
+    d.high = w.brickHigh;
     d.version = w.version;
     d.lightVersion = w.lightVersion;
+    d.lastSent = sent;
+    d.lastFull = full;
+    std::fill(w.dirty.begin(), w.dirty.end(), 0u);
+    w.dirtyCount = 0;
+    w.gridDirty = false;
+    w.fullDirty = false;
     return VXR_OK;
 }
 
@@ -269,14 +329,36 @@ extern "C" {
 
 int vxr_world_upload(vxr_world* w) {
     VXR_CHECK_ARG(w, "vxr_world_upload: null world");
+    w->w.mark_all();
     return vxr::upload(w->w);
+}
+
+int vxr_world_commit(vxr_world* w, uint32_t* bricks_sent, int* full) {
+    VXR_CHECK_ARG(w, "vxr_world_commit: null world");
+    const int r = vxr::upload(w->w);
+    if (r != VXR_OK) return r;
+    if (bricks_sent) *bricks_sent = w->w.dev->lastSent;
+    if (full) *full = w->w.dev->lastFull ? 1 : 0;
+    return VXR_OK;
+}
+
+int vxr_world_pending(const vxr_world* w, uint32_t* dirty_bricks, int* grid_changed, int* full) {
+    VXR_CHECK_ARG(w, "vxr_world_pending: null world");
+    const vxr::World& W = w->w;
+    const bool everything = W.fullDirty || !W.dev || W.brickHigh > W.dev->cap;
+    if (dirty_bricks) *dirty_bricks = everything ? W.brickHigh : W.dirtyCount;
+    if (grid_changed) *grid_changed = (everything || W.gridDirty) ? 1 : 0;
+    if (full) *full = everything ? 1 : 0;
+    return VXR_OK;
 }
 
 int vxr_world_device_bytes(const vxr_world* w, uint64_t* bytes) {
     VXR_CHECK_ARG(w && bytes, "vxr_world_device_bytes: null argument");
     const vxr::DeviceWorld* d = w->w.dev;
     // grid, uber grid and its boxes, bricks and their boxes, light tables
-    *bytes = d ? (uint64_t)(vxr::kGridSize * 4 + 32768 + 32768 * 4 + d->brickBytes + d->bboxBytes + d->lcap * 48) : 0;
+    *bytes = d ? (uint64_t)(vxr::kGridSize * 4 + 32768 + 32768 * 4 + (uint64_t)d->cap * (vxr::kBrick * 4 + 8) +
+                            (uint64_t)d->stageCap * (vxr::kBrick + 1) * 4 + d->lcap * 48)
+               : 0;
     return VXR_OK;
 }
 

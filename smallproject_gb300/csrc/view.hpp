@@ -15,11 +15,18 @@ struct DeviceWorld {
     uint32_t* grid = nullptr;
     uint8_t* uber = nullptr;
     uint32_t* bricks = nullptr;
-    size_t brickBytes = 0;
+    uint32_t cap = 0;                // bricks the pool (and the box tables) can hold
+    uint32_t high = 0;               // bricks [0, high) are on the device
     uint32_t* bbox = nullptr;        // boxes of the opaque voxels per brick (brick skipping),
-    uint32_t* bbox0 = nullptr;       // then those of the non-zero voxels (inside bbox's block)
+    uint32_t* bbox0 = nullptr;       // then those of the non-zero voxels (bbox + cap)
     uint32_t* ubox0 = nullptr;       // box of the non-zero voxels per uber cell (32^3)
-    size_t bboxBytes = 0;
+    // incremental commits: changed bricks (index list, then their voxels) staged in
+    // page-locked memory and copied to `stageDev` (capacity `stageCap` bricks)
+    uint32_t* stageHost = nullptr;
+    uint32_t* stageDev = nullptr;
+    uint32_t stageCap = 0;
+    uint32_t lastSent = 0;           // bricks sent by the last commit
+    bool lastFull = false;           // the last commit sent everything
     uint4* lraw = nullptr;
     float4* lgeom = nullptr;
     float4* lemit = nullptr;

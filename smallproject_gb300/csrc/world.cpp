@@ -19,6 +19,9 @@ void World::clear() {
     freeList.clear();
     brickHigh = 0;
     lights.clear();
+    dirty.clear();
+    dirtyCount = 0;
+    mark_all();
     touch();
     lightVersion++;
 }
@@ -83,6 +86,8 @@ void World::set(uint32_t x, uint32_t y, uint32_t z, uint32_t v) {
         std::fill(bricks.begin() + (size_t)b * kBrick, bricks.begin() + (size_t)(b + 1) * kBrick, colour);
         zeroes[b] = (colour == 0) ? kBrick : 0u;
         grid[ci] = (b << 1) | 1u;
+        mark_brick(b);
+        gridDirty = true;
     }
     const size_t vi = (size_t)b * kBrick + (x & 7) + (y & 7) * 8 + (z & 7) * 64;
     const uint32_t orig = bricks[vi];
@@ -94,9 +99,11 @@ void World::set(uint32_t x, uint32_t y, uint32_t z, uint32_t v) {
     zeroes[b] = (uint32_t)((int)zeroes[b] + zeroChange);
     if (zeroes[b] < kBrick) {
         bricks[vi] = v;
+        mark_brick(b);
     } else {
         grid[ci] = 0;
         free_brick(b);
+        gridDirty = true;
     }
     touch();
 }
@@ -118,7 +125,10 @@ uint32_t World::optimize() {
             replaced++;
         }
     }
-    if (replaced) touch();
+    if (replaced) {
+        gridDirty = true;
+        touch();
+    }
     return replaced;
 }
 

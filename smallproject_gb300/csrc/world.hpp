@@ -37,6 +37,25 @@ struct World {
     uint64_t version = 1;              // bumps on every edit (device copy stale when different)
     uint64_t lightVersion = 1;         // bumps on every light-list change (temporal reset)
     DeviceWorld* dev = nullptr;
+    // device commit state (World::Commit / IsDirty / Mark, world.cpp:2357-2420,
+    // world.h:565-613): bricks whose content changed since the last commit (1 bit each),
+    // whether the top-level grid changed, whether everything must be sent again
+    std::vector<uint32_t> dirty;
+    uint32_t dirtyCount = 0;
+    bool gridDirty = true;
+    bool fullDirty = true;
+    void mark_brick(uint32_t b) {
+        if ((b >> 5) >= dirty.size()) dirty.resize((b >> 5) + 1 + dirty.size() / 2, 0u);
+        const uint32_t m = 1u << (b & 31);
+        if (!(dirty[b >> 5] & m)) {
+            dirty[b >> 5] |= m;
+            dirtyCount++;
+        }
+    }
+    void mark_all() {
+        fullDirty = true;
+        gridDirty = true;
+    }
 
     World();
     ~World();

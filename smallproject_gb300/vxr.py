@@ -110,7 +110,8 @@ _SIGS = {
     "vxr_scene_height": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)],
     "vxr_camera_path": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.c_uint32, _F3, _F3],
     "vxr_world_checksum": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
-    "vxr_world_upload": [_P], "vxr_world_device_bytes": [_P, C.POINTER(C.c_uint64)],
+    "vxr_world_upload": [_P], "vxr_world_commit": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int)],
+    "vxr_world_pending": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_int)], "vxr_world_device_bytes": [_P, C.POINTER(C.c_uint64)],
     "vxr_view_default_desc": [C.POINTER(ViewDesc)],
     "vxr_view_create": [_P, C.POINTER(ViewDesc), C.POINTER(_P)], "vxr_view_destroy": [_P],
     "vxr_view_lookat": [_P, _F3, _F3], "vxr_view_set_camera_matrix": [_P, _F3],
@@ -271,7 +272,20 @@ class World:
         check(self._lib.vxr_scene_generate(self.h, C.byref(desc)))
 
     def upload(self):
+        """Send the whole world to the device (vxr_world_upload)."""
         check(self._lib.vxr_world_upload(self.h))
+
+    def commit(self):
+        """Send the edits since the last commit (vxr_world_commit): (bricks sent, everything sent)."""
+        n, full = C.c_uint32(), C.c_int()
+        check(self._lib.vxr_world_commit(self.h, C.byref(n), C.byref(full)))
+        return n.value, bool(full.value)
+
+    def pending(self):
+        """What the next commit would send: (changed bricks, grid changed, everything due)."""
+        n, g, full = C.c_uint32(), C.c_int(), C.c_int()
+        check(self._lib.vxr_world_pending(self.h, C.byref(n), C.byref(g), C.byref(full)))
+        return n.value, bool(g.value), bool(full.value)
 
     def device_bytes(self):
         b = C.c_uint64()

@@ -123,3 +123,14 @@ def test_camera_constants_match_oracle(lib):
         assert a == b, f"frame {f}"
         cam.end_frame()
         ocam.end()
+
+
+def test_pending_commit_before_any_device_copy(lib):
+    """Without a device copy the next commit is a full one: every brick and the grid."""
+    w = lib.World()
+    w.generate(lib.scene_preset(0))
+    n, grid, full = w.pending()
+    assert full and grid and n == len(w.arrays()[1])
+    w.set(5, 5, 5, 0xF123)
+    assert w.pending()[2]
+    w.close()
