@@ -578,9 +578,30 @@ def main():
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
                     "d2h_bytes_per_step": npx * 16, "image_ok": img_ok},
             "gpu_launches": launches, "clocks": clk,
-            "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report}
+            "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report,
+            "world_commit": world_commit_times(world, args)}
     print(json.dumps(line))
     view.close()
+
+
+def world_commit_times(world, args):
+    """Host wall time of sending the world to the device: everything (vxr_world_upload)
+    against incremental commits after editing 1 and 1,000 random voxels (after every other
+    measurement: it changes the world)."""
+    rng = np.random.default_rng(17)
+    out = {}
+    t0 = time.perf_counter()
+    world.upload()
+    out["full_upload_ms"] = (time.perf_counter() - t0) * 1e3
+    out["bricks"] = world.brick_count()
+    for n in (1, 1000):
+        for _ in range(n):
+            x, y, z = (int(v) for v in rng.integers(0, 1024, 3))
+            world.set(x, y, z, 0xF5A5)
+        t0 = time.perf_counter()
+        sent, full = world.commit()
+        out[f"edit_{n}_voxels"] = {"ms": (time.perf_counter() - t0) * 1e3, "bricks_sent": sent, "full": full}
+    return out
 
 
 if __name__ == "__main__":

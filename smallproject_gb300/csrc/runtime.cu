@@ -55,16 +55,18 @@ void release_device_world(World& w) {
 static int upload(World& w) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(VXR_E_NODEVICE, "no CUDA device visible");
-    // every brick cell must point into the pool
-    for (uint32_t i = 0; i < kGridSize; i++)
-        if ((w.grid[i] & 1u) && (w.grid[i] >> 1) >= w.brickHigh)
-            return set_error(VXR_E_STATE, "vxr_world_upload: grid cell references a brick outside the pool");
     int dev = 0;
     CU(cudaGetDevice(&dev), "cudaGetDevice");
+    const bool full = w.fullDirty || !w.dev || !w.dev->grid || w.dev->device != dev || w.brickHigh > w.dev->cap;
+    // every brick cell must point into the pool (edits through World::set / optimize keep
+    // this, so incremental commits skip the scan)
+    if (full)
+        for (uint32_t i = 0; i < kGridSize; i++)
+            if ((w.grid[i] & 1u) && (w.grid[i] >> 1) >= w.brickHigh)
+                return set_error(VXR_E_STATE, "vxr_world_upload: grid cell references a brick outside the pool");
     CU(cudaDeviceSynchronize(), "upload: wait for device work");
     if (!w.dev) w.dev = new DeviceWorld();
     DeviceWorld& d = *w.dev;
-    const bool full = w.fullDirty || !d.grid || d.device != dev || w.brickHigh > d.cap;
     d.device = dev;
     if (!d.grid) CU(cudaMalloc(&d.grid, kGridSize * sizeof(uint32_t)), "cudaMalloc(grid)");
     if (!d.uber) CU(cudaMalloc(&d.uber, 32 * 32 * 32), "cudaMalloc(uber)");
@@ -127,7 +129,19 @@ static int upload(World& w) {
         }
     }
     if (full || w.gridDirty) {
-        if (!full) CU(cudaMemcpy(d.grid, w.grid.data(), kGridSize * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload grid");
+        if (!full) {
+            // the changed y-layers of the grid (128^2 cells each), runs copied together
+            const size_t layer = (size_t)kGrid * kGrid;
+            for (uint32_t y = 0; y < kGrid;) {
+                if (!(w.gridRows[y >> 5] >> (y & 31) & 1u)) { y++; continue; }
+                uint32_t e = y + 1;
+                while (e < kGrid && (w.gridRows[e >> 5] >> (e & 31) & 1u)) e++;
+                CU(cudaMemcpy(d.grid + y * layer, w.grid.data() + y * layer, (e - y) * layer * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice),
+                   "upload grid layers");
+                y = e;
+            }
+        }
         launch_build_uber(d.grid, d.uber, 0);
     }
     if (full || w.gridDirty || sent) launch_build_uber_boxes(d.grid, d.bbox0, d.ubox0, 0);
@@ -160,6 +174,7 @@ static int upload(World& w) {
     std::fill(w.dirty.begin(), w.dirty.end(), 0u);
     w.dirtyCount = 0;
     w.gridDirty = false;
+    std::fill(std::begin(w.gridRows), std::end(w.gridRows), 0u);
     w.fullDirty = false;
     return VXR_OK;
 }

@@ -87,7 +87,7 @@ void World::set(uint32_t x, uint32_t y, uint32_t z, uint32_t v) {
         zeroes[b] = (colour == 0) ? kBrick : 0u;
         grid[ci] = (b << 1) | 1u;
         mark_brick(b);
-        gridDirty = true;
+        mark_row(by);
     }
     const size_t vi = (size_t)b * kBrick + (x & 7) + (y & 7) * 8 + (z & 7) * 64;
     const uint32_t orig = bricks[vi];
@@ -103,7 +103,7 @@ void World::set(uint32_t x, uint32_t y, uint32_t z, uint32_t v) {
     } else {
         grid[ci] = 0;
         free_brick(b);
-        gridDirty = true;
+        mark_row(by);
     }
     touch();
 }
@@ -122,13 +122,11 @@ uint32_t World::optimize() {
         if (solid) {
             grid[i] = first << 1;
             free_brick(c >> 1);
+            mark_row(i / (kGrid * kGrid));
             replaced++;
         }
     }
-    if (replaced) {
-        gridDirty = true;
-        touch();
-    }
+    if (replaced) touch();
     return replaced;
 }
 

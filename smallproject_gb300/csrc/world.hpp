@@ -43,7 +43,12 @@ struct World {
     std::vector<uint32_t> dirty;
     uint32_t dirtyCount = 0;
     bool gridDirty = true;
+    uint32_t gridRows[kGrid / 32] = {};   // grid y-layers (128^2 cells each) that changed
     bool fullDirty = true;
+    void mark_row(uint32_t by) {
+        gridDirty = true;
+        gridRows[by >> 5] |= 1u << (by & 31);
+    }
     void mark_brick(uint32_t b) {
         if ((b >> 5) >= dirty.size()) dirty.resize((b >> 5) + 1 + dirty.size() / 2, 0u);
         const uint32_t m = 1u << (b & 31);

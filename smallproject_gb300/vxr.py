@@ -275,6 +275,12 @@ class World:
         """Send the whole world to the device (vxr_world_upload)."""
         check(self._lib.vxr_world_upload(self.h))
 
+    def brick_count(self):
+        """Bricks in use (vxr_world_brick_count)."""
+        n = C.c_uint32()
+        check(self._lib.vxr_world_brick_count(self.h, C.byref(n)))
+        return n.value
+
     def commit(self):
         """Send the edits since the last commit (vxr_world_commit): (bricks sent, everything sent)."""
         n, full = C.c_uint32(), C.c_int()
