@@ -146,6 +146,13 @@ int vxr_world_optimize(vxr_world* w, uint32_t* replaced);
 int vxr_world_scan_lights(vxr_world* w, uint32_t* count);
 /* World::SetupLightBuffer (world.cpp:563-612) with an explicit list (replaces the list). */
 int vxr_world_set_lights(vxr_world* w, const vxr_light* lights, uint32_t n);
+/* World::MoveLights for one light (world.cpp:268-305): move voxel light `index` of the
+ * light list to (x, y, z). The voxel it covered is restored (0 if none was remembered),
+ * its emitter voxel is drawn at the new position and the non-emitter voxel there is
+ * remembered; the list keeps its order. Views restart temporal reuse for a moved light
+ * only when their spatial reuse is off, as the reference does (world.cpp:300-301).
+ * Brick lights (size 8) do not move: VXR_E_INVALID. */
+int vxr_world_move_light(vxr_world* w, uint32_t index, uint32_t x, uint32_t y, uint32_t z);
 /* Read-only views of the host arrays (valid until the next edit): top-level grid
  * (128^3 uint32, index x + z*128 + y*16384; 0 empty, even = solid colour << 1,
  * odd = brick index << 1 | 1), brick pool (nbricks * 512 uint32, voxel lx + ly*8 + lz*64),

@@ -112,6 +112,14 @@ int vxr_world_set_lights(vxr_world* w, const vxr_light* lights, uint32_t n) {
     return VXR_OK;
 }
 
+int vxr_world_move_light(vxr_world* w, uint32_t index, uint32_t x, uint32_t y, uint32_t z) {
+    VXR_CHECK_ARG(w, "vxr_world_move_light: null world");
+    const int r = w->w.move_light(index, x, y, z);
+    VXR_CHECK_ARG(r != -1, "vxr_world_move_light: light index or position out of range");
+    VXR_CHECK_ARG(r != -2, "vxr_world_move_light: only voxel lights (size 1) move");
+    return VXR_OK;
+}
+
 int vxr_world_arrays(const vxr_world* w, const uint32_t** grid, const uint32_t** bricks, uint32_t* nbricks,
                      const vxr_light** lights, uint32_t* nlights) {
     VXR_CHECK_ARG(w, "vxr_world_arrays: null world");

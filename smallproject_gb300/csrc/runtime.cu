@@ -145,7 +145,7 @@ static int upload(World& w) {
         launch_build_uber(d.grid, d.uber, 0);
     }
     if (full || w.gridDirty || sent) launch_build_uber_boxes(d.grid, d.bbox0, d.ubox0, 0);
-    if (full || d.lightVersion != w.lightVersion) {
+    if (full || d.lightVersion != w.lightVersion || d.lightMoveVersion != w.lightMoveVersion) {
         const uint32_t nl = (uint32_t)w.lights.size();
         const size_t need = std::max<uint32_t>(nl, 1u);
         if (need > d.lcap) {
@@ -169,6 +169,7 @@ static int upload(World& w) {
     d.high = w.brickHigh;
     d.version = w.version;
     d.lightVersion = w.lightVersion;
+    d.lightMoveVersion = w.lightMoveVersion;
     d.lastSent = sent;
     d.lastFull = full;
     std::fill(w.dirty.begin(), w.dirty.end(), 0u);
@@ -456,6 +457,7 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
         return r;
     }
     v->seenLightVersion = w->w.lightVersion;
+    v->seenLightMoveVersion = w->w.lightMoveVersion;
     *out = v;
     return VXR_OK;
 }
@@ -502,6 +504,11 @@ int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* out) {
     if (w.lightVersion != v->seenLightVersion) {
         v->cam.restirtemporalframe = 0;   // any light change resets temporal reuse (world.cpp:245)
         v->seenLightVersion = w.lightVersion;
+    }
+    if (w.lightMoveVersion != v->seenLightMoveVersion) {
+        // moved lights reset temporal reuse only without spatial reuse (world.cpp:300-301)
+        if (!v->desc.spatial) v->cam.restirtemporalframe = 0;
+        v->seenLightMoveVersion = w.lightMoveVersion;
     }
     vxr_frame_consts& k = v->k;
     std::memset(&k, 0, sizeof(k));

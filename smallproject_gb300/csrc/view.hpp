@@ -32,7 +32,7 @@ struct DeviceWorld {
     float4* lemit = nullptr;
     uint32_t nl = 0;
     size_t lcap = 0;
-    uint64_t version = 0, lightVersion = 0;
+    uint64_t version = 0, lightVersion = 0, lightMoveVersion = 0;
     int device = -1;
 };
 struct Proposal;   // learned candidate proposal state (proposal_api.cu)
@@ -79,7 +79,7 @@ struct vxr_view {
     bool useProposal = false;
     bool frameOpen = false;
     vxr_frame_consts k{};
-    uint64_t seenLightVersion = 0;
+    uint64_t seenLightVersion = 0, seenLightMoveVersion = 0;
     float times[5] = {};
     size_t npx = 0;
 };

@@ -19,6 +19,7 @@ void World::clear() {
     freeList.clear();
     brickHigh = 0;
     lights.clear();
+    covered.clear();
     dirty.clear();
     dirtyCount = 0;
     mark_all();
@@ -68,6 +69,37 @@ void World::remove_light(uint32_t x, uint32_t y, uint32_t z) {
     lights.erase(std::remove_if(lights.begin(), lights.end(), [p](const vxr_light& l) { return l.position == p; }),
                  lights.end());
     lightVersion++;
+}
+
+// World::MoveLights for one light (world.cpp:268-305): restore the voxel the light
+// covered (0 when none was remembered), draw its emitter voxel at (x, y, z) and remember
+// the non-emitter voxel it covers there; the list entry keeps its index. Voxel lights
+// (size 1) only. Returns 0, or -1 for an index or position out of range, -2 for a
+// brick light.
+int World::move_light(uint32_t index, uint32_t x, uint32_t y, uint32_t z) {
+    if (index >= lights.size() || x >= kMap || y >= kMap || z >= kMap) return -1;
+    vxr_light& l = lights[index];
+    if (l.size != 1u) return -2;
+    const uint32_t from = l.position, to = x + z * kMap + y * kMap * kMap;
+    if (from == to) return 0;
+    const uint32_t fx = from % kMap, fz = (from / kMap) % kMap, fy = from / (kMap * kMap);
+    const uint32_t under = get(x, y, z);
+    uint32_t restore = 0u;
+    const auto it = covered.find(from);
+    if (it != covered.end()) {
+        restore = it->second;
+        covered.erase(it);
+    }
+    if (!is_emitter(under)) covered[to] = under;
+    const bool track = trackLights;
+    trackLights = false;
+    set(fx, fy, fz, restore);
+    set(x, y, z, l.voxel);
+    trackLights = track;
+    l.position = to;
+    lightMoveVersion++;
+    touch();
+    return 0;
 }
 
 // World::Set (world.h:456-513): split a solid cell into a brick when needed, keep the

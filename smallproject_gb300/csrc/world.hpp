@@ -8,6 +8,7 @@
 // affects rendering (only the cell -> brick mapping is read by the DDA).
 #pragma once
 #include <cstdint>
+#include <unordered_map>
 #include <vector>
 #include "vxr.h"
 
@@ -36,6 +37,8 @@ struct World {
     bool trackLights = true;
     uint64_t version = 1;              // bumps on every edit (device copy stale when different)
     uint64_t lightVersion = 1;         // bumps on every light-list change (temporal reset)
+    uint64_t lightMoveVersion = 1;     // bumps when a light moves (list order kept)
+    std::unordered_map<uint32_t, uint32_t> covered;   // voxel under a moved light (defaultVoxel)
     DeviceWorld* dev = nullptr;
     // device commit state (World::Commit / IsDirty / Mark, world.cpp:2357-2420,
     // world.h:565-613): bricks whose content changed since the last commit (1 bit each),
@@ -74,6 +77,7 @@ struct World {
     uint32_t bricks_in_use() const { return brickHigh - (uint32_t)freeList.size(); }
     void add_light(uint32_t x, uint32_t y, uint32_t z, uint32_t size, uint32_t v);
     void remove_light(uint32_t x, uint32_t y, uint32_t z);
+    int move_light(uint32_t index, uint32_t x, uint32_t y, uint32_t z);
     void touch() { version++; }
 };
 

@@ -110,6 +110,7 @@ _SIGS = {
     "vxr_scene_height": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)],
     "vxr_camera_path": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.c_uint32, _F3, _F3],
     "vxr_world_checksum": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
+    "vxr_world_move_light": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "vxr_world_upload": [_P], "vxr_world_commit": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int)],
     "vxr_world_pending": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_int)], "vxr_world_device_bytes": [_P, C.POINTER(C.c_uint64)],
     "vxr_view_default_desc": [C.POINTER(ViewDesc)],
@@ -274,6 +275,10 @@ class World:
     def upload(self):
         """Send the whole world to the device (vxr_world_upload)."""
         check(self._lib.vxr_world_upload(self.h))
+
+    def move_light(self, index, x, y, z):
+        """Move voxel light `index` of the light list to (x, y, z) (vxr_world_move_light)."""
+        check(self._lib.vxr_world_move_light(self.h, index, x, y, z))
 
     def brick_count(self):
         """Bricks in use (vxr_world_brick_count)."""

@@ -87,3 +87,48 @@ def test_render_commits_pending_edits(lib, cuda_device):
     assert w.pending() == (0, False, False)
     w.upload()                                     # an explicit full upload still works
     assert w.pending() == (0, False, False)
+
+
+def _moves(lib, w):
+    _, _, lights = w.arrays()
+    idx = [k for k in range(len(lights)) if lights["size"][k] == 1][:6]
+    for n, i in enumerate(idx):
+        w.move_light(i, 70 + 23 * n, 140 + 3 * n, 60 + 29 * n)
+    return idx
+
+
+def test_moved_lights_render_like_a_fresh_upload(lib, cuda_device):
+    """Lights moved with vxr_world_move_light and committed incrementally (a few bricks,
+    the light table) render exactly like the same world sent whole."""
+    pos, tgt = (100.0, 170.0, 20.0), (128.0, 100.0, 128.0)
+    a = _world(lib)
+    _render(lib, a, pos, tgt)
+    moved = _moves(lib, a)
+    assert len(moved) == 6
+    n, _, full = a.pending()
+    assert 0 < n <= 24 and not full
+    ra = _render(lib, a, pos, tgt)
+    b = _world(lib)
+    _moves(lib, b)
+    rb = _render(lib, b, pos, tgt)
+    for key, name in (("g", "gbuffer"), ("c", "candidates"), ("h", "spatial"), ("f", "frame")):
+        assert_records_equal(name, ra[key], rb[key], "[moved lights]")
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("spatial", [0, 1])
+def test_moving_a_light_resets_temporal_reuse_only_without_spatial(lib, cuda_device, spatial):
+    w = _world(lib)
+    v = lib.View(w, lib.view_desc(64, 48, lib.LIGHTS_AREA, spatial=spatial, temporal=1))
+    try:
+        v.lookat((100.0, 170.0, 20.0), (128.0, 100.0, 128.0))
+        for _ in range(3):
+            v.render()
+        v.wait()
+        _moves(lib, w)
+        k = v.begin_frame()
+        assert (k.restirtemporalframe == 0) == (spatial == 0), k.restirtemporalframe
+    finally:
+        v.close()
+        w.close()

@@ -1,6 +1,7 @@
 """Host voxel store (World::Set/Get/OptimizeBricks/FindLightsInWord semantics) and the
 procedural scenes, against the oracle's restatement of the same functions."""
 import numpy as np
+import pytest
 
 from oracle import binding as ob
 
@@ -133,4 +134,29 @@ def test_pending_commit_before_any_device_copy(lib):
     assert full and grid and n == len(w.arrays()[1])
     w.set(5, 5, 5, 0xF123)
     assert w.pending()[2]
+    w.close()
+
+
+def test_move_light_restores_and_remembers_voxels(lib):
+    """vxr_world_move_light (World::MoveLights for one light): the emitter voxel moves,
+    the voxel it covered comes back, the list keeps its order, brick lights stay put."""
+    w = lib.World()
+    w.generate(lib.scene_preset(0, seed=5, emitters=12))
+    _, _, lights = w.arrays()
+    i = next(k for k in range(len(lights)) if lights["size"][k] == 1)
+    p0 = int(lights["position"][i])
+    v = int(lights["voxel"][i])
+    x0, z0, y0 = p0 % 1024, (p0 // 1024) % 1024, p0 // (1024 * 1024)
+    assert w.get(x0, y0, z0) == v
+    # onto a solid voxel: the solid voxel is remembered and restored later
+    w.set(30, 200, 30, 0xF321)
+    w.move_light(i, 30, 200, 30)
+    assert w.get(30, 200, 30) == v and w.get(x0, y0, z0) == 0
+    _, _, after = w.arrays()
+    assert len(after) == len(lights) and int(after["position"][i]) == 30 + 30 * 1024 + 200 * 1024 * 1024
+    assert np.array_equal(np.delete(after, i), np.delete(lights, i))
+    w.move_light(i, x0, y0, z0)
+    assert w.get(x0, y0, z0) == v and w.get(30, 200, 30) == 0xF321
+    with pytest.raises(lib.VxrError):
+        w.move_light(len(lights), 1, 1, 1)
     w.close()
