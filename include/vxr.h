@@ -301,6 +301,10 @@ int vxr_view_set_frame_consts(vxr_view* v, const vxr_frame_consts* k);
 #define VXR_STAGE_SPATIAL     3
 #define VXR_STAGE_SHADE       4
 #define VXR_STAGE_ACCUMULATE  5
+/* renderPathTracer with render_di_gfxexp (kernels.cl:177-260): the reference's
+ * ground-truth mode, one hemisphere sample per pixel into the frame buffer (follow with
+ * VXR_STAGE_ACCUMULATE, or vxr_view_sum64_add, to converge); not timed per stage. */
+#define VXR_STAGE_PATH_TRACE  6
 int vxr_view_stage(vxr_view* v, int stage);
 /* Frame counters (world.cpp:2335-2337). */
 int vxr_view_end_frame(vxr_view* v);

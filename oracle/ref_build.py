@@ -40,9 +40,10 @@ TOOLS_FUNCS = [
     "WangHash", "RandomInt", "RandomFloat", "GenerateCameraRay", "GetAlpha", "GetAlphaf",
     "ToFloatRGB", "FromFloatRGBA", "VoxelNormal", "getRandomIndex", "indexToCoordinates",
     "GridCoordinatesFromHit", "Uint3CubeEquals", "ReprojectWorldPoint", "IsInBounds",
-    "RandomPointOnVoxel", "GenerateLightCandidate", "PointOnVoxelLight",
+    "RandomPointOnVoxel", "GenerateLightCandidate", "PointOnVoxelLight", "UniformSampleHemisphere",
 ]
-KERNELS_FUNCS = ["accumulatorFinalizer", "updateUberGrid"]
+# render_di_gfxexp + renderPathTracer: the reference's ground-truth mode (GFXEXP = 1)
+KERNELS_FUNCS = ["accumulatorFinalizer", "updateUberGrid", "render_di_gfxexp", "renderPathTracer"]
 
 STUBS = r"""
 // ---- stubs: referenced by render_di_ris only under skyDomeSampling / editorEnabled,

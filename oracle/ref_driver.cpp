@@ -162,7 +162,8 @@ void VXREF_FN(vxref_begin_frame)(void* ctx) {
     std::swap(c->gbCurrent, c->gbPrevious);
 }
 
-// stage: 1 albedo, 2 candidates+temporal, 3 spatial, 4 shading, 5 accumulate
+// stage: 1 albedo, 2 candidates+temporal, 3 spatial, 4 shading, 5 accumulate,
+// 6 the path-tracer ground truth (renderPathTracer, kernels.cl:177-260) into the frame
 void VXREF_FN(vxref_stage)(void* ctx, const vxr_frame_consts* k, int stage) {
     Ctx* c = (Ctx*)ctx;
     fill_params(c, k);
@@ -210,6 +211,11 @@ void VXREF_FN(vxref_stage)(void* ctx, const vxr_frame_consts* k, int stage) {
         float4* frame = c->frame.data();
         float4* acc = c->accum.data();
         for_pixels(c, [&] { accumulatorFinalizer(img, frame, acc, params); });
+        break;
+    }
+    case 6: {
+        float4* frame = c->frame.data();
+        for_pixels(c, [&] { renderPathTracer(frame, params, grid, nullptr, nullptr, uber, brick0); });
         break;
     }
     default:

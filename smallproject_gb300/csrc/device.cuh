@@ -41,6 +41,7 @@ struct Frame {
     float oorx, oory;
     float4 Nl, Nr, Nt, Nb;
     uint32_t R0, framecount, restirtemporalframe;
+    uint32_t frame;              // frame counter (the path tracer's stratum, kernels.cl:219-220)
     int32_t spatial, temporal, accumulate;
     uint32_t nlights, ncand;     // ncand = min(numberOfLights, numberOfCandidates) (ris.cl:48)
     uint32_t maxTemporal, radius, taps;

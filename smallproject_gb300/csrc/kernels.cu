@@ -288,6 +288,71 @@ __global__ void __launch_bounds__(kMaxTileThreads) albedo_kernel(const __grid_co
     }
 }
 
+// ---- ground truth: renderPathTracer / render_di_gfxexp (kernels.cl:177-260, GFXEXP 1) ----
+// One-bounce estimate of the direct light: the primary hit's own emission plus the
+// emission met along one uniform hemisphere direction (stratified on a 16 x 16 grid by the
+// frame counter), weighted by 2 pi N.L and the BRDF, into the frame buffer as (rgb,
+// distance); no hit: (0, 0, 0, 1e20). Sky sampling is off (no sky texture). cos and sin
+// are the correctly rounded FP64 results rounded to FP32, the oracle's choice for the
+// implementation-defined OpenCL builtins.
+__device__ __forceinline__ float3 uniform_sample_hemisphere(float r1, float r2, float3 N) {   // tools.cl:31-51
+    float3 Nt;
+    if (fabsf(N.x) > fabsf(N.y)) {
+        const float l = sqrtf(N.x * N.x + N.z * N.z);
+        Nt = f3(N.z / l, 0.0f / l, -N.x / l);
+    } else {
+        const float l = sqrtf(N.y * N.y + N.z * N.z);
+        Nt = f3(0.0f / l, -N.z / l, N.y / l);
+    }
+    const float3 Nb = f3(N.y * Nt.z - N.z * Nt.y, N.z * Nt.x - N.x * Nt.z, N.x * Nt.y - N.y * Nt.x);
+    const float sinTheta = sqrtf(1.0f - r1 * r1);
+    const float phi = 6.28318530717958647692528f * r2;
+    const float x = sinTheta * (float)cos((double)phi);
+    const float z = sinTheta * (float)sin((double)phi);
+    return f3((x * Nb.x + r1 * N.x) + z * Nt.x, (x * Nb.y + r1 * N.y) + z * Nt.y, (x * Nb.z + r1 * N.z) + z * Nt.z);
+}
+
+__device__ __forceinline__ float4 path_trace_px(const World& w, const Frame& k, int x, int y) {
+    uint32_t seed = wang_hash((uint32_t)x * 171u + (uint32_t)y * 1773u + k.R0);
+    const float3 D = camera_ray(k, x, y);
+    float dist = 0.0f;
+    uint32_t side = 0;
+    const uint32_t voxel = trace<0>(w, k.E.x, k.E.y, k.E.z, D.x, D.y, D.z, 999999, 0u, 0u, &dist, &side);
+    if (voxel == 0u) return make_float4(0.0f, 0.0f, 0.0f, 1e20f);
+    const float INVPI = 0.31830988618379067153777f;
+    const float3 rgb = to_rgb(voxel);
+    const float es = (float)((voxel & 0xff0000u) >> 16);
+    const float3 contribution = mul(mul(rgb, es), INVPI);
+    const float3 brdf = f3(INVPI * rgb.x, INVPI * rgb.y, INVPI * rgb.z);
+    const float3 I = f3(k.E.x + D.x * dist, k.E.y + D.y * dist, k.E.z + D.z * dist);
+    const int sx = (int)(k.frame & 15u), sy = (int)(k.frame >> 4);
+    const float r0 = (float)sx * 0.0625f + rnd(seed) * 0.0625f;
+    const float r1 = (float)sy * 0.0625f + rnd(seed) * 0.0625f;
+    const float s = side_sign(side, D);
+    const float3 N = side_normal(side, s);
+    const float3 R = uniform_sample_hemisphere(r0, r1, N);
+    const float NdotL = fmaxf(0.0f, (N.x * R.x + N.y * R.y) + N.z * R.z);
+    float dist2 = 0.0f;
+    uint32_t side2 = 0;
+    const uint32_t voxel2 = trace<0>(w, I.x + 0.1f * N.x, I.y + 0.1f * N.y, I.z + 0.1f * N.z, R.x, R.y, R.z, 128, 0u, 0u,
+                                     &dist2, &side2);
+    const float3 sampleL = mul(mul(to_rgb(voxel2), (float)((voxel2 & 0xff0000u) >> 16)), INVPI);
+    const float TWOPI = 6.28318530717958647692528f;
+    return make_float4(((sampleL.x * TWOPI) * NdotL) * brdf.x + contribution.x,
+                       ((sampleL.y * TWOPI) * NdotL) * brdf.y + contribution.y,
+                       ((sampleL.z * TWOPI) * NdotL) * brdf.z + contribution.z, dist);
+}
+
+__global__ void __launch_bounds__(kMaxTileThreads) path_trace_kernel(const __grid_constant__ BatchDev bd) {
+    uint32_t tile, round = 0;
+    while (next_tile(bd, bd.counters + kCtrAlbedo, &tile, round)) {
+        int x, y;
+        const ViewDev* V = tile_pixel<0>(bd, tile, &x, &y);
+        const Frame& k = V->k;
+        if (x < k.W && y < k.H) V->b.frame[(size_t)y * k.W + x] = path_trace_px(V->w, k, x, y);
+    }
+}
+
 // Hit list of the frame over every view (blockIdx.y = view); pixels without a hit get
 // the empty reservoir (ris.cl:34,123).
 template <int VARIANT>
@@ -893,6 +958,12 @@ void launch_commit_bricks(const uint32_t* list, const uint32_t* voxels, uint32_t
 
 void launch_build_uber_boxes(const uint32_t* grid, const uint32_t* bbox0, uint32_t* ubox0, cudaStream_t s) {
     dev::build_uber_boxes_kernel<<<(32 * 32 * 32 + 255) / 256, 256, 0, s>>>(grid, bbox0, ubox0);
+}
+
+void launch_path_trace(const BatchDev& bd, cudaStream_t s) {
+    BatchDev b = bd;
+    b.timer = nullptr;
+    launch_tiles(dev::path_trace_kernel, b, kCtrAlbedo, s, K_ALBEDO);
 }
 
 void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {

@@ -126,6 +126,7 @@ void apply_tuning(BatchDev& bd, const Tuning& tu);
 // Stage launchers over a batch. variant: 0 single view / area lights, 1 single view /
 // point lights, 2 view table (light model per view). A learned proposal needs variant 0/1.
 void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s);
+void launch_path_trace(const BatchDev& bd, cudaStream_t s);
 void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s);
 void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s);
 void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s);

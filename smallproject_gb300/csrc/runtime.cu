@@ -217,6 +217,7 @@ vxr::dev::Frame dev_frame(const vxr_frame_consts& c) {
     k.p0 = make_float3(c.p0[0], c.p0[1], c.p0[2]);
     k.dx = make_float3(c.p1[0] - c.p0[0], c.p1[1] - c.p0[1], c.p1[2] - c.p0[2]);
     k.dy = make_float3(c.p2[0] - c.p0[0], c.p2[1] - c.p0[1], c.p2[2] - c.p0[2]);
+    k.frame = c.frame;
     k.oorx = c.oneOverRes[0];
     k.oory = c.oneOverRes[1];
     k.Nl = make_float4(c.Nleft[0], c.Nleft[1], c.Nleft[2], c.Nleft[3]);
@@ -546,6 +547,12 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     const vxr::dev::Frame k = dev_frame(v->k);
     const bool point = v->desc.light_model == VXR_LIGHTS_POINT;
     const vxr::Tuning sh = shape(v);
+    if (stage == VXR_STAGE_PATH_TRACE) {   // ground-truth mode: no stage timing
+        vxr::BatchDev bd = vxr::single_batch(w, k, v->buf, v->cur, point, sh);
+        vxr::launch_path_trace(bd, v->stream);
+        CUV(cudaGetLastError(), "kernel launch");
+        return VXR_OK;
+    }
     const int ri = (int)(v->frameSerial % vxr_view::kRing) * 6 + stage;
     CUV(cudaEventRecord(v->evs[stage], v->stream), "cudaEventRecord");
     CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libvxr.so")
 VXR_OK = 0
 VXR_E_INVALID, VXR_E_CUDA, VXR_E_NOMEM, VXR_E_STATE, VXR_E_DEVICE, VXR_E_NODEVICE, VXR_E_IO = -1, -2, -3, -4, -5, -6, -7
 LIGHTS_AREA, LIGHTS_POINT = 0, 1
-STAGE_ALBEDO, STAGE_CANDIDATES, STAGE_SPATIAL, STAGE_SHADE, STAGE_ACCUMULATE = 1, 2, 3, 4, 5
+STAGE_ALBEDO, STAGE_CANDIDATES, STAGE_SPATIAL, STAGE_SHADE, STAGE_ACCUMULATE, STAGE_PATH_TRACE = 1, 2, 3, 4, 5, 6
 EMIT_ABOVE_SURFACE, EMIT_AIR, EMIT_BLOBS, EMIT_LAYER = 0, 1, 2, 3
 
 

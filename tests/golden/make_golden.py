@@ -6,10 +6,11 @@ is stored and asserted), a small frame size, a few frames with a moving camera, 
 for every frame the frame constants plus every stage output of the reference:
 G-buffer after renderAlbedo, reservoirs after perPixelInitialSampling and after
 perPixelSpatialResampling (as left by renderRIS), the shaded frame and the
-accumulator.
+accumulator. The path-tracer fixture holds, per frame, the frame of the reference's
+ground-truth mode (renderPathTracer, GFXEXP) and the accumulator after it.
 
-Usage: python tests/golden/make_golden.py   (needs the reference checkout or a
-previously generated oracle/_ref/vxref_gen.inc)
+Usage: python tests/golden/make_golden.py [fixture names]   (all by default; needs the
+reference checkout or a previously generated oracle/_ref/vxref_gen.inc)
 """
 import ctypes as C
 import os
@@ -26,6 +27,9 @@ CASES = [
     ("config0_area_48x32", 48, 32, False, 3),
     ("config0_point_48x32", 48, 32, True, 3),
 ]
+# the path tracer's scene: config 0 with 4,096 emitters (seed 6, blob mode), so that
+# hemisphere samples hit emitters in a useful share of pixels
+PT_CASES = [("config0_pt_48x32", 48, 32, 8, dict(emitters=4096, emitter_mode=1, seed=6))]
 KNOBS = dict(numberOfCandidates=32, numberOfMaxTemporalImportance=20, spatialRadius=30, spatialTaps=5,
              spatial=1, temporal=1, accumulate=1)
 
@@ -44,7 +48,10 @@ def main():
     ck = w.checksum()
     g, b, l = w.arrays()
     arrays = ob.WorldArrays(g, b, l)
+    only = set(sys.argv[1:])
     for name, W, H, point, F in CASES:
+        if only and name not in only:
+            continue
         ref = ob.Renderer("ref", arrays, W, H, point)
         cam = ob.CameraPath(W, H)
         out = {"checksum": np.array(ck, np.uint64), "W": W, "H": H, "point": int(point), "frames": F}
@@ -69,6 +76,31 @@ def main():
                     out[f"frame{f}"] = ref.image(0)
                 else:
                     out[f"accum{f}"] = ref.image(1)
+            cam.end()
+        ref.close()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name)
+    for name, W, H, F, scene in PT_CASES:
+        if only and name not in only:
+            continue
+        wp = vx.World()
+        wp.generate(vx.scene_preset(0, **scene))
+        gp, bp, lp = wp.arrays()
+        ref = ob.Renderer("ref", ob.WorldArrays(gp, bp, lp), W, H, False)
+        cam = ob.CameraPath(W, H)
+        out = {"checksum": np.array(wp.checksum(), np.uint64), "W": W, "H": H, "frames": F,
+               "scene": np.array([scene["emitters"], scene["emitter_mode"], scene["seed"]], np.uint32)}
+        for f in range(F):
+            pos, tgt = camera(f)
+            cam.lookat(pos, tgt)
+            k = cam.begin(numberOfLights=len(lp), **KNOBS)
+            out[f"consts{f}"] = np.frombuffer(bytes(k), np.uint8)
+            out[f"camera{f}"] = np.array(pos + tgt, np.float32)
+            ref.frame_start()
+            ref.stage(k, 6)
+            out[f"frame{f}"] = ref.image(0)
+            ref.stage(k, 5)
+            out[f"accum{f}"] = ref.image(1)
             cam.end()
         ref.close()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)

@@ -10,7 +10,8 @@ import pytest
 from conftest import ROOT, assert_records_equal
 from oracle import binding as ob
 
-FIXTURES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
+# the render-path fixtures (the path tracer's have their own test, test_gpu_pt.py)
+FIXTURES = sorted(f for f in glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")) if "_pt_" not in f)
 
 
 def _load(path):
