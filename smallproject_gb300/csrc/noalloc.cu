@@ -162,6 +162,7 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     f.Nt = make_float4(k->Ntop[0], k->Ntop[1], k->Ntop[2], k->Ntop[3]);
     f.Nb = make_float4(k->Nbottom[0], k->Nbottom[1], k->Nbottom[2], k->Nbottom[3]);
     f.R0 = k->R0;
+    f.frame = k->frame;
     f.framecount = k->framecount;
     f.restirtemporalframe = 0;
     f.spatial = k->spatial;
