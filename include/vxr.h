@@ -130,6 +130,12 @@ int vxr_world_clear(vxr_world* w);
  * voxel is appended to the light list (World::AddLight, world.cpp:228-246) and an
  * overwritten emitter is removed (World::RemoveLight, world.cpp:506-561). */
 int vxr_world_set(vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t voxel);
+/* World::StampSpriteTo (world.cpp:1545-1563): vxr_world_set(x + ox, y + oy, z + oz,
+ * voxels[i] | or_mask) for i = 0 .. n-1 in order, with pos[i] = x | y << 10 | z << 20
+ * (a sprite's draw list; the reference stamps with or_mask 0xF000). The bulk path for
+ * loading scene files. */
+int vxr_world_stamp(vxr_world* w, const uint32_t* pos, const uint32_t* voxels, uint32_t n, uint32_t ox, uint32_t oy,
+                    uint32_t oz, uint32_t or_mask);
 /* World::Get (world.h:293-306) / Read (template.cpp:67). Out-of-map reads wrap like
  * the reference's masking. */
 int vxr_world_get(const vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t* voxel);

@@ -62,6 +62,20 @@ int vxr_world_set(vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t vox
     return VXR_OK;
 }
 
+int vxr_world_stamp(vxr_world* w, const uint32_t* pos, const uint32_t* voxels, uint32_t n, uint32_t ox, uint32_t oy,
+                    uint32_t oz, uint32_t or_mask) {
+    VXR_CHECK_ARG(w && ((pos && voxels) || n == 0), "vxr_world_stamp: null argument");
+    try {
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t p = pos[i];
+            w->w.set((p & 1023u) + ox, ((p >> 10) & 1023u) + oy, ((p >> 20) & 1023u) + oz, voxels[i] | or_mask);
+        }
+    } catch (const std::bad_alloc&) {
+        return set_error(VXR_E_NOMEM, "vxr_world_stamp: brick pool allocation failed");
+    }
+    return VXR_OK;
+}
+
 int vxr_world_get(const vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t* voxel) {
     VXR_CHECK_ARG(w && voxel, "vxr_world_get: null argument");
     *voxel = w->w.get(x, y, z);

@@ -111,6 +111,7 @@ _SIGS = {
     "vxr_camera_path": [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.c_uint32, _F3, _F3],
     "vxr_world_checksum": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
     "vxr_world_move_light": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
+    "vxr_world_stamp": [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "vxr_world_upload": [_P], "vxr_world_commit": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int)],
     "vxr_world_pending": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_int)], "vxr_world_device_bytes": [_P, C.POINTER(C.c_uint64)],
     "vxr_view_default_desc": [C.POINTER(ViewDesc)],
@@ -215,6 +216,10 @@ class World:
         check(self._lib.vxr_world_get(self.h, x, y, z, C.byref(out)))
         return out.value
 
+    def clear(self):
+        """World::Clear (vxr_world_clear): empty map, no bricks, no lights."""
+        check(self._lib.vxr_world_clear(self.h))
+
     def box(self, x1, y1, z1, x2, y2, z2, v):
         check(self._lib.vxr_world_box(self.h, x1, y1, z1, x2, y2, z2, v))
 
@@ -275,6 +280,16 @@ class World:
     def upload(self):
         """Send the whole world to the device (vxr_world_upload)."""
         check(self._lib.vxr_world_upload(self.h))
+
+    def stamp(self, pos, voxels, origin=(0, 0, 0), or_mask=0):
+        """Set voxels[i] | or_mask at origin + unpack(pos[i]) in order (vxr_world_stamp);
+        pos packs x | y << 10 | z << 20."""
+        p = np.ascontiguousarray(pos, dtype=np.uint32)
+        v = np.ascontiguousarray(voxels, dtype=np.uint32)
+        if p.shape != v.shape:
+            raise ValueError("pos and voxels differ in length")
+        check(self._lib.vxr_world_stamp(self.h, p.ctypes.data, v.ctypes.data, len(p), *(int(o) for o in origin),
+                                        or_mask))
 
     def move_light(self, index, x, y, z):
         """Move voxel light `index` of the light list to (x, y, z) (vxr_world_move_light)."""
