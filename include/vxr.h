@@ -130,6 +130,11 @@ int vxr_world_clear(vxr_world* w);
  * voxel is appended to the light list (World::AddLight, world.cpp:228-246) and an
  * overwritten emitter is removed (World::RemoveLight, world.cpp:506-561). */
 int vxr_world_set(vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t voxel);
+/* World::AddBrick (world.h:308-352): grid cell (bx, by, bz) becomes solid with value
+ * voxel; a brick stored there is recycled. With light tracking on, the cell's old
+ * emitters leave the light list and an emitter voxel joins it as one brick light
+ * (size 8, position = the cell's lowest corner). Out-of-grid cells are ignored. */
+int vxr_world_add_brick(vxr_world* w, uint32_t bx, uint32_t by, uint32_t bz, uint32_t voxel);
 /* World::StampSpriteTo (world.cpp:1545-1563): vxr_world_set(x + ox, y + oy, z + oz,
  * voxels[i] | or_mask) for i = 0 .. n-1 in order, with pos[i] = x | y << 10 | z << 20
  * (a sprite's draw list; the reference stamps with or_mask 0xF000). The bulk path for

@@ -62,6 +62,12 @@ int vxr_world_set(vxr_world* w, uint32_t x, uint32_t y, uint32_t z, uint32_t vox
     return VXR_OK;
 }
 
+int vxr_world_add_brick(vxr_world* w, uint32_t bx, uint32_t by, uint32_t bz, uint32_t voxel) {
+    VXR_CHECK_ARG(w, "vxr_world_add_brick: null world");
+    w->w.add_brick(bx, by, bz, voxel);
+    return VXR_OK;
+}
+
 int vxr_world_stamp(vxr_world* w, const uint32_t* pos, const uint32_t* voxels, uint32_t n, uint32_t ox, uint32_t oy,
                     uint32_t oz, uint32_t or_mask) {
     VXR_CHECK_ARG(w && ((pos && voxels) || n == 0), "vxr_world_stamp: null argument");

@@ -140,6 +140,32 @@ void World::set(uint32_t x, uint32_t y, uint32_t z, uint32_t v) {
     touch();
 }
 
+// World::AddBrick (world.h:308-352): the cell becomes solid with value v. A brick that
+// was there is freed and its emitter voxels leave the light list; a solid emitter cell
+// that was there leaves it as a brick light; an emitter v joins it as a brick light
+// (size 8, at the cell's lowest corner).
+void World::add_brick(uint32_t bx, uint32_t by, uint32_t bz, uint32_t v) {
+    if (bx >= kGrid || by >= kGrid || bz >= kGrid) return;
+    const uint32_t ci = cell_index(bx, by, bz);
+    const uint32_t c = grid[ci];
+    if (c & 1u) {
+        const uint32_t b = c >> 1;
+        free_brick(b);
+        if (trackLights)
+            for (uint32_t ly = 0; ly < 8; ly++)
+                for (uint32_t lz = 0; lz < 8; lz++)
+                    for (uint32_t lx = 0; lx < 8; lx++)
+                        if (is_emitter(bricks[(size_t)b * kBrick + lx + ly * 8 + lz * 64]))
+                            remove_light(bx * 8 + lx, by * 8 + ly, bz * 8 + lz);
+    } else if (trackLights && is_emitter(c >> 1)) {
+        remove_light(bx * 8, by * 8, bz * 8);
+    }
+    if (trackLights && is_emitter(v)) add_light(bx * 8, by * 8, bz * 8, 8, v);
+    grid[ci] = v << 1;
+    mark_row(by);
+    touch();
+}
+
 // World::OptimizeBricks (world.cpp:655-683)
 uint32_t World::optimize() {
     uint32_t replaced = 0;

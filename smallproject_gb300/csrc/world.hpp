@@ -70,6 +70,7 @@ struct World {
     void clear();
     uint32_t get(uint32_t x, uint32_t y, uint32_t z) const;
     void set(uint32_t x, uint32_t y, uint32_t z, uint32_t v);
+    void add_brick(uint32_t bx, uint32_t by, uint32_t bz, uint32_t v);
     uint32_t optimize();
     uint32_t scan_lights();
     uint32_t new_brick();

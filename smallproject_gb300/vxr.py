@@ -96,6 +96,7 @@ _SIGS = {
     "vxr_last_error": [], "vxr_version": [],
     "vxr_world_create": [C.POINTER(_P)], "vxr_world_destroy": [_P], "vxr_world_clear": [_P],
     "vxr_world_set": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
+    "vxr_world_add_brick": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "vxr_world_get": [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)],
     "vxr_world_box": [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32],
     "vxr_world_track_lights": [_P, C.c_int], "vxr_world_optimize": [_P, C.POINTER(C.c_uint32)],
@@ -210,6 +211,10 @@ class World:
 
     def set(self, x, y, z, v):
         check(self._lib.vxr_world_set(self.h, x, y, z, v))
+
+    def add_brick(self, bx, by, bz, v):
+        """World::AddBrick: grid cell (bx, by, bz) becomes solid with voxel value v."""
+        check(self._lib.vxr_world_add_brick(self.h, bx, by, bz, v))
 
     def get(self, x, y, z):
         out = C.c_uint32()

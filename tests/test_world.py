@@ -160,3 +160,29 @@ def test_move_light_restores_and_remembers_voxels(lib):
     with pytest.raises(lib.VxrError):
         w.move_light(len(lights), 1, 1, 1)
     w.close()
+
+
+def test_add_brick_solid_cell_and_brick_lights(lib):
+    """vxr_world_add_brick (World::AddBrick, world.h:308-352): the cell turns solid and its
+    brick is recycled; emitter voxels that were in it leave the light list, an emitter
+    value joins it as one size-8 light at the cell's corner, replacing that cell's old
+    brick light; a non-emitter leaves none; out-of-grid cells are ignored."""
+    w = lib.World()
+    em = 3 << 16 | 0xF0F0
+    w.set(17, 9, 25, em)
+    w.set(18, 9, 25, 0x0123)
+    w.set(3, 3, 3, em)
+    before = w.brick_count()
+    assert len(w.arrays()[2]) == 2
+    w.add_brick(2, 1, 3, 5 << 16 | 0xFFFF)               # the cell of (17, 9, 25)
+    assert w.brick_count() == before - 1
+    assert all(w.get(16 + i, 8 + i, 24 + i) == 5 << 16 | 0xFFFF for i in range(8))
+    pos = 2 * 8 + 3 * 8 * 1024 + 1 * 8 * 1024 * 1024
+    lights = w.arrays()[2]
+    assert sorted(zip(lights["position"].tolist(), lights["size"].tolist())) == [(3 + 3 * 1024 + 3 * 1024 * 1024, 1), (pos, 8)]
+    w.add_brick(2, 1, 3, 0xF777)                          # a solid emitter cell replaced: its light goes
+    assert w.arrays()[2]["position"].tolist() == [3 + 3 * 1024 + 3 * 1024 * 1024]
+    assert w.get(20, 12, 30) == 0xF777
+    w.add_brick(128, 0, 0, em)                            # outside the grid
+    assert len(w.arrays()[2]) == 1
+    w.close()
