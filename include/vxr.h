@@ -44,6 +44,10 @@ extern "C" {
 #define VXR_GRIDDIM    128u   /* GRIDWIDTH = MAPWIDTH / BRICKDIM */
 #define VXR_UBERDIM    32u    /* UBERWIDTH = GRIDWIDTH / 4 */
 #define VXR_BRICKSIZE  512u   /* BRICKSIZE = 8^3 voxels */
+/* Words of the blue-noise buffer (world.cpp:180-189): the 8-bit entries of E. Heitz's
+ * sampler tables, one per uint32: sequence at [0, 65536), scrambling at
+ * [65536, 196608), ranking at [196608, 327680). */
+#define VXR_BLUE_NOISE_WORDS 327680u
 
 /* Voxel payload: 32-bit 0x00MMARGB (common.h:32-37, tools.cl:294-322):
  * B bits 0-3, G 4-7, R 8-11, alpha 12-15 (0xF = opaque), emitter strength M 16-23. */
@@ -297,6 +301,26 @@ int vxr_view_set_camera_matrix(vxr_view* v, const float m[16]);
 /* Change the toggles/knobs of an existing view (RenderParams console knobs,
  * mygame.cpp:112-121); resolution and light model are fixed at creation. */
 int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d);
+
+/* Sky dome (RenderParams.skyDomeSampling, common.h:105-112; ris.cl:199-210, 254-290):
+ * rgba = NULL turns it off (the default). Otherwise rgba holds w * h texels of 4
+ * floats, row by row, as World::LoadSky leaves them (scale * (r, g, b, 1), world.cpp:
+ * 861-870); sky_light the 6 integrated sky colours of the axis normals, 4 floats each,
+ * in skyLight order (-x, +x, -z, +z, -y, +y of the sky's z-up frame, i.e. selected
+ * by the world normals -x, +x, -y, +y, -z, +z; vxr_sky_lights computes them);
+ * light_scale skyLightScale; blue_noise VXR_BLUE_NOISE_WORDS words. With the sky on,
+ * background pixels take the sky colour, translucent voxels (alpha < 15) blend it in,
+ * and shading adds one cosine-weighted ray (10-step budget, opaque voxels only) lit by
+ * the sky light of the normal it ends on. Copies everything to the device (blocking).
+ * w, h in [1, 65536]. */
+int vxr_view_set_sky(vxr_view* v, const float* rgba, uint32_t w, uint32_t h, const float sky_light[24],
+                     float light_scale, const uint32_t* blue_noise);
+/* World::UpdateSkylights (world.cpp:897-922): for each of the 6 normals of skyLight,
+ * the mean of 4,096 cosine-weighted samples of the sky (16 x 16 strata, 16 jittered
+ * samples each), bilinear like World::SampleSky (world.cpp:878-895). The jitter comes
+ * from an xorshift32 stream seeded with `seed` (the reference draws it from its global
+ * host RNG, so its values differ by that Monte Carlo noise). Host only. */
+int vxr_sky_lights(const float* rgba, uint32_t w, uint32_t h, uint32_t seed, float sky_light[24]);
 
 /* Host part of World::Render (world.cpp:2144-2223): frame constants from the camera,
  * R0, G-buffer swap. Writes the constants to *k when k is not NULL. */

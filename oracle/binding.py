@@ -89,6 +89,44 @@ def load_port():
     return lib
 
 
+def load_stb():
+    """The reference's stb_image (oracle/stb_ref.c), or None when not available here."""
+    from . import build as B  # noqa: PLC0415
+    try:
+        path = B.build_stb()
+    except RuntimeError:
+        path = None
+    if not path:
+        return None
+    lib = C.CDLL(path)
+    lib.stbref_loadf.restype = C.POINTER(C.c_float)
+    lib.stbref_loadf.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.stbref_free.argtypes = [C.c_void_p]
+    lib.stbref_write_hdr.restype = C.c_int
+    lib.stbref_write_hdr.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _P]
+    return lib
+
+
+def stb_loadf(path):
+    """float32[h, w, comp] through the reference's stbi_loadf, or None if it fails."""
+    lib = load_stb()
+    w, h, c = C.c_int(), C.c_int(), C.c_int()
+    p = lib.stbref_loadf(str(path).encode(), C.byref(w), C.byref(h), C.byref(c))
+    if not p:
+        return None
+    try:
+        return np.ctypeslib.as_array(p, (h.value, w.value, c.value)).copy()
+    finally:
+        lib.stbref_free(p)
+
+
+def stb_write_hdr(path, rgb):
+    """Write float[h, w, 3] with the reference's stbi_write_hdr."""
+    a = np.ascontiguousarray(rgb, np.float32)
+    if not load_stb().stbref_write_hdr(str(path).encode(), a.shape[1], a.shape[0], a.shape[2], a.ctypes.data):
+        raise RuntimeError("stbi_write_hdr failed")
+
+
 def load_ref():
     """The reference oracle, or None when it is not available on this machine."""
     global _ref
@@ -114,6 +152,7 @@ def load_ref():
             f"vxref_read_reservoirs_{v}": (None, [_P, C.c_int, _P]),
             f"vxref_write_reservoirs_{v}": (None, [_P, C.c_int, _P]),
             f"vxref_read_image_{v}": (None, [_P, C.c_int, _P]),
+            f"vxref_set_sky_{v}": (None, [_P, _P, C.c_uint32, C.c_uint32, _P, C.c_float, _P]),
             f"vxref_trace_{v}": (C.c_uint32, [_P, C.c_int, _F, _F, C.c_int, C.c_uint32, C.c_uint32, _F, _U32P]),
         }
         for n, (res, args) in sig.items():
@@ -210,6 +249,19 @@ class Renderer:
         out = np.zeros((self.n, 4), np.float32)
         (self.lib.orc_read_image if self.kind == "port" else self._f("read_image"))(self.h, which, out.ctypes.data)
         return out
+
+    def set_sky(self, tex, light, scale, blue_noise):
+        """Sky dome on (tex float32[h, w, 4], light float32[6, 4], blue_noise
+        uint32[VXR_BLUE_NOISE_WORDS]) or off (tex None); reference oracle only."""
+        if self.kind != "ref":
+            raise NotImplementedError("the sky dome is checked against the reference oracle")
+        if tex is None:
+            self._f("set_sky")(self.h, None, 0, 0, None, 0.0, None)
+            return
+        self._sky = (np.ascontiguousarray(tex, np.float32), np.ascontiguousarray(light, np.float32),
+                     np.ascontiguousarray(blue_noise, np.uint32))
+        t, l, b = self._sky
+        self._f("set_sky")(self.h, t.ctypes.data, t.shape[1], t.shape[0], l.ctypes.data, float(scale), b.ctypes.data)
 
     def trace(self, mode, O, D, steps=999999, through=0, mask=0):
         o = (C.c_float * 3)(*O)

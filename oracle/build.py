@@ -46,12 +46,25 @@ def build_ref(force=False):
     return mod.build(force=force, quiet=True)
 
 
+def build_stb():
+    """Returns the stb_image checker library path (oracle/stb_ref.c), or None."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ref_build", os.path.join(HERE, "ref_build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build_stb(quiet=True)
+
+
 def build_all(force=False):
     port = build_port(force)
     try:
         ref = build_ref(force)
     except RuntimeError:
         ref = None
+    try:
+        build_stb()
+    except RuntimeError:
+        pass
     return port, ref
 
 

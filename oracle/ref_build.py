@@ -15,8 +15,8 @@ recipe compiles the reference's OWN kernel source as C++17 for the host CPU:
    - double literals -> float literals (the reference builds with
      -cl-single-precision-constant, template/template.cpp:1419);
    - SCRWIDTH/SCRHEIGHT become runtime variables, VOXELSAREPOINTLIGHTS overridable;
-   - sky / editor helpers that the parity configuration never calls
-     (skyDomeSampling = editorEnabled = 0) are replaced by aborting stubs;
+   - editor helpers that the parity configuration never calls (editorEnabled = 0)
+     are replaced by aborting stubs;
 3. write the result to oracle/_ref/vxref_gen.inc (git-ignored: reference source is
    never committed) and compile it with oracle/ref_shim.inc + oracle/ref_driver.cpp
    into oracle/_ref/libvxref.so, once per light model (area / point).
@@ -41,16 +41,16 @@ TOOLS_FUNCS = [
     "ToFloatRGB", "FromFloatRGBA", "VoxelNormal", "getRandomIndex", "indexToCoordinates",
     "GridCoordinatesFromHit", "Uint3CubeEquals", "ReprojectWorldPoint", "IsInBounds",
     "RandomPointOnVoxel", "GenerateLightCandidate", "PointOnVoxelLight", "UniformSampleHemisphere",
+    # sky-dome sampling (skyDomeSampling = 1): SampleSky and its spherical angles, the
+    # blue-noise sampler and the cosine-weighted hemisphere sample
+    "SphericalTheta", "SphericalPhi", "SampleSky", "blueNoiseSampler", "DiffuseReflectionCosWeighted",
 ]
 # render_di_gfxexp + renderPathTracer: the reference's ground-truth mode (GFXEXP = 1)
 KERNELS_FUNCS = ["accumulatorFinalizer", "updateUberGrid", "render_di_gfxexp", "renderPathTracer"]
 
 STUBS = r"""
-// ---- stubs: referenced by render_di_ris only under skyDomeSampling / editorEnabled,
-// ---- both 0 in every configuration this oracle runs; reaching one is a test bug.
-inline float3 SampleSky(const float3, float4*, uint, uint) { std::abort(); }
-inline float blueNoiseSampler(const uint*, int, int, int, int) { std::abort(); }
-inline float3 DiffuseReflectionCosWeighted(const float, const float, const float3) { std::abort(); }
+// ---- stubs: referenced by render_di_ris only under editorEnabled, 0 in every
+// ---- configuration this oracle runs; reaching one is a test bug.
 inline bool HitSelectedBox(const float3, const float3, const float3, const float3, const float, float*) { std::abort(); }
 inline bool HitWorldGrid(const float3, const float3) { std::abort(); }
 """
@@ -218,11 +218,40 @@ def build(ref=DEFAULT_REF, force=False, quiet=False):
     return lib
 
 
+def build_stb(ref=DEFAULT_REF, quiet=False):
+    """Compile oracle/stb_ref.c against the reference's vendored stb_image headers
+    (lib/stb_image.h, lib/stb_image_write.h, included where they lie) into
+    oracle/_ref/libstbref.so. Returns the path, or None without the reference checkout
+    (and no earlier build)."""
+    os.makedirs(OUT, exist_ok=True)
+    lib = os.path.join(OUT, "libstbref.so")
+    inc = os.path.join(ref, "lib")
+    if not os.path.isfile(os.path.join(inc, "stb_image.h")):
+        return lib if os.path.exists(lib) else None
+    src = os.path.join(HERE, "stb_ref.c")
+    h = hashlib.sha256()
+    for s in (src, os.path.join(inc, "stb_image.h"), os.path.join(inc, "stb_image_write.h")):
+        h.update(open(s, "rb").read())
+    stamp = os.path.join(OUT, "libstbref.stamp")
+    if os.path.exists(lib) and os.path.exists(stamp) and open(stamp).read() == h.hexdigest():
+        return lib
+    cmd = ["gcc", "-O1", "-shared", "-fPIC", "-w", "-I" + inc, src, "-o", lib, "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("stb_image checker build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    with open(stamp, "w") as f:
+        f.write(h.hexdigest())
+    if not quiet:
+        print("built", lib)
+    return lib
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=DEFAULT_REF)
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args()
     r = build(a.reference, a.force)
+    build_stb(a.reference)
     if r is None:
         sys.exit("reference checkout not found and no generated source present")

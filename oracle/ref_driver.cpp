@@ -39,6 +39,12 @@ struct Ctx {
     int candOut = 0, candIn = 1, spatOut = 1, spatIn = 0, shadeOut = 0, shadeIn = 1;
     RenderParams params;
     DebugInfo dbg;
+    // sky dome (World::LoadSky / UpdateSkylights, world.cpp:803-923); off when empty
+    std::vector<float4> sky;
+    std::vector<uint> blueNoise;
+    uint skyW = 0, skyH = 0;
+    float skyLight[24] = {};
+    float skyLightScale = 0.0f;
 };
 
 void fill_params(Ctx* c, const vxr_frame_consts* k) {
@@ -60,7 +66,12 @@ void fill_params(Ctx* c, const vxr_frame_consts* k) {
     p.accumulate = k->accumulate;
     p.spatial = k->spatial;
     p.temporal = k->temporal;
-    p.skyDomeSampling = 0;
+    p.skyDomeSampling = c->sky.empty() ? 0 : 1;
+    p.skyWidth = c->skyW;
+    p.skyHeight = c->skyH;
+    for (int i = 0; i < 6; i++)
+        p.skyLight[i] = float4(c->skyLight[4 * i], c->skyLight[4 * i + 1], c->skyLight[4 * i + 2], c->skyLight[4 * i + 3]);
+    p.skyLightScale = c->skyLightScale;
     p.editorEnabled = 0;
     p.drawGrid = 0;
     p.numberOfLights = k->numberOfLights;
@@ -175,6 +186,8 @@ void VXREF_FN(vxref_stage)(void* ctx, const vxr_frame_consts* k, int stage) {
     const uint* brick0 = c->bricks;
     DebugInfo* dbg = &c->dbg;
     Light* lights = lights_ptr(c);
+    float4* sky = c->sky.empty() ? nullptr : c->sky.data();
+    const uint* bn = c->blueNoise.empty() ? nullptr : c->blueNoise.data();
     switch (stage) {
     case 1:
         for_pixels(c, [&] { renderAlbedo(dbg, prevAlbedo, albedo, params, grid, uber, brick0); });
@@ -200,7 +213,7 @@ void VXREF_FN(vxref_stage)(void* ctx, const vxr_frame_consts* k, int stage) {
         Reservoir* in = c->res[c->shadeIn].data();
         float4* frame = c->frame.data();
         for_pixels(c, [&] {
-            renderRIS(dbg, prevAlbedo, albedo, frame, params, lights, out, in, grid, nullptr, nullptr, uber, brick0);
+            renderRIS(dbg, prevAlbedo, albedo, frame, params, lights, out, in, grid, sky, bn, uber, brick0);
         });
         break;
     }
@@ -221,6 +234,25 @@ void VXREF_FN(vxref_stage)(void* ctx, const vxr_frame_consts* k, int stage) {
     default:
         std::abort();
     }
+}
+
+// Sky dome: texels (w * h float4), skyLight[6] (24 floats), skyLightScale and the
+// blue-noise buffer (VXR_BLUE_NOISE_WORDS words, world.cpp:180-189); rgba = null: off.
+void VXREF_FN(vxref_set_sky)(void* ctx, const float* rgba, uint32_t w, uint32_t h, const float* light, float scale,
+                             const uint32_t* bn) {
+    Ctx* c = (Ctx*)ctx;
+    c->sky.clear();
+    c->blueNoise.clear();
+    c->skyW = c->skyH = 0;
+    if (!rgba) return;
+    c->sky.resize((size_t)w * h);
+    for (size_t i = 0; i < (size_t)w * h; i++)
+        c->sky[i] = float4(rgba[4 * i], rgba[4 * i + 1], rgba[4 * i + 2], rgba[4 * i + 3]);
+    c->blueNoise.assign(bn, bn + VXR_BLUE_NOISE_WORDS);
+    c->skyW = w;
+    c->skyH = h;
+    std::memcpy(c->skyLight, light, sizeof(c->skyLight));
+    c->skyLightScale = scale;
 }
 
 // Rows [y0, y1) only (a bounded sample of a frame, for CPU timing).

@@ -19,7 +19,7 @@ LIB = os.path.join(LIBDIR, "libvxr.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CU_SOURCES = ["kernels.cu", "runtime.cu", "batch.cu", "noalloc.cu", "proposal.cu", "proposal_api.cu"]
-CPP_SOURCES = ["world.cpp", "scene.cpp", "camera.cpp", "capi_world.cpp", "cluster.cpp"]
+CPP_SOURCES = ["world.cpp", "scene.cpp", "camera.cpp", "capi_world.cpp", "cluster.cpp", "sky.cpp"]
 HEADERS = ["device.cuh", "kernels.hpp", "world.hpp", "camera.hpp", "internal.hpp", "proposal.cuh", "proposal.hpp", "view.hpp"]
 
 # the learned proposal is checked with tolerances, not bit for bit: FMA contraction on

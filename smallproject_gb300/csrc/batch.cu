@@ -166,6 +166,18 @@ int vxr_batch_render(vxr_batch* b) {
         const cudaError_t e = cudaEventSynchronize(b->slotDone[slot]);
         if (e != cudaSuccess) return cuda_error(e, "vxr_batch_render: wait for staging slot");
     }
+    // the shading kernel has a sky-dome variant: recorded graphs follow the views' skies
+    int sky = 0;
+    for (vxr_view* v : b->views) sky |= v->skyDev != nullptr ? 1 : 0;
+    if (sky != b->bd.sky) {
+        const cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) return cuda_error(e, "vxr_batch_render: wait before re-recording");
+        for (int i = 0; i < 2; i++) {
+            if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+            b->graph[i] = nullptr;
+        }
+        b->bd.sky = sky;
+    }
     // begin every view's frame (camera, frame constants, G-buffer swap) and fill the table
     uint32_t tileBase = 0;
     for (size_t i = 0; i < n; i++) {
@@ -178,6 +190,7 @@ int vxr_batch_render(vxr_batch* b) {
         d = vxr::ViewDev();
         d.w = vxr::dev_world(v);
         d.k = vxr::dev_frame(v->k);
+        d.k.sky = v->skyDev;
         d.b = v->buf;
         d.cur = v->cur;
         d.point = v->desc.light_model == VXR_LIGHTS_POINT ? 1 : 0;

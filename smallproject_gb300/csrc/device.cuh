@@ -35,6 +35,16 @@ struct World {
     uint32_t nlights;
 };
 
+// Sky dome in device memory: World::LoadSky / UpdateSkylights (world.cpp:803-923) and
+// the RenderParams sky fields (common.h:105-112).
+struct Sky {
+    const float4* tex;            // w * h texels, row by row
+    const uint32_t* blueNoise;    // blue-noise tables, 327,680 words (world.cpp:180-189)
+    uint32_t w, h;
+    float lightScale;             // skyLightScale
+    float4 light[6];              // skyLight: integrated sky per axis normal
+};
+
 // Frame constants (kernel parameter, by value; mirrors RenderParams, common.h:100-118)
 struct Frame {
     float3 E, p0, dx, dy;        // dx = p1 - p0, dy = p2 - p0 (the kernel's own subtractions)
@@ -46,6 +56,7 @@ struct Frame {
     uint32_t nlights, ncand;     // ncand = min(numberOfLights, numberOfCandidates) (ris.cl:48)
     uint32_t maxTemporal, radius, taps;
     int32_t W, H;
+    const Sky* sky;               // null: skyDomeSampling 0
 };
 
 // ---- small float3 helpers (each op one IEEE rounding) ---------------------------------
@@ -55,6 +66,9 @@ __device__ __forceinline__ float3 sub(float3 a, float3 b) { return f3(a.x - b.x,
 __device__ __forceinline__ float3 mul(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
 __device__ __forceinline__ float3 mulv(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
 __device__ __forceinline__ float comp(float3 v, uint32_t i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 // normalize = v * (1 / sqrt(dot(v, v))): the reference's own definition (precomp.h:283,656)
 __device__ __forceinline__ float3 normalize3(float3 v) {

@@ -764,6 +764,61 @@ __global__ void __launch_bounds__(128) shade_request_kernel(const __grid_constan
     }
 }
 
+// ---- sky dome (tools.cl:6-15, 21-28, 54-70, 130-144) --------------------------------
+// acos, atan2, sin and cos are the correctly rounded binary32 values (through double).
+
+// SampleSky with SphericalTheta / SphericalPhi: bilinear lookup of direction (tx, ty, tz)
+// in the z-up sky texture
+__device__ __forceinline__ float3 sample_sky(const Sky& s, float tx, float ty, float tz) {
+    const float PI = 3.14159265358979323846264f;
+    const float INV2PI = 0.15915494309189533576888f, INVPI = 0.31830988618379067153777f;
+    const float theta = (float)acos((double)fminf(fmaxf(tz, -1.0f), 1.0f));
+    float phi = (float)atan2((double)ty, (double)tx);
+    phi = phi < 0.0f ? phi + 2.0f * PI : phi;
+    const float u = ((float)s.w * phi) * INV2PI - 0.5f;
+    const float v = ((float)s.h * theta) * INVPI - 0.5f;
+    const float fu = u - floorf(u), fv = v - floorf(v);
+    const uint32_t iu = (uint32_t)f2i(u), iv = (uint32_t)f2i(v), n = s.w * s.h;
+    const float4 a = __ldg(s.tex + (iu + iv * s.w) % n), b = __ldg(s.tex + (iu + 1u + iv * s.w) % n);
+    const float4 c = __ldg(s.tex + (iu + (iv + 1u) * s.w) % n), d = __ldg(s.tex + (iu + 1u + (iv + 1u) * s.w) % n);
+    const float gu = 1.0f - fu, gv = 1.0f - fv;
+    return f3((((a.x * gu) * gv + (b.x * fu) * gv) + (c.x * gu) * fv) + (d.x * fu) * fv,
+              (((a.y * gu) * gv + (b.y * fu) * gv) + (c.y * gu) * fv) + (d.y * fu) * fv,
+              (((a.z * gu) * gv + (b.z * fu) * gv) + (c.z * gu) * fv) + (d.z * fu) * fv);
+}
+
+// blueNoiseSampler: E. Heitz's ranked, scrambled sequence, sample `idx`, dimension `dim`
+__device__ __forceinline__ float blue_noise(const uint32_t* bn, int x, int y, int idx, int dim) {
+    x &= 127, y &= 127, idx &= 255, dim &= 255;
+    const int ranked = (idx ^ (int)__ldg(bn + dim + (x + y * 128) * 8 + 65536 * 3)) & 255;
+    int value = (int)__ldg(bn + dim + ranked * 256);
+    value ^= (int)__ldg(bn + (dim & 7) + (x + y * 128) * 8 + 65536);
+    float r = (0.5f + (float)value) * (1.0f / 256.0f);
+    if (r >= 1.0f) r -= 1.0f;
+    return r;
+}
+
+// DiffuseReflectionCosWeighted: cosine-weighted direction around N
+__device__ __forceinline__ float3 cos_weighted(float r0, float r1, float3 N) {
+    const float3 T = normalize3(cross3(N, fabsf(N.y) > 0.99f ? f3(1.0f, 0.0f, 0.0f) : f3(0.0f, 1.0f, 0.0f)));
+    const float3 B = cross3(T, N);
+    const float term1 = 6.28318530717958647692528f * r0, term2 = sqrtf(1.0f - r1);
+    const float c = (float)cos((double)term1), s = (float)sin((double)term1);
+    const float ct = c * term2, st = s * term2, sr = sqrtf(r1);
+    return f3((ct * T.x + st * B.x) + sr * N.x, (ct * T.y + st * B.y) + sr * N.y, (ct * T.z + st * B.z) + sr * N.z);
+}
+
+// skyLight entry of an axis normal (ris.cl:279-285: the last matching test wins)
+__device__ __forceinline__ float4 sky_light(const Sky& s, float3 M) {
+    float4 l = s.light[0];
+    if (M.x > 0.9f) l = s.light[1];
+    if (M.y < -0.9f) l = s.light[2];
+    if (M.y > 0.9f) l = s.light[3];
+    if (M.z < -0.9f) l = s.light[4];
+    if (M.z > 0.9f) l = s.light[5];
+    return l;
+}
+
 // accumulatorFinalizer (kernels.cl:304-326): running mean over `framecount` frames
 __device__ __forceinline__ void accumulate_px(const ViewDev* V, size_t i, float4 px) {
     const Frame& k = V->k;
@@ -776,17 +831,33 @@ __device__ __forceinline__ void accumulate_px(const ViewDev* V, size_t i, float4
 }
 
 // 4c: colour per pixel once visibility has zeroed the occluded reservoirs; optionally
-// fused with the accumulator.
-template <bool POINT>
+// fused with the accumulator. SKY: the frame may carry a sky dome (the sky-less
+// instantiation keeps the common case's registers).
+template <bool POINT, bool SKY>
 __device__ __forceinline__ void shade_finish_px(const ViewDev* V, int x, int y, int fuse) {
     const Frame& k = V->k;
     const size_t i = (size_t)y * k.W + x;
     const uint2 g = V->b.vd[V->cur][i];
     const uint32_t voxel = g.x & 0x00FFFFFFu;
     const float dist = __uint_as_float(g.y);
+    const float INVPI = 0.31830988618379067153777f;
     float3 color = f3(0.0f, 0.0f, 0.0f);
+    const Sky* sky = SKY ? k.sky : nullptr;
+    if (sky && voxel == 0u) {
+        // background (ris.cl:197-202); the sky-light term adds its incoming light times a
+        // zero BRDF, which leaves non-negative sums as they are
+        const float3 D = camera_ray(k, x, y);
+        color = sample_sky(*sky, D.x, D.z, D.y);
+        const float4 l = sky_light(*sky, side_normal(g.x >> 24, side_sign(g.x >> 24, D)));
+        color = add(color, f3((0.0f + sky->lightScale * l.x) * 0.0f, (0.0f + sky->lightScale * l.y) * 0.0f,
+                              (0.0f + sky->lightScale * l.z) * 0.0f));
+    }
     if (voxel != 0u) {
-        const float INVPI = 0.31830988618379067153777f;
+        float3 skyC = f3(0.0f, 0.0f, 0.0f);   // sky seen through a translucent voxel (ris.cl:206-211)
+        if (sky && ((voxel & 0xf000u) >> 12) != 15u) {
+            const float3 D = camera_ray(k, x, y);
+            skyC = sample_sky(*sky, D.x, D.z, D.y);
+        }
         if (emitter(voxel)) {
             const float3 c = to_rgb(voxel);
             const float m = strength(voxel);
@@ -809,23 +880,48 @@ __device__ __forceinline__ void shade_finish_px(const ViewDev* V, int x, int y, 
             color = add(color, f3((inc.x * W) * qb.w, (inc.y * W) * qb.w, (inc.z * W) * qb.w));
         }
         const float a = alphaf(voxel);
-        color = f3(color.x + ((a * color.x) + ((1.0f - a) * 0.0f)), color.y + ((a * color.y) + ((1.0f - a) * 0.0f)),
-                   color.z + ((a * color.z) + ((1.0f - a) * 0.0f)));
+        color = f3(color.x + ((a * color.x) + ((1.0f - a) * skyC.x)), color.y + ((a * color.y) + ((1.0f - a) * skyC.y)),
+                   color.z + ((a * color.z) + ((1.0f - a) * skyC.z)));
+        if (sky) {
+            // sky light (ris.cl:258-290): one cosine-weighted ray, 10 steps, opaque voxels
+            // only; lit by the sky light of the normal it ends on
+            const uint32_t side = g.x >> 24;
+            const float3 D = camera_ray(k, x, y);
+            const float3 N = side_normal(side, side_sign(side, D));
+            const float r0 = blue_noise(sky->blueNoise, x, y, (int)k.frame, 0);
+            const float r1 = blue_noise(sky->blueNoise, x, y, (int)k.frame, 1);
+            const float3 R = cos_weighted(r0, r1, N);
+            const float3 sp = f3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+            float dist2 = 0.0f;
+            uint32_t side2 = 0;
+            const uint32_t voxel2 = trace<1>(V->w, sp.x + 0.1f * N.x, sp.y + 0.1f * N.y, sp.z + 0.1f * N.z, R.x, R.y, R.z,
+                                             10 /* GRIDWIDTH / 12 */, 0u, 0u, &dist2, &side2);
+            float3 toAdd = f3(sky->lightScale, sky->lightScale, sky->lightScale), M = N;
+            if (voxel2 != 0u) {
+                const float3 c2 = to_rgb(voxel2);
+                toAdd = f3(toAdd.x * (INVPI * c2.x), toAdd.y * (INVPI * c2.y), toAdd.z * (INVPI * c2.z));
+                M = side_normal(side2, side_sign(side2, R));
+            }
+            const float4 l = sky_light(*sky, M);
+            const float3 inc = f3(0.0f + toAdd.x * l.x, 0.0f + toAdd.y * l.y, 0.0f + toAdd.z * l.z);
+            const float3 brdf = mul(to_rgb(voxel), INVPI);
+            color = add(color, mulv(inc, brdf));
+        }
     }
     const float4 px = make_float4(color.x, color.y, color.z, dist);
     V->b.frame[i] = px;
     if (fuse) accumulate_px(V, i, px);
 }
 
-template <int VARIANT>
+template <int VARIANT, bool SKY>
 __global__ void __launch_bounds__(kMaxTileThreads) shade_finish_kernel(const __grid_constant__ BatchDev bd) {
     uint32_t tile, round = 0;
     while (next_tile(bd, bd.counters + kCtrFinish, &tile, round)) {
         int x, y;
         const ViewDev* V = tile_pixel<VARIANT>(bd, tile, &x, &y);
         if (x < V->k.W && y < V->k.H) {
-            if (point_of<VARIANT>(V)) shade_finish_px<true>(V, x, y, bd.fuse);
-            else shade_finish_px<false>(V, x, y, bd.fuse);
+            if (point_of<VARIANT>(V)) shade_finish_px<true, SKY>(V, x, y, bd.fuse);
+            else shade_finish_px<false, SKY>(V, x, y, bd.fuse);
         }
     }
 }
@@ -926,6 +1022,7 @@ BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffer
     bd.one.tileBase = 0;
     bd.one.tilesX = (uint32_t)((k.W + tu.bx - 1) / tu.bx);
     bd.nviews = 1;
+    bd.sky = k.sky != nullptr ? 1 : 0;
     bd.totalPixels = (uint32_t)k.W * (uint32_t)k.H;
     bd.totalTiles = bd.one.tilesX * (uint32_t)((k.H + tu.by - 1) / tu.by);
     apply_tuning(bd, tu);
@@ -1059,7 +1156,8 @@ static void shade_v(const BatchDev& bd, cudaStream_t s) {
         dev::shade_request_kernel<VARIANT < 2 ? 0 : 2><<<list_blocks(bd.totalPixels, 128, bd.listPerSm), 128, 0, s>>>(bd);
     }
     launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ2, 1, s);
-    launch_tiles(dev::shade_finish_kernel<VARIANT>, bd, kCtrFinish, s, K_SHADE_FINISH);
+    if (bd.sky) launch_tiles(dev::shade_finish_kernel<VARIANT, true>, bd, kCtrFinish, s, K_SHADE_FINISH);
+    else launch_tiles(dev::shade_finish_kernel<VARIANT, false>, bd, kCtrFinish, s, K_SHADE_FINISH);
 }
 
 void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s) {

@@ -85,6 +85,7 @@ struct BatchDev {
     int occupancy = 0;                    // 1: register-capped shadow / RIS kernels (more warps per SM)
     int schedule = 0;                     // shadow tracer: 1 = one DDA level per round (the majority's)
     int fuse = 0;                         // shading also accumulates
+    int sky = 0;                          // some view has a sky dome (shading runs its variant)
     uint32_t* hits = nullptr;             // hit list over all views
     float4* qA = nullptr;                 // shadow-ray requests: (origin, bits(entry))
     float4* qB = nullptr;                 //                      (direction, bits(light))

@@ -175,6 +175,7 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     f.taps = k->spatialTaps;
     f.W = (int32_t)k->width;
     f.H = (int32_t)k->height;
+    f.sky = nullptr;
 
     vxr::ViewBuffers b;
     b.vd[0] = (uint2*)(s + kOffVd);

@@ -237,6 +237,7 @@ vxr::dev::Frame dev_frame(const vxr_frame_consts& c) {
     k.taps = c.spatialTaps;
     k.W = (int32_t)c.width;
     k.H = (int32_t)c.height;
+    k.sky = nullptr;
     return k;
 }
 
@@ -256,6 +257,7 @@ void free_view(vxr_view* v) {
     cudaFree(b.frame); cudaFree(b.accum); cudaFree(b.err);
     cudaFree(b.hits); cudaFree(b.qA); cudaFree(b.qB); cudaFree(b.counters);
     cudaFree(v->sum64); cudaFree(v->errOut);
+    cudaFree(v->skyDev); cudaFree(v->skyTex); cudaFree(v->skyBlueNoise);
     if (v->prop) vxr::destroy_proposal(v->prop);
     v->prop = nullptr;
     delete v->ktimer;
@@ -498,6 +500,42 @@ int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d) {
     return VXR_OK;
 }
 
+int vxr_view_set_sky(vxr_view* v, const float* rgba, uint32_t w, uint32_t h, const float sky_light[24],
+                     float light_scale, const uint32_t* blue_noise) {
+    if (int r = check_view(v, "vxr_view_set_sky")) return r;
+    if (!rgba) {
+        CUV(cudaStreamSynchronize(v->stream), "vxr_view_set_sky: wait");
+        cudaFree(v->skyDev); cudaFree(v->skyTex); cudaFree(v->skyBlueNoise);
+        v->skyDev = nullptr;
+        v->skyTex = nullptr;
+        v->skyBlueNoise = nullptr;
+        return VXR_OK;
+    }
+    VXR_CHECK_ARG(sky_light && blue_noise, "vxr_view_set_sky: null sky_light or blue_noise");
+    VXR_CHECK_ARG(w >= 1 && h >= 1 && w <= 65536 && h <= 65536, "vxr_view_set_sky: size out of [1, 65536]");
+    const size_t texels = (size_t)w * h;
+    // the frames in flight may read the old sky
+    CUV(cudaStreamSynchronize(v->stream), "vxr_view_set_sky: wait");
+    if (!v->skyDev) CUV(cudaMalloc(&v->skyDev, sizeof(vxr::dev::Sky)), "cudaMalloc(sky)");
+    if (!v->skyBlueNoise) CUV(cudaMalloc(&v->skyBlueNoise, VXR_BLUE_NOISE_WORDS * sizeof(uint32_t)), "cudaMalloc(blue noise)");
+    cudaFree(v->skyTex);
+    v->skyTex = nullptr;
+    CUV(cudaMalloc(&v->skyTex, texels * sizeof(float4)), "cudaMalloc(sky texture)");
+    CUV(cudaMemcpy(v->skyTex, rgba, texels * sizeof(float4), cudaMemcpyHostToDevice), "copy sky texture");
+    CUV(cudaMemcpy(v->skyBlueNoise, blue_noise, VXR_BLUE_NOISE_WORDS * sizeof(uint32_t), cudaMemcpyHostToDevice),
+        "copy blue noise");
+    vxr::dev::Sky s;
+    s.tex = v->skyTex;
+    s.blueNoise = v->skyBlueNoise;
+    s.w = w;
+    s.h = h;
+    s.lightScale = light_scale;
+    for (int i = 0; i < 6; i++)
+        s.light[i] = make_float4(sky_light[4 * i], sky_light[4 * i + 1], sky_light[4 * i + 2], sky_light[4 * i + 3]);
+    CUV(cudaMemcpy(v->skyDev, &s, sizeof(s), cudaMemcpyHostToDevice), "copy sky constants");
+    return VXR_OK;
+}
+
 int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* out) {
     if (int r = check_view(v, "vxr_view_begin_frame")) return r;
     if (int r = ensure_world(v)) return r;
@@ -544,7 +582,8 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     if (!v->frameOpen) return set_error(VXR_E_STATE, "vxr_view_stage: call vxr_view_begin_frame first");
     if (int r = ensure_world(v)) return r;
     const vxr::dev::World w = dev_world(v);
-    const vxr::dev::Frame k = dev_frame(v->k);
+    vxr::dev::Frame k = dev_frame(v->k);
+    k.sky = v->skyDev;
     const bool point = v->desc.light_model == VXR_LIGHTS_POINT;
     const vxr::Tuning sh = shape(v);
     if (stage == VXR_STAGE_PATH_TRACE) {   // ground-truth mode: no stage timing

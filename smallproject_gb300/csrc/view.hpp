@@ -75,6 +75,9 @@ struct vxr_view {
     double* errOut = nullptr;                         // [mse sum, mae sum]
     vxr::Proposal* prop = nullptr;                    // learned proposal (optional)
     vxr::ViewKernelTimer* ktimer = nullptr;           // per-kernel timing (vxr_view_kernel_timing)
+    vxr::dev::Sky* skyDev = nullptr;                  // sky dome (vxr_view_set_sky), null = off
+    float4* skyTex = nullptr;
+    uint32_t* skyBlueNoise = nullptr;
     bool ktimerOn = false;
     bool useProposal = false;
     bool frameOpen = false;

@@ -15,6 +15,9 @@ path:
 * ``.dat`` frames: uint32 width, uint32 height, then width * height float4 pixels, row
   by row (saveScreenBuffer, mygame.cpp:518-549; the reference appends a time stamp to
   the file name, these functions use the name given).
+* ``.hdr`` sky domes (Radiance RGBE, the format World::LoadSky reads through
+  stb_image's stbi_loadf, world.cpp:803-876): read_hdr / write_hdr, and sky_texture for
+  LoadSky's conversion to the texture of vxr_view_set_sky.
 
 Files written by the reference's World::CreateSprite (world.cpp:1347-1386) begin with
 size_x * size_y * size_z / 4 zero entries (its draw list is created with that many
@@ -289,6 +292,189 @@ def stamp_sprite(world, path, origin=(0, 0, 0), frame=0):
     size, pos, vox = load_sprite(path)[frame]
     world.stamp(pos, vox, origin, STAMP_MASK)
     return size
+
+
+def _rgbe_to_float(rgbe):
+    """RGBE bytes [..., 4] -> float32 [..., 3]: c * 2^(e - 136), 0 where e == 0."""
+    e = rgbe[..., 3].astype(np.int32)
+    f = np.where(e != 0, np.ldexp(np.float32(1.0), e - 136), 0.0).astype(np.float32)
+    return rgbe[..., :3].astype(np.float32) * f[..., None]
+
+
+def read_hdr(path):
+    """float32[h, w, 3] linear RGB of a Radiance .hdr file, as stb_image's stbi_loadf
+    decodes one: a "#?RADIANCE" or "#?RGBE" signature, header lines up to an empty one
+    among which FORMAT=32-bit_rle_rgbe must appear, the resolution line "-Y h +X w"
+    (the only orientation read), then h scanlines. Images narrower than 8 or 32768 and
+    wider are flat RGBE; otherwise each scanline starts 2, 2, width (16 bits) and holds
+    the four byte planes in runs (count > 128: count - 128 copies of one byte, else
+    count literal bytes). A scanline without that start switches to flat RGBE from the
+    first pixel of the image on, as stb_image does. Channel = byte * 2^(e - 136)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    off = 0
+
+    def line():
+        nonlocal off
+        end = data.find(b"\n", off)
+        if end < 0:
+            end = len(data)
+        s = data[off:end]
+        off = end + 1
+        return s.decode("latin-1")
+
+    if line() not in ("#?RADIANCE", "#?RGBE"):
+        raise ValueError(f"{path}: not a Radiance HDR file")
+    valid = False
+    while True:
+        if off >= len(data):
+            raise ValueError(f"{path}: header without end")
+        t = line()
+        if t == "":
+            break
+        valid |= t == "FORMAT=32-bit_rle_rgbe"
+    if not valid:
+        raise ValueError(f"{path}: unsupported format")
+    parts = line().split()
+    if len(parts) != 4 or parts[0] != "-Y" or parts[2] != "+X":
+        raise ValueError(f"{path}: unsupported orientation")
+    h, w = int(parts[1]), int(parts[3])
+    if h < 1 or w < 1:
+        raise ValueError(f"{path}: bad size")
+    buf = np.frombuffer(data, np.uint8, len(data) - off, off)
+    pos = 0
+
+    def flat(first_pixel, p0):
+        need = 4 * (w * h - first_pixel)
+        if p0 + need > len(buf):
+            raise ValueError(f"{path}: truncated pixel data")
+        return buf[p0:p0 + need].reshape(-1, 4)
+
+    out = np.zeros((h * w, 4), np.uint8)
+    if w < 8 or w >= 32768:
+        out[:] = flat(0, 0)
+        return _rgbe_to_float(out).reshape(h, w, 3)
+    for j in range(h):
+        if pos + 4 > len(buf):
+            raise ValueError(f"{path}: truncated scanline {j}")
+        c1, c2, ln = int(buf[pos]), int(buf[pos + 1]), int(buf[pos + 2])
+        if c1 != 2 or c2 != 2 or (ln & 0x80):
+            out[0] = buf[pos:pos + 4]
+            out[1:] = flat(1, pos + 4)
+            break
+        if (ln << 8 | int(buf[pos + 3])) != w:
+            raise ValueError(f"{path}: invalid decoded scanline length")
+        pos += 4
+        row = np.empty((4, w), np.uint8)
+        for k in range(4):
+            i = 0
+            while i < w:
+                if pos >= len(buf):
+                    raise ValueError(f"{path}: truncated run data")
+                count = int(buf[pos])
+                pos += 1
+                if count > 128:
+                    count -= 128
+                    if count > w - i or pos >= len(buf):
+                        raise ValueError(f"{path}: bad RLE data")
+                    row[k, i:i + count] = buf[pos]
+                    pos += 1
+                else:
+                    if count > w - i or pos + count > len(buf):
+                        raise ValueError(f"{path}: bad RLE data")
+                    row[k, i:i + count] = buf[pos:pos + count]
+                    pos += count
+                i += count
+        out[j * w:(j + 1) * w] = row.T
+    return _rgbe_to_float(out).reshape(h, w, 3)
+
+
+def float_to_rgbe(rgb):
+    """float [..., 3] -> RGBE bytes [..., 4] (shared exponent of the largest channel,
+    mantissas truncated: v = m * 2^e with m in [0.5, 1), byte = c * m * 256 / v)."""
+    rgb = np.asarray(rgb, np.float32)
+    v = rgb.max(axis=-1)
+    m, e = np.frexp(v)
+    ok = v >= np.float32(1e-32)
+    scale = np.where(ok, m * np.float32(256.0) / np.where(ok, v, 1), 0).astype(np.float32)
+    out = np.zeros(rgb.shape[:-1] + (4,), np.uint8)
+    out[..., :3] = np.where(ok[..., None], (rgb * scale[..., None]).astype(np.int64), 0).clip(0, 255)
+    out[..., 3] = np.where(ok, e + 128, 0)
+    return out
+
+
+def write_hdr(path, rgb, rle=True):
+    """Write float [h, w, 3] as a Radiance .hdr file (header, "-Y h +X w", run-length
+    scanlines when rle and 8 <= w < 32768, flat RGBE otherwise)."""
+    rgb = np.asarray(rgb, np.float32)
+    h, w, _ = rgb.shape
+    px = float_to_rgbe(rgb).reshape(h, w, 4)
+    parts = [f"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y {h} +X {w}\n".encode()]
+    if not rle or w < 8 or w >= 32768:
+        parts.append(px.tobytes())
+    else:
+        for j in range(h):
+            parts.append(bytes([2, 2, w >> 8, w & 255]))
+            for k in range(4):
+                plane = px[j, :, k].tobytes()
+                i = 0
+                while i < w:
+                    r = 1
+                    while i + r < w and r < 127 and plane[i + r] == plane[i]:
+                        r += 1
+                    if r >= 3:
+                        parts.append(bytes([128 + r, plane[i]]))
+                        i += r
+                        continue
+                    s = i                      # literal block up to the next run of 3
+                    while i < w and i - s < 128:
+                        if i + 2 < w and plane[i] == plane[i + 1] == plane[i + 2]:
+                            break
+                        i += 1
+                    parts.append(bytes([i - s]) + plane[s:i])
+    with open(path, "wb") as f:
+        f.write(b"".join(parts))
+
+
+def _sky_directions(h, w):
+    """Per texel of a w x h sky image, LoadSky's direction (cos p cos t, sin p, cos p sin t)
+    with t = (x - w/2) / w * 2 pi, p = -(y - h/2) / h * pi, in binary32 (cos and sin
+    correctly rounded)."""
+    f = np.float32
+    x = np.arange(w, dtype=f)[None, :]
+    y = np.arange(h, dtype=f)[:, None]
+    fw, fh, pi = f(w), f(h), f(3.14159265358979323846264)
+    t = ((x - f(0.5) * fw) / fw * f(2)) * pi
+    p = (-(y - f(0.5) * fh) / fh) * pi
+    ct, st = np.cos(t.astype(np.float64)).astype(f), np.sin(t.astype(np.float64)).astype(f)
+    cp, sp = np.cos(p.astype(np.float64)).astype(f), np.sin(p.astype(np.float64)).astype(f)
+    return cp * ct, np.broadcast_to(sp, (h, w)), cp * st
+
+
+def sky_texture(rgb, scale=1.5, artificial_sun=True, debug_lights=False):
+    """World::LoadSky's texture (world.cpp:803-870) from decoded HDR pixels
+    float[h, w, 3]: optionally the debug-light marks (red 10 where -D.x > 0.97, else green
+    10 where -D.z > 0.97), then the artificial sun (rgb 24, 24, 18 where D . L > 0.999,
+    L = normalize(2, 1.5, 3); on by default, as Game::artificialSun), then
+    scale * (r, g, b, 1) per texel: the float32[h, w, 4] texture of vxr_view_set_sky.
+    LoadSky's checkerboard option is not provided: on its first row the reference
+    divides by a zero D.y."""
+    px = np.array(rgb, np.float32)
+    h, w, _ = px.shape
+    f = np.float32
+    if debug_lights or artificial_sun:
+        dx, dy, dz = _sky_directions(h, w)
+        if debug_lights:
+            red = -dx > f(0.97)
+            green = ~red & (-dz > f(0.97))
+            px[red] = (10, 0, 0)
+            px[green] = (0, 10, 0)
+        if artificial_sun:
+            L = np.array([2.0, 1.5, 3.0], f)
+            L = L * (f(1.0) / np.sqrt(np.float32((L[0] * L[0] + L[1] * L[1]) + L[2] * L[2])))
+            sun = ((dx * L[0] + dy * L[1]) + dz * L[2]) > f(0.999)
+            px[sun] = (24, 24, 18)
+    return (np.concatenate([px, np.ones((h, w, 1), f)], axis=2) * f(scale)).astype(f)
 
 
 def write_frame_dat(path, rgba, width, height):

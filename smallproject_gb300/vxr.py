@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libvxr.so")
 VXR_OK = 0
 VXR_E_INVALID, VXR_E_CUDA, VXR_E_NOMEM, VXR_E_STATE, VXR_E_DEVICE, VXR_E_NODEVICE, VXR_E_IO = -1, -2, -3, -4, -5, -6, -7
 LIGHTS_AREA, LIGHTS_POINT = 0, 1
+BLUE_NOISE_WORDS = 327680   # VXR_BLUE_NOISE_WORDS
 STAGE_ALBEDO, STAGE_CANDIDATES, STAGE_SPATIAL, STAGE_SHADE, STAGE_ACCUMULATE, STAGE_PATH_TRACE = 1, 2, 3, 4, 5, 6
 EMIT_ABOVE_SURFACE, EMIT_AIR, EMIT_BLOBS, EMIT_LAYER = 0, 1, 2, 3
 
@@ -119,6 +120,8 @@ _SIGS = {
     "vxr_view_create": [_P, C.POINTER(ViewDesc), C.POINTER(_P)], "vxr_view_destroy": [_P],
     "vxr_view_lookat": [_P, _F3, _F3], "vxr_view_set_camera_matrix": [_P, _F3],
     "vxr_view_set_params": [_P, C.POINTER(ViewDesc)],
+    "vxr_view_set_sky": [_P, _P, C.c_uint32, C.c_uint32, _P, C.c_float, _P],
+    "vxr_sky_lights": [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P],
     "vxr_view_begin_frame": [_P, C.POINTER(FrameConsts)], "vxr_view_set_frame_consts": [_P, C.POINTER(FrameConsts)],
     "vxr_view_stage": [_P, C.c_int], "vxr_view_end_frame": [_P], "vxr_view_render": [_P], "vxr_view_wait": [_P],
     "vxr_view_stage_times": [_P, _F3],
@@ -344,6 +347,15 @@ def camera_path(desc, seed, f, n):
     return list(p), list(t)
 
 
+def sky_lights(tex, seed=0x12345678):
+    """vxr_sky_lights: the six sky-light colours (float32[6, 4]) of a float32[h, w, 4]
+    sky texture (World::UpdateSkylights)."""
+    t = np.ascontiguousarray(tex, np.float32)
+    out = np.zeros((6, 4), np.float32)
+    check(load().vxr_sky_lights(t.ctypes.data, t.shape[1], t.shape[0], seed, out.ctypes.data))
+    return out
+
+
 def device_info():
     """(name, SM count, (major, minor)) of the current CUDA device."""
     buf = C.create_string_buffer(256)
@@ -398,6 +410,23 @@ class View:
     def set_params(self, desc):
         check(self._lib.vxr_view_set_params(self.h, C.byref(desc)))
         self.desc = desc
+
+    def set_sky(self, tex, light=None, scale=0.0, blue_noise=None):
+        """Sky dome on (vxr_view_set_sky): tex float32[h, w, 4] texels, light float32[6, 4]
+        sky lights (vxr_sky_lights of tex when None), scale = skyLightScale, blue_noise
+        uint32[BLUE_NOISE_WORDS]; tex None turns it off."""
+        if tex is None:
+            check(self._lib.vxr_view_set_sky(self.h, None, 0, 0, None, 0.0, None))
+            return
+        t = np.ascontiguousarray(tex, np.float32)
+        if t.ndim != 3 or t.shape[2] != 4:
+            raise ValueError("sky texture must be float32[h, w, 4]")
+        l = sky_lights(t) if light is None else np.ascontiguousarray(light, np.float32).reshape(6, 4)
+        bn = np.ascontiguousarray(blue_noise, np.uint32)
+        if bn.shape != (BLUE_NOISE_WORDS,):
+            raise ValueError(f"blue noise must be uint32[{BLUE_NOISE_WORDS}]")
+        check(self._lib.vxr_view_set_sky(self.h, t.ctypes.data, t.shape[1], t.shape[0], l.ctypes.data, float(scale),
+                                         bn.ctypes.data))
 
     def begin_frame(self):
         k = FrameConsts()

@@ -10,8 +10,10 @@ import pytest
 from conftest import ROOT, assert_records_equal
 from oracle import binding as ob
 
-# the render-path fixtures (the path tracer's have their own test, test_gpu_pt.py)
-FIXTURES = sorted(f for f in glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")) if "_pt_" not in f)
+# the render-path fixtures (the path tracer and the sky dome have their own GPU tests,
+# test_gpu_pt.py and test_gpu_sky.py: the C oracle restates neither)
+FIXTURES = sorted(f for f in glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz"))
+                  if "_pt_" not in f and "_sky_" not in f)
 
 
 def _load(path):
