@@ -538,6 +538,7 @@ def main():
     e2e_ms = max_over_ranks(dist, e2e_ms)
     img_ok = bool(np.isfinite(pinned.array).all() and pinned.array.max() > 0)
     pinned.close()
+    modes = other_modes(make_view, cams, min(args.steps, 30), warmup) if rank == 0 else None
 
     if rank != 0:
         return
@@ -579,9 +580,69 @@ def main():
                     "d2h_bytes_per_step": npx * 16, "image_ok": img_ok},
             "gpu_launches": launches, "clocks": clk,
             "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report,
-            "world_commit": world_commit_times(world, args)}
+            "modes": modes, "world_commit": world_commit_times(world, args)}
     print(json.dumps(line))
     view.close()
+
+
+def other_modes(make_view, cams, steps, warmup):
+    """Frame time of the renderer's two other modes on the bench's scene, resolution and
+    camera path (plain method, 32 candidates): the sky dome on (a synthetic 1024 x 512
+    sky: a horizon gradient with hashed noise and LoadSky's artificial sun, its sky
+    lights from vxr_sky_lights, random blue-noise tables), and the path tracer (one
+    renderPathTracer sample per pixel and frame, then the accumulator)."""
+    import smallproject_gb300 as vx
+    from smallproject_gb300 import scene_io
+    rng = np.random.default_rng(23)
+    h, w = 512, 1024
+    rows = np.linspace(1.0, 0.05, h, dtype=np.float32)[:, None, None]
+    rgb = (rows * np.array([0.6, 0.8, 1.2], np.float32) * (0.9 + 0.2 * rng.random((h, w, 1), dtype=np.float32)))
+    tex = scene_io.sky_texture(rgb.astype(np.float32), scale=1.5)
+    bn = rng.integers(0, 256, vx.BLUE_NOISE_WORDS, dtype=np.uint32)
+    out = {}
+    view = make_view(False, 32)
+
+    def run(frame):
+        for f in range(warmup):
+            frame(f)
+        view.wait()
+        view.kernel_timing(True)
+        view.kernel_stats(reset=True)
+        view.timer_begin()
+        for f in range(steps):
+            frame(warmup + f)
+        ms = view.timer_end() / steps
+        view.wait()
+        view.kernel_timing(False)
+        ks = view.kernel_stats(reset=True)
+        return ms, {k: v[0] / v[1] for k, v in ks.items() if v[1]}
+
+    def render(f):
+        pos, tgt = cams(f)
+        view.lookat(pos, tgt)
+        view.render()
+
+    ms, ks = run(render)
+    out["plain_ms_per_frame"] = ms
+    out["plain_shade_finish_ms"] = ks.get("shade_finish")
+    view.set_sky(tex, vx.sky_lights(tex), 0.5, bn)
+    ms, ks = run(render)
+    out["sky"] = {"ms_per_frame": ms, "shade_finish_ms": ks.get("shade_finish"),
+                  "sky_texels": [w, h], "light_scale": 0.5}
+    view.set_sky(None)
+
+    def path_trace(f):
+        pos, tgt = cams(f)
+        view.lookat(pos, tgt)
+        view.begin_frame()
+        view.stage(vx.STAGE_PATH_TRACE)
+        view.stage(vx.STAGE_ACCUMULATE)
+        view.end_frame()
+
+    ms, _ = run(path_trace)
+    out["path_trace"] = {"ms_per_frame": ms, "samples_per_pixel": 1}
+    view.close()
+    return out
 
 
 def world_commit_times(world, args):
