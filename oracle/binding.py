@@ -127,6 +127,58 @@ def stb_write_hdr(path, rgb):
         raise RuntimeError("stbi_write_hdr failed")
 
 
+def load_ogt():
+    """The reference's ogt_vox reader (oracle/ogt_ref.cpp), or None when not available."""
+    from . import build as B  # noqa: PLC0415
+    try:
+        path = B.build_ogt()
+    except RuntimeError:
+        path = None
+    if not path:
+        return None
+    lib = C.CDLL(path)
+    lib.ogtref_read.restype = C.c_void_p
+    lib.ogtref_read.argtypes = [C.c_char_p, C.c_uint32]
+    lib.ogtref_free.argtypes = [C.c_void_p]
+    lib.ogtref_counts.argtypes = [C.c_void_p, _P]
+    lib.ogtref_instance.restype = C.c_uint32
+    lib.ogtref_instance.argtypes = [C.c_void_p, C.c_uint32, _P]
+    lib.ogtref_model.argtypes = [C.c_void_p, C.c_uint32, _P, _P]
+    lib.ogtref_palette.argtypes = [C.c_void_p, _P]
+    return lib
+
+
+def ogt_scene(path):
+    """(models, instances, palette) of a .vox file through the reference's
+    ogt_vox_read_scene: models uint8[sz, sy, sx], instances (model index, float32[4, 4]
+    transform m00 .. m33), palette uint8[256, 4]; None when the reader rejects the file."""
+    lib = load_ogt()
+    data = open(path, "rb").read()
+    s = lib.ogtref_read(data, len(data))
+    if not s:
+        return None
+    try:
+        counts = np.zeros(2, np.uint32)
+        lib.ogtref_counts(s, counts.ctypes.data)
+        models = []
+        for m in range(int(counts[1])):
+            size = np.zeros(3, np.uint32)
+            lib.ogtref_model(s, m, size.ctypes.data, None)
+            vox = np.zeros(int(size.prod()), np.uint8)
+            lib.ogtref_model(s, m, size.ctypes.data, vox.ctypes.data)
+            models.append(vox.reshape(int(size[2]), int(size[1]), int(size[0])))
+        instances = []
+        for i in range(int(counts[0])):
+            t = np.zeros(16, np.float32)
+            mid = lib.ogtref_instance(s, i, t.ctypes.data)
+            instances.append((int(mid), t.reshape(4, 4)))
+        pal = np.zeros(1024, np.uint8)
+        lib.ogtref_palette(s, pal.ctypes.data)
+        return models, instances, pal.reshape(256, 4)
+    finally:
+        lib.ogtref_free(s)
+
+
 def load_ref():
     """The reference oracle, or None when it is not available on this machine."""
     global _ref

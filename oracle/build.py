@@ -55,16 +55,26 @@ def build_stb():
     return mod.build_stb(quiet=True)
 
 
+def build_ogt():
+    """Returns the ogt_vox checker library path (oracle/ogt_ref.cpp), or None."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ref_build", os.path.join(HERE, "ref_build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build_ogt(quiet=True)
+
+
 def build_all(force=False):
     port = build_port(force)
     try:
         ref = build_ref(force)
     except RuntimeError:
         ref = None
-    try:
-        build_stb()
-    except RuntimeError:
-        pass
+    for b in (build_stb, build_ogt):
+        try:
+            b()
+        except RuntimeError:
+            pass
     return port, ref
 
 

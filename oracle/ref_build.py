@@ -246,6 +246,33 @@ def build_stb(ref=DEFAULT_REF, quiet=False):
     return lib
 
 
+def build_ogt(ref=DEFAULT_REF, quiet=False):
+    """Compile oracle/ogt_ref.cpp against the reference's vendored lib/ogt_vox.h (included
+    where it lies) into oracle/_ref/libogtref.so. Returns the path, or None without the
+    reference checkout (and no earlier build)."""
+    os.makedirs(OUT, exist_ok=True)
+    lib = os.path.join(OUT, "libogtref.so")
+    inc = os.path.join(ref, "lib")
+    if not os.path.isfile(os.path.join(inc, "ogt_vox.h")):
+        return lib if os.path.exists(lib) else None
+    src = os.path.join(HERE, "ogt_ref.cpp")
+    h = hashlib.sha256()
+    for s in (src, os.path.join(inc, "ogt_vox.h")):
+        h.update(open(s, "rb").read())
+    stamp = os.path.join(OUT, "libogtref.stamp")
+    if os.path.exists(lib) and os.path.exists(stamp) and open(stamp).read() == h.hexdigest():
+        return lib
+    cmd = ["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-w", "-DNDEBUG", "-I" + inc, src, "-o", lib]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("ogt_vox checker build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    with open(stamp, "w") as f:
+        f.write(h.hexdigest())
+    if not quiet:
+        print("built", lib)
+    return lib
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=DEFAULT_REF)
@@ -253,5 +280,6 @@ if __name__ == "__main__":
     a = ap.parse_args()
     r = build(a.reference, a.force)
     build_stb(a.reference)
+    build_ogt(a.reference)
     if r is None:
         sys.exit("reference checkout not found and no generated source present")

@@ -10,8 +10,9 @@ path:
   world.cpp:1545-1563), entries in file order.
 * ``.vox`` sprites (MagicaVoxel): read as SpriteManager::LoadSprite reads them without
   its large-model flag (world.cpp:1140-1296), into the same frame format (read_vox).
-  The large-model branch (the third-party opengametools ogt_vox reader, with scene-graph
-  transforms) has no caller in the reference that enables it and is not provided.
+  With the large-model flag the reference parses the file with the third-party
+  opengametools reader instead and places every instance of the scene graph
+  (vox_scene.py, load_sprite(path, large_model=True)).
 * ``.dat`` frames: uint32 width, uint32 height, then width * height float4 pixels, row
   by row (saveScreenBuffer, mygame.cpp:518-549; the reference appends a time stamp to
   the file name, these functions use the name given).
@@ -281,15 +282,22 @@ def read_vox(path):
     return frames
 
 
-def load_sprite(path):
-    """SpriteManager::LoadSprite: the frames of a .vx (read_vx) or .vox (read_vox) file."""
-    return read_vx(path)[1] if ".vx" in str(path) else read_vox(path)    # strstr(path, ".vx")
+def load_sprite(path, large_model=False):
+    """SpriteManager::LoadSprite: the frames of a .vx file (read_vx), else of a .vox file:
+    with large_model the one frame of its scene (vox_scene.large_model_frame, the
+    opengametools path), without it read_vox."""
+    if ".vx" in str(path):                                   # strstr(path, ".vx")
+        return read_vx(path)[1]
+    if large_model:
+        from .vox_scene import large_model_frame
+        return [large_model_frame(path)]
+    return read_vox(path)
 
 
-def stamp_sprite(world, path, origin=(0, 0, 0), frame=0):
+def stamp_sprite(world, path, origin=(0, 0, 0), frame=0, large_model=False):
     """LoadSprite + StampSpriteTo: stamp frame `frame` of a sprite file into the world at
     `origin` with | 0xF000, entries in draw-list order. Returns the frame's size."""
-    size, pos, vox = load_sprite(path)[frame]
+    size, pos, vox = load_sprite(path, large_model)[frame]
     world.stamp(pos, vox, origin, STAMP_MASK)
     return size
 
