@@ -33,7 +33,7 @@ CASES = [
 # the path tracer's scene: config 0 with 4,096 emitters (seed 6, blob mode), so that
 # hemisphere samples hit emitters in a useful share of pixels
 PT_CASES = [("config0_pt_48x32", 48, 32, 8, dict(emitters=4096, emitter_mode=1, seed=6))]
-SKY_CASES = [("config0_sky_48x32", 48, 32, 3)]
+SKY_CASES = [("config0_sky_48x32", 48, 32, 3, False), ("config0_sky_point_48x32", 48, 32, 3, True)]
 KNOBS = dict(numberOfCandidates=32, numberOfMaxTemporalImportance=20, spatialRadius=30, spatialTaps=5,
              spatial=1, temporal=1, accumulate=1)
 
@@ -116,17 +116,17 @@ def main():
         ref.close()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print("wrote", name)
-    for name, W, H, F in SKY_CASES:
+    for name, W, H, F, point in SKY_CASES:
         if only and name not in only:
             continue
         ws = vx.World()
         ws.generate(vx.scene_preset(0))
         sky_inputs.add_panel(ws)
         gs, bs, ls = ws.arrays()
-        ref = ob.Renderer("ref", ob.WorldArrays(gs, bs, ls), W, H, False)
+        ref = ob.Renderer("ref", ob.WorldArrays(gs, bs, ls), W, H, point)
         ref.set_sky(sky_inputs.sky_texture(), sky_inputs.SKY_LIGHT, sky_inputs.LIGHT_SCALE, sky_inputs.blue_noise())
         cam = ob.CameraPath(W, H)
-        out = {"checksum": np.array(ws.checksum(), np.uint64), "W": W, "H": H, "frames": F}
+        out = {"checksum": np.array(ws.checksum(), np.uint64), "W": W, "H": H, "frames": F, "point": int(point)}
         for f in range(F):
             pos, tgt = sky_camera(f)
             cam.lookat(pos, tgt)

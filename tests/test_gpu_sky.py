@@ -1,7 +1,8 @@
 """Sky-dome sampling (vxr_view_set_sky; ris.cl:197-211, 254-290; tools.cl:6-28, 54-70,
 130-144) on the GPU against the reference's own shading kernel compiled for the CPU with
-skyDomeSampling = 1 (golden frames tests/golden/config0_sky_48x32.npz, made by
-tests/golden/make_golden.py from the synthetic sky of tests/golden/sky_inputs.py):
+skyDomeSampling = 1 (golden frames tests/golden/config0_sky_48x32.npz for area lights and
+config0_sky_point_48x32.npz for point lights, made by tests/golden/make_golden.py from the
+synthetic sky of tests/golden/sky_inputs.py):
 background pixels, sky seen through translucent voxels and the sky-light ray, bit for
 bit, with the accumulator; then the batched path with a sky view beside a sky-less one,
 against the same views rendered alone."""
@@ -18,7 +19,8 @@ import sky_inputs  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-FIXTURE = os.path.join(ROOT, "tests", "golden", "config0_sky_48x32.npz")
+FIXTURES = {"area": os.path.join(ROOT, "tests", "golden", "config0_sky_48x32.npz"),
+            "point": os.path.join(ROOT, "tests", "golden", "config0_sky_point_48x32.npz")}
 
 
 def _scene(lib):
@@ -32,12 +34,13 @@ def _set_sky(view):
     view.set_sky(sky_inputs.sky_texture(), sky_inputs.SKY_LIGHT, sky_inputs.LIGHT_SCALE, sky_inputs.blue_noise())
 
 
-def test_sky_dome_reproduces_reference(lib, cuda_device):
-    fx = dict(np.load(FIXTURE))
+@pytest.mark.parametrize("model", ["area", "point"])
+def test_sky_dome_reproduces_reference(lib, cuda_device, model):
+    fx = dict(np.load(FIXTURES[model]))
     w = _scene(lib)
     assert tuple(int(v) for v in fx["checksum"]) == w.checksum(), "scene drifted from the fixture"
     W, H, F = int(fx["W"]), int(fx["H"]), int(fx["frames"])
-    view = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1))
+    view = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_POINT if model == "point" else lib.LIGHTS_AREA, accumulate=1))
     _set_sky(view)
     seen = {"background": 0, "translucent": 0}
     try:
