@@ -312,7 +312,7 @@ int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d);
  * background pixels take the sky colour, translucent voxels (alpha < 15) blend it in,
  * and shading adds one cosine-weighted ray (10-step budget, opaque voxels only) lit by
  * the sky light of the normal it ends on. Copies everything to the device (blocking).
- * w, h in [1, 65536]. */
+ * w, h in [1, 65536], w * h < 2^31. */
 int vxr_view_set_sky(vxr_view* v, const float* rgba, uint32_t w, uint32_t h, const float sky_light[24],
                      float light_scale, const uint32_t* blue_noise);
 /* World::UpdateSkylights (world.cpp:897-922): for each of the 6 normals of skyLight,

@@ -512,7 +512,8 @@ int vxr_view_set_sky(vxr_view* v, const float* rgba, uint32_t w, uint32_t h, con
         return VXR_OK;
     }
     VXR_CHECK_ARG(sky_light && blue_noise, "vxr_view_set_sky: null sky_light or blue_noise");
-    VXR_CHECK_ARG(w >= 1 && h >= 1 && w <= 65536 && h <= 65536, "vxr_view_set_sky: size out of [1, 65536]");
+    VXR_CHECK_ARG(w >= 1 && h >= 1 && w <= 65536 && h <= 65536 && (uint64_t)w * h < (1ull << 31),
+                  "vxr_view_set_sky: size out of [1, 65536] or more than 2^31 - 1 texels");
     const size_t texels = (size_t)w * h;
     // the frames in flight may read the old sky
     CUV(cudaStreamSynchronize(v->stream), "vxr_view_set_sky: wait");
