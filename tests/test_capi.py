@@ -99,3 +99,19 @@ def test_out_of_map_set_is_ignored(lib):
     assert w.get(0, 0, 0) == 0
     g, b, l = w.arrays()
     assert not g.any() and len(l) == 0
+
+
+def test_worldapi_shim_compiles_links_and_runs(lib, tmp_path):
+    """The C++ shim that replaces worldapi.h's World-backed bodies (tests/native/
+    worldapi_shim.cpp) builds against include/vxr.h alone, links libvxr.so and drives the
+    world through Plot / Box / Read / ClearWorld."""
+    import subprocess
+    exe = str(tmp_path / "shim")
+    libdir = os.path.dirname(lib.LIB_PATH)
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "native", "worldapi_shim.cpp"), "-L" + libdir, "-lvxr",
+                        "-Wl,-rpath," + libdir, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.split() == ["f888", "f123", "0", "0"]
