@@ -127,24 +127,26 @@ def _frame_transform(rot, trans, path):
     return t
 
 
-def _walk(nodes, node_id, transform, models, instances, depth, path):
-    """generate_instances_for_node without group output: flattened transforms."""
-    if depth > 4096:
-        raise ValueError(f"{path}: scene graph too deep or cyclic")
-    node = nodes.get(node_id)
-    if node is None:              # referenced but never defined: no instance
-        return
-    kind = node[0]
-    if kind == "trn":
-        _, t, child = node
-        _walk(nodes, child, t @ transform, models, instances, depth + 1, path)
-    elif kind == "grp":
-        for c in node[1]:
-            _walk(nodes, c, transform, models, instances, depth + 1, path)
-    else:
-        mid = node[1]
-        if mid < len(models) and models[mid] is not None:
-            instances.append([mid, transform])
+def _walk(nodes, models, path):
+    """generate_instances_for_node from node 0 without group output (flattened
+    transforms), depth first in child order, with an explicit stack."""
+    instances, stack = [], [(0, np.eye(4), 0)]
+    while stack:
+        node_id, transform, depth = stack.pop()
+        if depth > 4096:
+            raise ValueError(f"{path}: scene graph too deep or cyclic")
+        node = nodes.get(node_id)
+        if node is None:              # referenced but never defined: no instance
+            continue
+        if node[0] == "trn":
+            _, t, child = node
+            stack.append((child, t @ transform, depth + 1))
+        elif node[0] == "grp":
+            for c in reversed(node[1]):
+                stack.append((c, transform, depth + 1))
+        elif node[1] < len(models) and models[node[1]] is not None:
+            instances.append([node[1], transform])
+    return instances
 
 
 def read_vox_scene(path):
@@ -225,7 +227,7 @@ def read_vox_scene(path):
             r.off = min(len(data), r.off + csize)
     instances = []
     if nodes:
-        _walk(nodes, 0, np.eye(4), models, instances, 0, path)
+        instances = _walk(nodes, models, path)
     elif len(models) == 1:
         if models[0] is None:
             raise ValueError(f"{path}: the only model is empty")

@@ -243,3 +243,12 @@ def test_sprite_dispatch_large_model(lib, tmp_path):
     io.stamp_sprite(w, path, (10, 10, 10), large_model=True)
     assert w.get(10, 10, 10) == 0xF000 | int(vox[0]) and w.get(12, 10, 10) == 0xF000 | int(vox[1])
     w.close()
+
+
+def test_cyclic_scene_graph_is_rejected(tmp_path):
+    """A transform node whose child leads back to it: ValueError (ogt_vox recurses
+    without end)."""
+    g = np.ones((1, 1, 1), np.uint8)
+    path = _write(tmp_path / "c.vox", [_model(g), _trn(0, 1), _grp(1, [2, 0]), _shp(2, 0)])
+    with pytest.raises(ValueError):
+        vs.read_vox_scene(path)
