@@ -513,8 +513,8 @@ int vxr_batch_set_tuning(vxr_batch* b, const vxr_tuning* t);
  *             rejected with VXR_E_INVALID
  *   out_rgba  device float4[width*height]: shaded rgb and primary-hit distance
  *   stream    cudaStream_t to run on (NULL = the legacy default stream)
- * The frame is rendered without temporal reuse or accumulation (no history is kept
- * between calls). The call is synchronous. On its first call on a device it looks up
+ * The frame is rendered without temporal reuse, accumulation or sky dome (no history is
+ * kept between calls; skyDomeSampling 0). The call is synchronous. On its first call on a device it looks up
  * the device address of its scratch array (cudaGetSymbolAddress), so make that first
  * call before any stream capture on that device. All calls share the one scratch
  * array per device and it keeps the last call's contents: calls that overlap on the
