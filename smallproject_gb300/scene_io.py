@@ -485,6 +485,19 @@ def sky_texture(rgb, scale=1.5, artificial_sun=True, debug_lights=False):
     return (np.concatenate([px, np.ones((h, w, 1), f)], axis=2) * f(scale)).astype(f)
 
 
+def load_sky(view, path, blue_noise, scale=1.5, light_scale=2.0, artificial_sun=True, seed=0x12345678):
+    """World::LoadSky + the sky fields of World::Render's parameters (world.cpp:803-870,
+    2185-2189) for one view: decode the .hdr file, build LoadSky's texture (scale 1.5 and
+    the artificial sun by default, as Game::skyDomeScale / Game::artificialSun), integrate
+    its sky lights (UpdateSkylights, vxr_sky_lights with `seed`) and turn the view's sky
+    dome on with skyLightScale = light_scale (Game::skyDomeLightScale, 2.0) and the
+    blue-noise tables `blue_noise` (uint32[327680]). Returns the texture."""
+    from .vxr import sky_lights
+    tex = sky_texture(read_hdr(path), scale=scale, artificial_sun=artificial_sun)
+    view.set_sky(tex, sky_lights(tex, seed), light_scale, blue_noise)
+    return tex
+
+
 def write_frame_dat(path, rgba, width, height):
     """saveScreenBuffer: uint32 width, height, then float4 pixels row by row."""
     a = np.ascontiguousarray(rgba, np.float32).reshape(height * width, 4)

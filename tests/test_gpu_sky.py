@@ -128,3 +128,31 @@ def test_batch_with_sky_matches_single_views(lib, cuda_device, graph):
         for v in alone + batched:
             v.close()
         w.close()
+
+
+def test_load_sky_from_hdr_file(lib, cuda_device, tmp_path):
+    """scene_io.load_sky (LoadSky from a Radiance file) renders the same bits as setting
+    the texture it builds, with its sky lights, by hand."""
+    from smallproject_gb300 import scene_io as io
+    rng = np.random.default_rng(9)
+    rgb = (rng.random((32, 64, 3)) * 2.0).astype(np.float32)
+    path = str(tmp_path / "sky.hdr")
+    io.write_hdr(path, rgb)
+    bn = sky_inputs.blue_noise()
+    w = _scene(lib)
+    a = lib.View(w, lib.view_desc(48, 32, lib.LIGHTS_AREA))
+    b = lib.View(w, lib.view_desc(48, 32, lib.LIGHTS_AREA))
+    try:
+        tex = io.load_sky(a, path, bn, scale=1.25, light_scale=0.75)
+        assert np.array_equal(tex, io.sky_texture(io.read_hdr(path), scale=1.25))
+        b.set_sky(tex, lib.sky_lights(tex), 0.75, bn)
+        for v in (a, b):
+            v.lookat((126.0, 150.0, 30.0), (128.0, 140.0, 230.0))
+            v.render()
+            v.wait()
+        assert_records_equal("frame", a.read_frame(), b.read_frame(), "load_sky")
+        assert (a.read_frame()[:, :3] > 0).mean() > 0.3
+    finally:
+        a.close()
+        b.close()
+        w.close()
