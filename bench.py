@@ -38,6 +38,8 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# clock samples and the autotuner's cache (VXR_BENCH_OUT overrides the folder)
+OUT_DIR = os.environ.get("VXR_BENCH_OUT", os.path.join(ROOT, "_build"))
 sys.path.insert(0, ROOT)
 
 METRIC = "ms/frame @1080p at equal MSE vs converged: learned proposal vs plain, 1 GB300"
@@ -69,7 +71,7 @@ class ClockSampler:
 
     def __init__(self, gpu_index=0):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(OUT_DIR, f"clocks_bench_{os.getpid()}.csv")
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
@@ -423,8 +425,7 @@ def main():
     if not args.no_tune:
         # launch parameters only (results are identical for every tuning); untimed setup
         from smallproject_gb300 import autotune as at
-        cache = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "_build",
-                             "vxr_tuning.json")
+        cache = os.path.join(OUT_DIR, "vxr_tuning.json")
         tuning, tuning_report = at.autotune(world, vdesc, lambda f: cams(1000 + f), frames=4, rounds=2,
                                             cache_path=cache)
 
