@@ -307,8 +307,10 @@ __device__ __forceinline__ float3 uniform_sample_hemisphere(float r1, float r2, 
     const float3 Nb = f3(N.y * Nt.z - N.z * Nt.y, N.z * Nt.x - N.x * Nt.z, N.x * Nt.y - N.y * Nt.x);
     const float sinTheta = sqrtf(1.0f - r1 * r1);
     const float phi = 6.28318530717958647692528f * r2;
-    const float x = sinTheta * (float)cos((double)phi);
-    const float z = sinTheta * (float)sin((double)phi);
+    double sd, cd;
+    sincos((double)phi, &sd, &cd);            // one argument reduction for both
+    const float x = sinTheta * (float)cd;
+    const float z = sinTheta * (float)sd;
     return f3((x * Nb.x + r1 * N.x) + z * Nt.x, (x * Nb.y + r1 * N.y) + z * Nt.y, (x * Nb.z + r1 * N.z) + z * Nt.z);
 }
 
@@ -803,7 +805,9 @@ __device__ __forceinline__ float3 cos_weighted(float r0, float r1, float3 N) {
     const float3 T = normalize3(cross3(N, fabsf(N.y) > 0.99f ? f3(1.0f, 0.0f, 0.0f) : f3(0.0f, 1.0f, 0.0f)));
     const float3 B = cross3(T, N);
     const float term1 = 6.28318530717958647692528f * r0, term2 = sqrtf(1.0f - r1);
-    const float c = (float)cos((double)term1), s = (float)sin((double)term1);
+    double sd, cd;
+    sincos((double)term1, &sd, &cd);          // one argument reduction for both
+    const float c = (float)cd, s = (float)sd;
     const float ct = c * term2, st = s * term2, sr = sqrtf(r1);
     return f3((ct * T.x + st * B.x) + sr * N.x, (ct * T.y + st * B.y) + sr * N.y, (ct * T.z + st * B.z) + sr * N.z);
 }
