@@ -155,7 +155,8 @@ __device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32
     for (int i = 0; i < 12; i++) u[i] = xs32(seed);
     const float size = g.w, h = 0.5f * size, area = size * size;
     const float c[3] = {g.x, g.y, g.z}, sp[3] = {spo.x, spo.y, spo.z};
-    float sa[6];
+    float sa[6], va[3];
+    bool fa[6];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const int at = (a + 1) % 3, ab = (a + 2) % 3;
@@ -175,6 +176,9 @@ __device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32
         const float val = (nl * area) / d;
         sa[a] = plus ? val : 0.0f;
         sa[a + 3] = minus ? val : 0.0f;
+        va[a] = val;
+        fa[a] = plus;
+        fa[a + 3] = minus;
     }
     float total = 0.0f;
 #pragma unroll
@@ -184,6 +188,25 @@ __device__ __forceinline__ float3 sample_area_light(float4 g, float3 spo, uint32
     float pdf;
     if (total == 0.0f) {
         pdf = __int_as_float(0x7fffffff);   // 0/0: NaN -> weight 0
+    } else if (total > 0.0f && total < __int_as_float(0x7f800000)) {
+        // finite total: a face's share is +0 when its solid angle is +0 and its solid
+        // angle over the total otherwise; only the facing face of each axis can be
+        // non-zero, so the three divisions are taken up front with the same operands
+        float q[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) q[a] = __float_as_uint(va[a]) == 0u ? 0.0f : va[a] / total;
+        pdf = fa[0] ? q[0] : 0.0f;
+        float cdf = pdf;
+        if (cdf < r2) {
+#pragma unroll
+            for (int i = 1; i < 6; i++) {
+                const float p = fa[i] ? q[i % 3] : 0.0f;
+                cdf = cdf + p;
+                index = i;
+                pdf = p;
+                if (cdf >= r2) break;
+            }
+        }
     } else {
         // +0 / a positive finite total is +0: skip those divisions
         const bool fin = total > 0.0f && total < __int_as_float(0x7f800000);
