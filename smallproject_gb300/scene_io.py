@@ -16,6 +16,8 @@ path:
 * ``.dat`` frames: uint32 width, uint32 height, then width * height float4 pixels, row
   by row (saveScreenBuffer, mygame.cpp:518-549; the reference appends a time stamp to
   the file name, these functions use the name given).
+* frame comparison as the reference's MSE tool does it (mse.cpp:19-63): frame_mse,
+  frame_mae, frame_energy, with its float / double arithmetic.
 * ``.hdr`` sky domes (Radiance RGBE, the format World::LoadSky reads through
   stb_image's stbi_loadf, world.cpp:803-876): read_hdr / write_hdr, and sky_texture for
   LoadSky's conversion to the texture of vxr_view_set_sky.
@@ -496,6 +498,38 @@ def load_sky(view, path, blue_noise, scale=1.5, light_scale=2.0, artificial_sun=
     tex = sky_texture(read_hdr(path), scale=scale, artificial_sun=artificial_sun)
     view.set_sky(tex, sky_lights(tex, seed), light_scale, blue_noise)
     return tex
+
+
+def _pixel_sum(per_pixel):
+    """Sequential double accumulation in pixel order (the reference's `total +=` loop;
+    numpy's sum would add pairwise)."""
+    return float(np.cumsum(per_pixel.astype(np.float64))[-1]) if per_pixel.size else 0.0
+
+
+def frame_mse(gt, img):
+    """CalculateMSE of the reference's frame-comparison tool (mse.cpp:33-48) for two
+    float[N, 4] frames: per pixel the squared differences of r, g, b in float, summed in
+    float, accumulated in double, divided by 3N, returned as a float."""
+    g = np.asarray(gt, np.float32).reshape(-1, 4)[:, :3]
+    d = np.asarray(img, np.float32).reshape(-1, 4)[:, :3]
+    y = (g - d) * (g - d)
+    return np.float32(_pixel_sum((y[:, 0] + y[:, 1]) + y[:, 2]) / (len(y) * 3))
+
+
+def frame_mae(gt, img):
+    """CalculateRMAE of the same tool (mse.cpp:50-63): the mean absolute difference of r,
+    g, b, computed like frame_mse (no normalisation despite the name)."""
+    g = np.asarray(gt, np.float32).reshape(-1, 4)[:, :3]
+    d = np.asarray(img, np.float32).reshape(-1, 4)[:, :3]
+    y = np.abs(g - d)
+    return np.float32(_pixel_sum((y[:, 0] + y[:, 1]) + y[:, 2]) / (len(y) * 3))
+
+
+def frame_energy(img, width, height):
+    """energyInRaster (mse.cpp:19-31): the mean over pixels of (r + g + b) / 3 in float,
+    accumulated in double, divided by the width, then by the height."""
+    v = np.asarray(img, np.float32).reshape(-1, 4)
+    return np.float32(_pixel_sum(((v[:, 0] + v[:, 1]) + v[:, 2]) / np.float32(3.0)) / width / height)
 
 
 def write_frame_dat(path, rgba, width, height):

@@ -252,3 +252,33 @@ def test_reference_cornell_box_export(lib):
     assert pls == 2 and fsize == size
     assert np.array_equal(fpos[lead:], pos) and np.array_equal(fvox[lead:], val & 0xFFFF)
     w.close()
+
+
+def _tool_metrics(gt, img, w, h):
+    """The comparison tool's loops (mse.cpp:19-63), one pixel at a time, float32 terms
+    and a Python float (double) accumulator."""
+    f = np.float32
+    mse = mae = en = 0.0
+    for i in range(len(gt)):
+        dg = [f(gt[i, c]) - f(img[i, c]) for c in range(3)]
+        sq = [f(v * v) for v in dg]
+        mse += float(f(f(sq[0] + sq[1]) + sq[2]))
+        ab = [f(abs(v)) for v in dg]
+        mae += float(f(f(ab[0] + ab[1]) + ab[2]))
+        en += float(f(f(f(img[i, 0]) + f(img[i, 1])) + f(img[i, 2])) / f(3.0))
+    n = len(gt)
+    return f(mse / (n * 3)), f(mae / (n * 3)), f(en / w / h)
+
+
+def test_frame_metrics_match_the_comparison_tool(tmp_path):
+    rng = np.random.default_rng(4)
+    w, h = 23, 17
+    gt = (rng.random((w * h, 4)) * 3).astype(np.float32)
+    img = (gt + rng.normal(0, 0.2, gt.shape)).astype(np.float32)
+    io.write_frame_dat(str(tmp_path / "gt.dat"), gt, w, h)
+    io.write_frame_dat(str(tmp_path / "img.dat"), img, w, h)
+    _, _, g = io.read_frame_dat(str(tmp_path / "gt.dat"))
+    _, _, d = io.read_frame_dat(str(tmp_path / "img.dat"))
+    mse, mae, en = _tool_metrics(g, d, w, h)
+    assert io.frame_mse(g, d) == mse and io.frame_mae(g, d) == mae and io.frame_energy(d, w, h) == en
+    assert io.frame_mse(g, g) == 0.0 and io.frame_mae(g, g) == 0.0
