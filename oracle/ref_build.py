@@ -32,7 +32,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
+# the reference checkout: VXR_REFERENCE, else where this container mounts it
+DEFAULT_REF = os.environ.get("VXR_REFERENCE", "/root/reference")
 
 # tools.cl functions on the render path (the rest of tools.cl is TAA / tonemapping /
 # editor code that the path never reaches)

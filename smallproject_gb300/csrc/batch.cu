@@ -271,8 +271,7 @@ int vxr_batch_wait(vxr_batch* b, float* ms) {
         }
     }
     if (any)
-        return vxr::set_error(VXR_E_DEVICE, "device error flags 0x" + std::to_string(any) +
-                                                " (2: temporal light index, 4: spatial light index, 8: shading light index)");
+        return vxr::set_error(VXR_E_DEVICE, vxr::device_flags_message(any));
     return VXR_OK;
 }
 

@@ -1,4 +1,5 @@
 // capi_world.cpp - C ABI of the host voxel store and the scene generator.
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -20,6 +21,22 @@ int set_error(int code, const std::string& msg) {
     return code;
 }
 void clear_error() { g_err.clear(); }
+
+std::string device_flags_message(uint32_t flags) {
+    static const char* const names[] = {"bit 0", "temporal light index", "spatial light index", "shading light index",
+                                         "tensor-core wait gave up"};
+    char hex[16];
+    std::snprintf(hex, sizeof(hex), "0x%x", flags);
+    std::string m = std::string("device error flags ") + hex + " (";
+    bool first = true;
+    for (int b = 0; b < 32; b++) {
+        if (!(flags >> b & 1u)) continue;
+        if (!first) m += ", ";
+        first = false;
+        m += std::to_string(1u << b) + ": " + (b < 5 ? names[b] : "unknown");
+    }
+    return m + ")";
+}
 }  // namespace vxr
 
 using vxr::set_error;

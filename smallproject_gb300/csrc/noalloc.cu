@@ -20,6 +20,7 @@
 
 #include "internal.hpp"
 #include "kernels.hpp"
+#include "view.hpp"
 
 namespace {
 
@@ -150,31 +151,10 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
 
     // a single frame: no temporal history is read (the scratch keeps the previous
     // call's contents, which may belong to another world or camera)
-    vxr::dev::Frame f;
-    f.E = make_float3(k->E[0], k->E[1], k->E[2]);
-    f.p0 = make_float3(k->p0[0], k->p0[1], k->p0[2]);
-    f.dx = make_float3(k->p1[0] - k->p0[0], k->p1[1] - k->p0[1], k->p1[2] - k->p0[2]);
-    f.dy = make_float3(k->p2[0] - k->p0[0], k->p2[1] - k->p0[1], k->p2[2] - k->p0[2]);
-    f.oorx = k->oneOverRes[0];
-    f.oory = k->oneOverRes[1];
-    f.Nl = make_float4(k->Nleft[0], k->Nleft[1], k->Nleft[2], k->Nleft[3]);
-    f.Nr = make_float4(k->Nright[0], k->Nright[1], k->Nright[2], k->Nright[3]);
-    f.Nt = make_float4(k->Ntop[0], k->Ntop[1], k->Ntop[2], k->Ntop[3]);
-    f.Nb = make_float4(k->Nbottom[0], k->Nbottom[1], k->Nbottom[2], k->Nbottom[3]);
-    f.R0 = k->R0;
-    f.frame = k->frame;
-    f.framecount = k->framecount;
+    vxr::dev::Frame f = vxr::dev_frame(*k);
     f.restirtemporalframe = 0;
-    f.spatial = k->spatial;
     f.temporal = 0;
     f.accumulate = 0;
-    f.nlights = nlights;
-    f.ncand = nlights < k->numberOfCandidates ? nlights : k->numberOfCandidates;
-    f.maxTemporal = k->numberOfMaxTemporalImportance;
-    f.radius = k->spatialRadius;
-    f.taps = k->spatialTaps;
-    f.W = (int32_t)k->width;
-    f.H = (int32_t)k->height;
     f.sky = nullptr;
 
     vxr::ViewBuffers b;
@@ -203,6 +183,6 @@ extern "C" int vxr_render_frame_noalloc(const uint32_t* grid, const uint32_t* br
     CUN(cudaGetLastError(), "stage kernels");
     CUN(cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "read error word");
     CUN(cudaStreamSynchronize(st), "vxr_render_frame_noalloc");
-    if (herr) return vxr::set_error(VXR_E_DEVICE, "vxr_render_frame_noalloc: device error flags 0x" + std::to_string(herr));
+    if (herr) return vxr::set_error(VXR_E_DEVICE, "vxr_render_frame_noalloc: " + vxr::device_flags_message(herr));
     return VXR_OK;
 }

@@ -659,8 +659,7 @@ int vxr_view_wait(vxr_view* v) {
     CUV(cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost), "read device error flags");
     if (err) {
         cudaMemset(v->buf.err, 0, sizeof(uint32_t));
-        return set_error(VXR_E_DEVICE, "device error flags 0x" + std::to_string(err) +
-                                           " (2: temporal light index, 4: spatial light index, 8: shading light index)");
+        return set_error(VXR_E_DEVICE, vxr::device_flags_message(err));
     }
     return VXR_OK;
 }

@@ -11,6 +11,7 @@ import sys
 import pytest
 
 from conftest import ROOT
+from oracle.ref_build import DEFAULT_REF
 
 
 def _free_port():
@@ -37,7 +38,7 @@ def test_multi_rank_helpers_gloo():
         assert d["quality"] == {"learned_at_equal_mse": {"candidates": 4}} and d["params"] == [0.25, -1.5]
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference") and not os.path.isfile(
+@pytest.mark.skipif(not os.path.isdir(DEFAULT_REF) and not os.path.isfile(
     os.path.join(ROOT, "oracle", "_ref", "vxref_gen.inc")), reason="the reference oracle cannot be built here")
 def test_reference_arm_two_ranks():
     r, lines = _torchrun(["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",

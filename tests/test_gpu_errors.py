@@ -35,7 +35,8 @@ def test_shading_light_index_error_is_reported_once(lib, cuda_device, scene0):
         v.end_frame()
         with pytest.raises(lib.VxrError) as e:
             v.wait()
-        assert e.value.code == -5 and "device error flags 0x8" in str(e.value)   # VXR_E_DEVICE, shading
+        assert e.value.code == -5                                   # VXR_E_DEVICE
+        assert "device error flags 0x8 (8: shading light index)" in str(e.value)
         assert np.isfinite(v.read_frame()).all()          # clamped, not faulted
         # the bad index also sits in the history the next temporal pass reads: empty it,
         # then later frames are clean (the word was cleared when it was reported)

@@ -10,7 +10,9 @@ import pytest
 
 from smallproject_gb300 import scene_io as io
 
-REF_SCENES = "/root/reference/scene_export"
+from oracle.ref_build import DEFAULT_REF
+
+REF_SCENES = os.path.join(DEFAULT_REF, "scene_export")
 
 
 def _lightset(lights):
@@ -94,7 +96,7 @@ def test_dat_frame_round_trip(tmp_path):
 
 # --- MagicaVoxel .vox (SpriteManager::LoadSprite without the large-model flag) ---------
 
-REF_TEMPLATE = "/root/reference/template/world.cpp"
+REF_TEMPLATE = os.path.join(DEFAULT_REF, "template", "world.cpp")
 REF_CORNELL = os.path.join(REF_SCENES, "cornellbox")
 
 

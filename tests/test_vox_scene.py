@@ -10,11 +10,12 @@ import numpy as np
 import pytest
 
 from oracle import binding as ob
+from oracle.ref_build import DEFAULT_REF
 from smallproject_gb300 import scene_io as io
 from smallproject_gb300 import vox_scene as vs
 
 needs_ogt = pytest.mark.skipif(ob.load_ogt() is None, reason="the reference's ogt_vox is not present")
-CORNELL = "/root/reference/scene_export/cornellbox/cornell-box.vox"
+CORNELL = os.path.join(DEFAULT_REF, "scene_export", "cornellbox", "cornell-box.vox")
 
 
 # ---- a .vox writer (chunk layout of the MagicaVoxel format) --------------------------

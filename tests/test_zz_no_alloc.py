@@ -4,7 +4,8 @@ for callers that cannot call cudaMalloc (they own every device buffer themselves
 The test owns the device buffers (allocated here through torch, as such a caller would
 through its own allocator), renders two different frames in a row through the C ABI,
 and requires each to match, bit for bit, the same frame rendered by the regular view
-path (vxr_view_*, temporal reuse and accumulation off)."""
+path (vxr_view_*, temporal reuse and accumulation off). A third call, bracketed by
+cudaMemGetInfo, must leave the device's free memory unchanged."""
 import ctypes as C
 
 import numpy as np
@@ -50,6 +51,16 @@ def test_noalloc_matches_view_path_twice(lib, cuda_device, scene0):
         assert (want[:, 3] > 0).any() and (want[:, :3] > 0).any()
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
             f"{int((got != want).any(axis=1).sum())} pixels differ"
+    # the promise itself: after a first call, a further call changes the device's free
+    # memory by nothing (no cudaMalloc, no lazily grown buffer, no library allocator)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    rc = L.vxr_render_frame_noalloc(C.c_void_p(d_grid.data_ptr()), C.c_void_p(d_bricks.data_ptr()), len(b),
+                                    C.c_void_p(d_lights.data_ptr()), len(l), lib.LIGHTS_AREA, C.byref(k),
+                                    C.c_void_p(d_out.data_ptr()), None)
+    assert rc == 0, L.vxr_last_error().decode()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
     view.close()
 
 
