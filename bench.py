@@ -9,13 +9,16 @@ albedo -> candidates (+ proposal inference) + temporal -> spatial -> shading+acc
 
 Quality protocol (untimed setup, --quality full): a converged render (FP64 mean of
 --conv-frames frames of the unbiased estimator: spatial and temporal reuse off) at path
-frame 150; the proposal trained online for --train-frames frames along the path on the
-plain method's reservoirs; then for each method and candidate count in CANDS, 32 seeds x
-16 frames at the static pose: device ms/frame and MSE against the converged render. The
-plain method's reference point is 32 candidates (the reference's NUMBEROFCANDIDATES).
-The timed configuration is the learned method at the smallest candidate count whose mean
-MSE is at most the plain method's (equal MSE), else plain at 32; `value` is its device
-ms/frame over the timed steps along the camera path.
+frame 150; the proposal's warm start, trained for --train-frames frames along the path on
+the plain method's reservoirs; then the plain method at 32 candidates (the reference's
+NUMBEROFCANDIDATES) and the learned method at every count in CANDS, the learned views
+running --online training steps (65,536 samples each) inside every frame on their own
+final reservoirs: per point --mse-seeds views x --mse-frames frames at the static pose,
+device ms/frame and per-frame MSE against the converged render. Intervals are 95%
+percentile-bootstrap intervals over seeds. The timed configuration is the learned method
+at the smallest candidate count whose interval of MSE(learned) / MSE(plain 32) lies at
+or below 1 (equal MSE), else plain at 32; `value` is its device ms/frame over the timed
+steps along the camera path, training steps included.
 
 Arms:
   --impl ours       the CUDA path (libvxr.so) - the JSON line's `value` is device time
@@ -23,8 +26,9 @@ Arms:
                     C ABI call that returns the image in page-locked host memory.
   --impl reference  the reference's own render-path kernel source compiled for the
                     host CPU (oracle/_ref, OpenMP over all host threads), else the C
-                    restatement; each step renders a bounded strip of the same frame
-                    and is scaled to a full frame.
+                    restatement; each step renders one whole frame of the same
+                    workload (scene and frame constants from host-only code: the
+                    CUDA library is not loaded).
 Multi-GPU (torchrun): replicas only - every rank renders its own copy of the view.
 """
 import argparse
@@ -145,36 +149,116 @@ def make_scene(config):
     return vx, desc, world
 
 
-def cpu_arm(args, desc, world, steps, warmup, W, H):
-    """Time the reference's CPU implementation on a strip of rows of the frame."""
-    import smallproject_gb300 as vx
+def cpu_model():
+    """The host CPU's model name (lscpu / /proc/cpuinfo), or None."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
+
+
+def probe_cpu_opencl():
+    """Whether a CPU OpenCL runtime exists on this host (the reference's own kernels could
+    then run unmodified on the host cores): ICD vendor files, an OpenCL loader, and the
+    CPU devices of every platform it lists. Enumerates only; creates no context."""
+    import ctypes
+    import ctypes.util
+    import glob
+    vendors = sorted(glob.glob("/etc/OpenCL/vendors/*.icd"))
+    names = [ctypes.util.find_library("OpenCL")] + sorted(glob.glob("/usr/lib/*/libOpenCL.so*")) + sorted(
+        glob.glob("/usr/local/cuda/targets/*/lib/libOpenCL.so*"))
+    out = {"icd_vendor_files": vendors, "loader": None, "platforms": [], "cpu_devices": 0}
+    for n in names:
+        if not n:
+            continue
+        try:
+            lib = ctypes.CDLL(n)
+        except OSError:
+            continue
+        out["loader"] = n
+        cnt = ctypes.c_uint(0)
+        rc = lib.clGetPlatformIDs(0, None, ctypes.byref(cnt))
+        if rc != 0 or cnt.value == 0:
+            out["platform_query"] = f"clGetPlatformIDs returned {rc}, {cnt.value} platforms"
+            break
+        ids = (ctypes.c_void_p * cnt.value)()
+        lib.clGetPlatformIDs(cnt.value, ids, None)
+        for pid in ids:
+            buf = ctypes.create_string_buffer(256)
+            lib.clGetPlatformInfo(ctypes.c_void_p(pid), 0x0902, 256, buf, None)   # CL_PLATFORM_NAME
+            nd = ctypes.c_uint(0)
+            lib.clGetDeviceIDs(ctypes.c_void_p(pid), ctypes.c_ulonglong(2), 0, None, ctypes.byref(nd))  # CPU
+            out["platforms"].append({"name": buf.value.decode(errors="replace"), "cpu_devices": nd.value})
+            out["cpu_devices"] += nd.value
+        break
+    out["status"] = ("present" if out["cpu_devices"] else
+                     "absent: " + ("no OpenCL loader" if not out["loader"] else "no platform with a CPU device") +
+                     ("" if vendors else ", no ICD vendor files"))
+    return out
+
+
+def workload_camera(config, path, f):
+    """Camera of frame f of a configuration's workload: config 0 a static camera at
+    (128, 160, 0) looking at the world centre; config 1 a 120-frame Catmull-Rom spline;
+    config 3 the 300-frame spline. path(seed, f, n) -> (pos, target) is the scene's."""
+    if config == 0:
+        return (128.0, 160.0, 0.0), (128.0, 128.0, 128.0)
+    n = 120 if config == 1 else NFR
+    return path(1, f % n, n)
+
+
+def cpu_arm(config, steps, warmup, W, H):
+    """Time the reference's CPU implementation on whole frames of the workload: the
+    reference's own kernel source compiled for the host (oracle/_ref, OpenMP over every
+    host thread), else the C restatement. The scene, camera path and frame constants come
+    from host-only code (oracle/scene_host.cpp with the project's scene generator, the
+    oracle's camera restatement): the CUDA library is not loaded. Each step is one frame
+    (albedo, candidates + temporal, spatial, shading, accumulation), timed with
+    time.perf_counter around the five stage calls, like World::Render's per-stage timers
+    (template/world.cpp:2439-2471)."""
     from oracle import binding as ob
-    g, b, l = world.arrays()
-    arrays = ob.WorldArrays(g, b, l)
+    scene = ob.HostScene(config)
+    arrays = ob.WorldArrays(scene.grid, scene.bricks, scene.lights)
     kind = "reference" if ob.load_ref() is not None else "port"
-    r = ob.Renderer("ref" if kind == "reference" else "port", arrays, W, H, False)
-    rows = args.cpu_rows
-    y0 = H // 2 - rows // 2
-    cam = vx.Camera()
-    times = []
+    point = config == 0
+    r = ob.Renderer("ref" if kind == "reference" else "port", arrays, W, H, point)
+    cam = ob.CameraPath(W, H)
+    times, stage_s = [], [0.0] * 5
     for f in range(warmup + steps):
-        pos, tgt = vx.camera_path(desc, 1, f, 300)
+        pos, tgt = workload_camera(config, scene.camera_path, f)
         cam.lookat(pos, tgt)
-        k = cam.begin_frame(W, H)
-        k.numberOfLights, k.numberOfCandidates, k.numberOfMaxTemporalImportance = len(l), 32, 20
-        k.spatialRadius, k.spatialTaps, k.spatial, k.temporal, k.accumulate = 30, 5, 1, 1, 0
+        k = cam.begin(numberOfLights=len(scene.lights), numberOfCandidates=32, numberOfMaxTemporalImportance=20,
+                      spatialRadius=30, spatialTaps=5, spatial=1, temporal=1, accumulate=0)
         r.frame_start()
         t0 = time.perf_counter()
         for s in range(1, 6):
-            r.stage(k, s, y0, y0 + rows)
+            ts = time.perf_counter()
+            r.stage(k, s)
+            if f >= warmup:
+                stage_s[s - 1] += time.perf_counter() - ts
         dt = time.perf_counter() - t0
-        cam.end_frame()
+        cam.end()
         if f >= warmup:
             times.append(dt)
     r.close()
-    per_frame_ms = statistics.median(times) * 1000.0 * (H / rows)
-    return per_frame_ms, kind, {"rows": rows, "y0": y0, "width": W, "frames": steps,
-                                "desc": f"{rows} rows x {W} px of each {W}x{H} frame, scaled by {H}/{rows}"}
+    ms = 1000.0 * sum(times) / len(times)
+    info = {"frames": steps, "warmup": warmup, "width": W, "height": H,
+            "median_ms": 1000.0 * statistics.median(times),
+            "stage_ms": {n: 1000.0 * t / steps for n, t in zip(STAGES, stage_s)},
+            "threads": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count())), "cpu_model": cpu_model(),
+            "desc": f"{steps} whole {W}x{H} frames of config {config} (after {warmup} untimed), "
+                    f"{'point' if point else 'area'} lights, 32 candidates, temporal and spatial reuse"}
+    return ms, kind, info
 
 
 CANDS = (4, 8, 12, 16, 24, 32)
@@ -186,19 +270,27 @@ NCU_TRAFFIC_1080P = {"shadow_candidates": 4 * (71.57e6 + 2.96e6), "shadow_shadin
                      "ris_candidates": 4 * (10.33e6 + 0.01e6), "albedo": 4 * (33.93e6 + 0.47e6)}
 
 
-def quality_eval(vx, world, desc, W, H, tuning, args):
-    """Converged render, online training, and the MSE / ms table of both methods."""
-    pos, tgt = vx.camera_path(desc, 1, POSE, NFR)
-    ref = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=77))
-    ref.set_tuning(tuning)
-    ref.lookat(pos, tgt)
-    ref.sum64_reset()
-    t0 = time.perf_counter()
-    for _ in range(args.conv_frames):
-        ref.render()
-        ref.sum64_add()
-    ref.wait()
-    conv_s = time.perf_counter() - t0
+def boot_ci(groups, stat, n=2000, seed=0):
+    """Percentile-bootstrap 95% interval of stat over the frames of resampled seeds (each
+    group holds one seed's per-frame MSEs: frames of one seed are not independent)."""
+    rng = np.random.default_rng(seed)
+    k = len(groups)
+    vals = [stat(np.concatenate([groups[i] for i in rng.integers(0, k, k)])) for _ in range(n)]
+    return [float(np.percentile(vals, 2.5)), float(np.percentile(vals, 97.5))]
+
+
+def boot_ratio(ga, gb, stat, n=2000, seed=1):
+    """95% interval of stat(a) / stat(b), the seeds of each arm resampled independently."""
+    rng = np.random.default_rng(seed)
+    ka, kb = len(ga), len(gb)
+    vals = [stat(np.concatenate([ga[i] for i in rng.integers(0, ka, ka)])) /
+            stat(np.concatenate([gb[i] for i in rng.integers(0, kb, kb)])) for _ in range(n)]
+    return [float(np.percentile(vals, 2.5)), float(np.percentile(vals, 97.5))]
+
+
+def pretrain(vx, world, W, H, tuning, args, desc):
+    """The proposal's warm start: trained online along the camera path on the plain
+    method's reservoirs (the uniform source is the fallback until the network exists)."""
     trainer = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5))
     trainer.set_tuning(tuning)
     trainer.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
@@ -218,63 +310,96 @@ def quality_eval(vx, world, desc, W, H, tuning, args):
     train_step_ms = trainer.timer_end() / 10
     params = trainer.proposal_params()
     trainer.close()
-    table = {}
-    for method in ("plain", "learned"):
-        for c in CANDS:
-            ms_l, mse_l, kms_l = [], [], {}
-            for seed in range(args.mse_seeds):
-                v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, num_candidates=c, rng_seed=1000 + seed))
-                v.set_tuning(tuning)
-                v.lookat(pos, tgt)
-                if method == "learned":
-                    v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
-                    v.proposal_set_params(params)
-                    v.proposal_use(True)
-                for _ in range(8):
-                    v.render()
-                v.wait()
-                v.kernel_timing(True)
-                v.timer_begin()
-                for _ in range(8):
-                    v.render()
-                ms_l.append(v.timer_end() / 8)
-                v.wait()
-                v.kernel_timing(False)
-                ks = v.kernel_stats(reset=True)
-                for k in ("proposal_infer", "ris_candidates"):
-                    kms_l.setdefault(k, []).append(ks[k][0] / max(ks[k][1], 1))
-                for _ in range(args.mse_frames):
-                    v.render()
-                    mse_l.append(v.error_vs(ref, 0)[0])
-                v.close()
-            table[f"{method}_{c}"] = {"method": method, "candidates": c, "ms": float(np.median(ms_l)),
-                                      "mse": float(np.mean(mse_l)), "mse_median": float(np.median(mse_l)),
-                                      "frames": len(mse_l),
-                                      "kernel_ms": {k: float(np.median(v)) for k, v in kms_l.items()}}
+    return params, {"train_frames": args.train_frames, "train_s": train_s, "train_batch": 65536,
+                    "train_step_ms": train_step_ms, "loss_first": float(np.mean(losses[:5])),
+                    "loss_last": float(np.mean(losses[-5:]))}
+
+
+def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
+    """Converged render, then the MSE / ms table: plain at 32 candidates, learned at every
+    count in CANDS with `online` training steps inside each of its frames. Per point
+    args.mse_seeds views (seeds) x args.mse_frames frames at the static pose; decisions on
+    bootstrap intervals over seeds."""
+    pos, tgt = vx.camera_path(desc, 1, POSE, NFR)
+    ref = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=77))
+    ref.set_tuning(tuning)
+    ref.lookat(pos, tgt)
+    ref.sum64_reset()
+    t0 = time.perf_counter()
+    for _ in range(args.conv_frames):
+        ref.render()
+        ref.sum64_add()
+    ref.wait()
+    conv_s = time.perf_counter() - t0
+    points = [("plain", 32)] + [("learned", c) for c in CANDS]
+    groups, table = {}, {}
+    for method, c in points:
+        ms_l, per_seed, kms_l = [], [], {}
+        for seed in range(args.mse_seeds):
+            v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, num_candidates=c, rng_seed=1000 + seed))
+            v.set_tuning(tuning)
+            v.lookat(pos, tgt)
+            if method == "learned":
+                v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
+                v.proposal_set_params(params)
+                v.proposal_use(True)
+                v.proposal_online(online)
+            for _ in range(8):
+                v.render()
+            v.wait()
+            v.kernel_timing(True)
+            v.timer_begin()
+            for _ in range(8):
+                v.render()
+            ms_l.append(v.timer_end() / 8)
+            v.wait()
+            v.kernel_timing(False)
+            ks = v.kernel_stats(reset=True)
+            for k in ("proposal_infer", "ris_candidates", "proposal_train"):
+                if ks[k][1]:
+                    kms_l.setdefault(k, []).append(ks[k][0] / ks[k][1])
+            e = []
+            for _ in range(args.mse_frames):
+                v.render()
+                e.append(v.error_vs(ref, 0)[0])
+            per_seed.append(np.array(e))
+            v.close()
+        key = f"{method}_{c}"
+        groups[key] = per_seed
+        allf = np.concatenate(per_seed)
+        table[key] = {"method": method, "candidates": c, "ms": float(np.median(ms_l)),
+                      "mse": float(allf.mean()), "mse_ci95": boot_ci(per_seed, np.mean),
+                      "mse_median": float(np.median(allf)), "mse_median_ci95": boot_ci(per_seed, np.median),
+                      "frames": int(allf.size), "seeds": len(per_seed),
+                      "kernel_ms": {k: float(np.median(x)) for k, x in kms_l.items()}}
     ref.close()
     p32 = table["plain_32"]
-    eq = None
     for c in CANDS:
-        if table[f"learned_{c}"]["mse"] <= p32["mse"]:
-            eq = table[f"learned_{c}"]
-            break
-    # the same decision on the median per-frame MSE (single-frame MSE is heavy-tailed)
-    eq_med = None
-    for c in CANDS:
-        if table[f"learned_{c}"]["mse_median"] <= p32["mse_median"]:
-            eq_med = table[f"learned_{c}"]
-            break
+        r = table[f"learned_{c}"]
+        r["mse_ratio_ci95"] = boot_ratio(groups[f"learned_{c}"], groups["plain_32"], np.mean)
+        r["median_mse_ratio_ci95"] = boot_ratio(groups[f"learned_{c}"], groups["plain_32"], np.median)
+    # equal MSE: the smallest candidate count whose MSE ratio to plain-32 is at most 1 with
+    # 95% confidence (upper end of the bootstrap interval <= 1)
+    eq = next((table[f"learned_{c}"] for c in CANDS if table[f"learned_{c}"]["mse_ratio_ci95"][1] <= 1.0), None)
+    eq_med = next((table[f"learned_{c}"] for c in CANDS
+                   if table[f"learned_{c}"]["median_mse_ratio_ci95"][1] <= 1.0), None)
+    # monotone within the intervals: a larger count is never significantly worse
+    mono = all(table[f"learned_{b}"]["mse_ci95"][0] <= table[f"learned_{a}"]["mse_ci95"][1]
+               for i, a in enumerate(CANDS) for b in CANDS[i + 1:])
     # equal time: the learned configuration with the largest ms/frame not above plain's
     at = [table[f"learned_{c}"] for c in CANDS if table[f"learned_{c}"]["ms"] <= p32["ms"]]
     et = max(at, key=lambda r: r["ms"]) if at else None
-    return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s, "epsilon": args.epsilon,
-            "train_frames": args.train_frames, "train_s": train_s, "train_batch": 65536,
-            "train_step_ms": train_step_ms,
-            "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:])),
-            "frames_per_point": args.mse_seeds * args.mse_frames, "table": table,
-            "plain_reference": p32, "learned_at_equal_mse": eq, "learned_at_equal_median_mse": eq_med,
-            "equal_time": None if et is None else {"learned": et, "mse_ratio": et["mse"] / p32["mse"],
-                                                   "median_mse_ratio": et["mse_median"] / p32["mse_median"]}}, params
+    return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s,
+            "epsilon": args.epsilon, "online_steps_per_frame": online,
+            "frames_per_point": args.mse_seeds * args.mse_frames, "seeds_per_point": args.mse_seeds,
+            "table": table, "plain_reference": p32, "learned_at_equal_mse": eq, "learned_at_equal_median_mse": eq_med,
+            "learned_mse_monotone_within_ci": mono,
+            "decision_rule": "equal MSE: smallest K whose bootstrap 95% interval of MSE(learned K) / MSE(plain 32) "
+                             "lies at or below 1; equal time: largest learned ms/frame not above plain's",
+            "equal_time": None if et is None else {
+                "learned": et, "mse_ratio": et["mse"] / p32["mse"], "mse_ratio_ci95": et["mse_ratio_ci95"],
+                "median_mse_ratio": et["mse_median"] / p32["mse_median"],
+                "median_mse_ratio_ci95": et["median_mse_ratio_ci95"]}}
 
 
 def run_batch(args, dist, rank, ws, warmup):
@@ -366,19 +491,20 @@ def main():
     ap.add_argument("--config", type=int, default=3)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--cpu-rows", type=int, default=96, help="rows of the frame timed on the CPU per step")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=10, help="whole frames of the CPU baseline leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="library default launch tuning instead of the autotuner")
+    ap.add_argument("--no-small-configs", action="store_true", help="skip the config 0 / config 1 measurements")
     ap.add_argument("--quality", choices=["full", "train", "off"], default="full",
                     help="train: train the proposal and time the learned method at --candidates (no converged "
                          "render, no sweep); off: time the plain method at 32 candidates")
     ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
     ap.add_argument("--train-frames", type=int, default=200)
-    ap.add_argument("--mse-seeds", type=int, default=32)
+    ap.add_argument("--mse-seeds", type=int, default=48)
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
+    ap.add_argument("--online", type=int, default=1, help="proposal training steps inside every learned frame")
     args = ap.parse_args()
     W, H = args.width, args.height
     warmup = max(args.warmup, 3)
@@ -394,17 +520,20 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from smallproject_gb300 import build as B
-        B.build()
-        vx, desc, world = make_scene(args.config)
-        ms, kind, sample = cpu_arm(args, desc, world, args.steps, args.warmup, W, H)
+        if args.config not in (0, 1, 3):
+            print(json.dumps({"impl": "reference", "unavailable": f"config {args.config} is a batch of views: the "
+                              "reference renders one view per World"}))
+            return
+        ms, kind, sample = cpu_arm(args.config, args.steps, args.warmup, W, H)
         config["method"] = "plain uniform-source RIS, 32 candidates"
         line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms/frame", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
                 "config": config,
-                "cpu_baseline": {"value": ms, "unit": "ms/frame", "cores": os.cpu_count(), "kind": kind,
-                                 "sample": sample["desc"]},
+                "cpu_baseline": {"value": ms, "unit": "ms/frame", "cores": sample["threads"], "kind": kind,
+                                 "sample": sample["desc"], "cpu_model": sample["cpu_model"]},
+                "stage_ms": sample["stage_ms"], "median_ms": sample["median_ms"],
+                "opencl_cpu_runtime": probe_cpu_opencl(),
                 "e2e": {"value": ms, "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -430,31 +559,27 @@ def main():
                                             cache_path=cache)
 
     quality, params = None, None
-    if args.quality == "full" and rank == 0:
-        quality, params = quality_eval(vx, world, desc, W, H, tuning, args)
-    elif args.quality == "train" and rank == 0:
-        trainer = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5))
-        trainer.set_tuning(tuning)
-        trainer.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
-        for f in range(args.train_frames):
-            p, t = cams(f)
-            trainer.lookat(p, t)
-            trainer.render()
-            trainer.proposal_train(1)
-        params = trainer.proposal_params()
-        trainer.close()
+    if args.quality in ("full", "train") and rank == 0:
+        params, train_info = pretrain(vx, world, W, H, tuning, args, desc)
+        if args.quality == "full":
+            quality = quality_eval(vx, world, desc, W, H, tuning, args, params, args.online)
+            quality.update(train_info)
+        else:
+            quality = train_info
     if dist is not None:
         obj = [quality, params]
         dist.broadcast_object_list(obj, src=0)
         quality, params = obj
     if args.quality == "train":
         learned, cand = True, args.candidates
-        config["method"] = f"learned proposal, {cand} candidates (trained {args.train_frames} frames)"
+        config["method"] = (f"learned proposal, {cand} candidates, {args.online} training step(s) per frame "
+                            f"(warm start: {args.train_frames} frames)")
     else:
         eq = quality["learned_at_equal_mse"] if quality else None
         learned = eq is not None
         cand = eq["candidates"] if learned else 32
-        config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32)" if learned
+        config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32), {args.online} "
+                            "training step(s) of 65,536 samples inside every frame" if learned
                             else "plain uniform-source RIS, 32 candidates")
 
     def make_view(learned_view, c):
@@ -464,6 +589,7 @@ def main():
             v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
             v.proposal_set_params(params)
             v.proposal_use(True)
+            v.proposal_online(args.online)
         return v
 
     def timed(view, steps, start):
@@ -528,18 +654,36 @@ def main():
     # end to end through the C ABI with a page-locked host image
     pinned = vx.PinnedBuffer(W * H * 4)
     e2e_steps = max(5, min(args.steps, 30))
-    for f in range(3):
-        pos, tgt = cams(f)
-        view.render_to_host(pos, tgt, pinned.array)
-    t0 = time.perf_counter()
-    for f in range(e2e_steps):
-        pos, tgt = cams(f)
-        view.render_to_host(pos, tgt, pinned.array)
-    e2e_ms = (time.perf_counter() - t0) * 1000.0 / e2e_steps
-    e2e_ms = max_over_ranks(dist, e2e_ms)
+
+    def e2e_of(v):
+        for f in range(3):
+            pos, tgt = cams(f)
+            v.render_to_host(pos, tgt, pinned.array)
+        t0 = time.perf_counter()
+        for f in range(e2e_steps):
+            pos, tgt = cams(f)
+            v.render_to_host(pos, tgt, pinned.array)
+        return max_over_ranks(dist, (time.perf_counter() - t0) * 1000.0 / e2e_steps)
+
+    e2e_ms = e2e_of(view)
     img_ok = bool(np.isfinite(pinned.array).all() and pinned.array.max() > 0)
+    e2e_plain_ms = None
+    if learned:
+        pv = make_view(False, 32)
+        e2e_plain_ms = e2e_of(pv)
+        pv.close()
     pinned.close()
     modes = other_modes(make_view, cams, min(args.steps, 30), warmup) if rank == 0 else None
+    configs01 = None
+    if rank == 0 and not args.no_small_configs:
+        def tune_small(w, d):
+            if args.no_tune:
+                return None
+            from smallproject_gb300 import autotune as at
+            cam = lambda f: ((128.0 + f, 160.0, 0.0), (128.0, 128.0, 128.0))
+            t, _ = at.autotune(w, d, cam, frames=3, rounds=1, cache_path=os.path.join(OUT_DIR, "vxr_tuning.json"))
+            return t
+        configs01 = small_configs(vx, tune_small, min(args.steps, 30), warmup)
 
     if rank != 0:
         return
@@ -554,7 +698,7 @@ def main():
     dom = max(kernel_ms, key=lambda k: kernel_ms[k] * (kstats[k][1] or 0))
     per_launch_bytes = {"shadow_candidates": 36.0 * rays_c, "shadow_shading": 36.0 * rays_s,
                         "ris_candidates": 80.0 * hits, "albedo": 12.0 * npx, "spatial": 80.0 * npx,
-                        "proposal_infer": 8.0 * hits + 8.0 * 32 * hits, "temporal": 48.0 * hits,
+                        "proposal_infer": 8.0 * hits + 8.0 * cand * hits, "temporal": 48.0 * hits,
                         "shade_finish": 72.0 * npx, "shade_request": 72.0 * hits, "compact_hits": 12.0 * npx,
                         "accumulate": 48.0 * npx}
     ab = per_launch_bytes.get(dom, 0.0)
@@ -567,9 +711,12 @@ def main():
     rays = hits + rays_c + rays_s
     cpu = None
     if not args.no_cpu_baseline:
-        cms, kind, sample = cpu_arm(args, desc, world, args.cpu_steps, 1, W, H)
-        cpu = {"value": cms, "unit": "ms/frame", "cores": os.cpu_count(), "kind": kind, "sample": sample["desc"]}
-    value = ms_frame / ws   # replicas: ws frames per ms_frame across the job
+        cms, kind, sample = cpu_arm(args.config, args.cpu_steps, 1, W, H)
+        cpu = {"value": cms, "unit": "ms/frame", "cores": sample["threads"], "kind": kind, "sample": sample["desc"],
+               "cpu_model": sample["cpu_model"]}
+    # replicas: every rank renders its own view; the job's frame time is the slowest
+    # rank's, and the job delivers ws frames per frame time
+    value = ms_frame
     line = {"metric": METRIC, "value": value, "unit": "ms/frame", "n_gpus": ws, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms_frame, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
@@ -577,13 +724,62 @@ def main():
             "stage_ms": stage_ms, "kernel_ms": kernel_ms, "stage_roofline": stage_rooflines,
             "rays_per_frame": rays, "rays_per_s": rays / (ms_frame * 1e-3),
             "roofline": roofline, "cpu_baseline": cpu, "quality": quality,
+            "frames_per_s_job": ws * 1000.0 / ms_frame,
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
-                    "d2h_bytes_per_step": npx * 16, "image_ok": img_ok},
+                    "d2h_bytes_per_step": npx * 16, "image_ok": img_ok,
+                    "plain_32": e2e_plain_ms if learned else e2e_ms},
             "gpu_launches": launches, "clocks": clk,
             "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report,
-            "modes": modes, "world_commit": world_commit_times(world, args)}
+            "modes": modes, "configs_0_1": configs01, "world_commit": world_commit_times(world, args)}
     print(json.dumps(line))
     view.close()
+
+
+def small_configs(vx, tuning_fn, steps, warmup):
+    """Configs 0 and 1 of the benchmark set on the GPU (plain method, 32 candidates):
+    config 0 - 256^3 fBm terrain (seed 1), 64 emitters, point lights, 640x360, static
+    camera; config 1 - 1024^3 terrain (seed 2), 4,096 emitters in the air, area lights,
+    1280x720, 120-frame spline. ms/frame and per-kernel ms over `steps` frames; config 0
+    also the reference's kernels on the host cores (16 frames, the reference arm's code)."""
+    out = {}
+    for c, (W, H, lm) in ((0, (640, 360, vx.LIGHTS_POINT)), (1, (1280, 720, vx.LIGHTS_AREA))):
+        d = vx.scene_preset(c)
+        w = vx.World()
+        w.generate(d)
+        v = vx.View(w, vx.view_desc(W, H, lm, accumulate=0))
+        t = tuning_fn(w, v.desc)
+        if t is not None:
+            v.set_tuning(t)
+        cam = lambda f, d=d, c=c: workload_camera(c, lambda sd, ff, n: vx.camera_path(d, sd, ff, n), f)
+        for f in range(warmup):
+            v.lookat(*cam(f))
+            v.render()
+        v.wait()
+        v.kernel_timing(True)
+        v.kernel_stats(reset=True)
+        v.stage_stats(reset=True)
+        v.timer_begin()
+        for f in range(steps):
+            v.lookat(*cam(warmup + f))
+            v.render()
+        ms = v.timer_end() / steps
+        v.wait()
+        v.kernel_timing(False)
+        ks = v.kernel_stats(reset=True)
+        sums, counts = v.stage_stats(reset=True)
+        hits, rc, rs = v.work_counts()
+        out[f"config{c}"] = {"resolution": [W, H], "light_model": "point" if lm == vx.LIGHTS_POINT else "area",
+                             "emitters": int(d.emitters), "ms_per_frame": ms, "frames": steps,
+                             "stage_ms": {STAGES[i]: (sums[i] / counts[i] if counts[i] else 0.0) for i in range(5)},
+                             "kernel_ms": {k: a / n for k, (a, n) in ks.items() if n},
+                             "rays_per_s": (hits + rc + rs) / (ms * 1e-3)}
+        v.close()
+        w.close()
+    cms, kind, sample = cpu_arm(0, 16, 1, 640, 360)
+    out["config0"]["cpu_reference"] = {"ms_per_frame": cms, "median_ms": sample["median_ms"], "kind": kind,
+                                       "threads": sample["threads"], "cpu_model": sample["cpu_model"],
+                                       "stage_ms": sample["stage_ms"], "sample": sample["desc"]}
+    return out
 
 
 def other_modes(make_view, cams, steps, warmup):

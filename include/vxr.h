@@ -376,8 +376,9 @@ int vxr_view_timer_end(vxr_view* v, float* ms);
  * view launches, while on. Kernel ids 0..VXR_KERNEL_COUNT-1 (names from
  * vxr_kernel_name): albedo, compact_hits, proposal_infer, ris_candidates,
  * shadow_candidates, temporal, spatial, shade_request, shadow_shading, shade_finish,
- * accumulate. Stats: summed milliseconds and launch counts since the last reset. */
-#define VXR_KERNEL_COUNT 11
+ * accumulate, proposal_train (a frame's online training steps, gather to Adam, as one
+ * timed unit). Stats: summed milliseconds and launch counts since the last reset. */
+#define VXR_KERNEL_COUNT 12
 int vxr_view_kernel_timing(vxr_view* v, int on);
 int vxr_view_kernel_stats(vxr_view* v, double sum_ms[VXR_KERNEL_COUNT], uint32_t count[VXR_KERNEL_COUNT], int reset);
 const char* vxr_kernel_name(int id);
@@ -397,7 +398,9 @@ int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[
  * it with p_hat / p_src, p_src(e) = (1 - epsilon) softmax_c(e) / |c(e)| + epsilon / N.
  * Inference: BF16 tensor cores, FP32 accumulation.
  * Training: online, weighted cross-entropy towards the cluster of each final reservoir's
- * emitter (weight W * p_hat), Adam; FP32 kernels. */
+ * emitter (weight W * p_hat), Adam on FP32 master parameters. The default step runs on
+ * the tensor cores (BF16 operands, FP32 accumulation; hidden 64, at most 256 clusters);
+ * the FP32 CUDA-core trainer stays selectable. */
 typedef struct vxr_proposal_desc {
     uint32_t hidden;          /* hidden width (64) */
     uint32_t table_log2;      /* hash-table entries per level, log2 (16) */
@@ -407,6 +410,7 @@ typedef struct vxr_proposal_desc {
     uint32_t batch;           /* training samples per step (65536) */
     uint32_t seed;            /* parameter initialisation */
     uint32_t inference;       /* 0 auto (tcgen05 when hidden = 64 and 256 clusters, else mma.sync), 1 mma.sync, 2 tcgen05 */
+    uint32_t training;        /* 0 auto (tensor cores when hidden = 64 and clusters <= 256, else FP32), 1 FP32, 2 tensor cores */
 } vxr_proposal_desc;
 int vxr_proposal_default_desc(vxr_proposal_desc* d);
 /* Allocate and initialise the network for this view; K = the world's cluster count. */
@@ -416,6 +420,18 @@ int vxr_view_proposal_use(vxr_view* v, int on);
 /* `steps` Adam steps, each on a batch gathered from the view's current frame (hit
  * pixels, final reservoirs); the last step's loss in *loss (may be NULL). */
 int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss);
+/* Online training inside the frame: every vxr_view_render (and vxr_view_render_to_host)
+ * of a view that samples from the proposal ends with `steps_per_frame` (0..16) training
+ * steps on that frame's own final reservoirs, enqueued on the view's stream after
+ * shading, so the frame's time includes them. 0 turns it off. */
+int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame);
+/* Test hook for the device error path (no reference counterpart): on = 1 makes the
+ * tcgen05 inference issue no MMA and give each tensor-core wait 64 tries, so every wait
+ * runs out with nothing in flight; the kernel raises error flag 16, skips its remaining
+ * tiles, frees its tensor memory and returns, the candidate stage falls back to uniform
+ * candidates for the entries it did not write, and vxr_view_wait reports VXR_E_DEVICE.
+ * on = 0 restores normal operation. */
+int vxr_view_proposal_test_timeout(vxr_view* v, int on);
 int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden);
 int vxr_view_proposal_get_params(vxr_view* v, float* out);
 int vxr_view_proposal_set_params(vxr_view* v, const float* in);
@@ -458,6 +474,8 @@ typedef struct vxr_tuning {
     uint32_t list_blocks_per_sm;   /* hit-list kernels (candidates, temporal, shading requests): blocks per SM (1..64) */
     uint32_t occupancy;            /* 1: shadow tracer and candidate kernels capped in registers for more warps per SM */
     uint32_t shadow_schedule;      /* shadow tracer: 0 every lane steps each round, 1 only the lanes at the DDA level most lanes are at */
+    uint32_t shadow_early_out;     /* shadow tracer: 1 stops a walk, as occluded, once its step budget cannot reach the emitter */
+    uint32_t brick_cache;          /* shadow tracer: bricks whose opacity masks each CTA keeps in shared memory (0 off, 128..2048 a power of two) */
 } vxr_tuning;
 int vxr_default_tuning(vxr_tuning* t);
 /* Current CUDA device: name (NUL-terminated, truncated to n bytes), SM count and compute

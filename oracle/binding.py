@@ -215,6 +215,69 @@ def load_ref():
     return lib
 
 
+class SceneDesc(C.Structure):
+    """vxr_scene_desc (include/vxr.h)."""
+    _fields_ = [("extent", C.c_uint32), ("seed", C.c_uint32), ("octaves", C.c_uint32), ("base_freq", C.c_float),
+                ("gain", C.c_float), ("height_base", C.c_float), ("height_amp", C.c_float),
+                ("albedo_lo", C.c_float), ("albedo_hi", C.c_float), ("cave_threshold", C.c_float),
+                ("emitters", C.c_uint32), ("emitter_mode", C.c_uint32), ("radiance_lo", C.c_float),
+                ("radiance_hi", C.c_float), ("blob_count", C.c_uint32), ("blob_sigma", C.c_float),
+                ("blob_fraction", C.c_float), ("layer_lo", C.c_uint32), ("layer_hi", C.c_uint32),
+                ("scatter_fraction", C.c_float)]
+
+
+_scene = None
+
+
+def load_scene_host():
+    """oracle/scene_host.cpp + the project's host scene generator (no CUDA library)."""
+    global _scene
+    if _scene is not None:
+        return _scene
+    from . import build as B  # noqa: PLC0415
+    lib = C.CDLL(B.build_scene_host())
+    sig = {"osh_preset": (C.c_int, [C.c_int, C.POINTER(SceneDesc)]),
+           "osh_generate": (_P, [C.POINTER(SceneDesc)]),
+           "osh_sizes": (None, [_P, _U32P, _U32P]), "osh_copy": (None, [_P, _P, _P, _P]),
+           "osh_camera_path": (C.c_int, [C.POINTER(SceneDesc), C.c_uint32, C.c_uint32, C.c_uint32, _F, _F]),
+           "osh_free": (None, [_P])}
+    for n, (res, args) in sig.items():
+        f = getattr(lib, n)
+        f.restype = res
+        f.argtypes = args
+    _scene = lib
+    return lib
+
+
+class HostScene:
+    """A benchmark scene (vxr_scene_preset(config)) generated on the host without the CUDA
+    library: grid, bricks and lights as numpy arrays, and the seeded camera path."""
+
+    def __init__(self, config):
+        lib = load_scene_host()
+        self.desc = SceneDesc()
+        if lib.osh_preset(config, C.byref(self.desc)) != 0:
+            raise ValueError(f"unknown scene configuration {config}")
+        h = lib.osh_generate(C.byref(self.desc))
+        if not h:
+            raise RuntimeError("scene generation failed")
+        try:
+            nb, nl = C.c_uint32(), C.c_uint32()
+            lib.osh_sizes(h, C.byref(nb), C.byref(nl))
+            self.grid = np.zeros(128 ** 3, np.uint32)
+            self.bricks = np.zeros((max(nb.value, 1), 512), np.uint32)
+            self.lights = np.zeros(nl.value, LIGHT_DTYPE)
+            lib.osh_copy(h, self.grid.ctypes.data, self.bricks.ctypes.data, self.lights.ctypes.data)
+        finally:
+            lib.osh_free(h)
+
+    def camera_path(self, seed, f, n):
+        p, t = (C.c_float * 3)(), (C.c_float * 3)()
+        if load_scene_host().osh_camera_path(C.byref(self.desc), seed, f, n, p, t) != 0:
+            raise ValueError("camera_path: bad arguments")
+        return list(p), list(t)
+
+
 class WorldArrays:
     """grid / uber / bricks / lights kept alive as numpy arrays for the oracles."""
 

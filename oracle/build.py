@@ -37,6 +37,33 @@ def build_port(force=False):
     return LIBORC
 
 
+LIBSCENE = os.path.join(BUILD, "libscenehost.so")
+
+
+def build_scene_host(force=False):
+    """The project's scene generator (host C++ only) behind oracle/scene_host.cpp, for the
+    reference arm of the benchmark: the same scenes without the CUDA library."""
+    os.makedirs(BUILD, exist_ok=True)
+    csrc = os.path.join(ROOT, "smallproject_gb300", "csrc")
+    srcs = [os.path.join(HERE, "scene_host.cpp"), os.path.join(csrc, "world.cpp"), os.path.join(csrc, "scene.cpp")]
+    deps = srcs + [os.path.join(csrc, "world.hpp"), os.path.join(ROOT, "include", "vxr.h")]
+    h = hashlib.sha256()
+    for s in deps:
+        h.update(open(s, "rb").read())
+    stamp = os.path.join(BUILD, "libscenehost.stamp")
+    if not force and os.path.exists(LIBSCENE) and os.path.exists(stamp) and open(stamp).read() == h.hexdigest():
+        return LIBSCENE
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-I" + os.path.join(ROOT, "include"), "-I" + csrc, *srcs, "-o", LIBSCENE + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("scene host build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    os.replace(LIBSCENE + ".tmp", LIBSCENE)
+    with open(stamp, "w") as f:
+        f.write(h.hexdigest())
+    return LIBSCENE
+
+
 def build_ref(force=False):
     """Returns the reference-oracle library path, or None when it cannot be built here."""
     import importlib.util
@@ -66,6 +93,7 @@ def build_ogt():
 
 def build_all(force=False):
     port = build_port(force)
+    build_scene_host(force)
     try:
         ref = build_ref(force)
     except RuntimeError:

@@ -81,13 +81,35 @@ def forward(params, samples, H, K, table_log2=16, res0=32, res1=128):
     return (L, P, X, cs, H1, H2, H3, Z)
 
 
+def bf16(x):
+    """Round to the nearest BF16 value, ties to even (cvt.rn.bf16.f32), as float64."""
+    x = np.asarray(x, np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
 def softmax(Z):
     e = np.exp(Z - Z.max(axis=1, keepdims=True))
     return e / e.sum(axis=1, keepdims=True)
 
 
-def loss_and_grad(params, samples, target, weight, H, K, table_log2=16, res0=32, res1=128):
+def loss_and_grad(params, samples, target, weight, H, K, table_log2=16, res0=32, res1=128, bf16_operands=False):
+    """Weighted softmax cross-entropy and its gradient in FP64. bf16_operands=True rounds
+    every tensor-core operand to BF16 where the tensor-core training step rounds it (the
+    network input, the four weight matrices, the three hidden activations, dZ, dH3, dH2,
+    dH1), so the result is the gradient of the BF16 network that step differentiates."""
     L, P, X, cs, H1, H2, H3, Z = forward(params, samples, H, K, table_log2, res0, res1)
+    r = bf16 if bf16_operands else (lambda a: a)
+    if bf16_operands:
+        X = r(X)
+        P = dict(P)
+        for n in ("W1", "W2", "W3", "W4"):
+            P[n] = r(P[n])
+        H1 = r(np.maximum(X @ P["W1"].T + P["b1"], 0))
+        H2 = r(np.maximum(H1 @ P["W2"].T + P["b2"], 0))
+        H3 = r(np.maximum(H2 @ P["W3"].T + P["b3"], 0))
+        Z = H3 @ P["W4"].T + P["b4"]
     w = np.asarray(weight, np.float64)
     t = np.asarray(target, np.int64)
     ws = w.sum()
@@ -99,15 +121,16 @@ def loss_and_grad(params, samples, target, weight, H, K, table_log2=16, res0=32,
     dZ[np.arange(B), t] -= 1.0
     dZ *= wn[:, None]
     g = {}
+    dZ = r(dZ)
     g["W4"] = dZ.T @ H3
     g["b4"] = dZ.sum(0)
-    dH3 = (dZ @ P["W4"]) * (H3 > 0)
+    dH3 = r((dZ @ P["W4"]) * (H3 > 0))
     g["W3"] = dH3.T @ H2
     g["b3"] = dH3.sum(0)
-    dH2 = (dH3 @ P["W3"]) * (H2 > 0)
+    dH2 = r((dH3 @ P["W3"]) * (H2 > 0))
     g["W2"] = dH2.T @ H1
     g["b2"] = dH2.sum(0)
-    dH1 = (dH2 @ P["W2"]) * (H1 > 0)
+    dH1 = r((dH2 @ P["W2"]) * (H1 > 0))
     g["W1"] = dH1.T @ X
     g["b1"] = dH1.sum(0)
     dX = dH1 @ P["W1"]

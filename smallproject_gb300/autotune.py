@@ -31,6 +31,8 @@ SPACE = [
     ("list_blocks_per_sm", [4, 8, 16, 32]),
     ("occupancy", [0, 1]),
     ("shadow_schedule", [0, 1]),
+    ("shadow_early_out", [0, 1]),
+    ("brick_cache", [0, 256, 1024]),
 ]
 
 
@@ -62,15 +64,16 @@ def config_key(world, desc):
 def _to_tuning(d):
     t = _v.tuning()
     t.tile_x, t.tile_y = d["tile"]
-    for k in ("persistent", "shadow_refill", "shadow_burst", "list_blocks_per_sm", "occupancy", "shadow_schedule"):
-        setattr(t, k, d[k])
+    for k in ("persistent", "shadow_refill", "shadow_burst", "list_blocks_per_sm", "occupancy", "shadow_schedule",
+              "shadow_early_out", "brick_cache"):
+        setattr(t, k, d.get(k, getattr(t, k)))
     return t
 
 
 def _from_tuning(t):
     return {"tile": (t.tile_x, t.tile_y), "persistent": t.persistent, "shadow_refill": t.shadow_refill,
             "shadow_burst": t.shadow_burst, "list_blocks_per_sm": t.list_blocks_per_sm, "occupancy": t.occupancy,
-            "shadow_schedule": t.shadow_schedule}
+            "shadow_schedule": t.shadow_schedule, "shadow_early_out": t.shadow_early_out, "brick_cache": t.brick_cache}
 
 
 def time_view(view, t, cams, frames, start=0):

@@ -18,12 +18,12 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvxr.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["kernels.cu", "runtime.cu", "batch.cu", "noalloc.cu", "proposal.cu", "proposal_api.cu"]
+CU_SOURCES = ["kernels.cu", "runtime.cu", "batch.cu", "noalloc.cu", "proposal.cu", "proposal_api.cu", "train.cu"]
 CPP_SOURCES = ["world.cpp", "scene.cpp", "camera.cpp", "capi_world.cpp", "cluster.cpp", "sky.cpp"]
-HEADERS = ["device.cuh", "kernels.hpp", "world.hpp", "camera.hpp", "internal.hpp", "proposal.cuh", "proposal.hpp", "view.hpp"]
+HEADERS = ["device.cuh", "kernels.hpp", "world.hpp", "camera.hpp", "internal.hpp", "proposal.cuh", "proposal.hpp", "proposal_dev.cuh", "view.hpp"]
 
 # the learned proposal is checked with tolerances, not bit for bit: FMA contraction on
-FMA_SOURCES = {"proposal.cu"}
+FMA_SOURCES = {"proposal.cu", "train.cu"}
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -33,6 +33,14 @@ struct World {
     const float4* __restrict__ lgeom;
     const float4* __restrict__ lemit;
     uint32_t nlights;
+    // shadow tracer's brick cache (walk_step<1> only): an open-addressed table of 2^bcLog2
+    // keys (brick << 11 | slot, kNoKey empty) and per slot the brick's 512-bit opacity mask
+    // (16 words), both in shared memory; bcCount (calibration, global): per brick the
+    // number of brick walks, or null
+    const uint32_t* bcKeys = nullptr;
+    const uint32_t* bcMask = nullptr;
+    uint32_t* bcCount = nullptr;
+    int bcLog2 = 0;
 };
 
 // Sky dome in device memory: World::LoadSky / UpdateSkylights (world.cpp:803-923) and
@@ -448,21 +456,48 @@ struct Walker {
     int stx, sty, stz;             // axis steps (+-1)
     float dist;                    // result
     uint32_t side, voxel;
+    uint32_t tlo, thi;             // grid cells (x | y << 10 | z << 20) of the cube a shadow ray must reach
+    int guard;                     // the early-out is tested while steps < guard (0: no target)
+    int cslot;                     // brick-cache slot of the current brick, or -1 (walk_step<1>)
     __device__ __forceinline__ int ox() const { return stx > 0 ? 1 : 0; }
     __device__ __forceinline__ int oy() const { return sty > 0 ? 1 : 0; }
     __device__ __forceinline__ int oz() const { return stz > 0 ? 1 : 0; }
 };
 enum : int { WALK_CONTINUE = 0, WALK_HIT = 1, WALK_MISS = 2 };
 constexpr int kWalkNoCap = 1 << 30;   // cnt above the brick level: never runs out
+constexpr uint32_t kNoTarget = 0xFFFFFFFFu;
 
-// value of the current cell at the current level
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
+
+// value of the current cell at the current level; CACHE: a voxel of a cached brick is
+// read from its opacity mask as 0xF000 (opaque) or 0 - all a shadow ray's walk reads of it
+// (the hit test; the voxel value of a shadow hit is never used)
+template <int CACHE = 0>
 __device__ __forceinline__ void walk_load(Walker& k, const World& w) {
-    if (k.level == 0)
+    if (k.level == 0) {
         k.o = __ldg(w.uber + k.cx + k.cz * 32 + k.cy * 1024);
-    else if (k.level == 1)
+    } else if (k.level == 1) {
         k.o = __ldg(w.grid + k.cx + k.cz * 128 + k.cy * 16384);
-    else
-        k.o = __ldg(w.bricks + (size_t)k.brick * 512u + (uint32_t)((k.cx & 7) | ((k.cy & 7) << 3) | ((k.cz & 7) << 6)));
+    } else {
+        const uint32_t vi = (uint32_t)((k.cx & 7) | ((k.cy & 7) << 3) | ((k.cz & 7) << 6));
+        if (CACHE && k.cslot >= 0)
+            k.o = ((w.bcMask[k.cslot * 16 + (vi >> 5)] >> (vi & 31u)) & 1u) ? 0xF000u : 0u;
+        else
+            k.o = __ldg(w.bricks + (size_t)k.brick * 512u + vi);
+    }
+}
+
+// slot of `brick` in the brick cache, or -1 (at most 4 probes)
+__device__ __forceinline__ int brick_cache_slot(const World& w, uint32_t brick) {
+    const uint32_t n = 1u << w.bcLog2;
+    uint32_t h = (brick * 2654435761u) >> (32 - w.bcLog2);
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+        const uint32_t key = w.bcKeys[(h + p) & (n - 1u)];
+        if ((key >> 11) == brick && key != kNoKey) return (int)(key & 2047u);
+        if (key == kNoKey) return -1;
+    }
+    return -1;
 }
 
 // TraceOpaqueRay prologue (trace.cl:219-243); returns WALK_MISS when the ray misses the map
@@ -509,21 +544,69 @@ __device__ __forceinline__ int walk_init(Walker& k, const World& w, float ax, fl
     k.steps = steps;
     k.level = 0;
     k.cnt = kWalkNoCap;
+    k.tlo = k.thi = kNoTarget;
+    k.guard = 0;
+    k.cslot = -1;
     walk_load(k, w);
     return WALK_CONTINUE;
+}
+
+// Visibility early-out for a shadow ray towards the emitter cube [pos, pos + size)
+// (packed x + z * 1024 + y * 1024^2, the Light record). Every uber-cell visit costs 4 of
+// the step budget and moves the walk at most 4 grid cells along each axis; every grid-cell
+// visit costs 1 and moves it at most 1 (brick walks cost nothing and stay in their grid
+// cell; a brick exit is followed by a grid visit). So once the budget left after a visit
+// is below the Chebyshev distance, in grid cells, between the current cell and the cube's
+// cells, no cell within one grid cell of the cube can be visited before the budget runs
+// out: the walk cannot hit the cube, nor a voxel whose rounded hit point could fall in it,
+// and ends as occluded whichever way it ends. The walk then stops as a miss, which the
+// visibility test reads as occluded (the origin is outside the cube: its cell is at least
+// one grid cell away, or the distance would be 0).
+// The ray heads for a point on the cube, so along each axis its grid cell approaches the
+// cube's cells until it gets there: the distance never exceeds the one of the starting
+// grid cell, and the test can wait until the budget drops below that (`guard`; the test
+// itself is exact whatever guard holds).
+__device__ __forceinline__ void walk_target(Walker& k, uint32_t pos, uint32_t size) {
+    const uint32_t ex = pos % 1024u, ez = (pos / 1024u) % 1024u, ey = pos / (1024u * 1024u);
+    const uint32_t s1 = size > 0u ? size - 1u : 0u;
+    const int lx = (int)(ex >> 3), ly = (int)(ey >> 3), lz = (int)(ez >> 3);
+    const int hx = (int)(min(ex + s1, 1023u) >> 3), hy = (int)(min(ey + s1, 1023u) >> 3), hz = (int)(min(ez + s1, 1023u) >> 3);
+    k.tlo = (uint32_t)lx | ((uint32_t)ly << 10) | ((uint32_t)lz << 20);
+    k.thi = (uint32_t)hx | ((uint32_t)hy << 10) | ((uint32_t)hz << 20);
+    const int gx = (int)min(f2u(k.ax) >> 3, 127u), gy = (int)min(f2u(k.ay) >> 3, 127u), gz = (int)min(f2u(k.az) >> 3, 127u);
+    const int dx = max(max(lx - gx, gx - hx), 0), dy = max(max(ly - gy, gy - hy), 0), dz = max(max(lz - gz, gz - hz), 0);
+    k.guard = max(dx, max(dy, dz)) + 1;
+}
+
+// Chebyshev distance in grid cells between the current cell (level 0: its 4^3 grid cells)
+// and the target cube's grid cells
+__device__ __forceinline__ int walk_target_distance(const Walker& k) {
+    const int s2 = k.level == 0 ? 2 : 0, span = (1 << s2) - 1;
+    const int lx = k.cx << s2, ly = k.cy << s2, lz = k.cz << s2;
+    const int dx = max(max((int)(k.tlo & 1023u) - (lx + span), lx - (int)(k.thi & 1023u)), 0);
+    const int dy = max(max((int)((k.tlo >> 10) & 1023u) - (ly + span), ly - (int)((k.thi >> 10) & 1023u)), 0);
+    const int dz = max(max((int)(k.tlo >> 20) - (lz + span), lz - (int)(k.thi >> 20)), 0);
+    return max(dx, max(dy, dz));
 }
 
 // One cell visit at the current level, then one action: the hit or the budget miss,
 // a descent into the cell (uber -> grid, trace.cl:262-273; grid -> brick, GRIDSTEP,
 // trace.cl:85-104), or a DDA step (BRICKSTEP / GRIDSTEP tail / uber loop,
 // trace.cl:66-80, 105-110, 274-279) that climbs a level each time it leaves the parent
-// cell and ends as a miss when it leaves the map.
+// cell and ends as a miss when it leaves the map. FLAGS (shadow tracer options, 0 for the
+// plain walk): kWalkCache - brick walks count into w.bcCount when it is set, and read cached
+// bricks' opacity masks from w.bcKeys / w.bcMask when bcLog2 > 0; kWalkEarly - the
+// visibility early-out of walk_target.
+constexpr int kWalkCache = 1, kWalkEarly = 2;
+template <int FLAGS = 0>
 __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
+    constexpr int CACHE = FLAGS & kWalkCache;
     const int lv = k.level;
     // a grid step with the budget exhausted always ends as a miss (the uber loop
     // re-checks the budget before any further cell is visited)
     k.steps -= lv == 0 ? 4 : (lv == 1 ? 1 : 0);
     if (lv < 2 && k.steps <= 0) return WALK_MISS;
+    if ((FLAGS & kWalkEarly) && lv < 2 && k.steps < k.guard && k.steps < walk_target_distance(k)) return WALK_MISS;
     // uber: descend into a non-empty cell; grid: descend into a brick, hit an opaque
     // brick-less cell; brick: hit an opaque voxel
     const uint32_t hv = lv == 1 ? k.o >> 1 : k.o;
@@ -552,6 +635,10 @@ __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
             k.gmx = k.tmx; k.gmy = k.tmy; k.gmz = k.tmz;
             k.gx = k.cx; k.gy = k.cy; k.gz = k.cz;
             k.brick = k.o >> 1;
+            if (CACHE) {
+                if (w.bcCount) atomicAdd(w.bcCount + k.brick, 1u);
+                k.cslot = w.bcLog2 > 0 ? brick_cache_slot(w, k.brick) : -1;
+            }
         }
         k.t *= S;
         const uint32_t qx = f2u(K * k.ax + k.vx * k.t), qy = f2u(K * k.ay + k.vy * k.t),
@@ -593,7 +680,7 @@ __device__ __forceinline__ int walk_step(Walker& k, const World& w) {
             k.level--;
         }
     }
-    walk_load(k, w);
+    walk_load<CACHE>(k, w);
     return WALK_CONTINUE;
 }
 

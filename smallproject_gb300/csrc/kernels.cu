@@ -428,7 +428,8 @@ __device__ __forceinline__ float phat(float3 pos, uint32_t ncode, float3 sp, uin
 // truncated) lies in the emitter cube [pos, pos + size) (GridCoordinatesFromHit /
 // Uint3CubeEquals, tools.cl:452-472). An occluded request zeroes sumOfWeights of its
 // pixel in reservoir plane C (plane 0) or H (plane 1) of its view (W follows:
-// ris.cl:79-80, 248-250). Lanes refill from the queue as soon as enough are idle.
+// ris.cl:79-80, 248-250). Lanes refill from the queue as soon as enough are idle. A walk
+// stops early, as occluded, once its budget cannot reach the emitter (walk_target).
 __device__ __forceinline__ void shadow_finish(const World& w, int st, const Walker& wk, float3 o, float3 L, uint32_t* plane,
                                               uint32_t pix, uint32_t li) {
     const float d2 = st == WALK_HIT ? wk.dist : 0.0f;
@@ -447,16 +448,36 @@ __device__ __forceinline__ void shadow_finish(const World& w, int st, const Walk
 
 // MINB > 0 caps registers so that MINB blocks of 128 threads fit on an SM (more warps to
 // hide L2 latency, at the price of a few spills); chosen by the launch tuning.
-template <int VARIANT, int MINB>
-__global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant__ BatchDev bd, int countIdx, int fetchIdx,
-                                                     int planeSel) {
+// CACHE = 1 (single views): blocks of 512 threads, brick walks through the cache walk: with
+// a brick cache (bd.bcLog2 > 0) every block first copies the table and the opacity masks
+// into shared memory; with bd.bcCount set they count brick walks (calibration).
+// EARLY = 1: walks stop as occluded once their budget cannot reach the emitter.
+template <int VARIANT, int MINB, int CACHE, int EARLY>
+__global__ void __launch_bounds__(CACHE ? 512 : 128, CACHE ? 1 : MINB) shadow_kernel(const __grid_constant__ BatchDev bd,
+                                                                                    int countIdx, int fetchIdx,
+                                                                                    int planeSel) {
     const int refill = bd.refill, burst = bd.burst, schedule = bd.schedule;
     const uint32_t n = bd.counters[countIdx];
     uint32_t* fetch = bd.counters + fetchIdx;
     const int lane = threadIdx.x & 31;
     Walker wk;
     World wt;   // a table batch: the world of this lane's ray; one view: the parameter's
-    const World& w = VARIANT < 2 ? bd.one.w : wt;
+    if (CACHE) {
+        extern __shared__ __align__(16) uint32_t bcs[];
+        wt = bd.one.w;
+        wt.bcCount = bd.bcCount;
+        wt.bcLog2 = bd.bcLog2;
+        if (bd.bcLog2 > 0) {
+            const uint32_t nk = 1u << bd.bcLog2, nm = (nk >> 1) * 16u;
+            for (uint32_t i = threadIdx.x; i < nk; i += blockDim.x) bcs[i] = __ldg(bd.bcKeys + i);
+            for (uint32_t i = threadIdx.x; i < nm / 4u; i += blockDim.x)
+                reinterpret_cast<uint4*>(bcs + nk)[i] = __ldg(reinterpret_cast<const uint4*>(bd.bcMask) + i);
+            wt.bcKeys = bcs;
+            wt.bcMask = bcs + nk;
+        }
+        __syncthreads();
+    }
+    const World& w = (VARIANT < 2 && !CACHE) ? bd.one.w : wt;
     uint32_t* plane = nullptr;
     bool active = false, exhausted = false;
     float3 o = f3(0.0f, 0.0f, 0.0f), L = f3(0.0f, 0.0f, 0.0f);
@@ -481,8 +502,13 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
                     if (VARIANT == 2) wt = V->w;
                     plane = reinterpret_cast<uint32_t*>(planeSel ? V->b.hA : V->b.cA);
                     const int st = walk_init(wk, w, o.x, o.y, o.z, L.x, L.y, L.z, 128);
-                    if (st == WALK_CONTINUE) active = true;
-                    else shadow_finish(w, st, wk, o, L, plane, pix, li);
+                    if (st == WALK_CONTINUE) {
+                        if (EARLY)
+                            walk_target(wk, __float_as_uint(__ldg(&w.lemit[li].w)), (uint32_t)__ldg(&w.lgeom[li].w));
+                        active = true;
+                    } else {
+                        shadow_finish(w, st, wk, o, L, plane, pix, li);
+                    }
                 }
             }
         }
@@ -502,7 +528,7 @@ __global__ void __launch_bounds__(128, MINB) shadow_kernel(const __grid_constant
         if (active && (sel < 0 || wk.level == sel)) {
 #pragma unroll 1
             for (int s = 0; s < burst; s++) {
-                const int st = walk_step(wk, w);
+                const int st = walk_step<(CACHE ? kWalkCache : 0) | (EARLY ? kWalkEarly : 0)>(wk, w);
                 if (st != WALK_CONTINUE) {
                     shadow_finish(w, st, wk, o, L, plane, pix, li);
                     active = false;
@@ -549,6 +575,12 @@ __device__ __forceinline__ void ris_item(const BatchDev& bd, const ViewDev* V, u
             const uint2 cq = __ldg(V->ll.cand + (size_t)c * V->ll.stride + j);
             li = (int)cq.x;
             p = __uint_as_float(cq.y);
+            // an entry the inference did not write (it gave up and raised its error flag):
+            // a uniform candidate instead, so no index leaves the light table
+            if (cq.x >= nL || !(p > 0.0f && p <= 1.0f)) {
+                li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
+                p = puni;
+            }
         } else {
             // GenerateLightCandidate (tools.cl:593-598)
             li = min(max(f2i(rnd(seed) * (float)nL), 0), (int)nL - 1);
@@ -1014,6 +1046,7 @@ void apply_tuning(BatchDev& bd, const Tuning& tu) {
     bd.listPerSm = tu.listPerSm;
     bd.occupancy = tu.occupancy;
     bd.schedule = tu.schedule;
+    bd.earlyOut = tu.earlyOut;
 }
 
 BatchDev single_batch(const dev::World& w, const dev::Frame& k, const ViewBuffers& b, int cur, bool point, const Tuning& tu) {
@@ -1072,17 +1105,40 @@ void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s) {
     else launch_tiles(dev::albedo_kernel<0>, bd, kCtrAlbedo, s, K_ALBEDO);
 }
 
-template <int VARIANT, int MINB>
+template <int VARIANT, int MINB, int EARLY>
 static void launch_shadow_k(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
-    const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT, MINB>, 128);
+    const size_t rb = resident_blocks((const void*)dev::shadow_kernel<VARIANT, MINB, 0, EARLY>, 128);
     const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 127) / 128));
     Timed tm(bd, planeSel ? K_SHADOW_SHADE : K_SHADOW_CAND, s);
-    dev::shadow_kernel<VARIANT, MINB><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel);
+    dev::shadow_kernel<VARIANT, MINB, 0, EARLY><<<nb, 128, 0, s>>>(bd, countIdx, countIdx + 1, planeSel);
+}
+// shared memory of the brick-cache variant: 2^log2 keys and 2^(log2 - 1) masks of 64 bytes
+size_t brick_cache_smem(int log2) { return log2 > 0 ? ((size_t)4 << log2) + ((size_t)64 << (log2 - 1)) : 0; }
+template <int EARLY>
+static void launch_shadow_cached(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
+    const void* fn = (const void*)dev::shadow_kernel<0, 0, 1, EARLY>;
+    const size_t sm = brick_cache_smem(bd.bcLog2);
+    if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 512, sm);
+    const size_t rb = (size_t)std::max(per, 1) * (size_t)sm_count();
+    const unsigned nb = (unsigned)std::max<size_t>(1, std::min<size_t>(rb, ((size_t)bd.totalPixels + 511) / 512));
+    Timed tm(bd, planeSel ? K_SHADOW_SHADE : K_SHADOW_CAND, s);
+    dev::shadow_kernel<0, 0, 1, EARLY><<<nb, 512, sm, s>>>(bd, countIdx, countIdx + 1, planeSel);
 }
 template <int VARIANT>
 static void launch_shadow(const BatchDev& bd, int countIdx, int planeSel, cudaStream_t s) {
-    if (bd.occupancy) launch_shadow_k<VARIANT, 8>(bd, countIdx, planeSel, s);
-    else launch_shadow_k<VARIANT, 0>(bd, countIdx, planeSel, s);
+    const bool early = bd.earlyOut != 0;
+    if (VARIANT < 2 && (bd.bcLog2 > 0 || bd.bcCount)) {
+        if (early) launch_shadow_cached<1>(bd, countIdx, planeSel, s);
+        else launch_shadow_cached<0>(bd, countIdx, planeSel, s);
+    } else if (bd.occupancy) {
+        if (early) launch_shadow_k<VARIANT, 8, 1>(bd, countIdx, planeSel, s);
+        else launch_shadow_k<VARIANT, 8, 0>(bd, countIdx, planeSel, s);
+    } else {
+        if (early) launch_shadow_k<VARIANT, 0, 1>(bd, countIdx, planeSel, s);
+        else launch_shadow_k<VARIANT, 0, 0>(bd, countIdx, planeSel, s);
+    }
 }
 template <int VARIANT, bool LEARNED>
 static void launch_ris(const BatchDev& bd, unsigned nb, cudaStream_t s) {

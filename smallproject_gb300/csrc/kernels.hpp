@@ -59,7 +59,7 @@ struct ViewDev {
 // with mark(id, false, s) / mark(id, true, s) when a timer is attached (runtime.cu).
 enum KernelId : int {
     K_ALBEDO = 0, K_COMPACT, K_INFER, K_RIS, K_SHADOW_CAND, K_TEMPORAL, K_SPATIAL, K_SHADE_REQ, K_SHADOW_SHADE,
-    K_SHADE_FINISH, K_ACCUM, K_COUNT
+    K_SHADE_FINISH, K_ACCUM, K_TRAIN, K_COUNT
 };
 struct KernelTimer {
     virtual void mark(int id, bool end, cudaStream_t s) = 0;
@@ -84,6 +84,13 @@ struct BatchDev {
     int listPerSm = 16;                   // blocks per SM of the hit-list kernels
     int occupancy = 0;                    // 1: register-capped shadow / RIS kernels (more warps per SM)
     int schedule = 0;                     // shadow tracer: 1 = one DDA level per round (the majority's)
+    int earlyOut = 0;                     // shadow tracer: stop a walk once its budget cannot reach the emitter
+    // shadow tracer's brick cache (single views): the table (global; each CTA copies it
+    // into shared memory) when bcLog2 > 0, and per-brick walk counts (calibration) or null
+    const uint32_t* bcKeys = nullptr;
+    const uint32_t* bcMask = nullptr;
+    uint32_t* bcCount = nullptr;
+    int bcLog2 = 0;
     int fuse = 0;                         // shading also accumulates
     int sky = 0;                          // some view has a sky dome (shading runs its variant)
     uint32_t* hits = nullptr;             // hit list over all views
@@ -102,8 +109,11 @@ struct Tuning {
     int listPerSm = 16;
     int occupancy = 0;
     int schedule = 0;
+    int earlyOut = 0;
+    int brickCache = 0;
 };
 
+size_t brick_cache_smem(int log2);   // shared memory of the shadow tracer's brick-cache variant
 void launch_build_light_table(const uint4* raw, uint32_t n, float4* geom, float4* emit, cudaStream_t s);
 void launch_build_uber(const uint32_t* grid, uint8_t* uber, cudaStream_t s);
 void launch_build_brick_boxes(const uint32_t* bricks, const uint32_t* list, uint32_t n, uint32_t* bbox, uint32_t* bbox0,

@@ -27,6 +27,8 @@ struct InferArgs {
     uint32_t candStride;              // hits per candidate row of `cand`
     uint2* cand;                      // out: [candidate][candStride] (emitter, bits(p_src))
     uint32_t* err;                    // device error flags (16: a tensor-core wait gave up)
+    uint32_t waitLimit;               // tries of each in-loop tensor-core wait (0: the full limit)
+    uint32_t skipMma;                 // test only: issue no MMA, so every wait runs out with nothing in flight
     // sample mode (tests): explicit inputs (x, y, z, bits(side code)) and softmax output
     const float4* samples;
     uint32_t n;
@@ -62,6 +64,62 @@ struct GemmArgs {
     int mode;     // 0 store, 1 +bias relu, 2 +bias, 3 masked by mask > 0, 4 atomic add
     long kchunk;  // split-K chunk (mode 4); 0 = whole K
 };
+
+// fused training step on the tensor cores (train.cu), hidden 64 and 16 <= K <= 256
+constexpr int kTrainWarpBytes = 16 * (kIn + 8) * 2 + 16 * (64 + 8) * 2 + 16 * 16 * 4;   // X, H1, dX per warp
+
+struct TrainArgs {
+    Dims dims;
+    Layout L;
+    const float* params;              // FP32 master (hash tables, biases)
+    const __nv_bfloat16* wbf;         // BF16 W1 | W2 | W3 | W4
+    const float4* samples;            // batch: (x, y, z, bits(side code))
+    const uint32_t* target;           // cluster of the selected emitter
+    const float* weight;              // W * pHat (0: no contribution)
+    const float* wpart;               // weight sums per wsum block
+    uint32_t nwpart;
+    uint32_t B;
+    float* grads;                     // full gradient vector; the hash-table part must be zero
+    uint4* frag;                      // weight-gradient operands as mma fragments (train_frag_bytes)
+    float* partials;                  // [chunk][MLP parameters] gradient sums
+    float* lossPart;                  // [CTA] loss sums
+};
+
+struct WgradArgs {
+    const uint4* frag;
+    uint32_t ntiles, chunkTiles;
+    int K, nmlp;
+    float* partials;
+};
+
+struct ReduceArgs {
+    const float* partials;
+    int nparts, nmlp, K;              // rows of the partial-gradient table
+    const float* lossPart;
+    int nloss;                        // entries of lossPart
+    const float* wpart;
+    uint32_t nwpart;
+    float* grads;                     // grads + L.W1
+    float* params;                    // params + L.W1
+    float* m;
+    float* v;
+    __nv_bfloat16* wbf;
+    int apply;                        // 0: gradients only (no update)
+    float lr, b1, b2, eps, c1, c2;
+    float* scal;                      // out: [loss, weight sum]
+};
+
+bool train_supported(const Dims& d);
+int train_mlp_count(const Dims& d);
+size_t train_smem_bytes(const Dims& d);
+size_t train_frag_bytes(const Dims& d, uint32_t B);
+uint32_t train_chunks(uint32_t B);   // rows of the partial-gradient table for a batch of B
+int train_max_ctas();
+uint32_t train_wsum_blocks();
+void launch_wsum(const float* w, uint32_t B, float* part, cudaStream_t s);
+cudaError_t launch_train(const TrainArgs& a, cudaStream_t s, int* nparts, int* nloss);
+void launch_train_reduce(const ReduceArgs& r, cudaStream_t s);
+void launch_adam_enc(float* p, float* g, float* m, float* v, size_t n, float lr, int step, cudaStream_t s);
 
 size_t infer_smem_bytes(const Dims& d);
 bool infer_supported(const Dims& d);

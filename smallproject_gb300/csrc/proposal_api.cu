@@ -43,6 +43,16 @@ struct Proposal {
     float* dB = nullptr;
     float* dX = nullptr;
     float* scal = nullptr;         // [loss, wsum]
+    // fused tensor-core step (train.cu)
+    bool fused = false;            // training on the tensor cores (else the FP32 layered trainer)
+    uint32_t fusedB = 0;           // batch size the fused buffers hold
+    uint4* frag = nullptr;         // weight-gradient operands as mma fragments
+    float* partials = nullptr;     // [chunk][MLP parameters] gradient sums
+    float* lossPart = nullptr;     // [CTA]
+    float* wpart = nullptr;        // weight sums per wsum block
+    bool encGradDirty = true;      // the hash-table gradient is not known to be zero
+    uint32_t online = 0;           // training steps run by every rendered frame
+    bool testTimeout = false;      // test hook: the inference issues no MMA and its waits give up
     int step = 0;
     uint32_t gatherOffset = 0;
 };
@@ -50,7 +60,8 @@ struct Proposal {
 void destroy_proposal(Proposal* p) {
     if (!p) return;
     void* bufs[] = {p->params, p->grads, p->m, p->v, p->wbf, p->clOff, p->clMembers, p->lightCluster, p->cand,
-                    p->samples, p->target, p->weight, p->X, p->H1, p->H2, p->H3, p->Z, p->dA, p->dB, p->dX, p->scal};
+                    p->samples, p->target, p->weight, p->X, p->H1, p->H2, p->H3, p->Z, p->dA, p->dB, p->dX, p->scal,
+                    p->partials, p->lossPart, p->wpart, p->frag};
     for (void* b : bufs) cudaFree(b);
     delete p;
 }
@@ -119,25 +130,138 @@ int upload_clusters(vxr_view* v, vxr::Proposal* p) {
     return VXR_OK;
 }
 
+// batch inputs (samples, targets, weights) for B samples, plus the working buffers of
+// the selected trainer: per-CTA sums (fused) or the layer activations (FP32)
 int ensure_batch(vxr::Proposal* p, uint32_t B) {
     using vxr::prop::kIn;
-    if (B <= p->B) return VXR_OK;
-    void** bufs[] = {(void**)&p->samples, (void**)&p->target, (void**)&p->weight, (void**)&p->X, (void**)&p->H1,
-                     (void**)&p->H2, (void**)&p->H3, (void**)&p->Z, (void**)&p->dA, (void**)&p->dB, (void**)&p->dX};
-    for (void** b : bufs) { cudaFree(*b); *b = nullptr; }
-    const size_t H = p->d.H, K = p->d.K;
-    CUP(cudaMalloc(&p->samples, B * sizeof(float4)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->target, B * sizeof(uint32_t)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->weight, B * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->X, (size_t)B * kIn * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->H1, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->H2, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->H3, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->Z, (size_t)B * K * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->dA, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->dB, (size_t)B * H * sizeof(float)), "cudaMalloc(batch)");
-    CUP(cudaMalloc(&p->dX, (size_t)B * kIn * sizeof(float)), "cudaMalloc(batch)");
-    p->B = B;
+    if (B > p->B) {
+        void** bufs[] = {(void**)&p->samples, (void**)&p->target, (void**)&p->weight, (void**)&p->X, (void**)&p->H1,
+                         (void**)&p->H2, (void**)&p->H3, (void**)&p->Z, (void**)&p->dA, (void**)&p->dB, (void**)&p->dX};
+        for (void** b : bufs) { cudaFree(*b); *b = nullptr; }
+        CUP(cudaMalloc(&p->samples, B * sizeof(float4)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->target, B * sizeof(uint32_t)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->weight, B * sizeof(float)), "cudaMalloc(batch)");
+        p->B = B;
+    }
+    if (p->fused) {
+        if (p->fusedB < p->B) {
+            cudaFree(p->partials);
+            cudaFree(p->frag);
+            p->partials = nullptr;
+            p->frag = nullptr;
+            p->fusedB = 0;
+            const size_t n = (size_t)vxr::prop::train_chunks(p->B) * vxr::prop::train_mlp_count(p->d);
+            CUP(cudaMalloc(&p->partials, n * sizeof(float)), "cudaMalloc(gradient sums)");
+            CUP(cudaMalloc(&p->frag, vxr::prop::train_frag_bytes(p->d, p->B)), "cudaMalloc(gradient operands)");
+            p->fusedB = p->B;
+        }
+        if (!p->lossPart) {
+            CUP(cudaMalloc(&p->lossPart, vxr::prop::train_max_ctas() * sizeof(float)), "cudaMalloc(loss sums)");
+            CUP(cudaMalloc(&p->wpart, vxr::prop::train_wsum_blocks() * sizeof(float)), "cudaMalloc(weight sums)");
+        }
+    } else if (!p->X) {
+        const size_t H = p->d.H, K = p->d.K, n = p->B;
+        CUP(cudaMalloc(&p->X, n * kIn * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->H1, n * H * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->H2, n * H * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->H3, n * H * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->Z, n * K * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->dA, n * H * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->dB, n * H * sizeof(float)), "cudaMalloc(batch)");
+        CUP(cudaMalloc(&p->dX, n * kIn * sizeof(float)), "cudaMalloc(batch)");
+    }
+    return VXR_OK;
+}
+
+void forward_backward(vxr::Proposal* p, uint32_t B, cudaStream_t s);
+
+// One gradient evaluation on the batch in p->samples/target/weight with the fused
+// tensor-core step; apply = 1 also takes the Adam step (and refreshes the BF16 weights),
+// apply = 0 leaves the full gradient in p->grads. [loss, weight sum] land in p->scal.
+int fused_step(vxr::Proposal* p, uint32_t B, bool apply, cudaStream_t s) {
+    using namespace vxr::prop;
+    if (p->encGradDirty) {
+        CUP(cudaMemsetAsync(p->grads + p->L.enc, 0, (size_t)kLevels * p->L.tableSize * kFeat * sizeof(float), s),
+            "clear gradient");
+        p->encGradDirty = false;
+    }
+    launch_wsum(p->weight, B, p->wpart, s);
+    TrainArgs a{};
+    a.dims = p->d;
+    a.L = p->L;
+    a.params = p->params;
+    a.wbf = p->wbf;
+    a.samples = p->samples;
+    a.target = p->target;
+    a.weight = p->weight;
+    a.wpart = p->wpart;
+    a.nwpart = train_wsum_blocks();
+    a.B = B;
+    a.grads = p->grads;
+    a.frag = p->frag;
+    a.partials = p->partials;
+    a.lossPart = p->lossPart;
+    int nparts = 0, nloss = 0;
+    CUP(launch_train(a, s, &nparts, &nloss), "proposal training step");
+    if (apply) p->step++;
+    ReduceArgs r{};
+    r.partials = p->partials;
+    r.nparts = nparts;
+    r.nmlp = train_mlp_count(p->d);
+    r.K = p->d.K;
+    r.lossPart = p->lossPart;
+    r.nloss = nloss;
+    r.wpart = p->wpart;
+    r.nwpart = train_wsum_blocks();
+    r.grads = p->grads + p->L.W1;
+    r.params = p->params + p->L.W1;
+    r.m = p->m + p->L.W1;
+    r.v = p->v + p->L.W1;
+    r.wbf = p->wbf;
+    r.apply = apply ? 1 : 0;
+    r.lr = p->desc.learning_rate;
+    r.b1 = 0.9f;
+    r.b2 = 0.999f;
+    r.eps = 1e-8f;
+    r.c1 = apply ? 1.0f / (1.0f - powf(r.b1, (float)p->step)) : 1.0f;
+    r.c2 = apply ? 1.0f / (1.0f - powf(r.b2, (float)p->step)) : 1.0f;
+    r.scal = p->scal;
+    launch_train_reduce(r, s);
+    if (apply) {
+        launch_adam_enc(p->params + p->L.enc, p->grads + p->L.enc, p->m + p->L.enc, p->v + p->L.enc, p->L.W1 - p->L.enc,
+                        p->desc.learning_rate, p->step, s);
+    } else {
+        p->encGradDirty = true;   // the caller reads the gradient; the next step clears it
+    }
+    CUP(cudaGetLastError(), "proposal training step");
+    return VXR_OK;
+}
+
+// one training step on a batch gathered from the view's current frame
+int train_on_frame(vxr_view* v, vxr::Proposal* p) {
+    const uint32_t B = p->desc.batch;
+    vxr::prop::GatherArgs ga{};
+    ga.k = vxr::dev_frame(v->k);
+    ga.vd = v->buf.vd[v->cur];
+    ga.hits = v->buf.hits;
+    ga.count = v->buf.counters;
+    ga.hA = v->buf.hA;
+    ga.lightCluster = p->lightCluster;
+    ga.nlights = (uint32_t)v->world->w.dev->nl;
+    ga.B = B;
+    ga.offset = p->gatherOffset;
+    ga.samples = p->samples;
+    ga.target = p->target;
+    ga.weight = p->weight;
+    p->gatherOffset = p->gatherOffset * 1664525u + 1013904223u;
+    vxr::prop::launch_gather(ga, v->stream);
+    if (p->fused) return fused_step(p, B, true, v->stream);
+    forward_backward(p, B, v->stream);
+    p->encGradDirty = true;
+    p->step++;
+    vxr::prop::launch_adam(p->params, p->grads, p->m, p->v, p->L.total, p->desc.learning_rate, p->step, v->stream);
+    refresh_bf16(p, v->stream);
+    CUP(cudaGetLastError(), "proposal training");
     return VXR_OK;
 }
 
@@ -203,6 +327,21 @@ void forward_backward(vxr::Proposal* p, uint32_t B, cudaStream_t s) {
 }  // namespace
 
 namespace vxr {
+// the online training steps of a rendered frame (after shading: the frame's final
+// reservoirs), enqueued on the view's stream; nothing when the view samples uniformly
+int proposal_frame_train(vxr_view* v) {
+    Proposal* p = v->prop;
+    if (!v->useProposal || !p || !p->online) return VXR_OK;
+    if (p->clusterVersion != v->world->w.clusterVersion)
+        if (int r = upload_clusters(v, p)) return r;
+    if (int r = ensure_batch(p, p->desc.batch)) return r;
+    if (v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, false, v->stream);
+    for (uint32_t i = 0; i < p->online; i++)
+        if (int r = train_on_frame(v, p)) return r;
+    if (v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, true, v->stream);
+    return VXR_OK;
+}
+
 // the candidate stage's hook (nullptr when the view samples uniformly)
 bool learned_hook(vxr_view* v, LearnedHook* h) {
     Proposal* p = v->prop;
@@ -212,6 +351,8 @@ bool learned_hook(vxr_view* v, LearnedHook* h) {
     h->infer.L = p->L;
     h->infer.params = p->params;
     h->infer.wbf = p->wbf;
+    h->infer.waitLimit = p->testTimeout ? 64u : 0u;
+    h->infer.skipMma = p->testTimeout ? 1u : 0u;
     h->cand = p->cand;
     h->clOff = p->clOff;
     h->clMembers = p->clMembers;
@@ -259,6 +400,10 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
                                         "clusters a multiple of 16");
     if (d.kernel == 2 && !vxr::prop::infer_tc_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tcgen05 inference needs hidden = 64 and 256 clusters");
+    VXR_CHECK_ARG(desc->training <= 2, "vxr_view_proposal_enable: training must be 0 (auto), 1 (FP32) or 2 (tensor cores)");
+    if (desc->training == 2 && !vxr::prop::train_supported(d))
+        return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tensor-core training step needs hidden = 64 and "
+                                        "16 <= clusters <= 256");
     if (v->prop) vxr::destroy_proposal(v->prop);
     vxr::Proposal* p = new (std::nothrow) vxr::Proposal();
     if (!p) return set_error(VXR_E_NOMEM, "vxr_view_proposal_enable: out of host memory");
@@ -266,6 +411,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     p->d = d;
     p->L = vxr::prop::layout(d);
     p->desc = *desc;
+    p->fused = desc->training == 2 || (desc->training == 0 && vxr::prop::train_supported(d));
     const size_t n = p->L.total;
     CUP(cudaMalloc(&p->params, n * sizeof(float)), "cudaMalloc(params)");
     CUP(cudaMalloc(&p->grads, n * sizeof(float)), "cudaMalloc(grads)");
@@ -299,30 +445,10 @@ int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_train: enable the proposal first");
     if (p->clusterVersion != v->world->w.clusterVersion)
         if (int r = upload_clusters(v, p)) return r;
-    const uint32_t B = p->desc.batch;
-    if (int r = ensure_batch(p, B)) return r;
+    if (int r = ensure_batch(p, p->desc.batch)) return r;
     float last = 0.0f;
     for (uint32_t it = 0; it < steps; it++) {
-        vxr::prop::GatherArgs ga{};
-        ga.k = vxr::dev_frame(v->k);
-        ga.vd = v->buf.vd[v->cur];
-        ga.hits = v->buf.hits;
-        ga.count = v->buf.counters;
-        ga.hA = v->buf.hA;
-        ga.lightCluster = p->lightCluster;
-        ga.nlights = (uint32_t)v->world->w.dev->nl;
-        ga.B = B;
-        ga.offset = p->gatherOffset;
-        ga.samples = p->samples;
-        ga.target = p->target;
-        ga.weight = p->weight;
-        p->gatherOffset = p->gatherOffset * 1664525u + 1013904223u;
-        vxr::prop::launch_gather(ga, v->stream);
-        forward_backward(p, B, v->stream);
-        p->step++;
-        vxr::prop::launch_adam(p->params, p->grads, p->m, p->v, p->L.total, p->desc.learning_rate, p->step, v->stream);
-        refresh_bf16(p, v->stream);
-        CUP(cudaGetLastError(), "proposal training");
+        if (int r = train_on_frame(v, p)) return r;
         if (it + 1 == steps && loss) {
             float h[2];
             CUP(cudaMemcpyAsync(h, p->scal, sizeof(h), cudaMemcpyDeviceToHost, v->stream), "read loss");
@@ -331,6 +457,23 @@ int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
         }
     }
     if (loss) *loss = last;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame) {
+    if (int r = check_view(v, "vxr_view_proposal_online")) return r;
+    if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_online: enable the proposal first");
+    VXR_CHECK_ARG(steps_per_frame <= 16, "vxr_view_proposal_online: at most 16 steps per frame");
+    if (steps_per_frame)
+        if (int r = ensure_batch(v->prop, v->prop->desc.batch)) return r;
+    v->prop->online = steps_per_frame;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_test_timeout(vxr_view* v, int on) {
+    if (int r = check_view(v, "vxr_view_proposal_test_timeout")) return r;
+    if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_test_timeout: enable the proposal first");
+    v->prop->testTimeout = on != 0;
     return VXR_OK;
 }
 
@@ -377,7 +520,12 @@ int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const 
     CUP(cudaMemcpy(p->samples, samples, B * sizeof(float4), cudaMemcpyHostToDevice), "upload samples");
     CUP(cudaMemcpy(p->target, target, B * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload targets");
     CUP(cudaMemcpy(p->weight, weight, B * sizeof(float), cudaMemcpyHostToDevice), "upload weights");
-    forward_backward(p, B, v->stream);
+    if (p->fused) {
+        if (int r = fused_step(p, B, false, v->stream)) return r;
+    } else {
+        forward_backward(p, B, v->stream);
+        p->encGradDirty = true;
+    }
     CUP(cudaGetLastError(), "proposal gradient");
     float h[2];
     CUP(cudaMemcpyAsync(h, p->scal, sizeof(h), cudaMemcpyDeviceToHost, v->stream), "read loss");

@@ -185,6 +185,7 @@ static int upload(World& w) {
 
 namespace vxr {
 bool learned_hook(vxr_view* v, LearnedHook* h);
+int proposal_frame_train(vxr_view* v);
 }
 
 using vxr::set_error;
@@ -258,6 +259,7 @@ void free_view(vxr_view* v) {
     cudaFree(b.hits); cudaFree(b.qA); cudaFree(b.qB); cudaFree(b.counters);
     cudaFree(v->sum64); cudaFree(v->errOut);
     cudaFree(v->skyDev); cudaFree(v->skyTex); cudaFree(v->skyBlueNoise);
+    cudaFree(v->bc.keys); cudaFree(v->bc.mask); cudaFree(v->bc.count);
     if (v->prop) vxr::destroy_proposal(v->prop);
     v->prop = nullptr;
     delete v->ktimer;
@@ -343,6 +345,83 @@ using vxr::shape;
         cudaError_t e_ = (call);                                                          \
         if (e_ != cudaSuccess) return set_error(VXR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
     } while (0)
+
+namespace vxr {
+// Brick cache: a frame that finds no table for the tuning's size and the world's version
+// calibrates (its shadow passes count brick walks); at its end the N most walked bricks
+// become the table. Both run only when the tuning asks for a cache.
+int brick_cache_begin(vxr_view* v) {
+    BrickCacheState& c = v->bc;
+    const int want = v->tuning.brickCache;
+    const uint64_t ver = v->world->w.version;
+    if (want <= 0 || (c.log2 > 0 && c.slots == want && c.worldVersion == ver)) return VXR_OK;
+    const uint32_t nb = std::max<uint32_t>(v->world->w.brickHigh, 1u);
+    if (c.countCap < nb) {
+        cudaFree(c.count);
+        c.count = nullptr;
+        c.countCap = 0;
+        CUV(cudaMalloc(&c.count, nb * sizeof(uint32_t)), "cudaMalloc(brick walk counts)");
+        c.countCap = nb;
+    }
+    CUV(cudaMemsetAsync(c.count, 0, nb * sizeof(uint32_t), v->stream), "clear brick walk counts");
+    c.calibrating = true;
+    return VXR_OK;
+}
+
+int brick_cache_end(vxr_view* v) {
+    BrickCacheState& c = v->bc;
+    if (!c.calibrating) return VXR_OK;
+    c.calibrating = false;
+    const World& w = v->world->w;
+    const uint32_t nb = std::max<uint32_t>(w.brickHigh, 1u);
+    std::vector<uint32_t> cnt(nb);
+    CUV(cudaMemcpyAsync(cnt.data(), c.count, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost, v->stream),
+        "read brick walk counts");
+    CUV(cudaStreamSynchronize(v->stream), "brick cache calibration");
+    const int N = v->tuning.brickCache;
+    std::vector<uint32_t> order;
+    for (uint32_t b = 0; b < nb; b++)
+        if (cnt[b] > 0) order.push_back(b);
+    const size_t top = std::min<size_t>((size_t)N, order.size());
+    std::partial_sort(order.begin(), order.begin() + top, order.end(),
+                      [&](uint32_t a, uint32_t b) { return cnt[a] != cnt[b] ? cnt[a] > cnt[b] : a < b; });
+    int log2 = 1;
+    while ((1 << log2) < 2 * N) log2++;
+    const uint32_t nk = 1u << log2;
+    std::vector<uint32_t> keys(nk, dev::kNoKey), mask((size_t)(nk / 2) * 16u, 0u);
+    uint32_t slot = 0;
+    for (size_t i = 0; i < top; i++) {
+        const uint32_t b = order[i];
+        if (b >= (1u << 21)) continue;
+        const uint32_t h = (b * 2654435761u) >> (32 - log2);
+        for (uint32_t p = 0; p < 4; p++) {
+            uint32_t& key = keys[(h + p) & (nk - 1u)];
+            if (key != dev::kNoKey) continue;
+            key = (b << 11) | slot;
+            for (uint32_t vi = 0; vi < 512; vi++)
+                if (((w.bricks[(size_t)b * 512 + vi] >> 12) & 15u) == 15u) mask[(size_t)slot * 16 + (vi >> 5)] |= 1u << (vi & 31u);
+            slot++;
+            break;
+        }
+    }
+    if (c.log2 != log2) {
+        cudaFree(c.keys);
+        cudaFree(c.mask);
+        c.keys = nullptr;
+        c.mask = nullptr;
+        c.log2 = 0;
+        CUV(cudaMalloc(&c.keys, nk * sizeof(uint32_t)), "cudaMalloc(brick cache)");
+        CUV(cudaMalloc(&c.mask, mask.size() * sizeof(uint32_t)), "cudaMalloc(brick cache)");
+    }
+    CUV(cudaMemcpy(c.keys, keys.data(), nk * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload brick cache");
+    CUV(cudaMemcpy(c.mask, mask.data(), mask.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload brick cache");
+    c.log2 = log2;
+    c.slots = N;
+    c.worldVersion = w.version;
+    return VXR_OK;
+}
+
+}  // namespace vxr
 
 extern "C" {
 
@@ -562,6 +641,7 @@ int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* out) {
     k.spatialRadius = v->desc.spatial_radius;
     k.spatialTaps = v->desc.spatial_taps;
     v->cur ^= 1;   // G-buffer swap (world.cpp:2221-2223)
+    if (int r = vxr::brick_cache_begin(v)) return r;
     v->frameOpen = true;
     for (int i = 0; i < 6; i++) v->ran[i] = false;
     if (out) *out = k;
@@ -599,6 +679,15 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     vxr::BatchDev bd = vxr::single_batch(w, k, v->buf, v->cur, point, sh);
     bd.fuse = fuse ? 1 : 0;
     bd.timer = v->ktimerOn ? v->ktimer : nullptr;
+    if (sh.brickCache > 0) {
+        if (v->bc.calibrating) {
+            bd.bcCount = v->bc.count;
+        } else if (v->bc.log2 > 0) {
+            bd.bcKeys = v->bc.keys;
+            bd.bcMask = v->bc.mask;
+            bd.bcLog2 = v->bc.log2;
+        }
+    }
     const int variant = point ? 1 : 0;
     switch (stage) {
     case VXR_STAGE_ALBEDO: vxr::launch_batch_albedo(bd, variant, v->stream); break;
@@ -632,7 +721,7 @@ int vxr_view_end_frame(vxr_view* v) {
     vxr::end_frame(v->cam);
     v->frameOpen = false;
     v->frameSerial++;
-    return VXR_OK;
+    return vxr::brick_cache_end(v);
 }
 
 int vxr_view_render(vxr_view* v) {
@@ -642,6 +731,7 @@ int vxr_view_render(vxr_view* v) {
     if (int r = run_stage(v, VXR_STAGE_CANDIDATES, false)) return r;
     if (int r = run_stage(v, VXR_STAGE_SPATIAL, false)) return r;
     if (int r = run_stage(v, VXR_STAGE_SHADE, true)) return r;
+    if (int r = vxr::proposal_frame_train(v)) return r;
     return vxr_view_end_frame(v);
 }
 
@@ -878,6 +968,9 @@ int check_tuning(const vxr_tuning* t, const char* fn) {
         return set_error(VXR_E_INVALID, std::string(fn) + ": list_blocks_per_sm out of range [1, 64]");
     if (t->occupancy > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": occupancy must be 0 or 1");
     if (t->shadow_schedule > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_schedule must be 0 or 1");
+    if (t->shadow_early_out > 1) return set_error(VXR_E_INVALID, std::string(fn) + ": shadow_early_out must be 0 or 1");
+    if (t->brick_cache != 0 && (t->brick_cache < 128 || t->brick_cache > 2048 || (t->brick_cache & (t->brick_cache - 1))))
+        return set_error(VXR_E_INVALID, std::string(fn) + ": brick_cache must be 0 or a power of two in [128, 2048]");
     return VXR_OK;
 }
 Tuning to_tuning(const vxr_tuning& t) {
@@ -890,6 +983,8 @@ Tuning to_tuning(const vxr_tuning& t) {
     u.listPerSm = (int)t.list_blocks_per_sm;
     u.occupancy = (int)t.occupancy;
     u.schedule = (int)t.shadow_schedule;
+    u.earlyOut = (int)t.shadow_early_out;
+    u.brickCache = (int)t.brick_cache;
     return u;
 }
 }  // namespace vxr
@@ -905,6 +1000,8 @@ extern "C" int vxr_default_tuning(vxr_tuning* t) {
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
     t->occupancy = (uint32_t)u.occupancy;
     t->shadow_schedule = (uint32_t)u.schedule;
+    t->shadow_early_out = (uint32_t)u.earlyOut;
+    t->brick_cache = (uint32_t)u.brickCache;
     return VXR_OK;
 }
 
@@ -943,6 +1040,8 @@ extern "C" int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t) {
     t->list_blocks_per_sm = (uint32_t)u.listPerSm;
     t->occupancy = (uint32_t)u.occupancy;
     t->shadow_schedule = (uint32_t)u.schedule;
+    t->shadow_early_out = (uint32_t)u.earlyOut;
+    t->brick_cache = (uint32_t)u.brickCache;
     return VXR_OK;
 }
 
@@ -1003,7 +1102,7 @@ extern "C" int vxr_view_work_counts(vxr_view* v, uint32_t counts[3]) {
 extern "C" const char* vxr_kernel_name(int id) {
     static const char* names[VXR_KERNEL_COUNT] = {"albedo", "compact_hits", "proposal_infer", "ris_candidates",
                                                   "shadow_candidates", "temporal", "spatial", "shade_request",
-                                                  "shadow_shading", "shade_finish", "accumulate"};
+                                                  "shadow_shading", "shade_finish", "accumulate", "proposal_train"};
     return id >= 0 && id < VXR_KERNEL_COUNT ? names[id] : "";
 }
 

@@ -51,6 +51,20 @@ struct ViewKernelTimer : KernelTimer {
     ~ViewKernelTimer() override;
 };
 void destroy_proposal(Proposal* p);
+
+// The shadow tracer's brick cache of a view (tuning brick_cache = N > 0): the N bricks its
+// shadow rays walked most in a calibration frame, as an open-addressed table of 2N keys
+// and their opacity masks (built on the host, copied into shared memory by every CTA).
+struct BrickCacheState {
+    uint32_t* keys = nullptr;       // device: 2N keys (brick << 11 | slot)
+    uint32_t* mask = nullptr;       // device: N x 16 words
+    uint32_t* count = nullptr;      // device: brick walks per brick (calibration)
+    uint32_t countCap = 0;
+    int log2 = 0;                   // log2(2N) of the built table, 0 = none
+    int slots = 0;                  // N of the built table
+    uint64_t worldVersion = 0;      // world the table was built for
+    bool calibrating = false;       // this frame counts brick walks
+};
 }  // namespace vxr
 
 struct vxr_view {
@@ -74,6 +88,7 @@ struct vxr_view {
     uint32_t sum64Count = 0;
     double* errOut = nullptr;                         // [mse sum, mae sum]
     vxr::Proposal* prop = nullptr;                    // learned proposal (optional)
+    vxr::BrickCacheState bc;                          // shadow tracer's brick cache (tuning)
     vxr::ViewKernelTimer* ktimer = nullptr;           // per-kernel timing (vxr_view_kernel_timing)
     vxr::dev::Sky* skyDev = nullptr;                  // sky dome (vxr_view_set_sky), null = off
     float4* skyTex = nullptr;

@@ -64,13 +64,14 @@ class SceneDesc(C.Structure):
 class ProposalDesc(C.Structure):
     _fields_ = [("hidden", C.c_uint32), ("table_log2", C.c_uint32), ("res0", C.c_uint32), ("res1", C.c_uint32),
                 ("epsilon", C.c_float), ("learning_rate", C.c_float), ("batch", C.c_uint32), ("seed", C.c_uint32),
-                ("inference", C.c_uint32)]
+                ("inference", C.c_uint32), ("training", C.c_uint32)]
 
 
 class Tuning(C.Structure):
     _fields_ = [("tile_x", C.c_uint32), ("tile_y", C.c_uint32), ("persistent", C.c_uint32),
                 ("shadow_refill", C.c_uint32), ("shadow_burst", C.c_uint32), ("list_blocks_per_sm", C.c_uint32),
-                ("occupancy", C.c_uint32), ("shadow_schedule", C.c_uint32)]
+                ("occupancy", C.c_uint32), ("shadow_schedule", C.c_uint32), ("shadow_early_out", C.c_uint32),
+                ("brick_cache", C.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -142,6 +143,8 @@ _SIGS = {
     "vxr_proposal_default_desc": [C.POINTER(ProposalDesc)],
     "vxr_view_proposal_enable": [_P, C.POINTER(ProposalDesc)], "vxr_view_proposal_use": [_P, C.c_int],
     "vxr_view_proposal_train": [_P, C.c_uint32, C.POINTER(C.c_float)],
+    "vxr_view_proposal_online": [_P, C.c_uint32],
+    "vxr_view_proposal_test_timeout": [_P, C.c_int],
     "vxr_view_proposal_param_count": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "vxr_view_proposal_get_params": [_P, _F3], "vxr_view_proposal_set_params": [_P, _F3],
     "vxr_view_proposal_grad": [_P, C.c_uint32, _F3, C.POINTER(C.c_uint32), _F3, C.POINTER(C.c_float), _F3],
@@ -525,6 +528,14 @@ class View:
         check(self._lib.vxr_view_proposal_train(self.h, steps, C.byref(loss)))
         return loss.value
 
+
+    def proposal_test_timeout(self, on):
+        """Test hook: the tensor-core inference's waits run out (error flag 16)."""
+        check(self._lib.vxr_view_proposal_test_timeout(self.h, 1 if on else 0))
+
+    def proposal_online(self, steps_per_frame=1):
+        """Train the proposal inside every rendered frame (0 turns it off)."""
+        check(self._lib.vxr_view_proposal_online(self.h, steps_per_frame))
     def proposal_shape(self):
         n, k, h = C.c_uint64(), C.c_uint32(), C.c_uint32()
         check(self._lib.vxr_view_proposal_param_count(self.h, C.byref(n), C.byref(k), C.byref(h)))
@@ -600,7 +611,7 @@ class View:
         check(self._lib.vxr_view_render_to_host(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3)))
 
 
-KERNEL_COUNT = 11
+KERNEL_COUNT = 12
 BATCH_MAX_VIEWS = 16
 BATCH_GRAPH = 1
 

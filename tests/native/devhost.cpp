@@ -26,6 +26,7 @@ static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f
 static inline float __uint2float_rn(unsigned u) { return (float)u; }
 static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 template <class T> static inline T __ldg(const T* p) { return *p; }
+static inline unsigned atomicAdd(unsigned* p, unsigned v) { const unsigned o = *p; *p = o + v; return o; }
 using std::isinf;
 using std::isnan;
 using std::max;
@@ -209,6 +210,35 @@ int dh_walk_skip(const uint32_t* grid, const uint8_t* uber, const uint32_t* bric
     *side = st == WALK_HIT ? k.side : 0u;
     *visits = n;
     return st;
+}
+
+// a shadow ray through the walker (brick skipping when bbox is given) as the persistent
+// tracer runs it, with or without the visibility early-out towards the emitter cube
+// [pos, pos + size); returns 1 when the visibility test passes (hit voxel in the cube),
+// *visits: cells visited
+int dh_shadow(const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks, const uint32_t* bbox, const float* O,
+              const float* D, uint32_t pos, uint32_t size, int early, int* visits) {
+    World w = make_world(grid, uber, bricks);
+    w.bbox = bbox;
+    Walker k;
+    int st = walk_init(k, w, O[0], O[1], O[2], D[0], D[1], D[2], 128);
+    if (early && st == WALK_CONTINUE) walk_target(k, pos, size);
+    int n = 0;
+    while (st == WALK_CONTINUE) {
+        st = early ? walk_step<kWalkEarly>(k, w) : walk_step(k, w);
+        n++;
+    }
+    *visits = n;
+    const float d2 = st == WALK_HIT ? k.dist : 0.0f;
+    const uint32_t s2 = st == WALK_HIT ? k.side : 0u;
+    const float3 L = f3(D[0], D[1], D[2]);
+    const float ns = side_sign(s2, L);
+    const float hx = L.x * d2 + O[0], hy = L.y * d2 + O[1], hz = L.z * d2 + O[2];
+    const uint32_t vx = f2u(hx - (s2 == 0 ? ns * 0.1f : 0.0f));
+    const uint32_t vy = f2u(hy - (s2 == 1 ? ns * 0.1f : 0.0f));
+    const uint32_t vz = f2u(hz - (s2 == 2 ? ns * 0.1f : 0.0f));
+    const uint32_t ey = pos / (1024u * 1024u), ez = (pos / 1024u) % 1024u, ex = pos % 1024u;
+    return ex <= vx && ex + size > vx && ey <= vy && ey + size > vy && ez <= vz && ez + size > vz;
 }
 
 void dh_sincos(float a, float* s, float* c) { sincos_vx(a, s, c); }

@@ -42,9 +42,10 @@ def test_multi_rank_helpers_gloo():
     os.path.join(ROOT, "oracle", "_ref", "vxref_gen.inc")), reason="the reference oracle cannot be built here")
 def test_reference_arm_two_ranks():
     r, lines = _torchrun(["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",
-                          "--config", "0", "--width", "64", "--height", "48", "--cpu-rows", "8"], 600)
+                          "--config", "0", "--width", "64", "--height", "48"], 600)
     assert r.returncode == 0, r.stderr[-3000:]
     assert len(lines) == 1, lines                               # rank 0 alone prints
     d = lines[0]
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["unit"] == "ms/frame" and d["value"] > 0
     assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert "whole 64x48 frames" in d["cpu_baseline"]["sample"] and d["opencl_cpu_runtime"]["status"]

@@ -65,8 +65,8 @@ def test_invalid_arguments_return_status(lib):
     assert L.vxr_batch_destroy(None) == lib.vxr.VXR_OK
     t = lib.tuning()
     assert (t.tile_x, t.tile_y, t.persistent, t.shadow_refill, t.shadow_burst, t.list_blocks_per_sm, t.occupancy,
-            t.shadow_schedule) == \
-        (16, 8, 0, 8, 4, 16, 0, 0)
+            t.shadow_schedule, t.shadow_early_out, t.brick_cache) == \
+        (16, 8, 0, 8, 4, 16, 0, 0, 0, 0)
     assert L.vxr_view_set_tuning(None, C.byref(t)) == lib.vxr.VXR_E_INVALID
     assert L.vxr_batch_set_tuning(None, C.byref(t)) == lib.vxr.VXR_E_INVALID
     assert L.vxr_default_tuning(None) == lib.vxr.VXR_E_INVALID
@@ -76,7 +76,7 @@ def test_autotune_cache_roundtrip(tmp_path):
     from smallproject_gb300 import autotune as at
     from smallproject_gb300 import vxr as V
     d = {"tile": [32, 4], "persistent": 1, "shadow_refill": 16, "shadow_burst": 2, "list_blocks_per_sm": 8, "occupancy": 1,
-         "shadow_schedule": 1}
+         "shadow_schedule": 1, "shadow_early_out": 0, "brick_cache": 256}
     t = at._to_tuning(d)
     assert isinstance(t, V.Tuning) and at._from_tuning(t) == {**d, "tile": (32, 4)}
     path = str(tmp_path / "c.json")

@@ -39,6 +39,8 @@ def dh():
     lib.dh_trace_skip.argtypes = [C.c_int, P, P, P, P, P, P, F, F, C.c_int, C.c_uint32, C.c_uint32, F,
                                   C.POINTER(C.c_uint32)]
     lib.dh_walk_skip.argtypes = [P, P, P, P, F, F, C.c_int, F, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
+    lib.dh_shadow.restype = C.c_int
+    lib.dh_shadow.argtypes = [P, P, P, P, F, F, C.c_uint32, C.c_uint32, C.c_int, C.POINTER(C.c_int)]
     return lib
 
 
@@ -268,3 +270,96 @@ def test_area_sample_per_axis_matches_per_face(dh):
         dh.dh_area_sample(0, lg, spo, seed, pa)
         dh.dh_area_sample(1, lg, spo, seed, pb)
         assert out_a.view(np.uint32).tolist() == out_b.view(np.uint32).tolist(), (i, c, size, sp, seed, out_a, out_b)
+
+
+def _candidate_shadow_rays(wa, lights, W, H, cam_path, point):
+    """The candidate stage's shadow rays of two oracle frames: origin = shading point +
+    0.1 N, direction towards the selected sample on the emitter, and the emitter."""
+    r = ob.Renderer("port", wa, W, H, point)
+    cam = ob.CameraPath(W, H)
+    out = []
+    for f in range(2):
+        cam.lookat(*cam_path(f))
+        k = cam.begin(numberOfLights=len(lights), numberOfCandidates=32, numberOfMaxTemporalImportance=20,
+                      spatialRadius=30, spatialTaps=5, spatial=1, temporal=1, accumulate=0)
+        r.frame_start()
+        r.stage(k, 1)
+        r.stage(k, 2)
+        g, res = r.gbuffer(0), r.reservoirs(0)
+        cam.end()
+        E, p0, p1, p2 = (np.array(v, np.float32) for v in (k.E, k.p0, k.p1, k.p2))
+        idx = np.nonzero((g["voxel"] != 0) & (res["streamLength"] > 0) & (res["pHat"] > 0))[0]
+        u = (idx % W).astype(np.float32) * np.float32(k.oneOverRes[0])
+        v = (idx // W).astype(np.float32) * np.float32(k.oneOverRes[1])
+        D = p0 + (p1 - p0) * u[:, None] + (p2 - p0) * v[:, None] - E
+        D /= np.linalg.norm(D, axis=1, keepdims=True)
+        sp = E + D * g["dist"][idx][:, None]
+        side = g["side"][idx]
+        n = np.arange(len(idx))
+        sp[n, side] += np.where(D[n, side] > 0, np.float32(-0.1), np.float32(0.1))
+        L = res["positionOnVoxel"][idx] - sp
+        L /= np.linalg.norm(L, axis=1, keepdims=True)
+        out.append((sp.astype(np.float32), L.astype(np.float32), res["lightIndex"][idx]))
+    r.close()
+    return [np.concatenate(x) for x in zip(*out)]
+
+
+def _early_out_case(dh, wa, lights, O, D, LI):
+    box = brick_boxes(wa.bricks)
+    n = C.c_int()
+    diff = visits = visits_early = visible = 0
+    for i in range(len(O)):
+        lt = lights[LI[i]]
+        o, d = _f3(O[i]), _f3(D[i])
+        a = dh.dh_shadow(wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, box.ctypes.data, o, d,
+                         int(lt["position"]), int(lt["size"]), 0, C.byref(n))
+        visits += n.value
+        b = dh.dh_shadow(wa.grid.ctypes.data, wa.uber.ctypes.data, wa.bricks.ctypes.data, box.ctypes.data, o, d,
+                         int(lt["position"]), int(lt["size"]), 1, C.byref(n))
+        visits_early += n.value
+        diff += a != b
+        visible += a
+    return diff, visits, visits_early, visible
+
+
+def test_shadow_early_out_is_exact(dh, world0_arrays):
+    """The visibility early-out (walk_target: stop as occluded once the step budget left is
+    below the grid-cell distance to the emitter) never changes a visibility result: the
+    candidate shadow rays of oracle frames (point and area lights) and surface-leaving
+    rays towards random emitters of world0."""
+    wa = world0_arrays
+    lights = wa.lights
+
+    def orbit(f):
+        return (128.0 + 40.0 * f, 170.0, -60.0 + 30.0 * f), (128.0, 100.0, 128.0)
+
+    total = [0, 0, 0]
+    for point in (True, False):
+        O, D, LI = _candidate_shadow_rays(wa, lights, 160, 96, orbit, point)
+        diff, v0, v1, _ = _early_out_case(dh, wa, lights, O, D, LI)
+        assert diff == 0
+        total = [total[0] + len(O), total[1] + v0, total[2] + v1]
+    rng = np.random.default_rng(3)
+    o, _, _ = _surface_rays(wa, 3000, 9)
+    LI = rng.integers(0, len(lights), len(o))
+    ex = lights["position"][LI] % 1024
+    ez = (lights["position"][LI] // 1024) % 1024
+    ey = lights["position"][LI] // (1024 * 1024)
+    tgt = np.stack([ex, ey, ez], 1).astype(np.float32) + np.float32(0.5)
+    d = tgt - o
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    diff, v0, v1, vis = _early_out_case(dh, wa, lights, o, d, LI)
+    assert diff == 0 and vis > 0
+    assert total[2] <= total[1] and v1 <= v0
+
+
+@pytest.mark.slow
+def test_shadow_early_out_is_exact_config3(dh):
+    """The same on the benchmark scene (config 3: 1024^3 terrain, 65,536 emitters in
+    blobs): every candidate shadow ray of two 240 x 135 frames along the camera path."""
+    hs = ob.HostScene(3)
+    wa = ob.WorldArrays(hs.grid, hs.bricks, hs.lights)
+    O, D, LI = _candidate_shadow_rays(wa, hs.lights, 240, 135, lambda f: hs.camera_path(1, 150 + f, 300), False)
+    assert len(O) > 20000
+    diff, v0, v1, _ = _early_out_case(dh, wa, hs.lights, O, D, LI)
+    assert diff == 0 and v1 < v0

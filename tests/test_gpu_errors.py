@@ -2,7 +2,10 @@
 input raises a bit in the view's error word, clamps the value and goes on; the host
 reads the word at vxr_view_wait, reports VXR_E_DEVICE once and clears it. The input
 comes from the host: a reservoir naming a light beyond the light list, written through
-the stage-level access between the spatial and shading stages."""
+the stage-level access between the spatial and shading stages. The tensor-core inference
+of the learned proposal bounds every mbarrier wait: with the test hook its waits run out
+with no MMA in flight, and the frame reports flag 16, stays finite, and later frames are
+clean."""
 import numpy as np
 import pytest
 
@@ -45,5 +48,34 @@ def test_shading_light_index_error_is_reported_once(lib, cuda_device, scene0):
             v.lookat(*_cam(f))
             v.render()
             v.wait()
+    finally:
+        v.close()
+
+
+def test_tensor_core_wait_timeout_is_reported_once(lib, cuda_device):
+    w = lib.World()
+    w.generate(lib.scene_preset(0, emitters=2048, emitter_mode=1))
+    w.cluster_lights(256, seed=3, iters=6)
+    v = lib.View(w, lib.view_desc(96, 64, lib.LIGHTS_AREA, num_candidates=8))
+    try:
+        v.proposal_enable(seed=7, batch=4096, inference=2)
+        v.proposal_use(True)
+        v.lookat(*_cam(0))
+        v.render()
+        v.wait()
+        v.proposal_test_timeout(True)
+        v.lookat(*_cam(1))
+        v.render()
+        with pytest.raises(lib.VxrError) as e:
+            v.wait()
+        assert e.value.code == -5                                   # VXR_E_DEVICE
+        assert "device error flags 0x10 (16: tensor-core wait gave up)" in str(e.value)
+        assert np.isfinite(v.read_frame()).all()
+        v.proposal_test_timeout(False)
+        for f in (2, 3):
+            v.lookat(*_cam(f))
+            v.render()
+            v.wait()
+        assert np.isfinite(v.read_frame()).all() and v.read_frame()[:, :3].max() > 0
     finally:
         v.close()

@@ -1,10 +1,11 @@
 """The headline workload at its full size (config 3: 1920 x 1080, the 1024^3 fBm world
-with 65,536 emitters, area lights, the bench's camera path), where the C oracle is too
-slow for whole frames: bit for bit against the oracle on a band of rows for the
-pixel-local stages of a first frame (primary rays; candidates with their visibility
-rays, no history yet), and whole frames through a size-independent property: a very
-different launch tuning on a second view changes no bit of any stage over several
-frames (the persistent work queues at full load)."""
+with 65,536 emitters, area lights, the bench's camera path): three whole consecutive
+frames against the C oracle (all host cores), every stage bit for bit - primary rays,
+candidates with visibility and temporal reuse, spatial reuse, shading with its
+visibility rays, the history reservoirs and the accumulator; a band of rows of a first
+frame; and a size-independent property: a very different launch tuning on a second view
+changes no bit of any stage over several frames (the persistent work queues at full
+load)."""
 import numpy as np
 import pytest
 
@@ -52,6 +53,43 @@ def test_full_frame_band_matches_oracle(lib, cuda_device, scene3):
         assert_records_equal("seed", view.read_gbuffer(0)["seed"][rows], port.gbuffer(0)["seed"][rows], "")
         view.end_frame()
         view.wait()
+    finally:
+        port.close()
+        view.close()
+
+
+def test_whole_frames_match_oracle(lib, cuda_device, scene3):
+    w, d = scene3
+    g, b, l = w.arrays()
+    port = ob.Renderer("port", ob.WorldArrays(g, b, l), W, H, False)
+    view = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1))
+    try:
+        for f in range(3):
+            view.lookat(*lib.camera_path(d, 1, 150 + f, PATH))
+            k = view.begin_frame()
+            assert (k.restirtemporalframe > 0) == (f > 0)   # temporal reuse from the second frame on
+            port.frame_start()
+            ctx = f"[1920x1080 config 3, frame {f}]"
+            for s in range(1, 6):
+                view.stage(s)
+                port.stage(k, s)
+                if s == 1:
+                    assert_records_equal("gbuffer", view.read_gbuffer(0), port.gbuffer(0), ctx)
+                elif s == 2:
+                    assert_records_equal("candidates", view.read_reservoirs(0), port.reservoirs(0), ctx)
+                    assert_records_equal("seed", view.read_gbuffer(0)["seed"], port.gbuffer(0)["seed"], ctx)
+                elif s == 3:
+                    assert_records_equal("spatial", view.read_reservoirs(1), port.reservoirs(1), ctx)
+                    assert_records_equal("seed", view.read_gbuffer(0)["seed"], port.gbuffer(0)["seed"], ctx)
+                elif s == 4:
+                    assert_records_equal("frame", view.read_frame(), port.image(0), ctx)
+                    assert_records_equal("history", view.read_reservoirs(1), port.reservoirs(2), ctx)
+                else:
+                    assert_records_equal("accum", view.read_accum(), port.image(1), ctx)
+            view.end_frame()
+            view.wait()
+        fr = view.read_frame()
+        assert (fr[:, :3] > 0).mean() > 0.2
     finally:
         port.close()
         view.close()

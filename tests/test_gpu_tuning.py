@@ -1,7 +1,9 @@
 """Launch tuning (vxr_tuning) changes speed, never results; the autotuner's cache.
 
 Every tuning renders the same bits as the defaults (G-buffer, reservoirs, frame,
-accumulator), for a single view and for a batch."""
+accumulator), for a single view and for a batch: among them the shadow tracer without its
+visibility early-out and with its shared-memory brick cache (the calibration frame and
+the frames that read the cached bricks' opacity masks)."""
 import json
 
 import pytest
@@ -11,9 +13,12 @@ from conftest import assert_records_equal
 pytestmark = pytest.mark.gpu
 
 ODD = dict(tile_x=32, tile_y=4, persistent=1, shadow_refill=16, shadow_burst=16, list_blocks_per_sm=4, occupancy=1,
-           shadow_schedule=1)
+           shadow_schedule=1, shadow_early_out=0, brick_cache=0)
 ODD2 = dict(tile_x=8, tile_y=16, persistent=1, shadow_refill=1, shadow_burst=1, list_blocks_per_sm=1, occupancy=0,
-            shadow_schedule=1)
+            shadow_schedule=1, shadow_early_out=1, brick_cache=128)
+# the shadow tracer's shared-memory brick cache (calibration frame, then the table)
+CACHED = dict(tile_x=16, tile_y=8, persistent=0, shadow_refill=8, shadow_burst=4, list_blocks_per_sm=16, occupancy=0,
+              shadow_schedule=0, shadow_early_out=0, brick_cache=1024)
 
 
 def _cam(f):
@@ -29,10 +34,11 @@ def test_tuning_does_not_change_results(lib, cuda_device, scene0, model):
     w, _ = scene0
     lm = lib.LIGHTS_POINT if model == "point" else lib.LIGHTS_AREA
     desc = lib.view_desc(150, 70, lm, accumulate=1)
-    views = [lib.View(w, desc) for _ in range(3)]
+    views = [lib.View(w, desc) for _ in range(4)]
     try:
         views[1].set_tuning(lib.tuning(**ODD))
         views[2].set_tuning(lib.tuning(**ODD2))
+        views[3].set_tuning(lib.tuning(**CACHED))
         assert views[1].get_tuning().as_dict() == ODD
         for f in range(4):
             for v in views:
@@ -55,7 +61,8 @@ def test_tuning_rejects_bad_values(lib, cuda_device, scene0):
     try:
         for bad in (dict(tile_x=5, tile_y=5), dict(tile_x=64, tile_y=32), dict(tile_x=32, tile_y=16), dict(persistent=2), dict(shadow_refill=0),
                     dict(shadow_refill=33), dict(shadow_burst=0), dict(shadow_burst=65), dict(list_blocks_per_sm=0), dict(occupancy=2),
-                    dict(shadow_schedule=2)):
+                    dict(shadow_schedule=2), dict(shadow_early_out=2), dict(brick_cache=100), dict(brick_cache=64),
+                    dict(brick_cache=4096)):
             with pytest.raises(lib.VxrError):
                 v.set_tuning(lib.tuning(**bad))
     finally:
