@@ -411,6 +411,8 @@ typedef struct vxr_proposal_desc {
     uint32_t seed;            /* parameter initialisation */
     uint32_t inference;       /* 0 auto (tcgen05 when hidden = 64 and 256 clusters, else mma.sync), 1 mma.sync, 2 tcgen05 */
     uint32_t training;        /* 0 auto (tensor cores when hidden = 64 and clusters <= 256, else FP32), 1 FP32, 2 tensor cores */
+    uint32_t pixels_per_eval; /* tcgen05 inference: 1 = one network evaluation per hit pixel, 2 = per two consecutive hit
+                                 pixels (both sample from the first one's distribution; still unbiased) */
 } vxr_proposal_desc;
 int vxr_proposal_default_desc(vxr_proposal_desc* d);
 /* Allocate and initialise the network for this view; K = the world's cluster count. */

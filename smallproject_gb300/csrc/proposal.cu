@@ -540,9 +540,14 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
     bool pending = false;   // an MMA was committed whose completion no wait has seen
     const uint32_t limit = a.waitLimit ? a.waitLimit : tc::kWaitLimit;
     const bool issue = !a.skipMma;
-    for (uint32_t tile = blockIdx.x * 2 + h; ok && (size_t)tile * tc::kTile < n; tile += gridDim.x * 2) {
-        const uint32_t j = tile * tc::kTile + tid;
-        const bool valid = j < n;
+    // render mode with sharing: a table row serves two consecutive hit pixels (the network
+    // runs on the first one's shading point; each draws its own candidates from the row)
+    const uint32_t span = (a.share && !a.samples && !a.probs) ? 2u : 1u;
+    const uint32_t rows = (n + span - 1u) / span;
+    for (uint32_t tile = blockIdx.x * 2 + h; ok && (size_t)tile * tc::kTile < rows; tile += gridDim.x * 2) {
+        const uint32_t row = tile * tc::kTile + tid;
+        const uint32_t j = row * span;
+        const bool valid = row < rows;
         float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
         uint32_t pix = 0;
         if (valid) {
@@ -685,15 +690,21 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
             }
             continue;
         }
-        uint32_t s = dev::wang_hash(pix * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
+        // the hit pixel this thread draws for: with sharing its own one of the pair (all its
+        // candidates), else the row's pixel (every other candidate, the other warpgroup
+        // taking the rest; both advance the pixel's RNG alike)
+        const uint32_t jm = j + (span == 2u ? (uint32_t)half : 0u);
+        if (jm >= n) continue;
+        const uint32_t pm = span == 2u ? a.hits[jm] : pix;
+        uint32_t s = dev::wang_hash(pm * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
         const float eps = d.eps, invN = 1.0f / (float)a.nlights;
-        uint2* out = a.cand + j;
+        uint2* out = a.cand + jm;
 #pragma unroll 4
         for (uint32_t m = 0; m < a.ncand; m++) {
             const float u = dev::rnd(s);
             const float v = dev::rnd(s);
             const float w = dev::rnd(s);
-            if ((int)(m & 1u) != half) continue;   // the other warpgroup's candidate
+            if (span == 1u && (int)(m & 1u) != half) continue;   // the other warpgroup's candidate
             int c;
             uint32_t e;
             float gw;

@@ -29,6 +29,7 @@ struct InferArgs {
     uint32_t* err;                    // device error flags (16: a tensor-core wait gave up)
     uint32_t waitLimit;               // tries of each in-loop tensor-core wait (0: the full limit)
     uint32_t skipMma;                 // test only: issue no MMA, so every wait runs out with nothing in flight
+    uint32_t share;                   // tcgen05 render mode: one network evaluation per two consecutive hit pixels
     // sample mode (tests): explicit inputs (x, y, z, bits(side code)) and softmax output
     const float4* samples;
     uint32_t n;

@@ -353,6 +353,7 @@ bool learned_hook(vxr_view* v, LearnedHook* h) {
     h->infer.wbf = p->wbf;
     h->infer.waitLimit = p->testTimeout ? 64u : 0u;
     h->infer.skipMma = p->testTimeout ? 1u : 0u;
+    h->infer.share = p->desc.pixels_per_eval == 2 ? 1u : 0u;
     h->cand = p->cand;
     h->clOff = p->clOff;
     h->clMembers = p->clMembers;
@@ -374,6 +375,7 @@ int vxr_proposal_default_desc(vxr_proposal_desc* d) {
     d->learning_rate = 1e-3f;
     d->batch = 65536;
     d->seed = 1;
+    d->pixels_per_eval = 1;
     return VXR_OK;
 }
 
@@ -401,6 +403,8 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     if (d.kernel == 2 && !vxr::prop::infer_tc_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tcgen05 inference needs hidden = 64 and 256 clusters");
     VXR_CHECK_ARG(desc->training <= 2, "vxr_view_proposal_enable: training must be 0 (auto), 1 (FP32) or 2 (tensor cores)");
+    VXR_CHECK_ARG(desc->pixels_per_eval == 1 || desc->pixels_per_eval == 2,
+                  "vxr_view_proposal_enable: pixels_per_eval must be 1 or 2");
     if (desc->training == 2 && !vxr::prop::train_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tensor-core training step needs hidden = 64 and "
                                         "16 <= clusters <= 256");

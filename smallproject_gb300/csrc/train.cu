@@ -40,6 +40,7 @@ namespace prop {
 namespace {
 
 constexpr int kTW = 8;          // warps per CTA
+constexpr int kTrainCtasPerSm = 2;   // train_kernel: 128 registers, two CTAs (16 warps) per SM
 constexpr int kTH = 64;         // hidden width handled by the fused step
 constexpr int kLd1 = kIn + 8;   // padded row of W1 and X in shared memory (BF16 elements)
 constexpr int kLdh = kTH + 8;   // padded row of W2, W3, W4 and H1
@@ -169,7 +170,7 @@ __global__ void wsum_kernel(const float* __restrict__ w, uint32_t B, float* __re
     }
 }
 
-__global__ void __launch_bounds__(kTW * 32, 1) train_kernel(TrainArgs a) {
+__global__ void __launch_bounds__(kTW * 32, kTrainCtasPerSm) train_kernel(TrainArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float s_inv;
     __shared__ float s_loss[kTW];
@@ -434,17 +435,30 @@ __global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
     for (int i = 0; i < 8; i++) c[i][0] = c[i][1] = c[i][2] = c[i][3] = 0.0f;
     const uint32_t k0 = (uint32_t)chunk * a.chunkTiles;
     const uint32_t k1 = min(k0 + a.chunkTiles, a.ntiles);
-    for (uint32_t kt = k0 + warp; kt < k1; kt += kTW) {
-        const uint4 av = __ldcs(a.frag + frag_at(ra, kt, mt, a.ntiles, kt4) + lane);
-        const uint32_t af[4] = {av.x, av.y, av.z, av.w};
+    // two tiles per iteration: both tiles' loads are in flight before the first mma
+    for (uint32_t kt = k0 + warp; kt < k1; kt += 2 * kTW) {
+        const uint32_t kt2 = kt + kTW;
+        const bool two = kt2 < k1;
+        uint4 av[2], bv[2][4];
+        av[0] = __ldcs(a.frag + frag_at(ra, kt, mt, a.ntiles, kt4) + lane);
+        av[1] = two ? __ldcs(a.frag + frag_at(ra, kt2, mt, a.ntiles, kt4) + lane) : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
         for (int p = 0; p < 4; p++) {
             if (p >= np) break;
-            const uint4 bv = __ldg(a.frag + frag_at(rb, kt, p, a.ntiles, kt4) + lane);
-            mma16816(c[2 * p], af, bv.x, bv.y);
-            mma16816(c[2 * p + 1], af, bv.z, bv.w);
+            bv[0][p] = __ldg(a.frag + frag_at(rb, kt, p, a.ntiles, kt4) + lane);
+            bv[1][p] = two ? __ldg(a.frag + frag_at(rb, kt2, p, a.ntiles, kt4) + lane) : make_uint4(0u, 0u, 0u, 0u);
         }
-        mma16816(cb, af, ones, ones);
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const uint32_t af[4] = {av[u].x, av[u].y, av[u].z, av[u].w};
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                if (p >= np) break;
+                mma16816(c[2 * p], af, bv[u][p].x, bv[u][p].y);
+                mma16816(c[2 * p + 1], af, bv[u][p].z, bv[u][p].w);
+            }
+            mma16816(cb, af, ones, ones);
+        }
     }
 #pragma unroll
     for (int i = 0; i < 8; i++)
@@ -479,13 +493,27 @@ __global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
     }
 }
 
-__global__ void train_reduce_kernel(ReduceArgs r) {
+// 256 threads per block: 64 parameters, each summed over the partial rows by 4 groups of
+// 64 threads (group q takes rows q, q + 4, ...; coalesced along the parameters), the
+// groups' sums added in a fixed order
+__global__ void __launch_bounds__(256) train_reduce_kernel(ReduceArgs r) {
+    __shared__ float part[4][64];
     const int H = kTH, K = r.K;
     const int sb1 = H * kIn, sW2 = sb1 + H, sb2 = sW2 + H * H, sW3 = sb2 + H, sb3 = sW3 + H * H, sW4 = sb3 + H,
               sb4 = sW4 + K * H;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r.nmlp; i += gridDim.x * blockDim.x) {
-        float g = 0.0f;
-        for (int c = 0; c < r.nparts; c++) g += r.partials[(size_t)c * r.nmlp + i];
+    const int q = threadIdx.x >> 6, col = threadIdx.x & 63;
+    for (int base = blockIdx.x * 64; base < r.nmlp; base += gridDim.x * 64) {
+        const int ic = base + col;
+        float gq = 0.0f;
+        if (ic < r.nmlp)
+            for (int c = q; c < r.nparts; c += 4) gq += r.partials[(size_t)c * r.nmlp + ic];
+        part[q][col] = gq;
+        __syncthreads();
+        const int i = ic;
+        const bool mine = q == 0 && i < r.nmlp;
+        const float g = (part[0][col] + part[1][col]) + (part[2][col] + part[3][col]);
+        __syncthreads();
+        if (!mine) continue;
         r.grads[i] = g;
         if (!r.apply) continue;
         const float mi = r.b1 * r.m[i] + (1.0f - r.b1) * g;
@@ -557,7 +585,7 @@ size_t train_frag_bytes(const Dims& d, uint32_t B) {
 
 uint32_t train_chunks(uint32_t B) { return std::max(1u, ((B + 15) / 16 + kChunkTiles - 1) / kChunkTiles); }
 
-int train_max_ctas() { return device_sms(); }
+int train_max_ctas() { return kTrainCtasPerSm * device_sms(); }
 uint32_t train_wsum_blocks() { return kWsumBlocks; }
 
 void launch_wsum(const float* w, uint32_t B, float* part, cudaStream_t s) {
@@ -569,7 +597,7 @@ cudaError_t launch_train(const TrainArgs& a, cudaStream_t s, int* nparts, int* n
     cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     const uint32_t tiles = (a.B + 15) / 16;
-    const int ctas = (int)std::max<uint32_t>(1, std::min<uint32_t>((tiles + kTW - 1) / kTW, (uint32_t)device_sms()));
+    const int ctas = (int)std::max<uint32_t>(1, std::min<uint32_t>((tiles + kTW - 1) / kTW, (uint32_t)train_max_ctas()));
     train_kernel<<<ctas, kTW * 32, sm, s>>>(a);
     *nloss = ctas;
     e = cudaGetLastError();
@@ -588,7 +616,7 @@ cudaError_t launch_train(const TrainArgs& a, cudaStream_t s, int* nparts, int* n
 }
 
 void launch_train_reduce(const ReduceArgs& r, cudaStream_t s) {
-    const int blocks = std::max(1, std::min((r.nmlp + 255) / 256, 1024));
+    const int blocks = std::max(1, std::min((r.nmlp + 63) / 64, 2048));
     train_reduce_kernel<<<blocks, 256, 0, s>>>(r);
 }
 

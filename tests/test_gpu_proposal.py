@@ -122,11 +122,11 @@ def test_checkpoint_round_trip(lib, clustered_view, tmp_path):
     assert np.array_equal(v.proposal_params(), p0)
 
 
-def _converged_mean(lib, world, learned, frames, pos, tgt, seed, W=96, H=64, train_view=None, inference=0):
+def _converged_mean(lib, world, learned, frames, pos, tgt, seed, W=96, H=64, train_view=None, inference=0, share=1):
     v = lib.View(world, lib.view_desc(W, H, lib.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=seed))
     v.lookat(pos, tgt)
     if learned:
-        v.proposal_enable(seed=5, batch=4096, inference=inference)
+        v.proposal_enable(seed=5, batch=4096, inference=inference, pixels_per_eval=share)
         if train_view is not None:
             v.proposal_set_params(train_view.proposal_params())
         v.proposal_use(True)
@@ -228,14 +228,16 @@ def test_tcgen05_inference_matches_mma_and_fp64(lib, world256):
         b.close()
 
 
-def test_tcgen05_learned_source_is_unbiased(lib, world256):
+@pytest.mark.parametrize("share", [1, 2])
+def test_tcgen05_learned_source_is_unbiased(lib, world256, share):
     """The tcgen05 inference kernel (256 clusters) samples candidates with the probability
     it reports: with spatial and temporal reuse off its learned source and the uniform
     one converge to the same image (a source pdf that differed from the sampling
-    frequencies would bias the RIS estimate)."""
+    frequencies would bias the RIS estimate). share = 2: two consecutive hit pixels
+    sample from one network evaluation (the first one's)."""
     pos, tgt = (110.0, 150.0, 10.0), (128.0, 110.0, 128.0)
     a = _converged_mean(lib, world256, False, 384, pos, tgt, 21)
-    b = _converged_mean(lib, world256, True, 384, pos, tgt, 22, inference=2)
+    b = _converged_mean(lib, world256, True, 384, pos, tgt, 22, inference=2, share=share)
     ma, mb = a.mean(), b.mean()
     assert ma > 0 and abs(ma - mb) / ma < 0.03, (ma, mb)
 
