@@ -40,7 +40,7 @@ namespace prop {
 namespace {
 
 constexpr int kTW = 8;          // warps per CTA
-constexpr int kTrainCtasPerSm = 2;   // train_kernel: 128 registers, two CTAs (16 warps) per SM
+constexpr int kTrainCtasPerSm = 1;   // train_kernel: one CTA per SM (two, capped at 128 registers, spill and run slower)
 constexpr int kTH = 64;         // hidden width handled by the fused step
 constexpr int kLd1 = kIn + 8;   // padded row of W1 and X in shared memory (BF16 elements)
 constexpr int kLdh = kTH + 8;   // padded row of W2, W3, W4 and H1
