@@ -1,7 +1,8 @@
 // worldapi_shim.cpp - the worldapi.h shim a maintainer adds on top of libvxr (the same
 // code as the integration guide shows), compiled and linked by tests/test_capi.py with a
 // prelude standing in for the reference's types, and driven through its world calls
-// (which need no GPU).
+// (which need no GPU) and, with the argument "render", through LookAt / RenderFrame /
+// CommitFrame on the GPU (tests/test_gpu_shim.py).
 #include <cstdio>
 #include <cstdlib>
 
@@ -38,8 +39,41 @@ void LookAt(const float3 pos, const float3 target)
 void RenderFrame() { ok(vxr_view_render(g_view)); }
 void CommitFrame() { ok(vxr_view_wait(g_view)); }
 
-// ---- driver: the world half, no device needed ------------------------------------------
-int main() {
+// ---- driver ----------------------------------------------------------------------------
+// "render": a ground slab and one emitter voxel through Plot / Box, the camera through
+// LookAt, three frames through RenderFrame / CommitFrame (needs a GPU), then the frame
+// read back; prints lit pixels, non-finite values and the brightest value. Without
+// arguments: the world half alone (no device needed).
+static int render_demo() {
+    InitVxr(96, 64);
+    Box(0, 0, 0, 64, 4, 64, 0xF888);
+    Plot(32, 10, 32, (10u << 16) | 0xFFFFu);        // strength 10, opaque, white
+    const float3 pos = {32.0f, 30.0f, -20.0f}, tgt = {32.0f, 4.0f, 32.0f};
+    for (int f = 0; f < 3; f++) {
+        LookAt(pos, tgt);
+        RenderFrame();
+        CommitFrame();
+    }
+    static float rgba[96 * 64 * 4];
+    ok(vxr_view_read_frame(g_view, rgba));
+    int lit = 0, bad = 0;
+    float mx = 0.0f;
+    for (int i = 0; i < 96 * 64; i++) {
+        for (int c = 0; c < 3; c++) {
+            const float v = rgba[i * 4 + c];
+            if (!(v == v) || v > 1e30f || v < -1e30f) bad++;
+            if (v > mx) mx = v;
+        }
+        if (rgba[i * 4] + rgba[i * 4 + 1] + rgba[i * 4 + 2] > 0.0f) lit++;
+    }
+    std::printf("%d %d %g\n", lit, bad, mx);
+    ok(vxr_view_destroy(g_view));
+    ok(vxr_world_destroy(g_world));
+    return (lit > 100 && bad == 0 && mx > 0.0f) ? 0 : 2;
+}
+
+int main(int argc, char** argv) {
+    if (argc > 1 && argv[1][0] == 'r') return render_demo();
     ok(vxr_world_create(&g_world));
     Plot(10, 20, 30, 0xF888);
     Box(0, 0, 0, 4, 4, 4, 0xF123);
