@@ -264,6 +264,12 @@ def cpu_arm(config, steps, warmup, W, H):
 
 CANDS = (4, 8, 12, 16, 24, 32)
 CANDS2 = (4, 8, 12)
+# Compulsory HBM bytes of the temporal kernel per hit pixel: own G-buffer 8, candidate
+# reservoir 32 and seed 4 always; the reprojected pixel's previous G-buffer 8 and history
+# reservoir 32 when it is on screen (99 % on the camera path); the combined reservoir 32
+# and seed 4 written when the history is accepted (58 %) - fractions measured with the
+# oracle on four consecutive frames of the path at 480 x 270.
+TEMPORAL_BYTES_PER_HIT = 44.0 + 0.99 * 40.0 + 0.58 * 36.0
 POSE = 150
 NFR = 300
 # DRAM bytes per launch of the dominant kernel from the ncu capture of the 960x540 case
@@ -717,7 +723,7 @@ def main():
     dom = max(kernel_ms, key=lambda k: kernel_ms[k] * (kstats[k][1] or 0))
     per_launch_bytes = {"shadow_candidates": 36.0 * rays_c, "shadow_shading": 36.0 * rays_s,
                         "ris_candidates": 80.0 * hits, "albedo": 12.0 * npx, "spatial": 80.0 * npx,
-                        "proposal_infer": 8.0 * hits + 8.0 * cand * hits, "temporal": 48.0 * hits,
+                        "proposal_infer": 8.0 * hits + 8.0 * cand * hits, "temporal": TEMPORAL_BYTES_PER_HIT * hits,
                         "shade_finish": 72.0 * npx, "shade_request": 72.0 * hits, "compact_hits": 12.0 * npx,
                         "accumulate": 48.0 * npx}
     ab = per_launch_bytes.get(dom, 0.0)
@@ -728,6 +734,14 @@ def main():
                 "bytes_per_launch": ab,
                 "note": "the DDA is latency / ALU bound (L2-resident bricks), not HBM bound: see rays_per_s"}
     rays = hits + rays_c + rays_s
+    # the reservoir passes against the HBM roofline (bytes per unit: see TEMPORAL_BYTES_PER_HIT
+    # and the kernels' docstrings in DESIGN)
+    reservoir_roofline = {}
+    for k in ("temporal", "spatial", "shade_finish", "shade_request"):
+        if kernel_ms.get(k, 0.0) > 0:
+            gbs = per_launch_bytes[k] / (kernel_ms[k] * 1e-3) / 1e9
+            reservoir_roofline[k] = {"ms": kernel_ms[k], "bytes_per_launch": per_launch_bytes[k], "GB/s": gbs,
+                                     "frac": gbs / hbm}
     cpu = None
     if not args.no_cpu_baseline:
         cms, kind, sample = cpu_arm(args.config, args.cpu_steps, 1, W, H)
@@ -742,7 +756,7 @@ def main():
             "config": config, "plain_ms_per_frame": plain_ms if learned else ms_frame,
             "stage_ms": stage_ms, "kernel_ms": kernel_ms, "stage_roofline": stage_rooflines,
             "rays_per_frame": rays, "rays_per_s": rays / (ms_frame * 1e-3),
-            "roofline": roofline, "cpu_baseline": cpu, "quality": quality,
+            "roofline": roofline, "reservoir_roofline": reservoir_roofline, "cpu_baseline": cpu, "quality": quality,
             "frames_per_s_job": ws * 1000.0 / ms_frame,
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
                     "d2h_bytes_per_step": npx * 16, "image_ok": img_ok,
