@@ -434,6 +434,12 @@ int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame);
  * candidates for the entries it did not write, and vxr_view_wait reports VXR_E_DEVICE.
  * on = 0 restores normal operation. */
 int vxr_view_proposal_test_timeout(vxr_view* v, int on);
+/* The candidates the proposal drew for the view's current frame (after
+ * VXR_STAGE_CANDIDATES, before the next frame; no reference counterpart): *nhits hit
+ * pixels, hits[j] = pixel of hit-list entry j, cand[(m * nhits + j) * 2 + {0, 1}] = light
+ * index and bits(source pdf) of candidate m of entry j, m < min(candidates, lights).
+ * hits and cand may be NULL (then only *nhits is written). */
+int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hits, uint32_t* cand);
 int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden);
 int vxr_view_proposal_get_params(vxr_view* v, float* out);
 int vxr_view_proposal_set_params(vxr_view* v, const float* in);

@@ -72,6 +72,7 @@ def load_port():
         "orc_end_frame": (None, [C.POINTER(Camera)]),
         "orc_create": (_P, [C.c_int, C.c_int, C.c_int]), "orc_destroy": (None, [_P]),
         "orc_set_world": (None, [_P, _P, _P, _P]), "orc_set_lights": (None, [_P, _P, C.c_uint32]),
+        "orc_set_candidates": (None, [_P, _P, _P, C.c_size_t]),
         "orc_frame_start": (None, [_P]),
         "orc_stage": (None, [_P, C.POINTER(FrameConsts), C.c_int, C.c_int, C.c_int]),
         "orc_read_gbuffer": (None, [_P, C.c_int, _P]),
@@ -327,6 +328,16 @@ class Renderer:
             self.close()
         except Exception:
             pass
+
+    def set_candidates(self, idx, p):
+        """Stage 2 draws its candidates from these [m][pixel] arrays (light index, source pdf)
+        instead of uniformly (port only); None restores the uniform draw."""
+        if idx is None:
+            self._cand = None
+            self.lib.orc_set_candidates(self.h, None, None, 0)
+            return
+        self._cand = (np.ascontiguousarray(idx, np.uint32), np.ascontiguousarray(p, np.float32))
+        self.lib.orc_set_candidates(self.h, self._cand[0].ctypes.data, self._cand[1].ctypes.data, self.n)
 
     def frame_start(self):
         if self.kind == "port":

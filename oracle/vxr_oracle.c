@@ -470,7 +470,18 @@ struct orc_ctx {
     float* accum;   /* float4 */
     int resOut, resIn, gbCur, gbPrev;
     int candOut, candIn, spatOut, spatIn, shadeOut, shadeIn;
+    /* explicit candidates (the learned proposal's draws), or null: candidate m of pixel i
+     * is light candIdx[m * candStride + i] with source pdf candP[...] */
+    const uint32_t* candIdx;
+    const float* candP;
+    size_t candStride;
 };
+
+void orc_set_candidates(orc_ctx* c, const uint32_t* idx, const float* p, size_t stride) {
+    c->candIdx = idx;
+    c->candP = p;
+    c->candStride = stride;
+}
 
 orc_ctx* orc_create(int W, int H, int point_lights) {
     orc_ctx* c = (orc_ctx*)calloc(1, sizeof(orc_ctx));
@@ -687,9 +698,19 @@ static void px_candidates(orc_ctx* c, const vxr_frame_consts* k, int x, int y) {
         const v3 spo = vadd(sp, vsmul(0.1f, N));
         const uint32_t nL = k->numberOfLights;
         const uint32_t K = nL < k->numberOfCandidates ? nL : k->numberOfCandidates;
+        const size_t pi = (size_t)y * c->W + x;
         for (uint32_t i = 0; i < K; i++) {
-            const uint32_t li = (uint32_t)clampi(f2i(rnd(seed) * (int)nL), 0, (int)nL - 1);
-            const float p = 1.0f / nL;
+            /* GenerateLightCandidate (tools.cl:593-598): uniform index, p = 1/N; or the
+             * candidate and pdf a caller-supplied source drew (no draw from the pixel seed) */
+            uint32_t li;
+            float p;
+            if (c->candIdx) {
+                li = c->candIdx[i * c->candStride + pi];
+                p = c->candP[i * c->candStride + pi];
+            } else {
+                li = (uint32_t)clampi(f2i(rnd(seed) * (int)nL), 0, (int)nL - 1);
+                p = 1.0f / nL;
+            }
             const vxr_light* L = &c->lights[li];
             uint32_t ex, ey, ez;
             light_coords(L->position, &ex, &ey, &ez);

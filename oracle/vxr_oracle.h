@@ -54,6 +54,10 @@ orc_ctx* orc_create(int W, int H, int point_lights);
 void orc_destroy(orc_ctx* c);
 void orc_set_world(orc_ctx* c, const uint32_t* grid, const uint8_t* uber, const uint32_t* bricks);
 void orc_set_lights(orc_ctx* c, const vxr_light* l, uint32_t n);
+/* candidates from another source pdf for stage 2 (null: uniform, the reference's): light
+ * idx[m * stride + pixel] with pdf p[m * stride + pixel], m < min(N, numberOfCandidates);
+ * the arrays stay owned by the caller */
+void orc_set_candidates(orc_ctx* c, const uint32_t* idx, const float* p, size_t stride);
 /* buffer bookkeeping at the start of World::Render (world.cpp:2209-2223) */
 void orc_frame_start(orc_ctx* c);
 /* 1 renderAlbedo, 2 perPixelInitialSampling, 3 perPixelSpatialResampling, 4 renderRIS,

@@ -1,5 +1,6 @@
 // proposal_api.cu - C ABI of the learned candidate proposal (no reference counterpart):
 // per-view network state, online training on the view's reservoirs, checkpoints.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -478,6 +479,25 @@ int vxr_view_proposal_test_timeout(vxr_view* v, int on) {
     if (int r = check_view(v, "vxr_view_proposal_test_timeout")) return r;
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_test_timeout: enable the proposal first");
     v->prop->testTimeout = on != 0;
+    return VXR_OK;
+}
+
+int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hits, uint32_t* cand) {
+    if (int r = check_view(v, "vxr_view_proposal_read_candidates")) return r;
+    VXR_CHECK_ARG(nhits, "vxr_view_proposal_read_candidates: null nhits");
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_read_candidates: enable the proposal first");
+    CUP(cudaStreamSynchronize(v->stream), "vxr_view_proposal_read_candidates");
+    uint32_t n = 0;
+    CUP(cudaMemcpy(&n, v->buf.counters + vxr::kCtrHits, sizeof(n), cudaMemcpyDeviceToHost), "read hit count");
+    *nhits = n;
+    if (hits && n) CUP(cudaMemcpy(hits, v->buf.hits, n * sizeof(uint32_t), cudaMemcpyDeviceToHost), "read hit list");
+    if (cand && n) {
+        const uint32_t K = std::min(v->k.numberOfCandidates, v->k.numberOfLights);
+        for (uint32_t m = 0; m < K; m++)
+            CUP(cudaMemcpy(cand + (size_t)m * n * 2, p->cand + (size_t)m * v->npx, n * sizeof(uint2), cudaMemcpyDeviceToHost),
+                "read candidates");
+    }
     return VXR_OK;
 }
 

@@ -145,6 +145,7 @@ _SIGS = {
     "vxr_view_proposal_train": [_P, C.c_uint32, C.POINTER(C.c_float)],
     "vxr_view_proposal_online": [_P, C.c_uint32],
     "vxr_view_proposal_test_timeout": [_P, C.c_int],
+    "vxr_view_proposal_read_candidates": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "vxr_view_proposal_param_count": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "vxr_view_proposal_get_params": [_P, _F3], "vxr_view_proposal_set_params": [_P, _F3],
     "vxr_view_proposal_grad": [_P, C.c_uint32, _F3, C.POINTER(C.c_uint32), _F3, C.POINTER(C.c_float), _F3],
@@ -528,6 +529,18 @@ class View:
         check(self._lib.vxr_view_proposal_train(self.h, steps, C.byref(loss)))
         return loss.value
 
+
+    def proposal_candidates(self, k):
+        """(hit pixels uint32[n], candidates uint32[k, n, 2] = light, bits(pdf)) drawn by the
+        proposal for the current frame (after the candidate stage)."""
+        n = C.c_uint32()
+        check(self._lib.vxr_view_proposal_read_candidates(self.h, C.byref(n), None, None))
+        hits = np.zeros(max(n.value, 1), np.uint32)
+        cand = np.zeros((k, max(n.value, 1), 2), np.uint32)
+        P = C.POINTER(C.c_uint32)
+        check(self._lib.vxr_view_proposal_read_candidates(self.h, C.byref(n), hits.ctypes.data_as(P),
+                                                           cand.ctypes.data_as(P)))
+        return hits[:n.value], cand[:, :n.value]
 
     def proposal_test_timeout(self, on):
         """Test hook: the tensor-core inference's waits run out (error flag 16)."""

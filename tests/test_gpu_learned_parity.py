@@ -1,0 +1,73 @@
+"""The learned candidate path bit for bit against the C oracle, given the proposal's draws.
+
+The proposal's network and sampler are checked with tolerances and unbiasedness tests
+(test_gpu_proposal.py); everything after the draw is the reference's arithmetic: the
+candidate kernel weighs each drawn emitter with p_hat / p_src, keeps one by weighted
+reservoir sampling, traces its visibility, reuses temporally, then the spatial and
+shading stages run. The oracle (oracle/vxr_oracle.c) runs the same stages with the same
+candidates (read back through vxr_view_proposal_read_candidates), and every stage output
+of every frame must match bit for bit - for the mma.sync and the tcgen05 inference, with
+one network evaluation per hit pixel and per two."""
+import numpy as np
+import pytest
+
+from conftest import assert_records_equal
+from oracle import binding as ob
+
+pytestmark = pytest.mark.gpu
+
+
+def _orbit(f):
+    return (120.0 + 5.0 * f, 150.0 - 2.0 * f, 8.0 + 3.0 * f), (128.0, 118.0, 128.0)
+
+
+@pytest.mark.parametrize("clusters,inference,share", [(16, 1, 1), (256, 2, 1), (256, 2, 2)])
+def test_learned_frames_match_oracle_given_candidates(lib, cuda_device, clusters, inference, share):
+    w = lib.World()
+    if clusters == 256:
+        w.generate(lib.scene_preset(0, emitters=2048, emitter_mode=1))
+    else:
+        w.generate(lib.scene_preset(0))
+    w.cluster_lights(clusters, seed=3, iters=6)
+    g, b, l = w.arrays()
+    W, H = 128, 80
+    view = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1, num_candidates=8))
+    port = ob.Renderer("port", ob.WorldArrays(g, b, l), W, H, False)
+    try:
+        view.proposal_enable(seed=11, batch=4096, inference=inference, pixels_per_eval=share)
+        view.proposal_use(True)
+        for f in range(3):
+            view.lookat(*_orbit(f))
+            k = view.begin_frame()
+            port.frame_start()
+            ctx = f"[learned, {clusters} clusters, inference {inference}, share {share}, frame {f}]"
+            view.stage(lib.STAGE_ALBEDO)
+            port.stage(k, 1)
+            assert_records_equal("gbuffer", view.read_gbuffer(0), port.gbuffer(0), ctx)
+            view.stage(lib.STAGE_CANDIDATES)
+            K = min(k.numberOfCandidates, k.numberOfLights)
+            hits, cand = view.proposal_candidates(K)
+            assert len(hits) > 100 and (cand[:, :, 0] < len(l)).all()
+            pdf = cand[:, :, 1].view(np.float32)
+            assert (pdf > 0).all() and (pdf <= 1).all()
+            idx = np.zeros((K, W * H), np.uint32)
+            p = np.ones((K, W * H), np.float32)
+            idx[:, hits] = cand[:, :, 0]
+            p[:, hits] = pdf
+            port.set_candidates(idx, p)
+            port.stage(k, 2)
+            assert_records_equal("candidates", view.read_reservoirs(0), port.reservoirs(0), ctx)
+            assert_records_equal("seed", view.read_gbuffer(0)["seed"], port.gbuffer(0)["seed"], ctx)
+            for s in (3, 4, 5):
+                view.stage(s)
+                port.stage(k, s)
+            assert_records_equal("spatial", view.read_reservoirs(1), port.reservoirs(2), ctx)
+            assert_records_equal("frame", view.read_frame(), port.image(0), ctx)
+            assert_records_equal("accum", view.read_accum(), port.image(1), ctx)
+            view.end_frame()
+            view.wait()
+        # the learned frames differ from the uniform source's: the proposal was used
+        assert (idx[:, hits] != 0).any()
+    finally:
+        port.close()
+        view.close()
