@@ -1181,6 +1181,13 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
             ia.probs = nullptr;
             if (bd.one.k.ncand > 0) {
                 Timed tm(bd, K_INFER, s);
+                if (learned->rows) {
+                    cudaMemsetAsync(learned->rowCount, 0, sizeof(uint32_t), s);
+                    prop::launch_pair_rows(ia.k, ia.vd, ia.hits, ia.count, (uint32_t)n, learned->pairDist, learned->rows,
+                                           learned->rowCount, s);
+                    ia.rows = learned->rows;
+                    ia.rowCount = learned->rowCount;
+                }
                 prop::launch_infer(ia, (uint32_t)n, s);
             }
             launch_ris<VARIANT, true>(lb, nb, s);

@@ -125,6 +125,9 @@ void launch_build_uber_boxes(const uint32_t* grid, const uint32_t* bbox0, uint32
 struct LearnedHook {
     prop::InferArgs infer;      // dims, layout, params, BF16 weights
     uint2* cand;                // [kMaxCand][pixels] scratch for the drawn candidates
+    uint32_t* rows;             // shared evaluations: table rows [pixels] and their count (null: one per pixel)
+    uint32_t* rowCount;
+    float pairDist;             // largest per-coordinate distance of a shared pair (voxels)
     const uint32_t* clOff;      // cluster CSR on the device
     const uint32_t* clMembers;
     const uint32_t* lightCluster;

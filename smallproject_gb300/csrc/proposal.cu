@@ -540,14 +540,20 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
     bool pending = false;   // an MMA was committed whose completion no wait has seen
     const uint32_t limit = a.waitLimit ? a.waitLimit : tc::kWaitLimit;
     const bool issue = !a.skipMma;
-    // render mode with sharing: a table row serves two consecutive hit pixels (the network
-    // runs on the first one's shading point; each draws its own candidates from the row)
-    const uint32_t span = (a.share && !a.samples && !a.probs) ? 2u : 1u;
-    const uint32_t rows = (n + span - 1u) / span;
+    // render mode with sharing: a table row may serve two consecutive hit pixels (the
+    // network runs on the first one's shading point; each draws its own candidates from the
+    // row's tables)
+    const bool useRows = a.rows && !a.samples && !a.probs;
+    const uint32_t rows = useRows ? *a.rowCount : n;
     for (uint32_t tile = blockIdx.x * 2 + h; ok && (size_t)tile * tc::kTile < rows; tile += gridDim.x * 2) {
         const uint32_t row = tile * tc::kTile + tid;
-        const uint32_t j = row * span;
         const bool valid = row < rows;
+        uint32_t j = row, span = 1u;
+        if (useRows && valid) {
+            const uint32_t e = a.rows[row];
+            j = e & 0x7FFFFFFFu;
+            span = (e >> 31) ? 2u : 1u;
+        }
         float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
         uint32_t pix = 0;
         if (valid) {
@@ -984,6 +990,69 @@ bool infer_tc_supported(const Dims& d) { return d.H == 64 && d.K == 256; }
 static size_t infer_tc_smem_bytes() {
     return (size_t)64 * kIn * 2 + 2 * 64 * 64 * 2 + 256 * 64 * 2 + (3 * 64 + 256) * 4 + 260 * 4 + 2 * 128 * 64 * 2 +
            2 * 128 * (512 + 16) + 2 * 8 + 16;
+}
+
+// Table rows for shared network evaluations: pair (2i, 2i + 1) of the hit list becomes one
+// row when both shading points lie on the same voxel side (axis and facing) within maxDist
+// of each other in every coordinate, else two rows; appended per warp (one atomic each).
+__global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, const uint32_t* __restrict__ hits,
+                                 const uint32_t* __restrict__ count, float maxDist, uint32_t* rows, uint32_t* rowCount) {
+    const uint32_t n = *count, np = (n + 1u) / 2u;
+    const int lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < np; base += stride) {
+        const uint32_t i = base + (uint32_t)lane;
+        uint32_t emit = 0, e0 = 0, e1 = 0;
+        if (i < np) {
+            const uint32_t j0 = 2u * i;
+            e0 = j0;
+            emit = 1;
+            if (j0 + 1u < n) {
+                float3 sp[2];
+                uint32_t code[2];
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const uint32_t pix = hits[j0 + q];
+                    const int x = (int)(pix % (uint32_t)k.W), y = (int)(pix / (uint32_t)k.W);
+                    const uint2 gv = vd[pix];
+                    const uint32_t side = gv.x >> 24;
+                    const float dist = __uint_as_float(gv.y);
+                    const float3 D = dev::camera_ray(k, x, y);
+                    code[q] = side_code(side, dev::side_sign(side, D));
+                    sp[q] = make_float3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+                }
+                const bool close = fabsf(sp[0].x - sp[1].x) <= maxDist && fabsf(sp[0].y - sp[1].y) <= maxDist &&
+                                   fabsf(sp[0].z - sp[1].z) <= maxDist;
+                if (code[0] == code[1] && close) {
+                    e0 = j0 | 0x80000000u;
+                } else {
+                    e1 = j0 + 1u;
+                    emit = 2;
+                }
+            }
+        }
+        // warp-aggregated append
+        uint32_t pre = emit;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= o) pre += u;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+        uint32_t at = 0;
+        if (lane == 31 && total) at = atomicAdd(rowCount, total);
+        at = __shfl_sync(0xffffffffu, at, 31);
+        const uint32_t slot = at + pre - emit;
+        if (emit >= 1) rows[slot] = e0;
+        if (emit == 2) rows[slot + 1] = e1;
+    }
+}
+
+void launch_pair_rows(const dev::Frame& k, const uint2* vd, const uint32_t* hits, const uint32_t* count, uint32_t n,
+                      float maxDist, uint32_t* rows, uint32_t* rowCount, cudaStream_t s) {
+    const uint32_t np = (n + 1u) / 2u;
+    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((np + 255) / 256, (uint32_t)sms() * 8u));
+    pair_rows_kernel<<<blocks, 256, 0, s>>>(k, vd, hits, count, maxDist, rows, rowCount);
 }
 
 cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s) {

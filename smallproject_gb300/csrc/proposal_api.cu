@@ -30,6 +30,8 @@ struct Proposal {
     uint32_t* lightCluster = nullptr;
     uint64_t clusterVersion = 0;
     uint2* cand = nullptr;         // [kMaxCand][pixels]
+    uint32_t* pairRows = nullptr;  // pixels_per_eval = 2: the inference's table rows [pixels] and their count
+    uint32_t* pairCount = nullptr;
     // training batch
     uint32_t B = 0;
     float4* samples = nullptr;
@@ -61,6 +63,7 @@ struct Proposal {
 void destroy_proposal(Proposal* p) {
     if (!p) return;
     void* bufs[] = {p->params, p->grads, p->m, p->v, p->wbf, p->clOff, p->clMembers, p->lightCluster, p->cand,
+                    p->pairRows, p->pairCount,
                     p->samples, p->target, p->weight, p->X, p->H1, p->H2, p->H3, p->Z, p->dA, p->dB, p->dX, p->scal,
                     p->partials, p->lossPart, p->wpart, p->frag};
     for (void* b : bufs) cudaFree(b);
@@ -354,7 +357,9 @@ bool learned_hook(vxr_view* v, LearnedHook* h) {
     h->infer.wbf = p->wbf;
     h->infer.waitLimit = p->testTimeout ? 64u : 0u;
     h->infer.skipMma = p->testTimeout ? 1u : 0u;
-    h->infer.share = p->desc.pixels_per_eval == 2 ? 1u : 0u;
+    h->rows = p->desc.pixels_per_eval == 2 ? p->pairRows : nullptr;
+    h->rowCount = p->pairCount;
+    h->pairDist = p->desc.share_distance;
     h->cand = p->cand;
     h->clOff = p->clOff;
     h->clMembers = p->clMembers;
@@ -377,6 +382,7 @@ int vxr_proposal_default_desc(vxr_proposal_desc* d) {
     d->batch = 65536;
     d->seed = 1;
     d->pixels_per_eval = 1;
+    d->share_distance = 2.0f;
     return VXR_OK;
 }
 
@@ -406,6 +412,8 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     VXR_CHECK_ARG(desc->training <= 2, "vxr_view_proposal_enable: training must be 0 (auto), 1 (FP32) or 2 (tensor cores)");
     VXR_CHECK_ARG(desc->pixels_per_eval == 1 || desc->pixels_per_eval == 2,
                   "vxr_view_proposal_enable: pixels_per_eval must be 1 or 2");
+    VXR_CHECK_ARG(desc->pixels_per_eval == 1 || (desc->share_distance >= 0.0f && desc->share_distance <= 1e30f),
+                  "vxr_view_proposal_enable: share_distance must be finite and >= 0");
     if (desc->training == 2 && !vxr::prop::train_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tensor-core training step needs hidden = 64 and "
                                         "16 <= clusters <= 256");
@@ -425,6 +433,10 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     CUP(cudaMalloc(&p->wbf, weights_count(d) * sizeof(__nv_bfloat16)), "cudaMalloc(bf16 weights)");
     CUP(cudaMalloc(&p->cand, v->npx * vxr::prop::kMaxCand * sizeof(uint2)), "cudaMalloc(candidates)");
     CUP(cudaMalloc(&p->scal, 2 * sizeof(float)), "cudaMalloc(scalars)");
+    if (desc->pixels_per_eval == 2) {
+        CUP(cudaMalloc(&p->pairRows, v->npx * sizeof(uint32_t)), "cudaMalloc(pair rows)");
+        CUP(cudaMalloc(&p->pairCount, sizeof(uint32_t)), "cudaMalloc(pair rows)");
+    }
     CUP(cudaMemsetAsync(p->m, 0, n * sizeof(float), v->stream), "clear adam");
     CUP(cudaMemsetAsync(p->v, 0, n * sizeof(float), v->stream), "clear adam");
     vxr::prop::launch_init(p->params, p->L, d, desc->seed, v->stream);

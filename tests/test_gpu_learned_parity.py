@@ -71,3 +71,68 @@ def test_learned_frames_match_oracle_given_candidates(lib, cuda_device, clusters
     finally:
         port.close()
         view.close()
+
+
+def _shading_points(k, gb, W):
+    """Shading points (float64) and side codes (axis * 2 + facing) of the given pixels."""
+    pix = np.arange(len(gb))
+    x, y = pix % W, pix // W
+    E, p0, p1, p2 = (np.array(v[:], np.float64) for v in (k.E, k.p0, k.p1, k.p2))
+    u = (x * k.oneOverRes[0])[:, None]
+    v = (y * k.oneOverRes[1])[:, None]
+    D = p0 + (p1 - p0) * u + (p2 - p0) * v - E
+    D /= np.linalg.norm(D, axis=1, keepdims=True)
+    side = gb["side"].astype(np.int64)
+    comp = D[np.arange(len(gb)), np.minimum(side, 2)]
+    code = side * 2 + (comp > 0)
+    return E + D * gb["dist"][:, None].astype(np.float64), code
+
+
+@pytest.mark.parametrize("dist", [2.0, 1e30])
+def test_shared_evaluations_pair_only_compatible_pixels(lib, cuda_device, dist):
+    """pixels_per_eval = 2: hit entries 2i and 2i + 1 share one network evaluation exactly
+    when their shading points lie on the same voxel side within share_distance voxels (each
+    coordinate). A shared pair draws from one distribution, so an emitter both pixels drew
+    carries the same source pdf in both; pairs that clearly fail the test evaluate twice."""
+    w = lib.World()
+    w.generate(lib.scene_preset(0, emitters=2048, emitter_mode=1))
+    w.cluster_lights(256, seed=3, iters=6)
+    W, H = 160, 96
+    view = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, num_candidates=32))
+    try:
+        view.proposal_enable(seed=11, batch=4096, inference=2, pixels_per_eval=2, share_distance=dist)
+        # large random parameters: the distribution changes visibly between shading points
+        p = view.proposal_params()
+        view.proposal_set_params(np.random.default_rng(5).normal(0.0, 0.3, p.shape).astype(p.dtype))
+        view.proposal_use(True)
+        view.lookat(*_orbit(1))
+        k = view.begin_frame()
+        view.stage(lib.STAGE_ALBEDO)
+        view.stage(lib.STAGE_CANDIDATES)
+        K = min(k.numberOfCandidates, k.numberOfLights)
+        hits, cand = view.proposal_candidates(K)
+        sp, code = _shading_points(k, view.read_gbuffer(0), W)
+        view.end_frame()
+        view.wait()
+        n = len(hits) // 2 * 2
+        a, b = hits[0:n:2], hits[1:n:2]
+        gap = np.abs(sp[a] - sp[b]).max(1)
+        same = code[a] == code[b]
+        shared = same & (gap < dist * 0.99)
+        apart = ~same | (gap > dist * 1.01)
+        equal, common = np.zeros(len(a), bool), np.zeros(len(a), bool)
+        for i in range(len(a)):
+            la, pa = cand[:, 2 * i, 0], cand[:, 2 * i, 1]
+            lb, pb = cand[:, 2 * i + 1, 0], cand[:, 2 * i + 1, 1]
+            m = la[:, None] == lb[None, :]
+            if m.any():
+                common[i] = True
+                ia, ib = np.nonzero(m)
+                equal[i] = bool((pa[ia] == pb[ib]).all())
+        assert (shared & common).sum() > 200
+        assert equal[shared & common].all()
+        if dist < 1e29:
+            assert (apart & common).sum() > 20
+            assert equal[apart & common].mean() < 0.05
+    finally:
+        view.close()
