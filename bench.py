@@ -11,8 +11,9 @@ Quality protocol (untimed setup, --quality full): a converged render (FP64 mean 
 --conv-frames frames of the unbiased estimator: spatial and temporal reuse off) at path
 frame 150; the proposal's warm start, trained for --train-frames frames along the path on
 the plain method's reservoirs; then the plain method at 32 candidates (the reference's
-NUMBEROFCANDIDATES) and the learned method at every count in CANDS (and, as "learned2",
-at CANDS2 with one network evaluation per two consecutive hit pixels), the learned views
+NUMBEROFCANDIDATES) and the learned method at every count in CANDS (and, as "learned2" /
+"learned4", at CANDS2 / CANDS4 with one network evaluation per run of up to two / four
+consecutive hit pixels on the same voxel side within 2 voxels), the learned views
 running --online training steps (65,536 samples each) inside every frame on their own
 final reservoirs: per point --mse-seeds views x --mse-frames frames at the static pose,
 device ms/frame and per-frame MSE against the converged render. Intervals are 95%
@@ -262,8 +263,11 @@ def cpu_arm(config, steps, warmup, W, H):
     return ms, kind, info
 
 
-CANDS = (4, 8, 12, 16, 24, 32)
-CANDS2 = (4, 8, 12)
+CANDS = (2, 3, 4, 8, 12, 16, 24, 32)
+CANDS2 = (2, 3, 4, 8, 12)
+CANDS4 = (2, 3, 4, 8)
+# hit pixels per network evaluation of each learned family (pixels_per_eval)
+FAMILY_PPE = {"learned": 1, "learned2": 2, "learned4": 4}
 # Compulsory HBM bytes of the temporal kernel per hit pixel: own G-buffer 8, candidate
 # reservoir 32 and seed 4 always; the reprojected pixel's previous G-buffer 8 and history
 # reservoir 32 when it is on screen (99 % on the camera path); the combined reservoir 32
@@ -339,9 +343,11 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
         ref.sum64_add()
     ref.wait()
     conv_s = time.perf_counter() - t0
-    # learned: one network evaluation per hit pixel; learned2: per two consecutive hit
-    # pixels (pixels_per_eval = 2: faster inference, the pair shares one distribution)
-    points = [("plain", 32)] + [("learned", c) for c in CANDS] + [("learned2", c) for c in CANDS2]
+    # learned: one network evaluation per hit pixel; learned2 / learned4: per run of up to
+    # two / four consecutive hit pixels on the same voxel side within 2 voxels of the run's
+    # first (pixels_per_eval = 2 / 4: faster inference, the run shares one distribution)
+    points = ([("plain", 32)] + [("learned", c) for c in CANDS] + [("learned2", c) for c in CANDS2] +
+              [("learned4", c) for c in CANDS4])
     groups, table = {}, {}
     for method, c in points:
         ms_l, per_seed, kms_l = [], [], {}
@@ -351,7 +357,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
             v.lookat(pos, tgt)
             if method != "plain":
                 v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon,
-                                  pixels_per_eval=2 if method == "learned2" else 1)
+                                  pixels_per_eval=FAMILY_PPE[method])
                 v.proposal_set_params(params)
                 v.proposal_use(True)
                 v.proposal_online(online)
@@ -404,7 +410,9 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
     def at_time(fam, cands):
         at = [table[f"{fam}_{c}"] for c in cands if table[f"{fam}_{c}"]["ms"] <= p32["ms"]]
         return max(at, key=lambda r: r["ms"]) if at else None
-    ets = [r for r in (at_time("learned", CANDS), at_time("learned2", CANDS2)) if r is not None]
+    fams = {"learned": at_time("learned", CANDS), "learned2": at_time("learned2", CANDS2),
+            "learned4": at_time("learned4", CANDS4)}
+    ets = [r for r in fams.values() if r is not None]
     et = min(ets, key=lambda r: r["mse_median"]) if ets else None
     return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s,
             "epsilon": args.epsilon, "online_steps_per_frame": online,
@@ -413,9 +421,10 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
             "learned_mse_monotone_within_ci": mono,
             "decision_rule": "equal MSE: the fastest learned configuration whose bootstrap 95% interval of "
                              "MSE(learned) / MSE(plain 32) lies at or below 1; equal time: per family (learned, "
-                             "learned2 = one network evaluation per two hit pixels) the largest learned ms/frame not "
-                             "above plain's, the family with the lower median MSE there",
-            "equal_time_per_family": {"learned": at_time("learned", CANDS), "learned2": at_time("learned2", CANDS2)},
+                             "learned2 / learned4 = one network evaluation per run of up to two / four compatible hit "
+                             "pixels) the largest learned ms/frame not above plain's, the family with the lowest median "
+                             "MSE there",
+            "equal_time_per_family": fams,
             "equal_time": None if et is None else {
                 "learned": et, "mse_ratio": et["mse"] / p32["mse"], "mse_ratio_ci95": et["mse_ratio_ci95"],
                 "median_mse_ratio": et["mse_median"] / p32["mse_median"],
@@ -525,7 +534,7 @@ def main():
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
     ap.add_argument("--online", type=int, default=1, help="proposal training steps inside every learned frame")
-    ap.add_argument("--pixels-per-eval", type=int, default=1, choices=[1, 2],
+    ap.add_argument("--pixels-per-eval", type=int, default=1, choices=[1, 2, 4],
                     help="learned method with --quality train: hit pixels per network evaluation")
     args = ap.parse_args()
     W, H = args.width, args.height
@@ -601,9 +610,9 @@ def main():
         eq = quality["learned_at_equal_mse"] if quality else None
         learned = eq is not None
         cand = eq["candidates"] if learned else 32
-        share = 2 if learned and eq["method"] == "learned2" else 1
+        share = FAMILY_PPE[eq["method"]] if learned else 1
         config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32), "
-                            f"{'one network evaluation per two hit pixels, ' if share == 2 else ''}{args.online} "
+                            f"{f'one network evaluation per run of up to {share} compatible hit pixels, ' if share > 1 else ''}{args.online} "
                             "training step(s) of 65,536 samples inside every frame" if learned
                             else "plain uniform-source RIS, 32 candidates")
 

@@ -411,10 +411,11 @@ typedef struct vxr_proposal_desc {
     uint32_t seed;            /* parameter initialisation */
     uint32_t inference;       /* 0 auto (tcgen05 when hidden = 64 and 256 clusters, else mma.sync), 1 mma.sync, 2 tcgen05 */
     uint32_t training;        /* 0 auto (tensor cores when hidden = 64 and clusters <= 256, else FP32), 1 FP32, 2 tensor cores */
-    uint32_t pixels_per_eval; /* tcgen05 inference: 1 = one network evaluation per hit pixel, 2 = one per two consecutive
-                                 hit pixels whose shading points lie on the same voxel side within share_distance
-                                 (both sample from the first one's distribution; still unbiased), one per pixel else */
-    float share_distance;     /* pixels_per_eval = 2: largest per-coordinate distance (voxels) of a shared pair */
+    uint32_t pixels_per_eval; /* tcgen05 inference: 1 = one network evaluation per hit pixel; 2 or 4 = one per run of up to
+                                 that many consecutive hit pixels whose shading points lie on the same voxel side as the
+                                 run's first within share_distance (all sample from the first one's distribution; still
+                                 unbiased) */
+    float share_distance;     /* pixels_per_eval > 1: largest per-coordinate distance (voxels) within a shared run */
 } vxr_proposal_desc;
 int vxr_proposal_default_desc(vxr_proposal_desc* d);
 /* Allocate and initialise the network for this view; K = the world's cluster count. */

@@ -1183,8 +1183,8 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
                 Timed tm(bd, K_INFER, s);
                 if (learned->rows) {
                     cudaMemsetAsync(learned->rowCount, 0, sizeof(uint32_t), s);
-                    prop::launch_pair_rows(ia.k, ia.vd, ia.hits, ia.count, (uint32_t)n, learned->pairDist, learned->rows,
-                                           learned->rowCount, s);
+                    prop::launch_pair_rows(ia.k, ia.vd, ia.hits, ia.count, (uint32_t)n, learned->group,
+                                           learned->pairDist, learned->rows, learned->rowCount, s);
                     ia.rows = learned->rows;
                     ia.rowCount = learned->rowCount;
                 }

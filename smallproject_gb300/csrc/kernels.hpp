@@ -127,7 +127,8 @@ struct LearnedHook {
     uint2* cand;                // [kMaxCand][pixels] scratch for the drawn candidates
     uint32_t* rows;             // shared evaluations: table rows [pixels] and their count (null: one per pixel)
     uint32_t* rowCount;
-    float pairDist;             // largest per-coordinate distance of a shared pair (voxels)
+    uint32_t group;             // hit entries a shared evaluation may serve (2 or 4)
+    float pairDist;             // largest per-coordinate distance within a shared row (voxels)
     const uint32_t* clOff;      // cluster CSR on the device
     const uint32_t* clMembers;
     const uint32_t* lightCluster;

@@ -540,9 +540,9 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
     bool pending = false;   // an MMA was committed whose completion no wait has seen
     const uint32_t limit = a.waitLimit ? a.waitLimit : tc::kWaitLimit;
     const bool issue = !a.skipMma;
-    // render mode with sharing: a table row may serve two consecutive hit pixels (the
-    // network runs on the first one's shading point; each draws its own candidates from the
-    // row's tables)
+    // render mode with sharing: a table row may serve up to four consecutive hit pixels
+    // (the network runs on the first one's shading point; each draws its own candidates
+    // from the row's tables)
     const bool useRows = a.rows && !a.samples && !a.probs;
     const uint32_t rows = useRows ? *a.rowCount : n;
     for (uint32_t tile = blockIdx.x * 2 + h; ok && (size_t)tile * tc::kTile < rows; tile += gridDim.x * 2) {
@@ -551,8 +551,8 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
         uint32_t j = row, span = 1u;
         if (useRows && valid) {
             const uint32_t e = a.rows[row];
-            j = e & 0x7FFFFFFFu;
-            span = (e >> 31) ? 2u : 1u;
+            j = e & 0x3FFFFFFFu;
+            span = (e >> 30) + 1u;
         }
         float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
         uint32_t pix = 0;
@@ -696,55 +696,55 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
             }
             continue;
         }
-        // the hit pixel this thread draws for: with sharing its own one of the pair (all its
-        // candidates), else the row's pixel (every other candidate, the other warpgroup
-        // taking the rest; both advance the pixel's RNG alike)
-        const uint32_t jm = j + (span == 2u ? (uint32_t)half : 0u);
-        if (jm >= n) continue;
-        const uint32_t pm = span == 2u ? a.hits[jm] : pix;
-        uint32_t s = dev::wang_hash(pm * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
+        // the hit pixels this thread draws for: in a shared row the row's entries j + half,
+        // j + half + 2 (all their candidates), else the row's pixel (every other candidate,
+        // the other warpgroup taking the rest; both advance the pixel's RNG alike)
         const float eps = d.eps, invN = 1.0f / (float)a.nlights;
-        uint2* out = a.cand + jm;
+        for (uint32_t jm = j + (span > 1u ? (uint32_t)half : 0u); jm < j + span; jm += 2u) {
+            const uint32_t pm = span > 1u ? a.hits[jm] : pix;
+            uint32_t s = dev::wang_hash(pm * 2654435761u + a.k.R0 * 0x85EBCA6Bu + 0x9E3779B9u);
+            uint2* out = a.cand + jm;
 #pragma unroll 4
-        for (uint32_t m = 0; m < a.ncand; m++) {
-            const float u = dev::rnd(s);
-            const float v = dev::rnd(s);
-            const float w = dev::rnd(s);
-            if (span == 1u && (int)(m & 1u) != half) continue;   // the other warpgroup's candidate
-            int c;
-            uint32_t e;
-            float gw;
-            if (u < eps) {
-                e = min((uint32_t)(v * (float)a.nlights), a.nlights - 1u);
-                c = (int)__ldg(a.lightCluster + e);
-                const int q = c / gs;
-                float lo = 0.0f, hi = P[0];
+            for (uint32_t m = 0; m < a.ncand; m++) {
+                const float u = dev::rnd(s);
+                const float v = dev::rnd(s);
+                const float w = dev::rnd(s);
+                if (span == 1u && (int)(m & 1u) != half) continue;   // the other warpgroup's candidate
+                int c;
+                uint32_t e;
+                float gw;
+                if (u < eps) {
+                    e = min((uint32_t)(v * (float)a.nlights), a.nlights - 1u);
+                    c = (int)__ldg(a.lightCluster + e);
+                    const int q = c / gs;
+                    float lo = 0.0f, hi = P[0];
 #pragma unroll
-                for (int i = 1; i < 16; i++)
-                    if (q == i) { lo = P[i - 1]; hi = P[i]; }
-                gw = hi - lo;
-            } else {
-                const float target = v * Z;
-                int q = 0;
-                float lo = 0.0f, hi = P[0];
+                    for (int i = 1; i < 16; i++)
+                        if (q == i) { lo = P[i - 1]; hi = P[i]; }
+                    gw = hi - lo;
+                } else {
+                    const float target = v * Z;
+                    int q = 0;
+                    float lo = 0.0f, hi = P[0];
 #pragma unroll
-                for (int i = 0; i < 15; i++)
-                    if (target >= P[i]) { q = i + 1; lo = P[i]; hi = P[i + 1]; }
-                gw = hi - lo;
-                const float x = gw > 0.0f ? (target - lo) * (65535.0f / gw) : 0.0f;
-                const uint4 a0 = *reinterpret_cast<const uint4*>(fp + q * 16);
-                const uint4 a1 = *reinterpret_cast<const uint4*>(fp + q * 16 + 8);
-                const uint32_t wv[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-                int in = 0;
+                    for (int i = 0; i < 15; i++)
+                        if (target >= P[i]) { q = i + 1; lo = P[i]; hi = P[i + 1]; }
+                    gw = hi - lo;
+                    const float x = gw > 0.0f ? (target - lo) * (65535.0f / gw) : 0.0f;
+                    const uint4 a0 = *reinterpret_cast<const uint4*>(fp + q * 16);
+                    const uint4 a1 = *reinterpret_cast<const uint4*>(fp + q * 16 + 8);
+                    const uint32_t wv[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                    int in = 0;
 #pragma unroll
-                for (int i = 0; i < 15; i++) in += x >= (float)((wv[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu) ? 1 : 0;
-                c = q * gs + in;
-                const uint32_t off = offs[c], sz = offs[c + 1] - off;
-                e = __ldg(a.clMembers + off + min((uint32_t)(w * (float)sz), sz - 1u));
+                    for (int i = 0; i < 15; i++) in += x >= (float)((wv[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu) ? 1 : 0;
+                    c = q * gs + in;
+                    const uint32_t off = offs[c], sz = offs[c + 1] - off;
+                    e = __ldg(a.clMembers + off + min((uint32_t)(w * (float)sz), sz - 1u));
+                }
+                const float sz = (float)(offs[c + 1] - offs[c]);
+                const float pe = (1.0f - eps) * (((gw * frac(c)) * invZ) / sz) + eps * invN;
+                out[(size_t)m * a.candStride] = make_uint2(e, __float_as_uint(pe));
             }
-            const float sz = (float)(offs[c + 1] - offs[c]);
-            const float pe = (1.0f - eps) * (((gw * frac(c)) * invZ) / sz) + eps * invN;
-            out[(size_t)m * a.candStride] = make_uint2(e, __float_as_uint(pe));
         }
     }
     // every MMA of this CTA has completed (each was waited for) unless a wait gave up
@@ -992,44 +992,57 @@ static size_t infer_tc_smem_bytes() {
            2 * 128 * (512 + 16) + 2 * 8 + 16;
 }
 
-// Table rows for shared network evaluations: pair (2i, 2i + 1) of the hit list becomes one
-// row when both shading points lie on the same voxel side (axis and facing) within maxDist
-// of each other in every coordinate, else two rows; appended per warp (one atomic each).
+// Table rows for shared network evaluations. The hit list is cut into aligned groups of
+// `group` entries (2 or 4); inside a group, a run of consecutive entries whose shading
+// points lie on the same voxel side (axis and facing) as the run's first entry, within
+// maxDist of it in every coordinate, becomes one row (first entry | (length - 1) << 30);
+// an entry that fails the test starts the next run. Rows are appended per warp (one
+// atomic each), so their order is not the hit list's.
 __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, const uint32_t* __restrict__ hits,
-                                 const uint32_t* __restrict__ count, float maxDist, uint32_t* rows, uint32_t* rowCount) {
-    const uint32_t n = *count, np = (n + 1u) / 2u;
+                                 const uint32_t* __restrict__ count, uint32_t group, float maxDist, uint32_t* rows,
+                                 uint32_t* rowCount) {
+    const uint32_t n = *count, ng = (n + group - 1u) / group;
     const int lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < np; base += stride) {
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < ng; base += stride) {
         const uint32_t i = base + (uint32_t)lane;
-        uint32_t emit = 0, e0 = 0, e1 = 0;
-        if (i < np) {
-            const uint32_t j0 = 2u * i;
-            e0 = j0;
-            emit = 1;
-            if (j0 + 1u < n) {
-                float3 sp[2];
-                uint32_t code[2];
+        uint32_t emit = 0, r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+        if (i < ng) {
+            const uint32_t j0 = i * group, m = min(group, n - j0);
+            float3 f = make_float3(0.0f, 0.0f, 0.0f);   // the current run's first shading point
+            uint32_t fcode = 0, start = 0;
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    const uint32_t pix = hits[j0 + q];
-                    const int x = (int)(pix % (uint32_t)k.W), y = (int)(pix / (uint32_t)k.W);
-                    const uint2 gv = vd[pix];
-                    const uint32_t side = gv.x >> 24;
-                    const float dist = __uint_as_float(gv.y);
-                    const float3 D = dev::camera_ray(k, x, y);
-                    code[q] = side_code(side, dev::side_sign(side, D));
-                    sp[q] = make_float3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+            for (uint32_t q = 0; q < 4; q++) {
+                if (q >= m) break;
+                const uint32_t pix = hits[j0 + q];
+                const int x = (int)(pix % (uint32_t)k.W), y = (int)(pix / (uint32_t)k.W);
+                const uint2 gv = vd[pix];
+                const uint32_t side = gv.x >> 24;
+                const float dist = __uint_as_float(gv.y);
+                const float3 D = dev::camera_ray(k, x, y);
+                const uint32_t code = side_code(side, dev::side_sign(side, D));
+                const float3 sp = make_float3(D.x * dist + k.E.x, D.y * dist + k.E.y, D.z * dist + k.E.z);
+                const bool join = q > 0 && code == fcode && fabsf(sp.x - f.x) <= maxDist &&
+                                  fabsf(sp.y - f.y) <= maxDist && fabsf(sp.z - f.z) <= maxDist;
+                if (q > 0 && !join) {
+                    const uint32_t row = (j0 + start) | ((q - start - 1u) << 30);
+                    r0 = emit == 0 ? row : r0;
+                    r1 = emit == 1 ? row : r1;
+                    r2 = emit == 2 ? row : r2;
+                    emit++;
+                    start = q;
                 }
-                const bool close = fabsf(sp[0].x - sp[1].x) <= maxDist && fabsf(sp[0].y - sp[1].y) <= maxDist &&
-                                   fabsf(sp[0].z - sp[1].z) <= maxDist;
-                if (code[0] == code[1] && close) {
-                    e0 = j0 | 0x80000000u;
-                } else {
-                    e1 = j0 + 1u;
-                    emit = 2;
+                if (!join) {
+                    f = sp;
+                    fcode = code;
                 }
             }
+            const uint32_t row = (j0 + start) | ((m - start - 1u) << 30);
+            r0 = emit == 0 ? row : r0;
+            r1 = emit == 1 ? row : r1;
+            r2 = emit == 2 ? row : r2;
+            r3 = emit == 3 ? row : r3;
+            emit++;
         }
         // warp-aggregated append
         uint32_t pre = emit;
@@ -1043,16 +1056,18 @@ __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, con
         if (lane == 31 && total) at = atomicAdd(rowCount, total);
         at = __shfl_sync(0xffffffffu, at, 31);
         const uint32_t slot = at + pre - emit;
-        if (emit >= 1) rows[slot] = e0;
-        if (emit == 2) rows[slot + 1] = e1;
+        if (emit > 0) rows[slot] = r0;
+        if (emit > 1) rows[slot + 1] = r1;
+        if (emit > 2) rows[slot + 2] = r2;
+        if (emit > 3) rows[slot + 3] = r3;
     }
 }
 
 void launch_pair_rows(const dev::Frame& k, const uint2* vd, const uint32_t* hits, const uint32_t* count, uint32_t n,
-                      float maxDist, uint32_t* rows, uint32_t* rowCount, cudaStream_t s) {
-    const uint32_t np = (n + 1u) / 2u;
-    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((np + 255) / 256, (uint32_t)sms() * 8u));
-    pair_rows_kernel<<<blocks, 256, 0, s>>>(k, vd, hits, count, maxDist, rows, rowCount);
+                      uint32_t group, float maxDist, uint32_t* rows, uint32_t* rowCount, cudaStream_t s) {
+    const uint32_t ng = (n + group - 1u) / group;
+    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((ng + 255) / 256, (uint32_t)sms() * 8u));
+    pair_rows_kernel<<<blocks, 256, 0, s>>>(k, vd, hits, count, group, maxDist, rows, rowCount);
 }
 
 cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s) {

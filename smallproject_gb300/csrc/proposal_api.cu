@@ -55,6 +55,13 @@ struct Proposal {
     float* wpart = nullptr;        // weight sums per wsum block
     bool encGradDirty = true;      // the hash-table gradient is not known to be zero
     uint32_t online = 0;           // training steps run by every rendered frame
+    // the frame's training step past its gather runs on a side stream and overlaps the next
+    // frame's primary rays; the view stream joins it (proposal_join) before anything reads
+    // the parameters or writes the batch again
+    cudaStream_t trainStream = nullptr;
+    cudaEvent_t forkEv = nullptr;
+    cudaEvent_t joinEv = nullptr;
+    bool trainPending = false;
     bool testTimeout = false;      // test hook: the inference issues no MMA and its waits give up
     int step = 0;
     uint32_t gatherOffset = 0;
@@ -62,6 +69,12 @@ struct Proposal {
 
 void destroy_proposal(Proposal* p) {
     if (!p) return;
+    if (p->trainStream) {
+        cudaStreamSynchronize(p->trainStream);
+        cudaStreamDestroy(p->trainStream);
+    }
+    if (p->forkEv) cudaEventDestroy(p->forkEv);
+    if (p->joinEv) cudaEventDestroy(p->joinEv);
     void* bufs[] = {p->params, p->grads, p->m, p->v, p->wbf, p->clOff, p->clMembers, p->lightCluster, p->cand,
                     p->pairRows, p->pairCount,
                     p->samples, p->target, p->weight, p->X, p->H1, p->H2, p->H3, p->Z, p->dA, p->dB, p->dX, p->scal,
@@ -242,7 +255,8 @@ int fused_step(vxr::Proposal* p, uint32_t B, bool apply, cudaStream_t s) {
 }
 
 // one training step on a batch gathered from the view's current frame
-int train_on_frame(vxr_view* v, vxr::Proposal* p) {
+// the frame's training batch (B samples of its final reservoirs), on the view stream
+static void gather_frame(vxr_view* v, vxr::Proposal* p) {
     const uint32_t B = p->desc.batch;
     vxr::prop::GatherArgs ga{};
     ga.k = vxr::dev_frame(v->k);
@@ -259,14 +273,24 @@ int train_on_frame(vxr_view* v, vxr::Proposal* p) {
     ga.weight = p->weight;
     p->gatherOffset = p->gatherOffset * 1664525u + 1013904223u;
     vxr::prop::launch_gather(ga, v->stream);
-    if (p->fused) return fused_step(p, B, true, v->stream);
-    forward_backward(p, B, v->stream);
+}
+
+// one training step on the gathered batch (forward, backward, Adam), on stream s
+static int train_batch(vxr::Proposal* p, cudaStream_t s) {
+    const uint32_t B = p->desc.batch;
+    if (p->fused) return fused_step(p, B, true, s);
+    forward_backward(p, B, s);
     p->encGradDirty = true;
     p->step++;
-    vxr::prop::launch_adam(p->params, p->grads, p->m, p->v, p->L.total, p->desc.learning_rate, p->step, v->stream);
-    refresh_bf16(p, v->stream);
+    vxr::prop::launch_adam(p->params, p->grads, p->m, p->v, p->L.total, p->desc.learning_rate, p->step, s);
+    refresh_bf16(p, s);
     CUP(cudaGetLastError(), "proposal training");
     return VXR_OK;
+}
+
+int train_on_frame(vxr_view* v, vxr::Proposal* p) {
+    gather_frame(v, p);
+    return train_batch(p, v->stream);
 }
 
 // forward + backward of the weighted cross-entropy on the batch in p->samples/target/weight;
@@ -331,23 +355,48 @@ void forward_backward(vxr::Proposal* p, uint32_t B, cudaStream_t s) {
 }  // namespace
 
 namespace vxr {
+void proposal_join(vxr_view* v);
+
 // the online training steps of a rendered frame (after shading: the frame's final
-// reservoirs), enqueued on the view's stream; nothing when the view samples uniformly
+// reservoirs): the gather on the view's stream, the rest on the proposal's side stream;
+// nothing when the view samples uniformly
 int proposal_frame_train(vxr_view* v) {
     Proposal* p = v->prop;
     if (!v->useProposal || !p || !p->online) return VXR_OK;
+    proposal_join(v);
     if (p->clusterVersion != v->world->w.clusterVersion)
         if (int r = upload_clusters(v, p)) return r;
     if (int r = ensure_batch(p, p->desc.batch)) return r;
-    if (v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, false, v->stream);
-    for (uint32_t i = 0; i < p->online; i++)
-        if (int r = train_on_frame(v, p)) return r;
-    if (v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, true, v->stream);
+    if (!p->trainStream) {
+        CUP(cudaStreamCreateWithFlags(&p->trainStream, cudaStreamNonBlocking), "cudaStreamCreate(training)");
+        CUP(cudaEventCreateWithFlags(&p->forkEv, cudaEventDisableTiming), "cudaEventCreate");
+        CUP(cudaEventCreateWithFlags(&p->joinEv, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    for (uint32_t i = 0; i < p->online; i++) {
+        proposal_join(v);   // a previous step still reads the batch the gather overwrites
+        gather_frame(v, p);
+        CUP(cudaEventRecord(p->forkEv, v->stream), "cudaEventRecord");
+        CUP(cudaStreamWaitEvent(p->trainStream, p->forkEv, 0), "cudaStreamWaitEvent");
+        if (i == 0 && v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, false, p->trainStream);
+        if (int r = train_batch(p, p->trainStream)) return r;
+        if (i + 1 == p->online && v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, true, p->trainStream);
+        CUP(cudaEventRecord(p->joinEv, p->trainStream), "cudaEventRecord");
+        p->trainPending = true;
+    }
     return VXR_OK;
+}
+
+void proposal_join(vxr_view* v) {
+    Proposal* p = v->prop;
+    if (p && p->trainPending) {
+        cudaStreamWaitEvent(v->stream, p->joinEv, 0);
+        p->trainPending = false;
+    }
 }
 
 // the candidate stage's hook (nullptr when the view samples uniformly)
 bool learned_hook(vxr_view* v, LearnedHook* h) {
+    proposal_join(v);   // the inference reads the weights the last training step wrote
     Proposal* p = v->prop;
     if (!v->useProposal || !p) return false;
     h->infer = prop::InferArgs{};
@@ -357,8 +406,9 @@ bool learned_hook(vxr_view* v, LearnedHook* h) {
     h->infer.wbf = p->wbf;
     h->infer.waitLimit = p->testTimeout ? 64u : 0u;
     h->infer.skipMma = p->testTimeout ? 1u : 0u;
-    h->rows = p->desc.pixels_per_eval == 2 ? p->pairRows : nullptr;
+    h->rows = p->desc.pixels_per_eval > 1 ? p->pairRows : nullptr;
     h->rowCount = p->pairCount;
+    h->group = p->desc.pixels_per_eval;
     h->pairDist = p->desc.share_distance;
     h->cand = p->cand;
     h->clOff = p->clOff;
@@ -388,6 +438,7 @@ int vxr_proposal_default_desc(vxr_proposal_desc* d) {
 
 int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     if (int r = check_view(v, "vxr_view_proposal_enable")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(desc, "vxr_view_proposal_enable: null desc");
     VXR_CHECK_ARG(desc->epsilon > 0.0f && desc->epsilon <= 1.0f, "vxr_view_proposal_enable: epsilon must be in (0, 1]");
     VXR_CHECK_ARG(desc->table_log2 >= 8 && desc->table_log2 <= 22, "vxr_view_proposal_enable: table_log2 in [8, 22]");
@@ -410,8 +461,8 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     if (d.kernel == 2 && !vxr::prop::infer_tc_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tcgen05 inference needs hidden = 64 and 256 clusters");
     VXR_CHECK_ARG(desc->training <= 2, "vxr_view_proposal_enable: training must be 0 (auto), 1 (FP32) or 2 (tensor cores)");
-    VXR_CHECK_ARG(desc->pixels_per_eval == 1 || desc->pixels_per_eval == 2,
-                  "vxr_view_proposal_enable: pixels_per_eval must be 1 or 2");
+    VXR_CHECK_ARG(desc->pixels_per_eval == 1 || desc->pixels_per_eval == 2 || desc->pixels_per_eval == 4,
+                  "vxr_view_proposal_enable: pixels_per_eval must be 1, 2 or 4");
     VXR_CHECK_ARG(desc->pixels_per_eval == 1 || (desc->share_distance >= 0.0f && desc->share_distance <= 1e30f),
                   "vxr_view_proposal_enable: share_distance must be finite and >= 0");
     if (desc->training == 2 && !vxr::prop::train_supported(d))
@@ -433,7 +484,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     CUP(cudaMalloc(&p->wbf, weights_count(d) * sizeof(__nv_bfloat16)), "cudaMalloc(bf16 weights)");
     CUP(cudaMalloc(&p->cand, v->npx * vxr::prop::kMaxCand * sizeof(uint2)), "cudaMalloc(candidates)");
     CUP(cudaMalloc(&p->scal, 2 * sizeof(float)), "cudaMalloc(scalars)");
-    if (desc->pixels_per_eval == 2) {
+    if (desc->pixels_per_eval > 1) {
         CUP(cudaMalloc(&p->pairRows, v->npx * sizeof(uint32_t)), "cudaMalloc(pair rows)");
         CUP(cudaMalloc(&p->pairCount, sizeof(uint32_t)), "cudaMalloc(pair rows)");
     }
@@ -449,6 +500,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
 
 int vxr_view_proposal_use(vxr_view* v, int on) {
     if (int r = check_view(v, "vxr_view_proposal_use")) return r;
+    vxr::proposal_join(v);
     if (on && !v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_use: enable the proposal first");
     if (on && v->prop->clusterVersion != v->world->w.clusterVersion)
         if (int r = upload_clusters(v, v->prop)) return r;
@@ -458,6 +510,7 @@ int vxr_view_proposal_use(vxr_view* v, int on) {
 
 int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
     if (int r = check_view(v, "vxr_view_proposal_train")) return r;
+    vxr::proposal_join(v);
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_train: enable the proposal first");
     if (p->clusterVersion != v->world->w.clusterVersion)
@@ -479,6 +532,7 @@ int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
 
 int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame) {
     if (int r = check_view(v, "vxr_view_proposal_online")) return r;
+    vxr::proposal_join(v);
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_online: enable the proposal first");
     VXR_CHECK_ARG(steps_per_frame <= 16, "vxr_view_proposal_online: at most 16 steps per frame");
     if (steps_per_frame)
@@ -489,6 +543,7 @@ int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame) {
 
 int vxr_view_proposal_test_timeout(vxr_view* v, int on) {
     if (int r = check_view(v, "vxr_view_proposal_test_timeout")) return r;
+    vxr::proposal_join(v);
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_test_timeout: enable the proposal first");
     v->prop->testTimeout = on != 0;
     return VXR_OK;
@@ -496,6 +551,7 @@ int vxr_view_proposal_test_timeout(vxr_view* v, int on) {
 
 int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hits, uint32_t* cand) {
     if (int r = check_view(v, "vxr_view_proposal_read_candidates")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(nhits, "vxr_view_proposal_read_candidates: null nhits");
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_read_candidates: enable the proposal first");
@@ -515,6 +571,7 @@ int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hi
 
 int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden) {
     if (int r = check_view(v, "vxr_view_proposal_param_count")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(n, "vxr_view_proposal_param_count: null output");
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_param_count: enable the proposal first");
     *n = v->prop->L.total;
@@ -525,6 +582,7 @@ int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, 
 
 int vxr_view_proposal_get_params(vxr_view* v, float* out) {
     if (int r = check_view(v, "vxr_view_proposal_get_params")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(out, "vxr_view_proposal_get_params: null output");
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_get_params: enable the proposal first");
     CUP(cudaStreamSynchronize(v->stream), "sync");
@@ -534,6 +592,7 @@ int vxr_view_proposal_get_params(vxr_view* v, float* out) {
 
 int vxr_view_proposal_set_params(vxr_view* v, const float* in) {
     if (int r = check_view(v, "vxr_view_proposal_set_params")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(in, "vxr_view_proposal_set_params: null input");
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_set_params: enable the proposal first");
     CUP(cudaStreamSynchronize(v->stream), "sync");
@@ -546,6 +605,7 @@ int vxr_view_proposal_set_params(vxr_view* v, const float* in) {
 int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const uint32_t* target, const float* weight,
                            float* loss, float* grad) {
     if (int r = check_view(v, "vxr_view_proposal_grad")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(B >= 1 && samples && target && weight && loss && grad, "vxr_view_proposal_grad: bad argument");
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_grad: enable the proposal first");
@@ -573,6 +633,7 @@ int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const 
 
 int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float* probs) {
     if (int r = check_view(v, "vxr_view_proposal_probs")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(n >= 1 && samples && probs, "vxr_view_proposal_probs: bad argument");
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_probs: enable the proposal first");
@@ -613,6 +674,7 @@ int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float
 // checkpoint: magic, version, dims, step, params, Adam moments
 int vxr_view_proposal_save(vxr_view* v, const char* path) {
     if (int r = check_view(v, "vxr_view_proposal_save")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(path, "vxr_view_proposal_save: null path");
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_save: enable the proposal first");
@@ -635,6 +697,7 @@ int vxr_view_proposal_save(vxr_view* v, const char* path) {
 
 int vxr_view_proposal_load(vxr_view* v, const char* path) {
     if (int r = check_view(v, "vxr_view_proposal_load")) return r;
+    vxr::proposal_join(v);
     VXR_CHECK_ARG(path, "vxr_view_proposal_load: null path");
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_load: enable the proposal first (same shape)");

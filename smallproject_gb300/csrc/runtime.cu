@@ -186,6 +186,7 @@ static int upload(World& w) {
 namespace vxr {
 bool learned_hook(vxr_view* v, LearnedHook* h);
 int proposal_frame_train(vxr_view* v);
+void proposal_join(vxr_view* v);   // the view stream waits for the frame's training step
 }
 
 using vxr::set_error;
@@ -735,8 +736,11 @@ int vxr_view_render(vxr_view* v) {
     return vxr_view_end_frame(v);
 }
 
-int vxr_view_wait(vxr_view* v) {
-    if (int r = check_view(v, "vxr_view_wait")) return r;
+// waits for the view's stream; join: also for the online training step still running on
+// its side stream (render_to_host returns once the image is on the host, the step
+// overlapping the caller's next frame)
+static int view_wait(vxr_view* v, bool join) {
+    if (join) vxr::proposal_join(v);
     CUV(cudaStreamSynchronize(v->stream), "vxr_view_wait");
     for (int s = 1; s <= 5; s++) {
         float ms = 0.0f;
@@ -744,7 +748,9 @@ int vxr_view_wait(vxr_view* v) {
         v->times[s - 1] = ms;
     }
     harvest(v);
-    if (v->ktimer) v->ktimer->harvest();
+    // kernel times once every marked kernel has run (the training step's marks are on its
+    // side stream)
+    if (v->ktimer && join) v->ktimer->harvest();
     uint32_t err = 0;
     CUV(cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost), "read device error flags");
     if (err) {
@@ -752,6 +758,11 @@ int vxr_view_wait(vxr_view* v) {
         return set_error(VXR_E_DEVICE, vxr::device_flags_message(err));
     }
     return VXR_OK;
+}
+
+int vxr_view_wait(vxr_view* v) {
+    if (int r = check_view(v, "vxr_view_wait")) return r;
+    return view_wait(v, true);
 }
 
 int vxr_view_stage_times(vxr_view* v, float ms[5]) {
@@ -875,7 +886,7 @@ int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[
     if (int r = vxr_view_lookat(v, pos, target)) return r;
     if (int r = vxr_view_render(v)) return r;
     CUV(cudaMemcpyAsync(host_rgba, v->buf.accum, v->npx * sizeof(float4), cudaMemcpyDeviceToHost, v->stream), "copy image");
-    return vxr_view_wait(v);
+    return view_wait(v, false);
 }
 
 }  // extern "C"
@@ -945,6 +956,7 @@ int vxr_view_timer_begin(vxr_view* v) {
 int vxr_view_timer_end(vxr_view* v, float* ms) {
     if (int r = check_view(v, "vxr_view_timer_end")) return r;
     VXR_CHECK_ARG(ms, "vxr_view_timer_end: null output");
+    vxr::proposal_join(v);   // the timed region ends after the last frame's training step
     CUV(cudaEventRecord(v->eve[0], v->stream), "cudaEventRecord");
     CUV(cudaEventSynchronize(v->eve[0]), "cudaEventSynchronize");
     CUV(cudaEventElapsedTime(ms, v->evs[0], v->eve[0]), "cudaEventElapsedTime");
