@@ -21,7 +21,7 @@ def _orbit(f):
     return (120.0 + 5.0 * f, 150.0 - 2.0 * f, 8.0 + 3.0 * f), (128.0, 118.0, 128.0)
 
 
-@pytest.mark.parametrize("clusters,inference,share", [(16, 1, 1), (256, 2, 1), (256, 2, 2)])
+@pytest.mark.parametrize("clusters,inference,share", [(16, 1, 1), (256, 2, 1), (256, 2, 2), (256, 2, 4)])
 def test_learned_frames_match_oracle_given_candidates(lib, cuda_device, clusters, inference, share):
     w = lib.World()
     if clusters == 256:
@@ -88,19 +88,40 @@ def _shading_points(k, gb, W):
     return E + D * gb["dist"][:, None].astype(np.float64), code
 
 
-@pytest.mark.parametrize("dist", [2.0, 1e30])
-def test_shared_evaluations_pair_only_compatible_pixels(lib, cuda_device, dist):
-    """pixels_per_eval = 2: hit entries 2i and 2i + 1 share one network evaluation exactly
-    when their shading points lie on the same voxel side within share_distance voxels (each
-    coordinate). A shared pair draws from one distribution, so an emitter both pixels drew
-    carries the same source pdf in both; pairs that clearly fail the test evaluate twice."""
+def _runs(sp, code, hits, group, dist):
+    """Runs of the hit list as the pairing kernel forms them (aligned groups of `group`
+    entries, a run extended while an entry is on the first one's voxel side within `dist`
+    of it in every coordinate), and whether any test sat within 1 % of `dist`."""
+    runs, unsure = [], False
+    n = len(hits)
+    for g0 in range(0, n, group):
+        m = min(group, n - g0)
+        start = 0
+        for q in range(1, m):
+            a, b = hits[g0 + start], hits[g0 + q]
+            gap = np.abs(sp[a] - sp[b]).max()
+            unsure |= code[a] == code[b] and abs(gap - dist) <= 0.01 * dist
+            if not (code[a] == code[b] and gap <= dist):
+                runs.append((g0 + start, q - start))
+                start = q
+        runs.append((g0 + start, m - start))
+    return runs, unsure
+
+
+@pytest.mark.parametrize("group,dist", [(2, 2.0), (2, 1e30), (4, 2.0)])
+def test_shared_evaluations_pair_only_compatible_pixels(lib, cuda_device, group, dist):
+    """pixels_per_eval = 2 or 4: the hit list in aligned groups of that many entries; a run
+    of entries on the voxel side of its first entry, within share_distance voxels of it in
+    every coordinate, shares one network evaluation. Pixels of one run draw from one
+    distribution, so an emitter two of them drew carries the same source pdf in both;
+    pixels of different runs evaluate separately."""
     w = lib.World()
     w.generate(lib.scene_preset(0, emitters=2048, emitter_mode=1))
     w.cluster_lights(256, seed=3, iters=6)
     W, H = 160, 96
     view = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, num_candidates=32))
     try:
-        view.proposal_enable(seed=11, batch=4096, inference=2, pixels_per_eval=2, share_distance=dist)
+        view.proposal_enable(seed=11, batch=4096, inference=2, pixels_per_eval=group, share_distance=dist)
         # large random parameters: the distribution changes visibly between shading points
         p = view.proposal_params()
         view.proposal_set_params(np.random.default_rng(5).normal(0.0, 0.3, p.shape).astype(p.dtype))
@@ -114,25 +135,35 @@ def test_shared_evaluations_pair_only_compatible_pixels(lib, cuda_device, dist):
         sp, code = _shading_points(k, view.read_gbuffer(0), W)
         view.end_frame()
         view.wait()
-        n = len(hits) // 2 * 2
-        a, b = hits[0:n:2], hits[1:n:2]
-        gap = np.abs(sp[a] - sp[b]).max(1)
-        same = code[a] == code[b]
-        shared = same & (gap < dist * 0.99)
-        apart = ~same | (gap > dist * 1.01)
-        equal, common = np.zeros(len(a), bool), np.zeros(len(a), bool)
-        for i in range(len(a)):
-            la, pa = cand[:, 2 * i, 0], cand[:, 2 * i, 1]
-            lb, pb = cand[:, 2 * i + 1, 0], cand[:, 2 * i + 1, 1]
-            m = la[:, None] == lb[None, :]
-            if m.any():
-                common[i] = True
-                ia, ib = np.nonzero(m)
-                equal[i] = bool((pa[ia] == pb[ib]).all())
-        assert (shared & common).sum() > 200
-        assert equal[shared & common].all()
+
+        def same_pdfs(i, j):
+            """(the two entries drew a common emitter, every common one has equal pdfs)"""
+            m = cand[:, i, 0][:, None] == cand[:, j, 0][None, :]
+            if not m.any():
+                return False, False
+            ia, ib = np.nonzero(m)
+            return True, bool((cand[ia, i, 1] == cand[ib, j, 1]).all())
+
+        inside, across = [], []
+        n = len(hits)
+        for g0 in range(0, n, group):
+            sub, unsure = _runs(sp, code, hits[g0:g0 + group], group, dist)
+            if unsure:
+                continue
+            run_of = {}
+            for r, (s0, ln) in enumerate(sub):
+                for q in range(ln):
+                    run_of[g0 + s0 + q] = r
+            ids = sorted(run_of)
+            for x in range(len(ids)):
+                for y in range(x + 1, len(ids)):
+                    common, equal = same_pdfs(ids[x], ids[y])
+                    if common:
+                        (inside if run_of[ids[x]] == run_of[ids[y]] else across).append(equal)
+        assert len(inside) > 200
+        assert all(inside)
         if dist < 1e29:
-            assert (apart & common).sum() > 20
-            assert equal[apart & common].mean() < 0.05
+            assert len(across) > 20
+            assert np.mean(across) < 0.05
     finally:
         view.close()
