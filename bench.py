@@ -441,7 +441,8 @@ def run_batch(args, dist, rank, ws, warmup):
         cams = wl.config2_cameras(descs, specs, frames=60)
         metric = "ms/frame, 8-view batch (config 2)"
         workload = ("config2: 8 views, worlds {256,512,1024}^3, emitters log-uniform [16, 65536], resolutions "
-                    "{360p, 720p, 1080p}, point/area at random, seed 3, one CUDA graph per frame")
+                    "{360p, 720p, 1080p}, point/area at random, seed 3, one CUDA graph per frame (views in 1, 2 or 4 "
+                    "chains of parallel branches: the fastest)")
     else:
         world, views, desc, seeds = wl.build_config4()
         worlds = [world]
@@ -450,30 +451,49 @@ def run_batch(args, dist, rank, ws, warmup):
         cams = [lambda f, sd=sd: vx.camera_path(desc, sd, f % 120, 120) for sd in seeds]
         metric = "ms/frame, 4 x 3840x2160 batch (config 4, plain method)"
         workload = ("config4: 4 views at 3840x2160, 1024^3 fBm 6 octaves + caves seed 5, 1,048,576 emitters "
-                    "(layer + 10% scattered), area lights, plain method, one CUDA graph per frame")
+                    "(layer + 10% scattered), area lights, plain method, one CUDA graph per frame (views in 1, 2 or 4 "
+                    "chains of parallel branches: the fastest)")
     batch = vx.Batch(views, graph=True)
     t, rep = at.autotune_batch(batch, cams, frames=2, rounds=1)
     step = [10000]
 
-    def frame():
-        for v, c in zip(views, cams):
-            pos, tgt = c(step[0])
-            v.lookat(pos, tgt)
-        step[0] += 1
-        batch.render()
+    def timed_batch(b):
+        """(GPU ms, host ms) per frame of batch b over the timed steps, after warm-up"""
+        def frame():
+            for v, c in zip(views, cams):
+                pos, tgt = c(step[0])
+                v.lookat(pos, tgt)
+            step[0] += 1
+            b.render()
 
-    for _ in range(warmup):
-        frame()
-    batch.wait()
-    barrier(dist)
-    t0 = time.perf_counter()
-    gpu_ms = 0.0
-    for _ in range(args.steps):
-        frame()
-        gpu_ms += batch.wait()
-    wall_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
-    barrier(dist)
-    ms = max_over_ranks(dist, gpu_ms / args.steps)
+        for _ in range(warmup):
+            frame()
+        b.wait()
+        barrier(dist)
+        t0 = time.perf_counter()
+        gpu = 0.0
+        for _ in range(args.steps):
+            frame()
+            gpu += b.wait()
+        host = (time.perf_counter() - t0) * 1000.0 / args.steps
+        barrier(dist)
+        return max_over_ranks(dist, gpu / args.steps), host
+
+    # one chain (every stage one launch over all views), then the views split into 2 and 4
+    # chains on parallel graph branches, with the tuning found for one chain
+    per_chains = {}
+    for nc in (1, 2, 4):
+        if nc > len(views):
+            continue
+        b = batch if nc == 1 else vx.Batch(views, graph=True, chains=nc)
+        if nc > 1:
+            b.set_tuning(t)
+        gpu_ms, host_ms = timed_batch(b)
+        per_chains[nc] = {"ms": gpu_ms, "host_ms": host_ms}
+        if nc > 1:
+            b.close()
+    best_chains = min(per_chains, key=lambda c: per_chains[c]["ms"])
+    ms, wall_ms = per_chains[best_chains]["ms"], per_chains[best_chains]["host_ms"]
     # the same views rendered individually (each on its own stream, all enqueued, then waited)
     for v in views:
         v.set_tuning(t)
@@ -503,6 +523,7 @@ def run_batch(args, dist, rank, ws, warmup):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
             "config": {"workload": workload, "views": specs, "pixels": npx},
             "pixels_per_s": npx / (ms * 1e-3), "host_ms_per_frame": wall_ms,
+            "chains": best_chains, "per_chains": per_chains,
             "individual_views_host_ms_per_frame": single_wall_ms,
             "tuning": rep["tuning"], "tuning_search": rep}
     print(json.dumps(line))

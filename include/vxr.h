@@ -507,9 +507,13 @@ int vxr_view_get_tuning(vxr_view* v, vxr_tuning* t);
  * Views must be on one device, hold at most 2^27 - 1 pixels each and not use a learned
  * proposal. tile_x * tile_y = threads of a pixel-stage block (0, 0 = 16 x 8), a multiple
  * of 32 up to 256. flags: VXR_BATCH_GRAPH records the frame once as a CUDA graph and
- * replays it: one graph launch per frame. */
+ * replays it: one graph launch per frame. VXR_BATCH_CHAINS(c), c in [1, min(n, 15)]:
+ * the views are split into c groups of about equal pixel count, each group's stages one
+ * launch over its views, on a branch stream of its own (parallel branches of the graph),
+ * so that different groups can be in different stages at once. */
 #define VXR_BATCH_MAX_VIEWS 16u
 #define VXR_BATCH_GRAPH     1u
+#define VXR_BATCH_CHAINS(c) (((uint32_t)(c) & 15u) << 8)
 typedef struct vxr_batch vxr_batch;
 int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32_t tile_y, uint32_t flags,
                      vxr_batch** out);

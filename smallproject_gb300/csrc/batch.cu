@@ -14,6 +14,13 @@
 // resolutions and the tile shape, all fixed at creation; everything that changes per
 // frame (frame constants, camera, world buffers after a re-upload, G-buffer plane) is in
 // the table.
+//
+// Chains (VXR_BATCH_CHAINS(c)): the views are split into c groups of about equal pixel
+// count, each with its own work lists and its slice of the table, and each group's four
+// stages run on a branch stream of its own, forked from and joined back to the batch
+// stream (in the graph: c parallel branches). One launch per stage then covers a group,
+// and different groups can be in different stages at once, as views on their own streams
+// are, while the frame stays one graph launch.
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -26,9 +33,21 @@
 #include "kernels.hpp"
 #include "view.hpp"
 
+// one group of views: its launch parameters, table slice and work lists
+struct BatchChain {
+    vxr::BatchDev bd;                       // table slice, totals, list buffers
+    uint32_t first = 0, count = 0;          // slice of the table
+    cudaStream_t stream = nullptr;          // branch stream (chains > 1)
+    cudaEvent_t join = nullptr;
+};
+
 struct vxr_batch {
     std::vector<vxr_view*> views;
-    vxr::BatchDev bd;                       // table pointer, totals, list buffers
+    std::vector<uint32_t> order;            // table slot -> index into views
+    std::vector<BatchChain> chains;
+    cudaEvent_t fork = nullptr;
+    int sky = 0;                            // some view has a sky dome (graphs record its shading variant)
+    int tx = 16, ty = 8;                    // tile shape
     vxr::ViewDev* table = nullptr;          // device table [n]
     vxr::ViewDev* staging[2] = {nullptr, nullptr};   // page-locked host slots
     cudaEvent_t slotDone[2] = {nullptr, nullptr};
@@ -53,10 +72,15 @@ void free_batch(vxr_batch* b) {
         if (b->slotDone[i]) cudaEventDestroy(b->slotDone[i]);
     }
     cudaFree(b->table);
-    cudaFree(b->bd.hits);
-    cudaFree(b->bd.qA);
-    cudaFree(b->bd.qB);
-    cudaFree(b->bd.counters);
+    for (BatchChain& c : b->chains) {
+        cudaFree(c.bd.hits);
+        cudaFree(c.bd.qA);
+        cudaFree(c.bd.qB);
+        cudaFree(c.bd.counters);
+        if (c.stream) cudaStreamDestroy(c.stream);
+        if (c.join) cudaEventDestroy(c.join);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     for (cudaEvent_t e : b->viewReady)
         if (e) cudaEventDestroy(e);
     if (b->frameDone) cudaEventDestroy(b->frameDone);
@@ -65,14 +89,29 @@ void free_batch(vxr_batch* b) {
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-// The frame's device work on the batch stream: table upload from slot `slot`, stages 1-4.
+void enqueue_stages(const vxr::BatchDev& bd, cudaStream_t s) {
+    vxr::launch_batch_albedo(bd, 2, s);
+    vxr::launch_batch_candidates(bd, 2, nullptr, s);
+    vxr::launch_batch_spatial(bd, 2, s);
+    vxr::launch_batch_shade(bd, 2, s);
+}
+
+// The frame's device work on the batch stream: table upload from slot `slot`, stages 1-4
+// of every chain (on the chains' branch streams when there are several).
 void enqueue_frame(vxr_batch* b, int slot) {
     const size_t n = b->views.size();
     cudaMemcpyAsync(b->table, b->staging[slot], n * sizeof(vxr::ViewDev), cudaMemcpyHostToDevice, b->stream);
-    vxr::launch_batch_albedo(b->bd, 2, b->stream);
-    vxr::launch_batch_candidates(b->bd, 2, nullptr, b->stream);
-    vxr::launch_batch_spatial(b->bd, 2, b->stream);
-    vxr::launch_batch_shade(b->bd, 2, b->stream);
+    if (b->chains.size() == 1) {
+        enqueue_stages(b->chains[0].bd, b->stream);
+        return;
+    }
+    cudaEventRecord(b->fork, b->stream);
+    for (BatchChain& c : b->chains) {
+        cudaStreamWaitEvent(c.stream, b->fork, 0);
+        enqueue_stages(c.bd, c.stream);
+        cudaEventRecord(c.join, c.stream);
+        cudaStreamWaitEvent(b->stream, c.join, 0);
+    }
 }
 
 int cuda_error(cudaError_t e, const char* what) {
@@ -87,7 +126,9 @@ extern "C" {
 int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32_t tile_y, uint32_t flags, vxr_batch** out) {
     VXR_CHECK_ARG(views && out, "vxr_batch_create: null argument");
     VXR_CHECK_ARG(n >= 1 && n <= VXR_BATCH_MAX_VIEWS, "vxr_batch_create: view count out of range [1, VXR_BATCH_MAX_VIEWS]");
-    VXR_CHECK_ARG((flags & ~VXR_BATCH_GRAPH) == 0, "vxr_batch_create: unknown flags");
+    VXR_CHECK_ARG((flags & ~(VXR_BATCH_GRAPH | VXR_BATCH_CHAINS(15u))) == 0, "vxr_batch_create: unknown flags");
+    const uint32_t nchains = std::max<uint32_t>((flags >> 8) & 15u, 1u);
+    VXR_CHECK_ARG(nchains <= n, "vxr_batch_create: more chains than views");
     const uint32_t tx = tile_x ? tile_x : 16, ty = tile_y ? tile_y : 8;
     VXR_CHECK_ARG(tx <= 256 && ty <= 256 && tx * ty >= 32 && tx * ty <= 256 && (tx * ty) % 32 == 0,
                   "vxr_batch_create: tile must hold a multiple of 32 threads, at most 256");
@@ -106,27 +147,59 @@ int vxr_batch_create(vxr_view* const* views, uint32_t n, uint32_t tile_x, uint32
     if (!b) return vxr::set_error(VXR_E_NOMEM, "vxr_batch_create: out of host memory");
     b->views.assign(views, views + n);
     b->useGraph = (flags & VXR_BATCH_GRAPH) != 0;
+    b->tx = (int)tx;
+    b->ty = (int)ty;
     cudaGetDevice(&b->device);
-    vxr::BatchDev& bd = b->bd;
-    bd.nviews = n;
-    bd.totalPixels = (uint32_t)total;
-    bd.totalTiles = (uint32_t)tiles;
+    // chains of about equal pixel count: the largest views first, each to the lightest chain
+    std::vector<uint32_t> byPixels(n);
+    for (uint32_t i = 0; i < n; i++) byPixels[i] = i;
+    std::stable_sort(byPixels.begin(), byPixels.end(),
+                     [&](uint32_t a, uint32_t c) { return views[a]->npx > views[c]->npx; });
+    std::vector<std::vector<uint32_t>> members(nchains);
+    std::vector<uint64_t> load(nchains, 0);
+    for (uint32_t i : byPixels) {
+        const size_t c = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+        members[c].push_back(i);
+        load[c] += views[i]->npx;
+    }
+    b->chains.resize(nchains);
     vxr::Tuning tu;
     tu.bx = (int)tx;
     tu.by = (int)ty;
-    vxr::apply_tuning(bd, tu);
-    bd.fuse = 1;
     cudaError_t e = cudaSuccess;
     auto dalloc = [&](void** p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, bytes);
         if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
     };
     dalloc((void**)&b->table, n * sizeof(vxr::ViewDev));
-    dalloc((void**)&bd.hits, total * sizeof(uint32_t));
-    dalloc((void**)&bd.qA, total * sizeof(float4));
-    dalloc((void**)&bd.qB, total * sizeof(float4));
-    dalloc((void**)&bd.counters, vxr::kCounters * sizeof(uint32_t));
-    bd.views = b->table;
+    for (uint32_t c = 0; c < nchains; c++) {
+        std::sort(members[c].begin(), members[c].end());
+        BatchChain& ch = b->chains[c];
+        ch.first = (uint32_t)b->order.size();
+        ch.count = (uint32_t)members[c].size();
+        uint64_t px = 0, tl = 0;
+        for (uint32_t i : members[c]) {
+            b->order.push_back(i);
+            px += views[i]->npx;
+            tl += (uint64_t)((views[i]->desc.width + tx - 1) / tx) * ((views[i]->desc.height + ty - 1) / ty);
+        }
+        vxr::BatchDev& bd = ch.bd;
+        bd.nviews = ch.count;
+        bd.totalPixels = (uint32_t)px;
+        bd.totalTiles = (uint32_t)tl;
+        vxr::apply_tuning(bd, tu);
+        bd.fuse = 1;
+        dalloc((void**)&bd.hits, px * sizeof(uint32_t));
+        dalloc((void**)&bd.qA, px * sizeof(float4));
+        dalloc((void**)&bd.qB, px * sizeof(float4));
+        dalloc((void**)&bd.counters, vxr::kCounters * sizeof(uint32_t));
+        bd.views = b->table + ch.first;
+        if (nchains > 1) {
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ch.stream, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ch.join, cudaEventDisableTiming);
+        }
+    }
+    if (nchains > 1 && e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         e = cudaHostAlloc((void**)&b->staging[i], n * sizeof(vxr::ViewDev), cudaHostAllocDefault);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->slotDone[i], cudaEventDisableTiming);
@@ -169,24 +242,30 @@ int vxr_batch_render(vxr_batch* b) {
     // the shading kernel has a sky-dome variant: recorded graphs follow the views' skies
     int sky = 0;
     for (vxr_view* v : b->views) sky |= v->skyDev != nullptr ? 1 : 0;
-    if (sky != b->bd.sky) {
+    if (sky != b->sky) {
         const cudaError_t e = cudaStreamSynchronize(b->stream);
         if (e != cudaSuccess) return cuda_error(e, "vxr_batch_render: wait before re-recording");
         for (int i = 0; i < 2; i++) {
             if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
             b->graph[i] = nullptr;
         }
-        b->bd.sky = sky;
+        b->sky = sky;
+        for (BatchChain& c : b->chains) c.bd.sky = sky;
     }
     // begin every view's frame (camera, frame constants, G-buffer swap) and fill the table
-    uint32_t tileBase = 0;
+    // (slot s holds view order[s]; tiles and hit-list view numbers count within a chain)
     for (size_t i = 0; i < n; i++) {
-        vxr_view* v = b->views[i];
-        if (int r = vxr_view_begin_frame(v, nullptr)) {
+        if (int r = vxr_view_begin_frame(b->views[i], nullptr)) {
             for (size_t j = 0; j < i; j++) vxr_view_end_frame(b->views[j]);
             return r;
         }
-        vxr::ViewDev& d = b->staging[slot][i];
+    }
+    uint32_t tileBase = 0;
+    for (size_t s = 0, c = 0; s < n; s++) {
+        if (s == b->chains[c].first + b->chains[c].count) c++;
+        if (s == b->chains[c].first) tileBase = 0;
+        vxr_view* v = b->views[b->order[s]];
+        vxr::ViewDev& d = b->staging[slot][s];
         d = vxr::ViewDev();
         d.w = vxr::dev_world(v);
         d.k = vxr::dev_frame(v->k);
@@ -194,9 +273,9 @@ int vxr_batch_render(vxr_batch* b) {
         d.b = v->buf;
         d.cur = v->cur;
         d.point = v->desc.light_model == VXR_LIGHTS_POINT ? 1 : 0;
-        d.tilesX = (v->desc.width + (uint32_t)b->bd.tx - 1) / (uint32_t)b->bd.tx;
+        d.tilesX = (v->desc.width + (uint32_t)b->tx - 1) / (uint32_t)b->tx;
         d.tileBase = tileBase;
-        tileBase += d.tilesX * ((v->desc.height + (uint32_t)b->bd.ty - 1) / (uint32_t)b->bd.ty);
+        tileBase += d.tilesX * ((v->desc.height + (uint32_t)b->ty - 1) / (uint32_t)b->ty);
     }
     cudaError_t e = cudaSuccess;
     // order after each view's earlier work
@@ -243,8 +322,17 @@ int vxr_batch_set_tuning(vxr_batch* b, const vxr_tuning* t) {
     for (vxr_view* v : b->views)
         tiles += (uint64_t)((v->desc.width + t->tile_x - 1) / t->tile_x) * ((v->desc.height + t->tile_y - 1) / t->tile_y);
     VXR_CHECK_ARG(tiles < (1ull << 32), "vxr_batch_set_tuning: batch too large");
-    vxr::apply_tuning(b->bd, vxr::to_tuning(*t));
-    b->bd.totalTiles = (uint32_t)tiles;
+    for (BatchChain& c : b->chains) {
+        uint64_t tl = 0;
+        for (uint32_t s = c.first; s < c.first + c.count; s++) {
+            const vxr_view* v = b->views[b->order[s]];
+            tl += (uint64_t)((v->desc.width + t->tile_x - 1) / t->tile_x) * ((v->desc.height + t->tile_y - 1) / t->tile_y);
+        }
+        vxr::apply_tuning(c.bd, vxr::to_tuning(*t));
+        c.bd.totalTiles = (uint32_t)tl;
+    }
+    b->tx = (int)t->tile_x;
+    b->ty = (int)t->tile_y;
     for (int i = 0; i < 2; i++) {
         if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
         b->graph[i] = nullptr;

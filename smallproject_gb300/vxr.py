@@ -633,13 +633,13 @@ BATCH_GRAPH = 1
 class Batch:
     """Several views rendered as one frame (vxr_batch): each stage is one launch over all."""
 
-    def __init__(self, views, tile=(0, 0), graph=False):
+    def __init__(self, views, tile=(0, 0), graph=False, chains=1):
         self._lib = load()
         self.views = list(views)
         arr = (_P * len(self.views))(*[v.h for v in self.views])
         self.h = _P()
-        check(self._lib.vxr_batch_create(arr, len(self.views), tile[0], tile[1], BATCH_GRAPH if graph else 0,
-                                         C.byref(self.h)))
+        flags = (BATCH_GRAPH if graph else 0) | ((chains & 15) << 8)
+        check(self._lib.vxr_batch_create(arr, len(self.views), tile[0], tile[1], flags, C.byref(self.h)))
 
     def close(self):
         if self.h:

@@ -54,12 +54,14 @@ def _compare(a, b, ctx):
     assert_records_equal("accum", a["a"], b["a"], ctx)
 
 
-@pytest.mark.parametrize("graph", [False, True], ids=["launches", "graph"])
-def test_batch_matches_single_views(lib, cuda_device, graph):
+@pytest.mark.parametrize("graph,chains", [(False, 1), (True, 1), (False, 2), (True, 3), (True, 5)],
+                         ids=["launches", "graph", "launches-2-chains", "graph-3-chains", "graph-5-chains"])
+def test_batch_matches_single_views(lib, cuda_device, graph, chains):
+    """chains > 1: the views split into groups whose stages run on parallel branches."""
     worlds = [_world(lib, s[0], s[1]) for s in SPECS]
     alone = _make_views(lib, worlds, SPECS)
     batched = _make_views(lib, worlds, SPECS)
-    batch = lib.Batch(batched, graph=graph)
+    batch = lib.Batch(batched, graph=graph, chains=chains)
     try:
         for f in range(4):
             for i, (va, vb) in enumerate(zip(alone, batched)):
@@ -73,7 +75,8 @@ def test_batch_matches_single_views(lib, cuda_device, graph):
             for i, (va, vb) in enumerate(zip(alone, batched)):
                 va.wait()
                 vb.wait()
-                _compare(_snapshot(vb), _snapshot(va), f"[view {i} {SPECS[i][4]} frame {f} graph={graph}]")
+                _compare(_snapshot(vb), _snapshot(va),
+                         f"[view {i} {SPECS[i][4]} frame {f} graph={graph} chains={chains}]")
     finally:
         batch.close()
         for v in alone + batched:
@@ -82,12 +85,12 @@ def test_batch_matches_single_views(lib, cuda_device, graph):
 
 def test_batch_tile_shape_and_mixed_sizes(lib, cuda_device):
     """A 32x4 batch tile against the default 16x8 of the single views, and a 512^3 world
-    next to a 256^3 one."""
+    next to a 256^3 one, each view in a chain of its own."""
     specs = [(21, 200, 120, 80, "area", 1, 1, 1), (22, 40, 200, 30, "point", 1, 1, 1)]
     worlds = [_world(lib, 21, 200, extent=512, mode=1), _world(lib, 22, 40)]
     alone = _make_views(lib, worlds, specs)
     batched = _make_views(lib, worlds, specs)
-    batch = lib.Batch(batched, tile=(32, 4), graph=True)
+    batch = lib.Batch(batched, tile=(32, 4), graph=True, chains=2)
     try:
         for f in range(3):
             for i, (va, vb) in enumerate(zip(alone, batched)):
@@ -116,5 +119,7 @@ def test_batch_rejects_bad_arguments(lib, cuda_device):
             lib.Batch([v], tile=(5, 5))
         with pytest.raises(lib.VxrError):
             lib.Batch([v] * 17)
+        with pytest.raises(lib.VxrError):
+            lib.Batch([v], chains=2)   # more chains than views
     finally:
         v.close()
