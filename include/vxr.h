@@ -411,7 +411,7 @@ typedef struct vxr_proposal_desc {
     uint32_t seed;            /* parameter initialisation */
     uint32_t inference;       /* 0 auto (tcgen05 when hidden = 64 and 256 clusters, else mma.sync), 1 mma.sync, 2 tcgen05 */
     uint32_t training;        /* 0 auto (tensor cores when hidden = 64 and clusters <= 256, else FP32), 1 FP32, 2 tensor cores */
-    uint32_t pixels_per_eval; /* tcgen05 inference: 1 = one network evaluation per hit pixel; 2 or 4 = one per run of up to
+    uint32_t pixels_per_eval; /* tcgen05 inference: 1 = one network evaluation per hit pixel; 2, 4 or 8 = one per run of up to
                                  that many consecutive hit pixels whose shading points lie on the same voxel side as the
                                  run's first within share_distance (all sample from the first one's distribution; still
                                  unbiased) */

@@ -127,7 +127,7 @@ struct LearnedHook {
     uint2* cand;                // [kMaxCand][pixels] scratch for the drawn candidates
     uint32_t* rows;             // shared evaluations: table rows [pixels] and their count (null: one per pixel)
     uint32_t* rowCount;
-    uint32_t group;             // hit entries a shared evaluation may serve (2 or 4)
+    uint32_t group;             // hit entries a shared evaluation may serve (2, 4 or 8)
     float pairDist;             // largest per-coordinate distance within a shared row (voxels)
     const uint32_t* clOff;      // cluster CSR on the device
     const uint32_t* clMembers;

@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
     bool pending = false;   // an MMA was committed whose completion no wait has seen
     const uint32_t limit = a.waitLimit ? a.waitLimit : tc::kWaitLimit;
     const bool issue = !a.skipMma;
-    // render mode with sharing: a table row may serve up to four consecutive hit pixels
+    // render mode with sharing: a table row may serve up to eight consecutive hit pixels
     // (the network runs on the first one's shading point; each draws its own candidates
     // from the row's tables)
     const bool useRows = a.rows && !a.samples && !a.probs;
@@ -551,8 +551,8 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
         uint32_t j = row, span = 1u;
         if (useRows && valid) {
             const uint32_t e = a.rows[row];
-            j = e & 0x3FFFFFFFu;
-            span = (e >> 30) + 1u;
+            j = e & 0x1FFFFFFFu;
+            span = (e >> 29) + 1u;
         }
         float4 pin = make_float4(0.f, 0.f, 0.f, __uint_as_float(6u));
         uint32_t pix = 0;
@@ -697,7 +697,7 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
             continue;
         }
         // the hit pixels this thread draws for: in a shared row the row's entries j + half,
-        // j + half + 2 (all their candidates), else the row's pixel (every other candidate,
+        // j + half + 2, ... (all their candidates), else the row's pixel (every other candidate,
         // the other warpgroup taking the rest; both advance the pixel's RNG alike)
         const float eps = d.eps, invN = 1.0f / (float)a.nlights;
         for (uint32_t jm = j + (span > 1u ? (uint32_t)half : 0u); jm < j + span; jm += 2u) {
@@ -993,9 +993,9 @@ static size_t infer_tc_smem_bytes() {
 }
 
 // Table rows for shared network evaluations. The hit list is cut into aligned groups of
-// `group` entries (2 or 4); inside a group, a run of consecutive entries whose shading
+// `group` entries (2, 4 or 8); inside a group, a run of consecutive entries whose shading
 // points lie on the same voxel side (axis and facing) as the run's first entry, within
-// maxDist of it in every coordinate, becomes one row (first entry | (length - 1) << 30);
+// maxDist of it in every coordinate, becomes one row (first entry | (length - 1) << 29);
 // an entry that fails the test starts the next run. Rows are appended per warp (one
 // atomic each), so their order is not the hit list's.
 __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, const uint32_t* __restrict__ hits,
@@ -1006,13 +1006,15 @@ __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, con
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < ng; base += stride) {
         const uint32_t i = base + (uint32_t)lane;
-        uint32_t emit = 0, r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+        uint32_t emit = 0, r[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) r[q] = 0;
         if (i < ng) {
             const uint32_t j0 = i * group, m = min(group, n - j0);
             float3 f = make_float3(0.0f, 0.0f, 0.0f);   // the current run's first shading point
             uint32_t fcode = 0, start = 0;
 #pragma unroll
-            for (uint32_t q = 0; q < 4; q++) {
+            for (uint32_t q = 0; q < 8; q++) {
                 if (q >= m) break;
                 const uint32_t pix = hits[j0 + q];
                 const int x = (int)(pix % (uint32_t)k.W), y = (int)(pix / (uint32_t)k.W);
@@ -1025,10 +1027,9 @@ __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, con
                 const bool join = q > 0 && code == fcode && fabsf(sp.x - f.x) <= maxDist &&
                                   fabsf(sp.y - f.y) <= maxDist && fabsf(sp.z - f.z) <= maxDist;
                 if (q > 0 && !join) {
-                    const uint32_t row = (j0 + start) | ((q - start - 1u) << 30);
-                    r0 = emit == 0 ? row : r0;
-                    r1 = emit == 1 ? row : r1;
-                    r2 = emit == 2 ? row : r2;
+                    const uint32_t row = (j0 + start) | ((q - start - 1u) << 29);
+#pragma unroll
+                    for (uint32_t t = 0; t < 8; t++) r[t] = emit == t ? row : r[t];
                     emit++;
                     start = q;
                 }
@@ -1037,11 +1038,9 @@ __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, con
                     fcode = code;
                 }
             }
-            const uint32_t row = (j0 + start) | ((m - start - 1u) << 30);
-            r0 = emit == 0 ? row : r0;
-            r1 = emit == 1 ? row : r1;
-            r2 = emit == 2 ? row : r2;
-            r3 = emit == 3 ? row : r3;
+            const uint32_t row = (j0 + start) | ((m - start - 1u) << 29);
+#pragma unroll
+            for (uint32_t t = 0; t < 8; t++) r[t] = emit == t ? row : r[t];
             emit++;
         }
         // warp-aggregated append
@@ -1056,10 +1055,9 @@ __global__ void pair_rows_kernel(dev::Frame k, const uint2* __restrict__ vd, con
         if (lane == 31 && total) at = atomicAdd(rowCount, total);
         at = __shfl_sync(0xffffffffu, at, 31);
         const uint32_t slot = at + pre - emit;
-        if (emit > 0) rows[slot] = r0;
-        if (emit > 1) rows[slot + 1] = r1;
-        if (emit > 2) rows[slot + 2] = r2;
-        if (emit > 3) rows[slot + 3] = r3;
+#pragma unroll
+        for (uint32_t t = 0; t < 8; t++)
+            if (t < emit) rows[slot + t] = r[t];
     }
 }
 

@@ -30,7 +30,7 @@ struct InferArgs {
     uint32_t waitLimit;               // tries of each in-loop tensor-core wait (0: the full limit)
     uint32_t skipMma;                 // test only: issue no MMA, so every wait runs out with nothing in flight
     // tcgen05 render mode with sharing: the table rows (pair_rows_kernel): row r serves hit
-    // entries (rows[r] & 0x3FFFFFFF) + [0, (rows[r] >> 30) + 1); null: one row per hit entry
+    // entries (rows[r] & 0x1FFFFFFF) + [0, (rows[r] >> 29) + 1); null: one row per hit entry
     const uint32_t* rows;
     const uint32_t* rowCount;
     // sample mode (tests): explicit inputs (x, y, z, bits(side code)) and softmax output
@@ -130,7 +130,7 @@ bool infer_supported(const Dims& d);
 bool infer_tc_supported(const Dims& d);   // the tcgen05 kernel (H = 64, K = 256)
 cudaError_t launch_infer(const InferArgs& a, uint32_t max_items, cudaStream_t s);
 // rows of the tcgen05 inference that shares one network evaluation between up to `group`
-// (2 or 4) consecutive hit entries whose shading points lie on the same voxel side as the
+// (2, 4 or 8) consecutive hit entries whose shading points lie on the same voxel side as the
 // first one's within maxDist voxels (each coordinate); other entries start rows of their
 // own. rowCount must be zero before.
 void launch_pair_rows(const dev::Frame& k, const uint2* vd, const uint32_t* hits, const uint32_t* count, uint32_t n,

@@ -461,8 +461,10 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     if (d.kernel == 2 && !vxr::prop::infer_tc_supported(d))
         return set_error(VXR_E_INVALID, "vxr_view_proposal_enable: the tcgen05 inference needs hidden = 64 and 256 clusters");
     VXR_CHECK_ARG(desc->training <= 2, "vxr_view_proposal_enable: training must be 0 (auto), 1 (FP32) or 2 (tensor cores)");
-    VXR_CHECK_ARG(desc->pixels_per_eval == 1 || desc->pixels_per_eval == 2 || desc->pixels_per_eval == 4,
-                  "vxr_view_proposal_enable: pixels_per_eval must be 1, 2 or 4");
+    VXR_CHECK_ARG(desc->pixels_per_eval == 1 || desc->pixels_per_eval == 2 || desc->pixels_per_eval == 4 ||
+                      desc->pixels_per_eval == 8,
+                  "vxr_view_proposal_enable: pixels_per_eval must be 1, 2, 4 or 8");
+    VXR_CHECK_ARG(v->npx < (1ull << 29), "vxr_view_proposal_enable: at most 2^29 - 1 pixels per view");
     VXR_CHECK_ARG(desc->pixels_per_eval == 1 || (desc->share_distance >= 0.0f && desc->share_distance <= 1e30f),
                   "vxr_view_proposal_enable: share_distance must be finite and >= 0");
     if (desc->training == 2 && !vxr::prop::train_supported(d))

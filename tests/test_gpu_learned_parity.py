@@ -21,7 +21,7 @@ def _orbit(f):
     return (120.0 + 5.0 * f, 150.0 - 2.0 * f, 8.0 + 3.0 * f), (128.0, 118.0, 128.0)
 
 
-@pytest.mark.parametrize("clusters,inference,share", [(16, 1, 1), (256, 2, 1), (256, 2, 2), (256, 2, 4)])
+@pytest.mark.parametrize("clusters,inference,share", [(16, 1, 1), (256, 2, 1), (256, 2, 2), (256, 2, 4), (256, 2, 8)])
 def test_learned_frames_match_oracle_given_candidates(lib, cuda_device, clusters, inference, share):
     w = lib.World()
     if clusters == 256:
@@ -108,9 +108,9 @@ def _runs(sp, code, hits, group, dist):
     return runs, unsure
 
 
-@pytest.mark.parametrize("group,dist", [(2, 2.0), (2, 1e30), (4, 2.0)])
+@pytest.mark.parametrize("group,dist", [(2, 2.0), (2, 1e30), (4, 2.0), (8, 2.0), (8, 1e30)])
 def test_shared_evaluations_pair_only_compatible_pixels(lib, cuda_device, group, dist):
-    """pixels_per_eval = 2 or 4: the hit list in aligned groups of that many entries; a run
+    """pixels_per_eval = 2, 4 or 8: the hit list in aligned groups of that many entries; a run
     of entries on the voxel side of its first entry, within share_distance voxels of it in
     every coordinate, shares one network evaluation. Pixels of one run draw from one
     distribution, so an emitter two of them drew carries the same source pdf in both;

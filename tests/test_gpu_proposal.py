@@ -228,13 +228,13 @@ def test_tcgen05_inference_matches_mma_and_fp64(lib, world256):
         b.close()
 
 
-@pytest.mark.parametrize("share", [1, 2, 4])
+@pytest.mark.parametrize("share", [1, 2, 4, 8])
 def test_tcgen05_learned_source_is_unbiased(lib, world256, share):
     """The tcgen05 inference kernel (256 clusters) samples candidates with the probability
     it reports: with spatial and temporal reuse off its learned source and the uniform
     one converge to the same image (a source pdf that differed from the sampling
-    frequencies would bias the RIS estimate). share = 2 / 4: runs of up to two / four
-    consecutive hit pixels sample from one network evaluation (the run's first)."""
+    frequencies would bias the RIS estimate). share = 2 / 4 / 8: runs of up to two / four /
+    eight consecutive hit pixels sample from one network evaluation (the run's first)."""
     pos, tgt = (110.0, 150.0, 10.0), (128.0, 110.0, 128.0)
     a = _converged_mean(lib, world256, False, 384, pos, tgt, 21)
     b = _converged_mean(lib, world256, True, 384, pos, tgt, 22, inference=2, share=share)
