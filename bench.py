@@ -359,7 +359,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
             v.lookat(pos, tgt)
             if method != "plain":
                 v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon,
-                                  pixels_per_eval=FAMILY_PPE[method])
+                                  pixels_per_eval=FAMILY_PPE[method], training_lag=args.training_lag)
                 v.proposal_set_params(params)
                 v.proposal_use(True)
                 v.proposal_online(online)
@@ -561,6 +561,9 @@ def main():
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
     ap.add_argument("--online", type=int, default=1, help="proposal training steps inside every learned frame")
+    ap.add_argument("--training-lag", type=int, default=1, choices=[0, 1],
+                    help="1 (default): a frame's inference uses the weights of the training step two frames back, "
+                         "each step overlapping the whole next frame; 0: of the previous frame's step")
     ap.add_argument("--pixels-per-eval", type=int, default=1, choices=[1, 2, 4, 8],
                     help="learned method with --quality train: hit pixels per network evaluation")
     args = ap.parse_args()
@@ -640,14 +643,17 @@ def main():
         share = FAMILY_PPE[eq["method"]] if learned else 1
         config["method"] = (f"learned proposal, {cand} candidates (equal MSE to plain at 32), "
                             f"{f'one network evaluation per run of up to {share} compatible hit pixels, ' if share > 1 else ''}{args.online} "
-                            "training step(s) of 65,536 samples inside every frame" if learned
+                            "training step(s) of 65,536 samples inside every frame"
+                            f"{' (each used two frames later, overlapping the next frame)' if args.training_lag else ''}"
+                            if learned
                             else "plain uniform-source RIS, 32 candidates")
 
     def make_view(learned_view, c):
         v = vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, accumulate=0, num_candidates=c))
         v.set_tuning(tuning)
         if learned_view:
-            v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon, pixels_per_eval=share)
+            v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon, pixels_per_eval=share,
+                              training_lag=args.training_lag)
             v.proposal_set_params(params)
             v.proposal_use(True)
             v.proposal_online(args.online)

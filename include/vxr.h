@@ -416,6 +416,9 @@ typedef struct vxr_proposal_desc {
                                  run's first within share_distance (all sample from the first one's distribution; still
                                  unbiased) */
     float share_distance;     /* pixels_per_eval > 1: largest per-coordinate distance (voxels) within a shared run */
+    uint32_t training_lag;    /* online training (vxr_view_proposal_online): 0 = a frame's inference uses the weights of
+                                 the previous frame's training step; 1 = of the step before that, so each step can
+                                 overlap the whole next frame */
 } vxr_proposal_desc;
 int vxr_proposal_default_desc(vxr_proposal_desc* d);
 /* Allocate and initialise the network for this view; K = the world's cluster count. */

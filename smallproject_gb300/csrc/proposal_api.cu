@@ -56,12 +56,19 @@ struct Proposal {
     bool encGradDirty = true;      // the hash-table gradient is not known to be zero
     uint32_t online = 0;           // training steps run by every rendered frame
     // the frame's training step past its gather runs on a side stream and overlaps the next
-    // frame's primary rays; the view stream joins it (proposal_join) before anything reads
-    // the parameters or writes the batch again
+    // frame; the view stream joins it (proposal_join) before anything reads the parameters
+    // it writes or writes the batch it reads. Frame training steps are numbered (gen);
+    // step g signals joinEv[g & 1].
     cudaStream_t trainStream = nullptr;
     cudaEvent_t forkEv = nullptr;
-    cudaEvent_t joinEv = nullptr;
-    bool trainPending = false;
+    cudaEvent_t joinEv[2] = {nullptr, nullptr};
+    bool trainPending[2] = {false, false};
+    uint64_t gen = 0;
+    // desc.training_lag = 1: step g ends by publishing its parameters into slot g & 1, and
+    // a frame's inference reads the slot of the step two frames back (joining only that
+    // one), so a step has the whole next frame to run in
+    float* pubParams[2] = {nullptr, nullptr};
+    __nv_bfloat16* pubWbf[2] = {nullptr, nullptr};
     bool testTimeout = false;      // test hook: the inference issues no MMA and its waits give up
     int step = 0;
     uint32_t gatherOffset = 0;
@@ -74,7 +81,11 @@ void destroy_proposal(Proposal* p) {
         cudaStreamDestroy(p->trainStream);
     }
     if (p->forkEv) cudaEventDestroy(p->forkEv);
-    if (p->joinEv) cudaEventDestroy(p->joinEv);
+    for (int i = 0; i < 2; i++) {
+        if (p->joinEv[i]) cudaEventDestroy(p->joinEv[i]);
+        cudaFree(p->pubParams[i]);
+        cudaFree(p->pubWbf[i]);
+    }
     void* bufs[] = {p->params, p->grads, p->m, p->v, p->wbf, p->clOff, p->clMembers, p->lightCluster, p->cand,
                     p->pairRows, p->pairCount,
                     p->samples, p->target, p->weight, p->X, p->H1, p->H2, p->H3, p->Z, p->dA, p->dB, p->dX, p->scal,
@@ -113,6 +124,17 @@ void refresh_bf16(vxr::Proposal* p, cudaStream_t s) {
     launch_to_bf16(p->params + L.W3, o, (size_t)d.H * d.H, s);
     o += (size_t)d.H * d.H;
     launch_to_bf16(p->params + L.W4, o, (size_t)d.K * d.H, s);
+}
+
+// copies the current parameters (FP32 master, BF16 weights) into published slot `slot`
+// (training_lag = 1), or into both slots (slot < 0); nothing without published slots
+void publish(vxr::Proposal* p, int slot, cudaStream_t s) {
+    if (!p->pubParams[0]) return;
+    for (int i = 0; i < 2; i++) {
+        if (slot >= 0 && i != slot) continue;
+        cudaMemcpyAsync(p->pubParams[i], p->params, p->L.total * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(p->pubWbf[i], p->wbf, weights_count(p->d) * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, s);
+    }
 }
 
 // cluster CSR (members sorted by cluster, then light index) from the world's clustering
@@ -368,10 +390,17 @@ int proposal_frame_train(vxr_view* v) {
         if (int r = upload_clusters(v, p)) return r;
     if (int r = ensure_batch(p, p->desc.batch)) return r;
     if (!p->trainStream) {
-        CUP(cudaStreamCreateWithFlags(&p->trainStream, cudaStreamNonBlocking), "cudaStreamCreate(training)");
+        // training_lag = 1: the lowest priority (the frames' kernels take free SM slots
+        // first; a step has the whole next frame to finish); else the view stream's (the
+        // next frame's inference waits for the step)
+        int least = 0, greatest = 0;
+        CUP(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange");
+        CUP(cudaStreamCreateWithPriority(&p->trainStream, cudaStreamNonBlocking, p->desc.training_lag ? least : greatest),
+            "cudaStreamCreate(training)");
         CUP(cudaEventCreateWithFlags(&p->forkEv, cudaEventDisableTiming), "cudaEventCreate");
-        CUP(cudaEventCreateWithFlags(&p->joinEv, cudaEventDisableTiming), "cudaEventCreate");
+        for (int i = 0; i < 2; i++) CUP(cudaEventCreateWithFlags(&p->joinEv[i], cudaEventDisableTiming), "cudaEventCreate");
     }
+    const int slot = (int)(p->gen & 1u);
     for (uint32_t i = 0; i < p->online; i++) {
         proposal_join(v);   // a previous step still reads the batch the gather overwrites
         gather_frame(v, p);
@@ -379,31 +408,45 @@ int proposal_frame_train(vxr_view* v) {
         CUP(cudaStreamWaitEvent(p->trainStream, p->forkEv, 0), "cudaStreamWaitEvent");
         if (i == 0 && v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, false, p->trainStream);
         if (int r = train_batch(p, p->trainStream)) return r;
-        if (i + 1 == p->online && v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, true, p->trainStream);
-        CUP(cudaEventRecord(p->joinEv, p->trainStream), "cudaEventRecord");
-        p->trainPending = true;
+        if (i + 1 == p->online) {
+            publish(p, slot, p->trainStream);
+            if (v->ktimerOn && v->ktimer) v->ktimer->mark(K_TRAIN, true, p->trainStream);
+        }
+        CUP(cudaEventRecord(p->joinEv[slot], p->trainStream), "cudaEventRecord");
+        p->trainPending[slot] = true;
     }
+    p->gen++;
     return VXR_OK;
 }
 
-void proposal_join(vxr_view* v) {
+// the view stream waits for the frame training steps still running on the side stream
+// (slot < 0: all of them; else the one that signals joinEv[slot])
+static void join_slot(vxr_view* v, int slot) {
     Proposal* p = v->prop;
-    if (p && p->trainPending) {
-        cudaStreamWaitEvent(v->stream, p->joinEv, 0);
-        p->trainPending = false;
+    if (!p) return;
+    for (int i = 0; i < 2; i++) {
+        if ((slot >= 0 && i != slot) || !p->trainPending[i]) continue;
+        cudaStreamWaitEvent(v->stream, p->joinEv[i], 0);
+        p->trainPending[i] = false;
     }
 }
 
+void proposal_join(vxr_view* v) { join_slot(v, -1); }
+
 // the candidate stage's hook (nullptr when the view samples uniformly)
 bool learned_hook(vxr_view* v, LearnedHook* h) {
-    proposal_join(v);   // the inference reads the weights the last training step wrote
     Proposal* p = v->prop;
+    // the inference reads the weights of the last training step, or with training_lag = 1
+    // the published ones of the step before it (slot (gen - 2) & 1 = gen & 1)
+    const bool lag = p && p->pubParams[0];
+    const int slot = p ? (int)(p->gen & 1u) : 0;
+    join_slot(v, lag ? slot : -1);
     if (!v->useProposal || !p) return false;
     h->infer = prop::InferArgs{};
     h->infer.dims = p->d;
     h->infer.L = p->L;
-    h->infer.params = p->params;
-    h->infer.wbf = p->wbf;
+    h->infer.params = lag ? p->pubParams[slot] : p->params;
+    h->infer.wbf = lag ? p->pubWbf[slot] : p->wbf;
     h->infer.waitLimit = p->testTimeout ? 64u : 0u;
     h->infer.skipMma = p->testTimeout ? 1u : 0u;
     h->rows = p->desc.pixels_per_eval > 1 ? p->pairRows : nullptr;
@@ -465,6 +508,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
                       desc->pixels_per_eval == 8,
                   "vxr_view_proposal_enable: pixels_per_eval must be 1, 2, 4 or 8");
     VXR_CHECK_ARG(v->npx < (1ull << 29), "vxr_view_proposal_enable: at most 2^29 - 1 pixels per view");
+    VXR_CHECK_ARG(desc->training_lag <= 1, "vxr_view_proposal_enable: training_lag must be 0 or 1");
     VXR_CHECK_ARG(desc->pixels_per_eval == 1 || (desc->share_distance >= 0.0f && desc->share_distance <= 1e30f),
                   "vxr_view_proposal_enable: share_distance must be finite and >= 0");
     if (desc->training == 2 && !vxr::prop::train_supported(d))
@@ -486,6 +530,12 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     CUP(cudaMalloc(&p->wbf, weights_count(d) * sizeof(__nv_bfloat16)), "cudaMalloc(bf16 weights)");
     CUP(cudaMalloc(&p->cand, v->npx * vxr::prop::kMaxCand * sizeof(uint2)), "cudaMalloc(candidates)");
     CUP(cudaMalloc(&p->scal, 2 * sizeof(float)), "cudaMalloc(scalars)");
+    if (desc->training_lag) {
+        for (int i = 0; i < 2; i++) {
+            CUP(cudaMalloc(&p->pubParams[i], n * sizeof(float)), "cudaMalloc(published params)");
+            CUP(cudaMalloc(&p->pubWbf[i], weights_count(d) * sizeof(__nv_bfloat16)), "cudaMalloc(published weights)");
+        }
+    }
     if (desc->pixels_per_eval > 1) {
         CUP(cudaMalloc(&p->pairRows, v->npx * sizeof(uint32_t)), "cudaMalloc(pair rows)");
         CUP(cudaMalloc(&p->pairCount, sizeof(uint32_t)), "cudaMalloc(pair rows)");
@@ -494,6 +544,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     CUP(cudaMemsetAsync(p->v, 0, n * sizeof(float), v->stream), "clear adam");
     vxr::prop::launch_init(p->params, p->L, d, desc->seed, v->stream);
     refresh_bf16(p, v->stream);
+    publish(p, -1, v->stream);
     CUP(cudaGetLastError(), "proposal init");
     if (int r = upload_clusters(v, p)) return r;
     CUP(cudaStreamSynchronize(v->stream), "proposal init");
@@ -528,6 +579,7 @@ int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
             last = h[0];
         }
     }
+    publish(p, -1, v->stream);
     if (loss) *loss = last;
     return VXR_OK;
 }
@@ -600,6 +652,7 @@ int vxr_view_proposal_set_params(vxr_view* v, const float* in) {
     CUP(cudaStreamSynchronize(v->stream), "sync");
     CUP(cudaMemcpy(v->prop->params, in, v->prop->L.total * sizeof(float), cudaMemcpyHostToDevice), "write params");
     refresh_bf16(v->prop, v->stream);
+    publish(v->prop, -1, v->stream);
     CUP(cudaStreamSynchronize(v->stream), "sync");
     return VXR_OK;
 }
@@ -721,6 +774,7 @@ int vxr_view_proposal_load(vxr_view* v, const char* path) {
     CUP(cudaMemcpy(p->v, buf.data() + 2 * n, n * sizeof(float), cudaMemcpyHostToDevice), "write adam");
     p->step = (int)hdr[7];
     refresh_bf16(p, v->stream);
+    publish(p, -1, v->stream);
     CUP(cudaStreamSynchronize(v->stream), "sync");
     return VXR_OK;
 }

@@ -515,7 +515,11 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     alloc((void**)&b.qA, n * sizeof(float4));
     alloc((void**)&b.qB, n * sizeof(float4));
     alloc((void**)&b.counters, vxr::kCounters * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking);
+    // the highest stream priority: a learned view's training steps (a side stream of the
+    // lowest priority with training_lag = 1) fill only the SM slots its frames leave free
+    int leastPrio = 0, greatestPrio = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&leastPrio, &greatestPrio);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&v->stream, cudaStreamNonBlocking, greatestPrio);
     v->ringS.assign(vxr_view::kRing * 6, nullptr);
     v->ringE.assign(vxr_view::kRing * 6, nullptr);
     v->ringUsed.assign(vxr_view::kRing * 6, 0);

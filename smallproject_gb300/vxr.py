@@ -65,7 +65,7 @@ class ProposalDesc(C.Structure):
     _fields_ = [("hidden", C.c_uint32), ("table_log2", C.c_uint32), ("res0", C.c_uint32), ("res1", C.c_uint32),
                 ("epsilon", C.c_float), ("learning_rate", C.c_float), ("batch", C.c_uint32), ("seed", C.c_uint32),
                 ("inference", C.c_uint32), ("training", C.c_uint32), ("pixels_per_eval", C.c_uint32),
-                ("share_distance", C.c_float)]
+                ("share_distance", C.c_float), ("training_lag", C.c_uint32)]
 
 
 class Tuning(C.Structure):

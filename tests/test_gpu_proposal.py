@@ -262,11 +262,13 @@ def test_tcgen05_learned_render_runs_clean(lib, world256):
         v.close()
 
 
-def test_online_training_inside_the_frame(lib, cuda_device):
+@pytest.mark.parametrize("lag", [0, 1])
+def test_online_training_inside_the_frame(lib, cuda_device, lag):
     """A learned view that trains itself: each vxr_view_render ends with one training
     step on that frame's own final reservoirs (timed as proposal_train). Starting from
     random parameters, after 80 such frames its single-frame MSE against the converged
-    render is below the uniform source's at the same candidate count."""
+    render is below the uniform source's at the same candidate count. lag = 1: a frame's
+    inference uses the weights of the step two frames back (published copies)."""
     w = lib.World()
     w.generate(lib.scene_preset(3))
     w.cluster_lights(256, seed=1, iters=6)
@@ -284,7 +286,7 @@ def test_online_training_inside_the_frame(lib, cuda_device):
         v = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, num_candidates=8, rng_seed=31))
         v.lookat(pos, tgt)
         if learned:
-            v.proposal_enable(seed=2, batch=8192)
+            v.proposal_enable(seed=2, batch=8192, training_lag=lag)
             v.proposal_use(True)
             v.proposal_online(1)
             p0 = v.proposal_params()
