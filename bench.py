@@ -26,7 +26,10 @@ training steps included.
 Arms:
   --impl ours       the CUDA path (libvxr.so) - the JSON line's `value` is device time
                     per frame with all inputs resident in HBM; `e2e` goes through the
-                    C ABI call that returns the image in page-locked host memory.
+                    C ABI calls that return each frame's image in page-locked host
+                    memory, pipelined (vxr_view_render_to_host_async: frame f + 1 renders
+                    while the host waits for image f), and synchronously
+                    (vxr_view_render_to_host, `e2e.synchronous`).
   --impl reference  the reference's own render-path kernel source compiled for the
                     host CPU (oracle/_ref, OpenMP over all host threads), else the C
                     restatement; each step renders one whole frame of the same
@@ -718,28 +721,42 @@ def main():
     launches = sum(v[1] for v in kstats.values())
     hits, rays_c, rays_s = view.work_counts()
 
-    # end to end through the C ABI with a page-locked host image
-    pinned = vx.PinnedBuffer(W * H * 4)
+    # end to end through the C ABI with page-locked host images: pipelined (frame f + 1
+    # renders while the host waits for image f; two host buffers) and synchronous
+    # (vxr_view_render_to_host: each frame waits for its own image)
+    pinned = [vx.PinnedBuffer(W * H * 4), vx.PinnedBuffer(W * H * 4)]
     e2e_steps = max(5, min(args.steps, 30))
 
     def e2e_of(v):
         for f in range(3):
             pos, tgt = cams(f)
-            v.render_to_host(pos, tgt, pinned.array)
+            v.render_to_host(pos, tgt, pinned[0].array)
+        t0 = time.perf_counter()
+        prev = None
+        for f in range(e2e_steps):
+            pos, tgt = cams(f)
+            t = v.render_to_host_async(pos, tgt, pinned[f % 2].array)
+            if prev is not None:
+                v.image_wait(prev)
+            prev = t
+        v.image_wait(prev)
+        piped = (time.perf_counter() - t0) * 1000.0 / e2e_steps
         t0 = time.perf_counter()
         for f in range(e2e_steps):
             pos, tgt = cams(f)
-            v.render_to_host(pos, tgt, pinned.array)
-        return max_over_ranks(dist, (time.perf_counter() - t0) * 1000.0 / e2e_steps)
+            v.render_to_host(pos, tgt, pinned[0].array)
+        sync = (time.perf_counter() - t0) * 1000.0 / e2e_steps
+        return max_over_ranks(dist, piped), max_over_ranks(dist, sync)
 
-    e2e_ms = e2e_of(view)
-    img_ok = bool(np.isfinite(pinned.array).all() and pinned.array.max() > 0)
-    e2e_plain_ms = None
+    e2e_ms, e2e_sync_ms = e2e_of(view)
+    img_ok = all(bool(np.isfinite(p.array).all() and p.array.max() > 0) for p in pinned)
+    e2e_plain_ms = e2e_plain_sync_ms = None
     if learned:
         pv = make_view(False, 32)
-        e2e_plain_ms = e2e_of(pv)
+        e2e_plain_ms, e2e_plain_sync_ms = e2e_of(pv)
         pv.close()
-    pinned.close()
+    for p in pinned:
+        p.close()
     modes = other_modes(make_view, cams, min(args.steps, 30), warmup) if rank == 0 else None
     configs01 = None
     if rank == 0 and not args.no_small_configs:
@@ -801,8 +818,10 @@ def main():
             "roofline": roofline, "reservoir_roofline": reservoir_roofline, "cpu_baseline": cpu, "quality": quality,
             "frames_per_s_job": ws * 1000.0 / ms_frame,
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
-                    "d2h_bytes_per_step": npx * 16, "image_ok": img_ok,
-                    "plain_32": e2e_plain_ms if learned else e2e_ms},
+                    "d2h_bytes_per_step": npx * 16, "image_ok": img_ok, "pipelined": True,
+                    "synchronous": e2e_sync_ms,
+                    "plain_32": e2e_plain_ms if learned else e2e_ms,
+                    "plain_32_synchronous": e2e_plain_sync_ms if learned else e2e_sync_ms},
             "gpu_launches": launches, "clocks": clk,
             "tuning": view.get_tuning().as_dict(), "tuning_search": tuning_report,
             "modes": modes, "configs_0_1": configs01, "world_commit": world_commit_times(world, args)}

@@ -388,6 +388,15 @@ int vxr_view_work_counts(vxr_view* v, uint32_t counts[3]);
 /* End-to-end frame through host memory: LookAt(pos, target), render, copy the
  * accumulated image into host_rgba (W*H float4; page-locked memory is fastest), wait. */
 int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[3], float* host_rgba);
+/* The same, pipelined: enqueues the frame and the image copy and returns at once with
+ * *ticket; vxr_view_image_wait(v, ticket) returns once that image is in host_rgba (and
+ * reports device error flags like vxr_view_wait). Up to 4 images may be in flight (a
+ * fifth call first waits for the oldest); give each in-flight image its own host buffer
+ * (page-locked, vxr_host_alloc, for the copy to overlap). Rendering frame f + 1 while the
+ * host reads image f hides the host's per-frame work behind the device's. */
+int vxr_view_render_to_host_async(vxr_view* v, const float pos[3], const float target[3], float* host_rgba,
+                                  uint64_t* ticket);
+int vxr_view_image_wait(vxr_view* v, uint64_t ticket);
 
 /* ---- learned candidate proposal (no reference counterpart) ------------------------------
  * Replaces the uniform source pdf of RIS (GenerateLightCandidate, tools.cl:593-598) by a

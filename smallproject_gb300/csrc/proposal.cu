@@ -545,7 +545,8 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
     // from the row's tables)
     const bool useRows = a.rows && !a.samples && !a.probs;
     const uint32_t rows = useRows ? *a.rowCount : n;
-    for (uint32_t tile = blockIdx.x * 2 + h; ok && (size_t)tile * tc::kTile < rows; tile += gridDim.x * 2) {
+    uint32_t tile = blockIdx.x * 2 + h;
+    for (; ok && (size_t)tile * tc::kTile < rows; tile += gridDim.x * 2) {
         const uint32_t row = tile * tc::kTile + tid;
         const bool valid = row < rows;
         uint32_t j = row, span = 1u;
@@ -745,6 +746,24 @@ __global__ void __launch_bounds__(512, 1) infer_tc_kernel(InferArgs a) {
                 const float pe = (1.0f - eps) * (((gw * frac(c)) * invZ) / sz) + eps * invN;
                 out[(size_t)m * a.candStride] = make_uint2(e, __float_as_uint(pe));
             }
+        }
+    }
+    // a wait gave up: the candidate entries of this half's remaining rows, from the tile it
+    // stopped in, are marked as not drawn (light index ~0), which the candidate kernel
+    // replaces by uniform candidates - so no entry of an earlier frame, or of memory never
+    // written, is read as a draw of this one
+    if (!ok && a.cand && !a.samples && !a.probs && half == 0) {
+        for (; (size_t)tile * tc::kTile < rows; tile += gridDim.x * 2) {
+            const uint32_t row = tile * tc::kTile + tid;
+            if (row >= rows) continue;
+            uint32_t j = row, span = 1u;
+            if (useRows) {
+                const uint32_t e = a.rows[row];
+                j = e & 0x1FFFFFFFu;
+                span = (e >> 29) + 1u;
+            }
+            for (uint32_t jm = j; jm < j + span && jm < n; jm++)
+                for (uint32_t m = 0; m < a.ncand; m++) a.cand[(size_t)m * a.candStride + jm] = make_uint2(0xFFFFFFFFu, 0u);
         }
     }
     // every MMA of this CTA has completed (each was waited for) unless a wait gave up

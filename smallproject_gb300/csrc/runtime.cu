@@ -271,6 +271,8 @@ void free_view(vxr_view* v) {
     }
     for (cudaEvent_t e : v->ringS) cudaEventDestroy(e);
     for (cudaEvent_t e : v->ringE) cudaEventDestroy(e);
+    for (cudaEvent_t e : v->imgEv)
+        if (e) cudaEventDestroy(e);
     if (v->stream) cudaStreamDestroy(v->stream);
 }
 
@@ -891,6 +893,36 @@ int vxr_view_render_to_host(vxr_view* v, const float pos[3], const float target[
     if (int r = vxr_view_render(v)) return r;
     CUV(cudaMemcpyAsync(host_rgba, v->buf.accum, v->npx * sizeof(float4), cudaMemcpyDeviceToHost, v->stream), "copy image");
     return view_wait(v, false);
+}
+
+int vxr_view_render_to_host_async(vxr_view* v, const float pos[3], const float target[3], float* host_rgba,
+                                  uint64_t* ticket) {
+    if (int r = check_view(v, "vxr_view_render_to_host_async")) return r;
+    VXR_CHECK_ARG(pos && target && host_rgba && ticket, "vxr_view_render_to_host_async: null argument");
+    const int slot = (int)(v->imgSerial % vxr_view::kImages);
+    if (v->imgSerial >= (uint64_t)vxr_view::kImages)   // the slot's previous image must be done
+        CUV(cudaEventSynchronize(v->imgEv[slot]), "vxr_view_render_to_host_async: wait for an earlier image");
+    if (!v->imgEv[slot]) CUV(cudaEventCreateWithFlags(&v->imgEv[slot], cudaEventDisableTiming), "cudaEventCreate");
+    if (int r = vxr_view_lookat(v, pos, target)) return r;
+    if (int r = vxr_view_render(v)) return r;
+    CUV(cudaMemcpyAsync(host_rgba, v->buf.accum, v->npx * sizeof(float4), cudaMemcpyDeviceToHost, v->stream), "copy image");
+    CUV(cudaEventRecord(v->imgEv[slot], v->stream), "cudaEventRecord");
+    *ticket = v->imgSerial++;
+    return VXR_OK;
+}
+
+int vxr_view_image_wait(vxr_view* v, uint64_t ticket) {
+    if (int r = check_view(v, "vxr_view_image_wait")) return r;
+    VXR_CHECK_ARG(ticket < v->imgSerial && v->imgSerial - ticket <= (uint64_t)vxr_view::kImages,
+                  "vxr_view_image_wait: unknown or expired ticket");
+    CUV(cudaEventSynchronize(v->imgEv[ticket % vxr_view::kImages]), "vxr_view_image_wait");
+    uint32_t err = 0;
+    CUV(cudaMemcpy(&err, v->buf.err, sizeof(err), cudaMemcpyDeviceToHost), "read device error flags");
+    if (err) {
+        cudaMemset(v->buf.err, 0, sizeof(uint32_t));
+        return set_error(VXR_E_DEVICE, vxr::device_flags_message(err));
+    }
+    return VXR_OK;
 }
 
 }  // extern "C"

@@ -84,6 +84,10 @@ struct vxr_view {
     uint64_t frameSerial = 0, harvested = 0;
     double statSum[6] = {};
     uint32_t statCount[6] = {};
+    // vxr_view_render_to_host_async: one event per outstanding image, ticket % kImages
+    static constexpr int kImages = 4;
+    cudaEvent_t imgEv[kImages] = {};
+    uint64_t imgSerial = 0;
     double* sum64 = nullptr;                          // FP64 running sum of shaded frames (rgb)
     uint32_t sum64Count = 0;
     double* errOut = nullptr;                         // [mse sum, mae sum]

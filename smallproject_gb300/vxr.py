@@ -126,6 +126,8 @@ _SIGS = {
     "vxr_sky_lights": [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P],
     "vxr_view_begin_frame": [_P, C.POINTER(FrameConsts)], "vxr_view_set_frame_consts": [_P, C.POINTER(FrameConsts)],
     "vxr_view_stage": [_P, C.c_int], "vxr_view_end_frame": [_P], "vxr_view_render": [_P], "vxr_view_wait": [_P],
+    "vxr_view_render_to_host_async": [_P, _F3, _F3, _F3, C.POINTER(C.c_uint64)],
+    "vxr_view_image_wait": [_P, C.c_uint64],
     "vxr_view_stage_times": [_P, _F3],
     "vxr_view_read_gbuffer": [_P, C.c_int, _P], "vxr_view_write_gbuffer": [_P, C.c_int, _P],
     "vxr_view_read_reservoirs": [_P, C.c_int, _P], "vxr_view_write_reservoirs": [_P, C.c_int, _P],
@@ -623,6 +625,17 @@ class View:
     def render_to_host(self, pos, target, out):
         assert out.dtype == np.float32 and out.size == self.n * 4 and out.flags.c_contiguous
         check(self._lib.vxr_view_render_to_host(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3)))
+
+    def render_to_host_async(self, pos, target, out):
+        """Enqueue a frame and its image copy into out; returns a ticket for image_wait."""
+        assert out.dtype == np.float32 and out.size == self.n * 4 and out.flags.c_contiguous
+        t = C.c_uint64()
+        check(self._lib.vxr_view_render_to_host_async(self.h, _f3(pos), _f3(target), out.ctypes.data_as(_F3),
+                                                      C.byref(t)))
+        return t.value
+
+    def image_wait(self, ticket):
+        check(self._lib.vxr_view_image_wait(self.h, ticket))
 
 
 KERNEL_COUNT = 12

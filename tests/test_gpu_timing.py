@@ -36,3 +36,38 @@ def test_kernel_timing_counts_every_launch(lib, cuda_device, scene0):
         assert all(c == 0 for _, c in v.kernel_stats().values())
     finally:
         v.close()
+
+
+def test_pipelined_images_equal_synchronous_ones(lib, cuda_device, scene0):
+    """vxr_view_render_to_host_async returns, image for image, what vxr_view_render_to_host
+    returns for the same camera sequence (two views with the same seed), with frame f + 1
+    enqueued before image f is waited for; a ticket older than the four in flight is
+    rejected."""
+    w, _ = scene0
+    W, H = 128, 72
+    va = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1, rng_seed=9))
+    vb = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1, rng_seed=9))
+    bufs = [lib.PinnedBuffer(W * H * 4) for _ in range(2)]
+    sync = lib.PinnedBuffer(W * H * 4)
+    try:
+        cams = [((110.0 + 3 * f, 150.0, 10.0 + 2 * f), (128.0, 120.0, 128.0)) for f in range(6)]
+        want = []
+        for pos, tgt in cams:
+            va.render_to_host(pos, tgt, sync.array)
+            want.append(sync.array.copy())
+        tickets = [vb.render_to_host_async(*cams[0], bufs[0].array)]
+        for f in range(1, len(cams)):
+            tickets.append(vb.render_to_host_async(*cams[f], bufs[f % 2].array))
+            vb.image_wait(tickets[f - 1])
+            assert (bufs[(f - 1) % 2].array.view("u4") == want[f - 1].view("u4")).all(), f - 1
+        vb.image_wait(tickets[-1])
+        assert (bufs[(len(cams) - 1) % 2].array.view("u4") == want[-1].view("u4")).all()
+        with pytest.raises(lib.VxrError):
+            vb.image_wait(tickets[0])    # six images ago: no longer tracked
+        with pytest.raises(lib.VxrError):
+            vb.image_wait(tickets[-1] + 1)   # not issued
+    finally:
+        for b in bufs + [sync]:
+            b.close()
+        va.close()
+        vb.close()
