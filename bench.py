@@ -305,6 +305,44 @@ def boot_ratio(ga, gb, stat, n=2000, seed=1):
     return [float(np.percentile(vals, 2.5)), float(np.percentile(vals, 97.5))]
 
 
+def decide(table, groups):
+    """The quality protocol's decisions over table[key] = {"ms", "mse", "mse_ci95",
+    "mse_median", ...} (key "plain_32" or "<family>_<K>") and groups[key] = per-seed arrays
+    of per-frame MSEs. Adds each learned point's bootstrap ratio intervals against plain 32
+    and returns (equal MSE pick, pick by the mean alone, pick by the median alone, learned
+    MSE monotone within the intervals, equal-time point per family, equal-time pick)."""
+    p32 = table["plain_32"]
+    learned = [k for k in table if k != "plain_32"]
+    for k in learned:
+        r = table[k]
+        r["mse_ratio_ci95"] = boot_ratio(groups[k], groups["plain_32"], np.mean)
+        r["median_mse_ratio_ci95"] = boot_ratio(groups[k], groups["plain_32"], np.median)
+    # equal MSE: among the learned configurations whose mean-MSE and median-MSE ratios to
+    # plain-32 are both at most 1 with 95 % confidence (upper ends of the bootstrap
+    # intervals <= 1), the fastest; also the fastest by each criterion alone
+    ok_mean = [table[k] for k in learned if table[k]["mse_ratio_ci95"][1] <= 1.0]
+    ok_med = [table[k] for k in learned if table[k]["median_mse_ratio_ci95"][1] <= 1.0]
+    ok = [r for r in ok_mean if r in ok_med]
+    eq = min(ok, key=lambda r: r["ms"]) if ok else None
+    eq_mean = min(ok_mean, key=lambda r: r["ms"]) if ok_mean else None
+    eq_med = min(ok_med, key=lambda r: r["ms"]) if ok_med else None
+    # monotone within the intervals: a larger count is never significantly worse
+    cands = sorted(int(k.split("_")[1]) for k in learned if k.startswith("learned_"))
+    mono = all(table[f"learned_{b}"]["mse_ci95"][0] <= table[f"learned_{a}"]["mse_ci95"][1]
+               for i, a in enumerate(cands) for b in cands[i + 1:])
+
+    # equal time: per family, the learned configuration with the largest ms/frame not above
+    # plain's; the headline one is the family with the lowest median MSE there
+    def at_time(fam):
+        at = [table[k] for k in learned if k.rsplit("_", 1)[0] == fam and table[k]["ms"] <= p32["ms"]]
+        return max(at, key=lambda r: r["ms"]) if at else None
+
+    fams = {f: at_time(f) for f in sorted({k.rsplit("_", 1)[0] for k in learned})}
+    ets = [r for r in fams.values() if r is not None]
+    et = min(ets, key=lambda r: r["mse_median"]) if ets else None
+    return eq, eq_mean, eq_med, mono, fams, et
+
+
 def pretrain(vx, world, W, H, tuning, args, desc):
     """The proposal's warm start: trained online along the camera path on the plain
     method's reservoirs (the uniform source is the fallback until the network exists)."""
@@ -396,32 +434,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
                       "kernel_ms": {k: float(np.median(x)) for k, x in kms_l.items()}}
     ref.close()
     p32 = table["plain_32"]
-    learned = [k for k in table if k != "plain_32"]
-    for k in learned:
-        r = table[k]
-        r["mse_ratio_ci95"] = boot_ratio(groups[k], groups["plain_32"], np.mean)
-        r["median_mse_ratio_ci95"] = boot_ratio(groups[k], groups["plain_32"], np.median)
-    # equal MSE: among the learned configurations whose mean-MSE and median-MSE ratios to
-    # plain-32 are both at most 1 with 95 % confidence (upper ends of the bootstrap
-    # intervals <= 1), the fastest; also the fastest by each criterion alone
-    ok_mean = [table[k] for k in learned if table[k]["mse_ratio_ci95"][1] <= 1.0]
-    ok_med = [table[k] for k in learned if table[k]["median_mse_ratio_ci95"][1] <= 1.0]
-    ok = [r for r in ok_mean if r in ok_med]
-    eq = min(ok, key=lambda r: r["ms"]) if ok else None
-    eq_mean = min(ok_mean, key=lambda r: r["ms"]) if ok_mean else None
-    eq_med = min(ok_med, key=lambda r: r["ms"]) if ok_med else None
-    # monotone within the intervals: a larger count is never significantly worse
-    mono = all(table[f"learned_{b}"]["mse_ci95"][0] <= table[f"learned_{a}"]["mse_ci95"][1]
-               for i, a in enumerate(CANDS) for b in CANDS[i + 1:])
-    # equal time: per family, the learned configuration with the largest ms/frame not above
-    # plain's; the headline one is the family with the lower median MSE there
-    def at_time(fam, cands):
-        at = [table[f"{fam}_{c}"] for c in cands if table[f"{fam}_{c}"]["ms"] <= p32["ms"]]
-        return max(at, key=lambda r: r["ms"]) if at else None
-    fams = {"learned": at_time("learned", CANDS), "learned2": at_time("learned2", CANDS2),
-            "learned4": at_time("learned4", CANDS4)}
-    ets = [r for r in fams.values() if r is not None]
-    et = min(ets, key=lambda r: r["mse_median"]) if ets else None
+    eq, eq_mean, eq_med, mono, fams, et = decide(table, groups)
     return {"pose_frame": POSE, "converged_frames": args.conv_frames, "converged_s": conv_s,
             "epsilon": args.epsilon, "online_steps_per_frame": online,
             "frames_per_point": args.mse_seeds * args.mse_frames, "seeds_per_point": args.mse_seeds,
