@@ -269,7 +269,7 @@ def cpu_arm(config, steps, warmup, W, H):
 
 CANDS = (2, 3, 4, 8, 12, 16, 24, 32)
 CANDS2 = (2, 3, 4, 8, 12)
-CANDS4 = (2, 3, 4, 8)
+CANDS4 = (1, 2, 3, 4, 8)
 # hit pixels per network evaluation of each learned family (pixels_per_eval; runs of up to
 # eight measured no faster than runs of up to four at config 3)
 FAMILY_PPE = {"learned": 1, "learned2": 2, "learned4": 4}
@@ -572,7 +572,7 @@ def main():
                          "render, no sweep); off: time the plain method at 32 candidates")
     ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
-    ap.add_argument("--train-frames", type=int, default=200)
+    ap.add_argument("--train-frames", type=int, default=800)
     ap.add_argument("--mse-seeds", type=int, default=40)
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
