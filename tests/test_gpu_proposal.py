@@ -306,3 +306,49 @@ def test_online_training_inside_the_frame(lib, cuda_device, lag):
         v.close()
     ref.close()
     assert errs[True] < errs[False], errs
+
+
+@pytest.mark.parametrize("lag", [0, 1])
+def test_online_training_weights_reach_the_right_frame(lib, world256, lag):
+    """With one online training step per frame, the inference of frame f uses the
+    parameters after step f - 1 (training_lag = 0) or after step f - 2 (training_lag = 1,
+    the published copies; the initial parameters before that). Checked bit for bit: the
+    candidates a training view draws in frames 1 and 2 equal, pixel for pixel, those of
+    views that never train and hold the expected parameters (same camera and seeds; one
+    network evaluation per pixel, so no draw depends on the hit list's order)."""
+    W, H = 96, 64
+    pos, tgt = (110.0, 150.0, 10.0), (128.0, 110.0, 128.0)
+
+    def make(params=None, online=0):
+        v = lib.View(world256, lib.view_desc(W, H, lib.LIGHTS_AREA, num_candidates=4, rng_seed=41))
+        v.lookat(pos, tgt)
+        v.proposal_enable(seed=3, batch=4096, training_lag=lag)
+        if params is not None:
+            v.proposal_set_params(params)
+        v.proposal_use(True)
+        v.proposal_online(online)
+        return v
+
+    tv = make(online=1)
+    p0 = tv.proposal_params()
+    got, after = [], [p0]
+    for f in range(3):
+        tv.render()
+        tv.wait()
+        got.append(tv.proposal_candidates(4))
+        after.append(tv.proposal_params())      # after step f
+    tv.close()
+    assert not np.array_equal(after[1], p0) and not np.array_equal(after[2], after[1])
+    for f in (1, 2):
+        want_params = after[f - lag] if f - lag >= 1 else p0   # step f - 1 - lag, or the initial
+        rv = make(params=want_params)
+        for g in range(f + 1):
+            rv.render()
+            rv.wait()
+        hits, cand = rv.proposal_candidates(4)
+        rv.close()
+        # the hit list's order depends on the compaction's atomics: compare per pixel
+        ga, gc = got[f]
+        oa, ob = np.argsort(ga), np.argsort(hits)
+        assert np.array_equal(ga[oa], hits[ob]), f
+        assert np.array_equal(gc[:, oa], cand[:, ob]), (f, lag)
