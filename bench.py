@@ -453,6 +453,118 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
                 "median_mse_ratio_ci95": et["median_mse_ratio_ci95"]}}
 
 
+def config4_learned(vx, world, cams, tuning, args, warmup, W, H):
+    """Config 4 with the learned proposal built here (256 emitter clusters, hidden width
+    64: config 4 names 4,096 clusters and width 128, which are not built), each 3840x2160
+    view on its own stream: a warm start along the views' paths at 960x540 (the network's
+    hash grid is in world space), an equal-MSE check at 960x540 on view 0's pose (plain at
+    32 against one evaluation per run of up to four at 2, 4 and 8 candidates; 32 seeds x 8
+    frames against a 2048-frame converged render; the decision of the config-3 protocol),
+    then the four views' frame time at the chosen count (4 when none qualifies, marked so)
+    beside plain at 32 on the same per-view streams (host wall time per frame, every view
+    waited for)."""
+    world.cluster_lights(256, seed=1, iters=6)
+    QW, QH = 960, 540
+    trainer = vx.View(world, vx.view_desc(QW, QH, vx.LIGHTS_AREA, rng_seed=5))
+    trainer.set_tuning(tuning)
+    trainer.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon)
+    t0 = time.perf_counter()
+    for f in range(args.train_frames):
+        pos, tgt = cams[f % len(cams)](f // len(cams))
+        trainer.lookat(pos, tgt)
+        trainer.render()
+        trainer.proposal_train(1)
+    trainer.wait()
+    params = trainer.proposal_params()
+    train_s = time.perf_counter() - t0
+    trainer.close()
+
+    def learned_view(w_, h_, k, seed):
+        v = vx.View(world, vx.view_desc(w_, h_, vx.LIGHTS_AREA, num_candidates=k, rng_seed=seed))
+        v.set_tuning(tuning)
+        v.proposal_enable(seed=2, batch=65536, epsilon=args.epsilon, pixels_per_eval=4, training_lag=1)
+        v.proposal_set_params(params)
+        v.proposal_use(True)
+        v.proposal_online(1)
+        return v
+
+    pos, tgt = cams[0](60)
+    ref = vx.View(world, vx.view_desc(QW, QH, vx.LIGHTS_AREA, spatial=0, temporal=0, accumulate=0, rng_seed=77))
+    ref.set_tuning(tuning)
+    ref.lookat(pos, tgt)
+    ref.sum64_reset()
+    for _ in range(2048):
+        ref.render()
+        ref.sum64_add()
+    ref.wait()
+    groups, table = {}, {}
+    for method, k in [("plain", 32), ("learned4", 2), ("learned4", 4), ("learned4", 8)]:
+        per_seed = []
+        for seed in range(32):
+            if method == "plain":
+                v = vx.View(world, vx.view_desc(QW, QH, vx.LIGHTS_AREA, num_candidates=k, rng_seed=3000 + seed))
+                v.set_tuning(tuning)
+            else:
+                v = learned_view(QW, QH, k, 3000 + seed)
+            v.lookat(pos, tgt)
+            for _ in range(8):
+                v.render()
+            e = []
+            for _ in range(8):
+                v.render()
+                e.append(v.error_vs(ref, 0)[0])
+            per_seed.append(np.array(e))
+            v.close()
+        key = f"{method}_{k}"
+        groups[key] = per_seed
+        allf = np.concatenate(per_seed)
+        table[key] = {"method": method, "candidates": k, "ms": float(k), "mse": float(allf.mean()),
+                      "mse_ci95": boot_ci(per_seed, np.mean), "mse_median": float(np.median(allf)),
+                      "mse_median_ci95": boot_ci(per_seed, np.median), "frames": int(allf.size),
+                      "seeds": len(per_seed)}
+    ref.close()
+    # the fewest candidates that qualify ("ms" holds the count here: fewer is faster)
+    eq, _, _, _, _, _ = decide(table, groups)
+    for r in table.values():
+        r.pop("ms")
+    out = {"clusters": 256, "hidden": 64, "train_frames": args.train_frames, "train_s": train_s,
+           "quality_960x540": table, "equal_mse_candidates": eq["candidates"] if eq else None}
+    k_timed = eq["candidates"] if eq else 4
+    out["timed_candidates"] = k_timed
+    out["timed_at_equal_mse"] = eq is not None
+
+    def timed(vs):
+        step = 20000
+        for _ in range(warmup):
+            for v, c in zip(vs, cams):
+                v.lookat(*c(step))
+                v.render()
+            step += 1
+        for v in vs:
+            v.wait()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for v, c in zip(vs, cams):
+                v.lookat(*c(step))
+                v.render()
+            step += 1
+            for v in vs:
+                v.wait()
+        return (time.perf_counter() - t0) * 1000.0 / args.steps
+
+    lviews = [learned_view(W, H, k_timed, 5000 + i) for i in range(len(cams))]
+    out["learned_views_host_ms_per_frame"] = timed(lviews)
+    for v in lviews:
+        v.close()
+    pviews = [vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5000 + i)) for i in range(len(cams))]
+    for v in pviews:
+        v.set_tuning(tuning)
+    out["plain_views_host_ms_per_frame"] = timed(pviews)
+    for v in pviews:
+        v.close()
+    return out
+
+
 def run_batch(args, dist, rank, ws, warmup):
     """Configs 2 and 4: several views rendered as one batch per frame (CUDA graph), autotuned."""
     import smallproject_gb300 as vx
@@ -537,6 +649,13 @@ def run_batch(args, dist, rank, ws, warmup):
         for v in views:
             v.wait()
     single_wall_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    learned4 = None
+    if args.config == 4 and not args.no_learned and rank == 0:
+        for v in views:
+            v.close()
+        batch.close()
+        views, batch = [], None
+        learned4 = config4_learned(vx, world, cams, t, args, warmup, specs[0]["width"], specs[0]["height"])
     if rank != 0:
         return
     npx = sum(s["width"] * s["height"] for s in specs)
@@ -548,8 +667,11 @@ def run_batch(args, dist, rank, ws, warmup):
             "chains": best_chains, "per_chains": per_chains,
             "individual_views_host_ms_per_frame": single_wall_ms,
             "tuning": rep["tuning"], "tuning_search": rep}
+    if learned4 is not None:
+        line["learned"] = learned4
     print(json.dumps(line))
-    batch.close()
+    if batch is not None:
+        batch.close()
     for v in views:
         v.close()
 
@@ -567,6 +689,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="library default launch tuning instead of the autotuner")
     ap.add_argument("--no-small-configs", action="store_true", help="skip the config 0 / config 1 measurements")
+    ap.add_argument("--no-learned", action="store_true", help="config 4: skip the learned-proposal measurement")
     ap.add_argument("--quality", choices=["full", "train", "off"], default="full",
                     help="train: train the proposal and time the learned method at --candidates (no converged "
                          "render, no sweep); off: time the plain method at 32 candidates")
