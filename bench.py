@@ -534,6 +534,7 @@ def config4_learned(vx, world, cams, tuning, args, warmup, W, H):
     out["timed_at_equal_mse"] = eq is not None
 
     def timed(vs):
+        """host ms per frame of the views; per-kernel mean ms of view 0 (CUDA events)"""
         step = 20000
         for _ in range(warmup):
             for v, c in zip(vs, cams):
@@ -542,6 +543,8 @@ def config4_learned(vx, world, cams, tuning, args, warmup, W, H):
             step += 1
         for v in vs:
             v.wait()
+        vs[0].kernel_timing(True)
+        vs[0].kernel_stats(reset=True)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             for v, c in zip(vs, cams):
@@ -550,16 +553,19 @@ def config4_learned(vx, world, cams, tuning, args, warmup, W, H):
             step += 1
             for v in vs:
                 v.wait()
-        return (time.perf_counter() - t0) * 1000.0 / args.steps
+        ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+        vs[0].kernel_timing(False)
+        ks = {k: (a / n if n else 0.0) for k, (a, n) in vs[0].kernel_stats(reset=True).items()}
+        return ms, ks
 
     lviews = [learned_view(W, H, k_timed, 5000 + i) for i in range(len(cams))]
-    out["learned_views_host_ms_per_frame"] = timed(lviews)
+    out["learned_views_host_ms_per_frame"], out["learned_view0_kernel_ms"] = timed(lviews)
     for v in lviews:
         v.close()
     pviews = [vx.View(world, vx.view_desc(W, H, vx.LIGHTS_AREA, rng_seed=5000 + i)) for i in range(len(cams))]
     for v in pviews:
         v.set_tuning(tuning)
-    out["plain_views_host_ms_per_frame"] = timed(pviews)
+    out["plain_views_host_ms_per_frame"], out["plain_view0_kernel_ms"] = timed(pviews)
     for v in pviews:
         v.close()
     return out
