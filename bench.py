@@ -685,7 +685,7 @@ def run_batch(args, dist, rank, ws, warmup):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=250)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", type=int, default=3)
@@ -730,10 +730,13 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": f"config {args.config} is a batch of views: the "
                               "reference renders one view per World"}))
             return
-        ms, kind, sample = cpu_arm(args.config, args.steps, args.warmup, W, H)
+        # whole frames of ~0.85 s each at config 3: at most 30 of them, so the arm stays
+        # within a minute whatever --steps the GPU arm times
+        ref_steps = min(args.steps, 30)
+        ms, kind, sample = cpu_arm(args.config, ref_steps, args.warmup, W, H)
         config["method"] = "plain uniform-source RIS, 32 candidates"
         line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms/frame", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+                "steps": ref_steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
                 "config": config,
                 "cpu_baseline": {"value": ms, "unit": "ms/frame", "cores": sample["threads"], "kind": kind,
