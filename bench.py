@@ -267,7 +267,7 @@ def cpu_arm(config, steps, warmup, W, H):
     return ms, kind, info
 
 
-CANDS = (2, 3, 4, 8, 12, 16, 24, 32)
+CANDS = (2, 3, 4, 8, 12)
 CANDS2 = (2, 3, 4, 8, 12)
 CANDS4 = (1, 2, 3, 4, 8)
 # hit pixels per network evaluation of each learned family (pixels_per_eval; runs of up to
@@ -702,7 +702,7 @@ def main():
     ap.add_argument("--candidates", type=int, default=8, help="candidate count of the learned method (--quality train)")
     ap.add_argument("--conv-frames", type=int, default=4096)
     ap.add_argument("--train-frames", type=int, default=800)
-    ap.add_argument("--mse-seeds", type=int, default=40)
+    ap.add_argument("--mse-seeds", type=int, default=96)
     ap.add_argument("--mse-frames", type=int, default=16)
     ap.add_argument("--epsilon", type=float, default=0.1, help="defensive (uniform emitter) share of the proposal")
     ap.add_argument("--online", type=int, default=1, help="proposal training steps inside every learned frame")
