@@ -332,14 +332,14 @@ def decide(table, groups):
                for i, a in enumerate(cands) for b in cands[i + 1:])
 
     # equal time: per family, the learned configuration with the largest ms/frame not above
-    # plain's; the headline one is the family with the lowest median MSE there
+    # plain's; the headline one is the family whose point is closest to plain's time
     def at_time(fam):
         at = [table[k] for k in learned if k.rsplit("_", 1)[0] == fam and table[k]["ms"] <= p32["ms"]]
         return max(at, key=lambda r: r["ms"]) if at else None
 
     fams = {f: at_time(f) for f in sorted({k.rsplit("_", 1)[0] for k in learned})}
     ets = [r for r in fams.values() if r is not None]
-    et = min(ets, key=lambda r: r["mse_median"]) if ets else None
+    et = max(ets, key=lambda r: r["ms"]) if ets else None
     return eq, eq_mean, eq_med, mono, fams, et
 
 
@@ -445,7 +445,7 @@ def quality_eval(vx, world, desc, W, H, tuning, args, params, online):
                              "mean-MSE(learned) / mean-MSE(plain 32) and of median-MSE(learned) / median-MSE(plain 32) "
                              "both lie at or below 1; equal time: per family (learned, learned2 / 4 = one network "
                              "evaluation per run of up to two / four compatible hit pixels) the largest learned "
-                             "ms/frame not above plain's, the family with the lowest median MSE there",
+                             "ms/frame not above plain's, the family whose point is closest to plain's ms/frame",
             "equal_time_per_family": fams,
             "equal_time": None if et is None else {
                 "learned": et, "mse_ratio": et["mse"] / p32["mse"], "mse_ratio_ci95": et["mse_ratio_ci95"],
