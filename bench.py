@@ -72,6 +72,17 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    """dense BF16 TFLOP/s for a kernel timed inside a long step (the sustained figure)"""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if "bf16_tflops_sustained" in d:
+            return float(d["bf16_tflops_sustained"]), "measured (sustained)"
+    return 1700.0, "fallback (sustained)"
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -865,6 +876,23 @@ def main():
     kernel_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in kstats.items()}
     launches = sum(v[1] for v in kstats.values())
     hits, rays_c, rays_s = view.work_counts()
+    # the proposal MLP on the tensor cores: its multiply-adds per network evaluation
+    # (32 -> H -> H -> H -> K) times the frame's evaluations, over the inference kernel's
+    # mean time (which also builds the sampling tables and draws every pixel's candidates)
+    mlp = None
+    if learned:
+        _, K_, H_ = view.proposal_shape()
+        rows = view.proposal_rows()
+        flop = 2.0 * (32 * H_ + 2 * H_ * H_ + H_ * K_) * rows
+        peak_tf, peak_tf_kind = bf16_peak()
+        infer_ms = kernel_ms.get("proposal_infer", 0.0)
+        if infer_ms > 0:
+            tf = flop / (infer_ms * 1e-3) / 1e12
+            mlp = {"kernel": "proposal_infer", "bound": "tensor", "evaluations_per_frame": rows,
+                   "hit_pixels": hits, "flop_per_launch": flop, "achieved": tf, "peak": peak_tf,
+                   "peak_kind": peak_tf_kind, "unit": "TFLOP/s", "frac": tf / peak_tf,
+                   "note": "MLP multiply-adds only; the kernel's time also covers the sampling tables and draws "
+                           "(ncu: tensor pipe 4.6 - 5.4 % active)"}
 
     # end to end through the C ABI with page-locked host images: pipelined (frame f + 1
     # renders while the host waits for image f; two host buffers) and synchronous
@@ -960,7 +988,8 @@ def main():
             "config": config, "plain_ms_per_frame": plain_ms if learned else ms_frame,
             "stage_ms": stage_ms, "kernel_ms": kernel_ms, "stage_roofline": stage_rooflines,
             "rays_per_frame": rays, "rays_per_s": rays / (ms_frame * 1e-3),
-            "roofline": roofline, "reservoir_roofline": reservoir_roofline, "cpu_baseline": cpu, "quality": quality,
+            "roofline": roofline, "reservoir_roofline": reservoir_roofline, "mlp_roofline": mlp,
+            "cpu_baseline": cpu, "quality": quality,
             "frames_per_s_job": ws * 1000.0 / ms_frame,
             "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": 4 * 176,
                     "d2h_bytes_per_step": npx * 16, "image_ok": img_ok, "pipelined": True,

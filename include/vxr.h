@@ -455,6 +455,9 @@ int vxr_view_proposal_test_timeout(vxr_view* v, int on);
  * index and bits(source pdf) of candidate m of entry j, m < min(candidates, lights).
  * hits and cand may be NULL (then only *nhits is written). */
 int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hits, uint32_t* cand);
+/* Network evaluations of the view's current frame (no reference counterpart): one per hit
+ * pixel, or with pixels_per_eval > 1 one per run of pixels sharing an evaluation. */
+int vxr_view_proposal_rows(vxr_view* v, uint32_t* rows);
 int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden);
 int vxr_view_proposal_get_params(vxr_view* v, float* out);
 int vxr_view_proposal_set_params(vxr_view* v, const float* in);

@@ -623,6 +623,18 @@ int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hi
     return VXR_OK;
 }
 
+int vxr_view_proposal_rows(vxr_view* v, uint32_t* rows) {
+    if (int r = check_view(v, "vxr_view_proposal_rows")) return r;
+    vxr::proposal_join(v);
+    VXR_CHECK_ARG(rows, "vxr_view_proposal_rows: null rows");
+    vxr::Proposal* p = v->prop;
+    if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_rows: enable the proposal first");
+    CUP(cudaStreamSynchronize(v->stream), "vxr_view_proposal_rows");
+    const uint32_t* src = p->desc.pixels_per_eval > 1 ? p->pairCount : v->buf.counters + vxr::kCtrHits;
+    CUP(cudaMemcpy(rows, src, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read evaluation count");
+    return VXR_OK;
+}
+
 int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden) {
     if (int r = check_view(v, "vxr_view_proposal_param_count")) return r;
     vxr::proposal_join(v);

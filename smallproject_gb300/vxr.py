@@ -127,6 +127,7 @@ _SIGS = {
     "vxr_view_begin_frame": [_P, C.POINTER(FrameConsts)], "vxr_view_set_frame_consts": [_P, C.POINTER(FrameConsts)],
     "vxr_view_stage": [_P, C.c_int], "vxr_view_end_frame": [_P], "vxr_view_render": [_P], "vxr_view_wait": [_P],
     "vxr_view_render_to_host_async": [_P, _F3, _F3, _F3, C.POINTER(C.c_uint64)],
+    "vxr_view_proposal_rows": [_P, C.POINTER(C.c_uint32)],
     "vxr_view_image_wait": [_P, C.c_uint64],
     "vxr_view_stage_times": [_P, _F3],
     "vxr_view_read_gbuffer": [_P, C.c_int, _P], "vxr_view_write_gbuffer": [_P, C.c_int, _P],
@@ -544,6 +545,12 @@ class View:
         check(self._lib.vxr_view_proposal_read_candidates(self.h, C.byref(n), hits.ctypes.data_as(P),
                                                            cand.ctypes.data_as(P)))
         return hits[:n.value], cand[:, :n.value]
+
+    def proposal_rows(self):
+        """Network evaluations of the current frame (runs sharing one count once)."""
+        n = C.c_uint32()
+        check(self._lib.vxr_view_proposal_rows(self.h, C.byref(n)))
+        return n.value
 
     def proposal_test_timeout(self, on):
         """Test hook: the tensor-core inference's waits run out (error flag 16)."""

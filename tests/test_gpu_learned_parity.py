@@ -132,9 +132,19 @@ def test_shared_evaluations_pair_only_compatible_pixels(lib, cuda_device, group,
         view.stage(lib.STAGE_CANDIDATES)
         K = min(k.numberOfCandidates, k.numberOfLights)
         hits, cand = view.proposal_candidates(K)
+        rows = view.proposal_rows()
         sp, code = _shading_points(k, view.read_gbuffer(0), W)
         view.end_frame()
         view.wait()
+        # the frame's evaluation count is its number of runs (a group with a test within 1 %
+        # of share_distance may split either way)
+        n_runs, n_unsure = 0, 0
+        for g0 in range(0, len(hits), group):
+            sub, unsure = _runs(sp, code, hits[g0:g0 + group], group, dist)
+            n_runs += len(sub)
+            n_unsure += int(unsure)
+        assert abs(rows - n_runs) <= n_unsure * (group - 1), (rows, n_runs, n_unsure)
+        assert rows < len(hits)
 
         def same_pdfs(i, j):
             """(the two entries drew a common emitter, every common one has equal pdfs)"""
