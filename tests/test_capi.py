@@ -29,6 +29,27 @@ def test_struct_layouts_match_header(lib):
     assert C.sizeof(V.FrameConsts) == 44 * 4
     assert C.sizeof(V.ReservoirRec) == 48 and C.sizeof(V.GBufferRec) == 16 and C.sizeof(V.Light) == 12
     assert C.sizeof(V.SceneDesc) == 20 * 4 and C.sizeof(V.ViewDesc) == 13 * 4
+    assert C.sizeof(V.ProposalDesc) == 13 * 4
+
+
+def test_proposal_defaults_and_new_entry_points_check_arguments(lib):
+    from smallproject_gb300 import vxr as V
+    L = lib.load()
+    d = V.ProposalDesc()
+    assert L.vxr_proposal_default_desc(C.byref(d)) == 0
+    assert (d.hidden, d.table_log2, d.res0, d.res1, d.batch, d.seed, d.inference, d.training, d.pixels_per_eval,
+            d.training_lag) == (64, 16, 32, 128, 65536, 1, 0, 0, 1, 0)
+    assert abs(d.epsilon - 0.1) < 1e-7 and abs(d.learning_rate - 1e-3) < 1e-9 and d.share_distance == 2.0
+    t = C.c_uint64()
+    n = C.c_uint32()
+    img = (C.c_float * 4)()
+    p3 = (C.c_float * 3)()
+    assert L.vxr_view_render_to_host_async(None, p3, p3, img, C.byref(t)) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_view_image_wait(None, 0) == lib.vxr.VXR_E_INVALID
+    assert L.vxr_view_proposal_rows(None, C.byref(n)) == lib.vxr.VXR_E_INVALID
+    h = C.c_void_p()
+    arr = (C.c_void_p * 1)(None)
+    assert L.vxr_batch_create(arr, 1, 0, 0, 1 | (2 << 8), C.byref(h)) == lib.vxr.VXR_E_INVALID   # 2 chains, 1 view
 
 
 def test_invalid_arguments_return_status(lib):
