@@ -951,8 +951,11 @@ def main():
                            / hbm if stage_ms[s] > 0 else 0.0}
                        for s in ("albedo", "candidates", "spatial", "shade")}
     # dominant kernel (largest share of the timed frames); algorithmic bytes per launch:
-    # shadow tracers read the 32-byte request and write at most a 4-byte flag per ray
-    dom = max(kernel_ms, key=lambda k: kernel_ms[k] * (kstats[k][1] or 0))
+    # shadow tracers read the 32-byte request and write at most a 4-byte flag per ray.
+    # The training step is left out: it runs on a low-priority side stream beside the next
+    # frame, and its marks span the time from its fork to its last kernel, most of it
+    # spent waiting for free SM slots (its own kernels: mlp_roofline and the launch list)
+    dom = max((k for k in kernel_ms if k != "proposal_train"), key=lambda k: kernel_ms[k] * (kstats[k][1] or 0))
     per_launch_bytes = {"shadow_candidates": 36.0 * rays_c, "shadow_shading": 36.0 * rays_s,
                         "ris_candidates": 80.0 * hits, "albedo": 12.0 * npx, "spatial": 80.0 * npx,
                         "proposal_infer": 8.0 * hits + 8.0 * cand * hits, "temporal": TEMPORAL_BYTES_PER_HIT * hits,

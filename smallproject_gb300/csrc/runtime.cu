@@ -273,6 +273,9 @@ void free_view(vxr_view* v) {
     for (cudaEvent_t e : v->ringE) cudaEventDestroy(e);
     for (cudaEvent_t e : v->imgEv)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {v->evSpatial, v->evAlbedo, v->evNow})
+        if (e) cudaEventDestroy(e);
+    if (v->stream2) cudaStreamDestroy(v->stream2);
     if (v->stream) cudaStreamDestroy(v->stream);
 }
 
@@ -522,6 +525,10 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     int leastPrio = 0, greatestPrio = 0;
     if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&leastPrio, &greatestPrio);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&v->stream, cudaStreamNonBlocking, greatestPrio);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&v->stream2, cudaStreamNonBlocking, greatestPrio);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evSpatial, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evAlbedo, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evNow, cudaEventDisableTiming);
     v->ringS.assign(vxr_view::kRing * 6, nullptr);
     v->ringE.assign(vxr_view::kRing * 6, nullptr);
     v->ringUsed.assign(vxr_view::kRing * 6, 0);
@@ -575,6 +582,7 @@ int vxr_view_set_camera_matrix(vxr_view* v, const float m[16]) {
 
 int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d) {
     if (int r = check_view(v, "vxr_view_set_params")) return r;
+    v->spatialEvOk = false;
     VXR_CHECK_ARG(d, "vxr_view_set_params: null desc");
     VXR_CHECK_ARG(d->width == v->desc.width && d->height == v->desc.height && d->light_model == v->desc.light_model,
                   "vxr_view_set_params: resolution and light model are fixed at creation");
@@ -589,6 +597,7 @@ int vxr_view_set_params(vxr_view* v, const vxr_view_desc* d) {
 int vxr_view_set_sky(vxr_view* v, const float* rgba, uint32_t w, uint32_t h, const float sky_light[24],
                      float light_scale, const uint32_t* blue_noise) {
     if (int r = check_view(v, "vxr_view_set_sky")) return r;
+    v->spatialEvOk = false;
     if (!rgba) {
         CUV(cudaStreamSynchronize(v->stream), "vxr_view_set_sky: wait");
         cudaFree(v->skyDev); cudaFree(v->skyTex); cudaFree(v->skyBlueNoise);
@@ -625,6 +634,7 @@ int vxr_view_set_sky(vxr_view* v, const float* rgba, uint32_t w, uint32_t h, con
 
 int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* out) {
     if (int r = check_view(v, "vxr_view_begin_frame")) return r;
+    v->spatialEvOk = false;
     if (int r = ensure_world(v)) return r;
     vxr::World& w = v->world->w;
     if (w.lightVersion != v->seenLightVersion) {
@@ -666,7 +676,7 @@ int vxr_view_set_frame_consts(vxr_view* v, const vxr_frame_consts* k) {
     return VXR_OK;
 }
 
-static int run_stage(vxr_view* v, int stage, bool fuse) {
+static int run_stage(vxr_view* v, int stage, bool fuse, cudaStream_t s) {
     if (!v->frameOpen) return set_error(VXR_E_STATE, "vxr_view_stage: call vxr_view_begin_frame first");
     if (int r = ensure_world(v)) return r;
     const vxr::dev::World w = dev_world(v);
@@ -676,13 +686,13 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     const vxr::Tuning sh = shape(v);
     if (stage == VXR_STAGE_PATH_TRACE) {   // ground-truth mode: no stage timing
         vxr::BatchDev bd = vxr::single_batch(w, k, v->buf, v->cur, point, sh);
-        vxr::launch_path_trace(bd, v->stream);
+        vxr::launch_path_trace(bd, s);
         CUV(cudaGetLastError(), "kernel launch");
         return VXR_OK;
     }
     const int ri = (int)(v->frameSerial % vxr_view::kRing) * 6 + stage;
-    CUV(cudaEventRecord(v->evs[stage], v->stream), "cudaEventRecord");
-    CUV(cudaEventRecord(v->ringS[ri], v->stream), "cudaEventRecord");
+    CUV(cudaEventRecord(v->evs[stage], s), "cudaEventRecord");
+    CUV(cudaEventRecord(v->ringS[ri], s), "cudaEventRecord");
     vxr::BatchDev bd = vxr::single_batch(w, k, v->buf, v->cur, point, sh);
     bd.fuse = fuse ? 1 : 0;
     bd.timer = v->ktimerOn ? v->ktimer : nullptr;
@@ -697,21 +707,21 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
     }
     const int variant = point ? 1 : 0;
     switch (stage) {
-    case VXR_STAGE_ALBEDO: vxr::launch_batch_albedo(bd, variant, v->stream); break;
+    case VXR_STAGE_ALBEDO: vxr::launch_batch_albedo(bd, variant, s); break;
     case VXR_STAGE_CANDIDATES: {
         vxr::LearnedHook hook;
         const bool learned = vxr::learned_hook(v, &hook);
-        vxr::launch_batch_candidates(bd, variant, learned ? &hook : nullptr, v->stream);
+        vxr::launch_batch_candidates(bd, variant, learned ? &hook : nullptr, s);
         break;
     }
-    case VXR_STAGE_SPATIAL: vxr::launch_batch_spatial(bd, variant, v->stream); break;
-    case VXR_STAGE_SHADE: vxr::launch_batch_shade(bd, variant, v->stream); break;
-    case VXR_STAGE_ACCUMULATE: vxr::launch_batch_accumulate(bd, variant, v->stream); break;
+    case VXR_STAGE_SPATIAL: vxr::launch_batch_spatial(bd, variant, s); break;
+    case VXR_STAGE_SHADE: vxr::launch_batch_shade(bd, variant, s); break;
+    case VXR_STAGE_ACCUMULATE: vxr::launch_batch_accumulate(bd, variant, s); break;
     default: return set_error(VXR_E_INVALID, "vxr_view_stage: unknown stage");
     }
     CUV(cudaGetLastError(), "kernel launch");
-    CUV(cudaEventRecord(v->eve[stage], v->stream), "cudaEventRecord");
-    CUV(cudaEventRecord(v->ringE[ri], v->stream), "cudaEventRecord");
+    CUV(cudaEventRecord(v->eve[stage], s), "cudaEventRecord");
+    CUV(cudaEventRecord(v->ringE[ri], s), "cudaEventRecord");
     v->ringUsed[ri] = 1;
     v->ran[stage] = true;
     return VXR_OK;
@@ -719,7 +729,7 @@ static int run_stage(vxr_view* v, int stage, bool fuse) {
 
 int vxr_view_stage(vxr_view* v, int stage) {
     if (int r = check_view(v, "vxr_view_stage")) return r;
-    return run_stage(v, stage, false);
+    return run_stage(v, stage, false, v->stream);
 }
 
 int vxr_view_end_frame(vxr_view* v) {
@@ -731,15 +741,28 @@ int vxr_view_end_frame(vxr_view* v) {
     return vxr::brick_cache_end(v);
 }
 
+// One frame. The primary rays write the G-buffer plane and the seeds that the previous
+// frame's candidate and spatial passes were the last to touch (its shading reads only the
+// other plane, the reservoirs and the hit list), so when the previous frame was rendered
+// here with nothing in between, they run on the second stream from the end of that
+// frame's spatial pass, beside its shading. The candidate pass waits for them.
 int vxr_view_render(vxr_view* v) {
     if (int r = check_view(v, "vxr_view_render")) return r;
+    const bool overlap = v->spatialEvOk && shape(v).brickCache <= 0;
     if (int r = vxr_view_begin_frame(v, nullptr)) return r;
-    if (int r = run_stage(v, VXR_STAGE_ALBEDO, false)) return r;
-    if (int r = run_stage(v, VXR_STAGE_CANDIDATES, false)) return r;
-    if (int r = run_stage(v, VXR_STAGE_SPATIAL, false)) return r;
-    if (int r = run_stage(v, VXR_STAGE_SHADE, true)) return r;
+    if (!overlap) CUV(cudaEventRecord(v->evNow, v->stream), "cudaEventRecord");
+    CUV(cudaStreamWaitEvent(v->stream2, overlap ? v->evSpatial : v->evNow, 0), "cudaStreamWaitEvent");
+    if (int r = run_stage(v, VXR_STAGE_ALBEDO, false, v->stream2)) return r;
+    CUV(cudaEventRecord(v->evAlbedo, v->stream2), "cudaEventRecord");
+    CUV(cudaStreamWaitEvent(v->stream, v->evAlbedo, 0), "cudaStreamWaitEvent");
+    if (int r = run_stage(v, VXR_STAGE_CANDIDATES, false, v->stream)) return r;
+    if (int r = run_stage(v, VXR_STAGE_SPATIAL, false, v->stream)) return r;
+    CUV(cudaEventRecord(v->evSpatial, v->stream), "cudaEventRecord");
+    if (int r = run_stage(v, VXR_STAGE_SHADE, true, v->stream)) return r;
     if (int r = vxr::proposal_frame_train(v)) return r;
-    return vxr_view_end_frame(v);
+    if (int r = vxr_view_end_frame(v)) return r;
+    v->spatialEvOk = true;
+    return VXR_OK;
 }
 
 // waits for the view's stream; join: also for the online training step still running on
@@ -798,6 +821,7 @@ int vxr_view_read_gbuffer(vxr_view* v, int which, vxr_gbuffer_rec* out) {
 
 int vxr_view_write_gbuffer(vxr_view* v, int which, const vxr_gbuffer_rec* in) {
     if (int r = check_view(v, "vxr_view_write_gbuffer")) return r;
+    v->spatialEvOk = false;
     VXR_CHECK_ARG(in && (which == 0 || which == 1), "vxr_view_write_gbuffer: bad argument");
     const size_t n = v->npx;
     std::vector<uint2> vd(n);
@@ -846,6 +870,7 @@ int vxr_view_read_reservoirs(vxr_view* v, int role, vxr_reservoir_rec* out) {
 
 int vxr_view_write_reservoirs(vxr_view* v, int role, const vxr_reservoir_rec* in) {
     if (int r = check_view(v, "vxr_view_write_reservoirs")) return r;
+    v->spatialEvOk = false;
     VXR_CHECK_ARG(in && (role == 0 || role == 1), "vxr_view_write_reservoirs: bad argument");
     const size_t n = v->npx;
     std::vector<uint4> a(n);
@@ -985,6 +1010,7 @@ int vxr_host_free(void* p) {
 
 int vxr_view_timer_begin(vxr_view* v) {
     if (int r = check_view(v, "vxr_view_timer_begin")) return r;
+    v->spatialEvOk = false;   // the next frame's primary rays start after this mark
     CUV(cudaEventRecord(v->evs[0], v->stream), "cudaEventRecord");
     return VXR_OK;
 }

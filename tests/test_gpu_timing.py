@@ -1,5 +1,6 @@
 """Per-kernel timing (vxr_view_kernel_timing / vxr_view_kernel_stats) and the work
 counts of a frame (vxr_view_work_counts)."""
+import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -69,5 +70,39 @@ def test_pipelined_images_equal_synchronous_ones(lib, cuda_device, scene0):
     finally:
         for b in bufs + [sync]:
             b.close()
+        va.close()
+        vb.close()
+
+
+def test_overlapped_frames_equal_stage_by_stage_ones(lib, cuda_device, scene0):
+    """vxr_view_render starts a frame's primary rays beside the previous frame's shading
+    when the frames follow each other with no other call on the view; the images, G-buffer
+    planes and reservoirs equal those of the same frames rendered stage by stage (every
+    stage in order on the view's stream), bit for bit."""
+    w, _ = scene0
+    W, H = 320, 180
+    va = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1, rng_seed=5))
+    vb = lib.View(w, lib.view_desc(W, H, lib.LIGHTS_AREA, accumulate=1, rng_seed=5))
+    try:
+        for f in range(8):
+            pos, tgt = (100.0 + 4 * f, 150.0, 10.0 + 3 * f), (128.0, 120.0, 128.0)
+            va.lookat(pos, tgt)
+            va.render()
+            vb.lookat(pos, tgt)
+            vb.begin_frame()
+            for s in (lib.STAGE_ALBEDO, lib.STAGE_CANDIDATES, lib.STAGE_SPATIAL, lib.STAGE_SHADE,
+                      lib.STAGE_ACCUMULATE):
+                vb.stage(s)
+            vb.end_frame()
+        va.wait()
+        vb.wait()
+        assert np.array_equal(va.read_frame().view(np.uint32), vb.read_frame().view(np.uint32))
+        assert np.array_equal(va.read_accum().view(np.uint32), vb.read_accum().view(np.uint32))
+        bits = lambda a: np.ascontiguousarray(a).view(np.uint8)
+        for which in (0, 1):
+            assert np.array_equal(bits(va.read_gbuffer(which)), bits(vb.read_gbuffer(which)))
+        for role in (0, 1):
+            assert np.array_equal(bits(va.read_reservoirs(role)), bits(vb.read_reservoirs(role)))
+    finally:
         va.close()
         vb.close()
