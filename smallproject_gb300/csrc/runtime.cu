@@ -560,6 +560,7 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
 
 int vxr_view_destroy(vxr_view* v) {
     if (!v) return VXR_OK;
+    if (v->stream2) cudaStreamSynchronize(v->stream2);
     cudaStreamSynchronize(v->stream);
     free_view(v);
     delete v;
