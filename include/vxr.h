@@ -345,8 +345,9 @@ int vxr_view_stage(vxr_view* v, int stage);
 int vxr_view_end_frame(vxr_view* v);
 /* World::Render: begin_frame, the five stages (shading and accumulation fused in one
  * kernel), end_frame. Asynchronous. When the previous frame was also rendered by this
- * call with no other call on the view in between, the primary rays run on the view's
- * second stream beside the previous frame's shading (same results). */
+ * call with no other call on the view in between, this frame's primary rays, candidates
+ * and candidate visibility run on the view's second stream beside the previous frame's
+ * shading (same results). */
 int vxr_view_render(vxr_view* v);
 /* World::Commit's wait (world.cpp:2432-2438): block until the view's work is done,
  * read the stage timings, and report device-side errors as VXR_E_DEVICE. */

@@ -1148,7 +1148,8 @@ static void launch_ris(const BatchDev& bd, unsigned nb, cudaStream_t s) {
 }
 
 template <int VARIANT>
-static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStream_t s) {
+static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStream_t s, cudaStream_t tail,
+                         cudaEvent_t ev) {
     const size_t n = bd.totalPixels;
     cudaMemsetAsync(bd.counters + kCtrHits, 0, 3 * sizeof(uint32_t), s);   // hits, q1 requests, q1 fetch
     uint32_t maxPx = VARIANT < 2 ? bd.totalPixels : 0;
@@ -1196,6 +1197,11 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
     }
     if (!learnedDone) launch_ris<VARIANT, false>(bd, nb, s);
     launch_shadow<VARIANT < 2 ? 0 : 2>(bd, kCtrQ1, 0, s);
+    if (tail && tail != s) {
+        cudaEventRecord(ev, s);
+        cudaStreamWaitEvent(tail, ev, 0);
+        s = tail;
+    }
     // a single view without temporal reuse this frame skips the launch (a table checks per view)
     if (VARIANT == 2 || (bd.one.k.restirtemporalframe > 0 && bd.one.k.temporal)) {
         Timed tm(bd, K_TEMPORAL, s);
@@ -1203,10 +1209,11 @@ static void candidates_v(const BatchDev& bd, const LearnedHook* learned, cudaStr
     }
 }
 
-void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s) {
-    if (variant == 0) candidates_v<0>(bd, learned, s);
-    else if (variant == 1) candidates_v<1>(bd, learned, s);
-    else candidates_v<2>(bd, nullptr, s);
+void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s,
+                             cudaStream_t tail, cudaEvent_t ev) {
+    if (variant == 0) candidates_v<0>(bd, learned, s, tail, ev);
+    else if (variant == 1) candidates_v<1>(bd, learned, s, tail, ev);
+    else candidates_v<2>(bd, nullptr, s, tail, ev);
 }
 
 void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s) {

@@ -23,6 +23,13 @@ struct ViewBuffers {
     float4* qA = nullptr;
     float4* qB = nullptr;
     uint32_t* counters = nullptr;         // kCounters words
+    // the previous frame's work lists (swapped with the four above as a frame begins):
+    // a frame's candidate passes fill their own lists while the previous frame's shading
+    // still reads its hit list and shadow-ray queue
+    uint32_t* hitsAlt = nullptr;
+    float4* qAAlt = nullptr;
+    float4* qBAlt = nullptr;
+    uint32_t* countersAlt = nullptr;
 };
 
 // Work-list counters of a batch: list lengths and work-queue cursors.
@@ -142,7 +149,10 @@ void apply_tuning(BatchDev& bd, const Tuning& tu);
 // point lights, 2 view table (light model per view). A learned proposal needs variant 0/1.
 void launch_batch_albedo(const BatchDev& bd, int variant, cudaStream_t s);
 void launch_path_trace(const BatchDev& bd, cudaStream_t s);
-void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s);
+// tail, ev (optional): the temporal pass runs on stream tail after an event ev that s
+// records behind the candidate visibility pass
+void launch_batch_candidates(const BatchDev& bd, int variant, const LearnedHook* learned, cudaStream_t s,
+                             cudaStream_t tail = nullptr, cudaEvent_t ev = nullptr);
 void launch_batch_spatial(const BatchDev& bd, int variant, cudaStream_t s);
 void launch_batch_shade(const BatchDev& bd, int variant, cudaStream_t s);
 void launch_batch_accumulate(const BatchDev& bd, int variant, cudaStream_t s);

@@ -419,28 +419,30 @@ int proposal_frame_train(vxr_view* v) {
     return VXR_OK;
 }
 
-// the view stream waits for the frame training steps still running on the side stream
-// (slot < 0: all of them; else the one that signals joinEv[slot])
-static void join_slot(vxr_view* v, int slot) {
+// stream s (the view's, or the one running the candidate passes) waits for the frame
+// training steps still running on the side stream (slot < 0: all of them; else the one
+// that signals joinEv[slot]); work that s hands on to the view's stream by an event
+// carries the wait with it
+static void join_slot(vxr_view* v, int slot, cudaStream_t s) {
     Proposal* p = v->prop;
     if (!p) return;
     for (int i = 0; i < 2; i++) {
         if ((slot >= 0 && i != slot) || !p->trainPending[i]) continue;
-        cudaStreamWaitEvent(v->stream, p->joinEv[i], 0);
+        cudaStreamWaitEvent(s, p->joinEv[i], 0);
         p->trainPending[i] = false;
     }
 }
 
-void proposal_join(vxr_view* v) { join_slot(v, -1); }
+void proposal_join(vxr_view* v) { join_slot(v, -1, v->stream); }
 
 // the candidate stage's hook (nullptr when the view samples uniformly)
-bool learned_hook(vxr_view* v, LearnedHook* h) {
+bool learned_hook(vxr_view* v, LearnedHook* h, cudaStream_t s) {
     Proposal* p = v->prop;
     // the inference reads the weights of the last training step, or with training_lag = 1
     // the published ones of the step before it (slot (gen - 2) & 1 = gen & 1)
     const bool lag = p && p->pubParams[0];
     const int slot = p ? (int)(p->gen & 1u) : 0;
-    join_slot(v, lag ? slot : -1);
+    join_slot(v, lag ? slot : -1, s);
     if (!v->useProposal || !p) return false;
     h->infer = prop::InferArgs{};
     h->infer.dims = p->d;

@@ -184,7 +184,7 @@ static int upload(World& w) {
 
 
 namespace vxr {
-bool learned_hook(vxr_view* v, LearnedHook* h);
+bool learned_hook(vxr_view* v, LearnedHook* h, cudaStream_t s);
 int proposal_frame_train(vxr_view* v);
 void proposal_join(vxr_view* v);   // the view stream waits for the frame's training step
 }
@@ -258,6 +258,7 @@ void free_view(vxr_view* v) {
     cudaFree(b.cA); cudaFree(b.cB); cudaFree(b.hA); cudaFree(b.hB);
     cudaFree(b.frame); cudaFree(b.accum); cudaFree(b.err);
     cudaFree(b.hits); cudaFree(b.qA); cudaFree(b.qB); cudaFree(b.counters);
+    cudaFree(b.hitsAlt); cudaFree(b.qAAlt); cudaFree(b.qBAlt); cudaFree(b.countersAlt);
     cudaFree(v->sum64); cudaFree(v->errOut);
     cudaFree(v->skyDev); cudaFree(v->skyTex); cudaFree(v->skyBlueNoise);
     cudaFree(v->bc.keys); cudaFree(v->bc.mask); cudaFree(v->bc.count);
@@ -273,7 +274,7 @@ void free_view(vxr_view* v) {
     for (cudaEvent_t e : v->ringE) cudaEventDestroy(e);
     for (cudaEvent_t e : v->imgEv)
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {v->evSpatial, v->evAlbedo, v->evNow})
+    for (cudaEvent_t e : {v->evSpatial, v->evFront, v->evNow})
         if (e) cudaEventDestroy(e);
     if (v->stream2) cudaStreamDestroy(v->stream2);
     if (v->stream) cudaStreamDestroy(v->stream);
@@ -520,6 +521,10 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     alloc((void**)&b.qA, n * sizeof(float4));
     alloc((void**)&b.qB, n * sizeof(float4));
     alloc((void**)&b.counters, vxr::kCounters * sizeof(uint32_t));
+    alloc((void**)&b.hitsAlt, n * sizeof(uint32_t));
+    alloc((void**)&b.qAAlt, n * sizeof(float4));
+    alloc((void**)&b.qBAlt, n * sizeof(float4));
+    alloc((void**)&b.countersAlt, vxr::kCounters * sizeof(uint32_t));
     // the highest stream priority: a learned view's training steps (a side stream of the
     // lowest priority with training_lag = 1) fill only the SM slots its frames leave free
     int leastPrio = 0, greatestPrio = 0;
@@ -527,7 +532,7 @@ int vxr_view_create(vxr_world* w, const vxr_view_desc* d, vxr_view** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&v->stream, cudaStreamNonBlocking, greatestPrio);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&v->stream2, cudaStreamNonBlocking, greatestPrio);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evSpatial, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evAlbedo, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evFront, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->evNow, cudaEventDisableTiming);
     v->ringS.assign(vxr_view::kRing * 6, nullptr);
     v->ringE.assign(vxr_view::kRing * 6, nullptr);
@@ -659,6 +664,10 @@ int vxr_view_begin_frame(vxr_view* v, vxr_frame_consts* out) {
     k.spatialRadius = v->desc.spatial_radius;
     k.spatialTaps = v->desc.spatial_taps;
     v->cur ^= 1;   // G-buffer swap (world.cpp:2221-2223)
+    std::swap(v->buf.hits, v->buf.hitsAlt);   // this frame's work lists
+    std::swap(v->buf.qA, v->buf.qAAlt);
+    std::swap(v->buf.qB, v->buf.qBAlt);
+    std::swap(v->buf.counters, v->buf.countersAlt);
     if (int r = vxr::brick_cache_begin(v)) return r;
     v->frameOpen = true;
     for (int i = 0; i < 6; i++) v->ran[i] = false;
@@ -677,7 +686,10 @@ int vxr_view_set_frame_consts(vxr_view* v, const vxr_frame_consts* k) {
     return VXR_OK;
 }
 
-static int run_stage(vxr_view* v, int stage, bool fuse, cudaStream_t s) {
+// s: the stream of the stage's launches; tail (candidate stage): the stream of its
+// temporal pass, handed on by an event (null: s)
+static int run_stage(vxr_view* v, int stage, bool fuse, cudaStream_t s, cudaStream_t tail = nullptr) {
+    if (!tail) tail = s;
     if (!v->frameOpen) return set_error(VXR_E_STATE, "vxr_view_stage: call vxr_view_begin_frame first");
     if (int r = ensure_world(v)) return r;
     const vxr::dev::World w = dev_world(v);
@@ -711,8 +723,8 @@ static int run_stage(vxr_view* v, int stage, bool fuse, cudaStream_t s) {
     case VXR_STAGE_ALBEDO: vxr::launch_batch_albedo(bd, variant, s); break;
     case VXR_STAGE_CANDIDATES: {
         vxr::LearnedHook hook;
-        const bool learned = vxr::learned_hook(v, &hook);
-        vxr::launch_batch_candidates(bd, variant, learned ? &hook : nullptr, s);
+        const bool learned = vxr::learned_hook(v, &hook, s);
+        vxr::launch_batch_candidates(bd, variant, learned ? &hook : nullptr, s, tail, v->evFront);
         break;
     }
     case VXR_STAGE_SPATIAL: vxr::launch_batch_spatial(bd, variant, s); break;
@@ -721,8 +733,8 @@ static int run_stage(vxr_view* v, int stage, bool fuse, cudaStream_t s) {
     default: return set_error(VXR_E_INVALID, "vxr_view_stage: unknown stage");
     }
     CUV(cudaGetLastError(), "kernel launch");
-    CUV(cudaEventRecord(v->eve[stage], s), "cudaEventRecord");
-    CUV(cudaEventRecord(v->ringE[ri], s), "cudaEventRecord");
+    CUV(cudaEventRecord(v->eve[stage], tail), "cudaEventRecord");
+    CUV(cudaEventRecord(v->ringE[ri], tail), "cudaEventRecord");
     v->ringUsed[ri] = 1;
     v->ran[stage] = true;
     return VXR_OK;
@@ -742,11 +754,14 @@ int vxr_view_end_frame(vxr_view* v) {
     return vxr::brick_cache_end(v);
 }
 
-// One frame. The primary rays write the G-buffer plane and the seeds that the previous
-// frame's candidate and spatial passes were the last to touch (its shading reads only the
-// other plane, the reservoirs and the hit list), so when the previous frame was rendered
-// here with nothing in between, they run on the second stream from the end of that
-// frame's spatial pass, beside its shading. The candidate pass waits for them.
+// One frame. Its front half (primary rays, hit list, proposal, candidates and their
+// visibility) writes the G-buffer plane, the seeds and the candidate reservoirs that the
+// previous frame's candidate and spatial passes were the last to touch, and this frame's
+// own work lists; the previous frame's shading reads only the other plane, the spatial
+// reservoirs and its own lists. So when the previous frame was rendered here with
+// nothing in between, the front half runs on the second stream from the end of that
+// frame's spatial pass, beside its shading; the temporal pass (which reads the history
+// that shading patches) and everything after it run on the view's stream.
 int vxr_view_render(vxr_view* v) {
     if (int r = check_view(v, "vxr_view_render")) return r;
     const bool overlap = v->spatialEvOk && shape(v).brickCache <= 0;
@@ -754,9 +769,7 @@ int vxr_view_render(vxr_view* v) {
     if (!overlap) CUV(cudaEventRecord(v->evNow, v->stream), "cudaEventRecord");
     CUV(cudaStreamWaitEvent(v->stream2, overlap ? v->evSpatial : v->evNow, 0), "cudaStreamWaitEvent");
     if (int r = run_stage(v, VXR_STAGE_ALBEDO, false, v->stream2)) return r;
-    CUV(cudaEventRecord(v->evAlbedo, v->stream2), "cudaEventRecord");
-    CUV(cudaStreamWaitEvent(v->stream, v->evAlbedo, 0), "cudaStreamWaitEvent");
-    if (int r = run_stage(v, VXR_STAGE_CANDIDATES, false, v->stream)) return r;
+    if (int r = run_stage(v, VXR_STAGE_CANDIDATES, false, v->stream2, v->stream)) return r;
     if (int r = run_stage(v, VXR_STAGE_SPATIAL, false, v->stream)) return r;
     CUV(cudaEventRecord(v->evSpatial, v->stream), "cudaEventRecord");
     if (int r = run_stage(v, VXR_STAGE_SHADE, true, v->stream)) return r;

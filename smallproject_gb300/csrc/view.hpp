@@ -75,12 +75,13 @@ struct vxr_view {
     vxr::Tuning tuning;                               // launch parameters (vxr_view_set_tuning)
     int cur = 0;
     cudaStream_t stream = nullptr;
-    // vxr_view_render: a frame's primary rays run on stream2 as soon as the previous
-    // frame's spatial pass is done (evSpatial), beside that frame's shading; the
-    // candidate stage waits for them (evAlbedo). spatialEvOk: evSpatial marks the last
-    // frame's spatial pass and nothing has touched the buffers since.
+    // vxr_view_render: a frame's front half (primary rays to candidate visibility) runs
+    // on stream2 as soon as the previous frame's spatial pass is done (evSpatial), beside
+    // that frame's shading; the temporal pass on the view's stream waits for it
+    // (evFront). spatialEvOk: evSpatial marks the last frame's spatial pass and nothing
+    // has touched the buffers since.
     cudaStream_t stream2 = nullptr;
-    cudaEvent_t evSpatial = nullptr, evAlbedo = nullptr, evNow = nullptr;
+    cudaEvent_t evSpatial = nullptr, evFront = nullptr, evNow = nullptr;
     bool spatialEvOk = false;
     cudaEvent_t evs[6] = {}, eve[6] = {};            // [0]: vxr_view_timer_*, [1..5]: last frame's stages
     bool ran[6] = {};

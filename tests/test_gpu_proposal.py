@@ -352,3 +352,51 @@ def test_online_training_weights_reach_the_right_frame(lib, world256, lag):
         oa, ob = np.argsort(ga), np.argsort(hits)
         assert np.array_equal(ga[oa], hits[ob]), f
         assert np.array_equal(gc[:, oa], cand[:, ob]), (f, lag)
+
+
+def test_overlapped_learned_frames_equal_stage_by_stage_ones(lib, world256):
+    """A learned view's front half (primary rays, hit list, inference, candidates and
+    their visibility) runs beside the previous frame's shading when frames follow each
+    other through vxr_view_render; with the same network (no training in the frames; one
+    evaluation per pixel, so no draw depends on the hit list's order) the images,
+    G-buffer planes and reservoirs equal those of frames rendered stage by stage."""
+    W, H = 240, 136
+    trainer = lib.View(world256, lib.view_desc(W, H, lib.LIGHTS_AREA, num_candidates=4))
+    trainer.proposal_enable(seed=5, batch=8192, inference=2)
+    trainer.lookat((110.0, 150.0, 10.0), (128.0, 110.0, 128.0))
+    for _ in range(3):
+        trainer.render()
+        trainer.proposal_train(1)
+    params = trainer.proposal_params()
+    trainer.close()
+    views = []
+    try:
+        for _ in range(2):
+            v = lib.View(world256, lib.view_desc(W, H, lib.LIGHTS_AREA, num_candidates=4, accumulate=1, rng_seed=17))
+            v.proposal_enable(seed=5, batch=8192, inference=2)
+            v.proposal_set_params(params)
+            v.proposal_use(True)
+            views.append(v)
+        va, vb = views
+        for f in range(6):
+            pos, tgt = (104.0 + 3 * f, 150.0, 10.0 + 2 * f), (128.0, 110.0, 128.0)
+            va.lookat(pos, tgt)
+            va.render()
+            vb.lookat(pos, tgt)
+            vb.begin_frame()
+            for s in (lib.STAGE_ALBEDO, lib.STAGE_CANDIDATES, lib.STAGE_SPATIAL, lib.STAGE_SHADE,
+                      lib.STAGE_ACCUMULATE):
+                vb.stage(s)
+            vb.end_frame()
+        va.wait()
+        vb.wait()
+        bits = lambda a: np.ascontiguousarray(a).view(np.uint8)
+        assert np.array_equal(bits(va.read_frame()), bits(vb.read_frame()))
+        assert np.array_equal(bits(va.read_accum()), bits(vb.read_accum()))
+        for which in (0, 1):
+            assert np.array_equal(bits(va.read_gbuffer(which)), bits(vb.read_gbuffer(which)))
+        for role in (0, 1):
+            assert np.array_equal(bits(va.read_reservoirs(role)), bits(vb.read_reservoirs(role)))
+    finally:
+        for v in views:
+            v.close()
