@@ -1039,15 +1039,20 @@ def small_configs(vx, tuning_fn, steps, warmup):
             v.lookat(*cam(f))
             v.render()
         v.wait()
-        v.kernel_timing(True)
-        v.kernel_stats(reset=True)
-        v.stage_stats(reset=True)
         v.timer_begin()
         for f in range(steps):
             v.lookat(*cam(warmup + f))
             v.render()
         ms = v.timer_end() / steps
         v.wait()
+        # stage and kernel times from frames each waited for (no overlap between frames)
+        v.kernel_timing(True)
+        v.kernel_stats(reset=True)
+        v.stage_stats(reset=True)
+        for f in range(min(steps, KERNEL_PASS_FRAMES)):
+            v.lookat(*cam(warmup + steps + f))
+            v.render()
+            v.wait()
         v.kernel_timing(False)
         ks = v.kernel_stats(reset=True)
         sums, counts = v.stage_stats(reset=True)
@@ -1087,13 +1092,18 @@ def other_modes(make_view, cams, steps, warmup):
         for f in range(warmup):
             frame(f)
         view.wait()
-        view.kernel_timing(True)
-        view.kernel_stats(reset=True)
         view.timer_begin()
         for f in range(steps):
             frame(warmup + f)
         ms = view.timer_end() / steps
         view.wait()
+        # kernel times from frames each waited for (back to back, a frame's front half
+        # runs beside the previous frame's shading)
+        view.kernel_timing(True)
+        view.kernel_stats(reset=True)
+        for f in range(min(steps, KERNEL_PASS_FRAMES)):
+            frame(warmup + steps + f)
+            view.wait()
         view.kernel_timing(False)
         ks = view.kernel_stats(reset=True)
         return ms, {k: v[0] / v[1] for k, v in ks.items() if v[1]}
