@@ -483,6 +483,7 @@ int vxr_proposal_default_desc(vxr_proposal_desc* d) {
 
 int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
     if (int r = check_view(v, "vxr_view_proposal_enable")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(desc, "vxr_view_proposal_enable: null desc");
     VXR_CHECK_ARG(desc->epsilon > 0.0f && desc->epsilon <= 1.0f, "vxr_view_proposal_enable: epsilon must be in (0, 1]");
@@ -555,6 +556,7 @@ int vxr_view_proposal_enable(vxr_view* v, const vxr_proposal_desc* desc) {
 
 int vxr_view_proposal_use(vxr_view* v, int on) {
     if (int r = check_view(v, "vxr_view_proposal_use")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     if (on && !v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_use: enable the proposal first");
     if (on && v->prop->clusterVersion != v->world->w.clusterVersion)
@@ -565,6 +567,7 @@ int vxr_view_proposal_use(vxr_view* v, int on) {
 
 int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
     if (int r = check_view(v, "vxr_view_proposal_train")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     vxr::Proposal* p = v->prop;
     if (!p) return set_error(VXR_E_STATE, "vxr_view_proposal_train: enable the proposal first");
@@ -588,6 +591,7 @@ int vxr_view_proposal_train(vxr_view* v, uint32_t steps, float* loss) {
 
 int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame) {
     if (int r = check_view(v, "vxr_view_proposal_online")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_online: enable the proposal first");
     VXR_CHECK_ARG(steps_per_frame <= 16, "vxr_view_proposal_online: at most 16 steps per frame");
@@ -599,6 +603,7 @@ int vxr_view_proposal_online(vxr_view* v, uint32_t steps_per_frame) {
 
 int vxr_view_proposal_test_timeout(vxr_view* v, int on) {
     if (int r = check_view(v, "vxr_view_proposal_test_timeout")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_test_timeout: enable the proposal first");
     v->prop->testTimeout = on != 0;
@@ -607,6 +612,7 @@ int vxr_view_proposal_test_timeout(vxr_view* v, int on) {
 
 int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hits, uint32_t* cand) {
     if (int r = check_view(v, "vxr_view_proposal_read_candidates")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(nhits, "vxr_view_proposal_read_candidates: null nhits");
     vxr::Proposal* p = v->prop;
@@ -627,6 +633,7 @@ int vxr_view_proposal_read_candidates(vxr_view* v, uint32_t* nhits, uint32_t* hi
 
 int vxr_view_proposal_rows(vxr_view* v, uint32_t* rows) {
     if (int r = check_view(v, "vxr_view_proposal_rows")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(rows, "vxr_view_proposal_rows: null rows");
     vxr::Proposal* p = v->prop;
@@ -639,6 +646,7 @@ int vxr_view_proposal_rows(vxr_view* v, uint32_t* rows) {
 
 int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, uint32_t* hidden) {
     if (int r = check_view(v, "vxr_view_proposal_param_count")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(n, "vxr_view_proposal_param_count: null output");
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_param_count: enable the proposal first");
@@ -650,6 +658,7 @@ int vxr_view_proposal_param_count(vxr_view* v, uint64_t* n, uint32_t* clusters, 
 
 int vxr_view_proposal_get_params(vxr_view* v, float* out) {
     if (int r = check_view(v, "vxr_view_proposal_get_params")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(out, "vxr_view_proposal_get_params: null output");
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_get_params: enable the proposal first");
@@ -660,6 +669,7 @@ int vxr_view_proposal_get_params(vxr_view* v, float* out) {
 
 int vxr_view_proposal_set_params(vxr_view* v, const float* in) {
     if (int r = check_view(v, "vxr_view_proposal_set_params")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(in, "vxr_view_proposal_set_params: null input");
     if (!v->prop) return set_error(VXR_E_STATE, "vxr_view_proposal_set_params: enable the proposal first");
@@ -674,6 +684,7 @@ int vxr_view_proposal_set_params(vxr_view* v, const float* in) {
 int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const uint32_t* target, const float* weight,
                            float* loss, float* grad) {
     if (int r = check_view(v, "vxr_view_proposal_grad")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(B >= 1 && samples && target && weight && loss && grad, "vxr_view_proposal_grad: bad argument");
     vxr::Proposal* p = v->prop;
@@ -702,6 +713,7 @@ int vxr_view_proposal_grad(vxr_view* v, uint32_t B, const float* samples, const 
 
 int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float* probs) {
     if (int r = check_view(v, "vxr_view_proposal_probs")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(n >= 1 && samples && probs, "vxr_view_proposal_probs: bad argument");
     vxr::Proposal* p = v->prop;
@@ -743,6 +755,7 @@ int vxr_view_proposal_probs(vxr_view* v, uint32_t n, const float* samples, float
 // checkpoint: magic, version, dims, step, params, Adam moments
 int vxr_view_proposal_save(vxr_view* v, const char* path) {
     if (int r = check_view(v, "vxr_view_proposal_save")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(path, "vxr_view_proposal_save: null path");
     vxr::Proposal* p = v->prop;
@@ -766,6 +779,7 @@ int vxr_view_proposal_save(vxr_view* v, const char* path) {
 
 int vxr_view_proposal_load(vxr_view* v, const char* path) {
     if (int r = check_view(v, "vxr_view_proposal_load")) return r;
+    v->spatialEvOk = false;   // the next frame starts after this call's work
     vxr::proposal_join(v);
     VXR_CHECK_ARG(path, "vxr_view_proposal_load: null path");
     vxr::Proposal* p = v->prop;
