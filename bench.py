@@ -280,7 +280,9 @@ def cpu_arm(config, steps, warmup, W, H):
 
 CANDS = (2, 3, 4, 8, 12)
 CANDS2 = (2, 3, 4, 8, 12)
-CANDS4 = (1, 2, 3, 4, 8)
+# runs of four are the fastest family: 10 and 12 candidates land near plain's frame time,
+# where the equal-time comparison is made
+CANDS4 = (1, 2, 3, 4, 8, 10, 12)
 # hit pixels per network evaluation of each learned family (pixels_per_eval; runs of up to
 # eight measured no faster than runs of up to four at config 3)
 FAMILY_PPE = {"learned": 1, "learned2": 2, "learned4": 4}
