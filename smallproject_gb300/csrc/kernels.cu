@@ -7,7 +7,8 @@
 //   reservoirs C, H   uint4 + float4 planes (see Res in device.cuh), 32 B/pixel each:
 //              C = candidate+temporal output, H = spatial output = temporal history
 //   frame      float4 (rgb, dist); accum float4 (running mean, the output image)
-// and per batch of views:
+// and per batch of views (a single view holds two sets and takes the other one as each
+// frame begins, so its candidate passes can run beside the previous frame's shading):
 //   hits       uint32 list of (view << 27 | pixel) whose primary ray hit a voxel
 //   queue      float4 x 2 per entry: shadow-ray requests (origin | entry, dir | light)
 //   counters   uint32[kCounters]: list lengths and work-queue cursors (kernels.hpp)
